@@ -1,0 +1,215 @@
+/*
+ * sbpmg.h - C ABI of libsbpmg, a GB300 (sm_103a) matrix-free SBP-SAT 2D
+ * Poisson solver: operator apply, matrix-free CG, and geometric-multigrid
+ * preconditioned CG (MGCG), in FP64 and in mixed precision.
+ *
+ * It replaces the GPU entry points of AlexandreChern/SC_2022 (Julia +
+ * CUDA.jl).  Each declaration names the reference function it stands in for
+ * (path:line inside that repository).
+ *
+ * Conventions
+ *  - Grid functions are column-major n x n double (or float) arrays in
+ *    device memory: point (i, j) at p[j*n + i], i the fast index (x), exactly
+ *    the CuArray{Float64,2} layout of the reference.  n = 2^k + 1 for the
+ *    multigrid entry points; any n >= 3 for the single-grid ones.
+ *  - A is the SPD operator of the reference's Assembling_matrix
+ *    (preconditioned_CG/level_2_multigrid_new.jl:125-188):
+ *    A = -H~ (D2 + SAT_W + SAT_E + SAT_S + SAT_N), 2nd-order SBP, Dirichlet
+ *    SAT on the j = 0 / n-1 sides (tau = -13/h, beta = 1), Neumann SAT on the
+ *    i = 0 / n-1 sides (tau = -1).
+ *  - Callers own inputs and outputs.  Solver handles own all temporaries.
+ *  - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls are
+ *    stream ordered; the solve entry points return after the solve finished.
+ *  - Every function returns 0 (SBP_OK) or a negative sbp_status; no
+ *    exceptions cross the ABI.  A handle may be used by one host thread at a
+ *    time.
+ */
+#ifndef SBPMG_H_
+#define SBPMG_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum sbp_status {
+  SBP_OK = 0,
+  SBP_ERR_ARGS = -1,        /* invalid argument (size, null pointer, option) */
+  SBP_ERR_CUDA = -2,        /* a CUDA runtime call failed */
+  SBP_ERR_NOMEM = -3,       /* device or host allocation failed */
+  SBP_ERR_MAXITER = -4,     /* solver stopped at maxiter without converging */
+  SBP_ERR_BREAKDOWN = -5,   /* p'Ap == 0 or a non-finite residual */
+  SBP_ERR_UNSUPPORTED = -6  /* option combination not supported */
+} sbp_status;
+
+typedef enum sbp_smoother { SBP_SMOOTH_JACOBI = 0, SBP_SMOOTH_RICHARDSON = 1 } sbp_smoother;
+
+/* Residual restriction on the multigrid hierarchy.
+ * NORMAL:   full weighting with zero padding, restriction_matrix_normal
+ *           (level_2_multigrid_new.jl:220-233); what the reference's GPU
+ *           restriction kernel computes (matrix_free_mg_cg.jl:98-131).
+ * SBP:      kron of the SBP-preserving restriction_matrix (:205-218).
+ * GALERKIN: P^T, the SBP-compatible restriction H2h^-1 P^T Hh re-expressed
+ *           for the H~-scaled residuals of this operator (= 4 x NORMAL). */
+typedef enum sbp_restriction {
+  SBP_RESTRICT_NORMAL = 0,
+  SBP_RESTRICT_SBP = 1,
+  SBP_RESTRICT_GALERKIN = 2
+} sbp_restriction;
+
+typedef enum sbp_precision {
+  SBP_PREC_FP64 = 0,  /* everything in FP64 */
+  SBP_PREC_MIXED = 1  /* FP32 V-cycle (apply, smoother, transfers) inside
+                         FP64 PCG; FP64 residual, update, dots, coarse solve */
+} sbp_precision;
+
+typedef struct sbp_options {
+  int smoother;     /* sbp_smoother */
+  double omega;     /* smoother weight (0 = default: 2/3 Jacobi, 0.15 Richardson) */
+  int nu_pre;       /* pre-smoothing sweeps */
+  int nu_post;      /* post-smoothing sweeps */
+  int restriction;  /* sbp_restriction */
+  int coarse_n;     /* grid size of the direct coarse solve (<= 65) */
+  int precision;    /* sbp_precision */
+  int reserved[5];
+} sbp_options;
+
+typedef struct sbp_result {
+  int iters;           /* completed (P)CG iterations */
+  int status;          /* 0 converged, or SBP_ERR_MAXITER / SBP_ERR_BREAKDOWN */
+  double initial_norm; /* ||b - A x0||_2 */
+  double final_norm;   /* ||r||_2 of the last iterate (recurrence residual) */
+  double threshold;    /* the absolute stopping threshold used */
+} sbp_result;
+
+typedef struct sbp_solver sbp_solver;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int sbp_version(void);
+const char* sbp_status_string(int status);
+
+/* Default options: the V-cycle preconditioner of the N=4097 benchmark
+ * configuration: Jacobi omega = 2/3, 3 + 3 sweeps, GALERKIN restriction,
+ * coarse direct solve at 65 x 65, FP64. */
+void sbp_options_default(sbp_options* opts);
+
+/* The reference's own two-level GPU preconditioner
+ * (matrix_free_Two_level_multigrid, matrix_free_mg_cg.jl:143-176):
+ * Richardson omega = 0.15, nu = 3 + 3, NORMAL restriction, exact coarse
+ * solve at (n+1)/2.  Requires (n+1)/2 <= 65. */
+void sbp_options_reference_two_level(sbp_options* opts, int n);
+
+/* ---- single-grid operators (no handle) ------------------------------- */
+
+/* out = sign * A * u, sign = -1 reproduces the reference's
+ * matrix_free_A_full_GPU(idata, odata), which writes -A*idata
+ * (split_matrix_free.jl:444-486). */
+int sbp_apply_f64(const double* u, double* out, int n, int sign, void* stream);
+int sbp_apply_f32(const float* u, float* out, int n, int sign, void* stream);
+
+/* out = sign*A*u and *dot = sum(u .* out) (device pointer) in one pass: the
+ * fused operator + p'Ap of the CG loop (split_matrix_free.jl:665-666,
+ * matrix_free_mg_cg.jl:303-304).  Uses stream-ordered scratch
+ * (cudaMallocAsync) for the per-CTA partial sums. */
+int sbp_apply_dot_f64(const double* u, double* out, int n, int sign, double* dot,
+                      void* stream);
+
+/* *norm_host = ||b - sign*A*x||_2 (blocking).  The reference's residual
+ * check norm(-Av - b) (matrix_free_mg_cg.jl:175). */
+int sbp_residual_norm_f64(const double* x, const double* b, int n, int sign, double* norm_host,
+                          void* stream);
+
+/* coarse = R fine, fine n_fine x n_fine, coarse (n_fine+1)/2 squared, R one
+ * of sbp_restriction.  SBP_RESTRICT_NORMAL reproduces
+ * matrix_free_restriction_2d_GPU (matrix_free_mg_cg.jl:120-131). */
+int sbp_restrict_f64(const double* fine, double* coarse, int n_fine, int kind, void* stream);
+
+/* fine = P coarse (accumulate != 0: fine += P coarse), bilinear, coarse
+ * n_coarse^2 -> fine (2 n_coarse - 1)^2.  matrix_free_prolongation_2d_GPU
+ * (matrix_free_mg_cg.jl:69-77). */
+int sbp_prolong_f64(const double* coarse, double* fine, int n_coarse, int accumulate,
+                    void* stream);
+
+/* `iters` Richardson sweeps v <- v + omega (b - A v) on the caller's v,
+ * using `tmp` (n x n) as the second buffer; on return v and tmp both hold
+ * the result.  matrix_free_richardson(idata, odata, b; maxiter, omega)
+ * (matrix_free_mg_cg.jl:134-140), which mutates both arrays. */
+int sbp_richardson_f64(double* v, double* tmp, const double* b, int n, int iters, double omega,
+                       void* stream);
+
+/* Weighted Jacobi v <- v + omega D^-1 (b - A v), `iters` sweeps, same
+ * buffer contract (jacobi_brittany!, level_2_multigrid_new.jl:335-344). */
+int sbp_jacobi_f64(double* v, double* tmp, const double* b, int n, int iters, double omega,
+                   void* stream);
+
+/* b = -H~ (fsign*f + SAT_W_r gW + SAT_E_r gE + SAT_S_r gS + SAT_N_r gN): the
+ * right-hand side of Assembling_matrix (level_2_multigrid_new.jl:169-185).
+ * f is n x n in the D2 convention (Delta u = f) times fsign (fsign = -1 for
+ * -Delta u = f); gW/gE are the Dirichlet data along j = 0 / n-1 (indexed by
+ * i), gS/gN the outward normal derivatives along i = 0 / n-1 (indexed by j). */
+int sbp_rhs_f64(const double* f, const double* gW, const double* gE, const double* gS,
+                const double* gN, double* b, int n, double fsign, void* stream);
+
+/* Transpose of sbp_rhs_f64's map: given lam (n x n), writes df (n x n) and
+ * dgW, dgE, dgS, dgN (length n) with lam.b = df.f + sum dg_side.g_side.
+ * Any output may be NULL.  No reference counterpart: the adjoint path is
+ * new. */
+int sbp_rhs_adjoint_f64(const double* lam, double* df, double* dgW, double* dgE, double* dgS,
+                        double* dgN, int n, double fsign, void* stream);
+
+/* ---- solver handle ---------------------------------------------------- */
+
+/* Create a solver for n x n grids on the current device.  opts == NULL
+ * creates a plain-CG solver (no multigrid hierarchy); otherwise the MG
+ * hierarchy, its buffers and the dense inverse of the coarse operator are
+ * built (the reference's lu(A_2h), matrix_free_mg_cg.jl:460). */
+int sbp_solver_create(sbp_solver** out, int n, const sbp_options* opts);
+int sbp_solver_destroy(sbp_solver* s);
+/* Number of levels of the hierarchy (1 for a plain-CG solver). */
+int sbp_solver_levels(const sbp_solver* s);
+/* Bytes of device memory held by the handle. */
+long long sbp_solver_device_bytes(const sbp_solver* s);
+/* Kernel launches of the last solve on this handle (set-up, every
+ * iteration graph launched, including the one queued past convergence). */
+long long sbp_solver_last_launches(const sbp_solver* s);
+
+/* Preconditioned CG: solve A x = b from the caller's initial x (overwritten
+ * with the solution).  Stops when ||r||_2 < abstol (abstol > 0) or
+ * ||r||_2 < reltol * ||b - A x0|| (abstol <= 0), or after maxiter
+ * iterations.  norms (host, capacity norms_cap, may be NULL) receives
+ * ||r_k||_2 for k = 0..iters.  matrix_free_MGCG(b, x; A_2h, maxiter, abstol,
+ * nu) (matrix_free_mg_cg.jl:281-324), which returns (iters, norms, x).
+ * Returns SBP_OK, SBP_ERR_MAXITER or SBP_ERR_BREAKDOWN (res filled in all
+ * three cases). */
+int sbp_mgcg_solve(sbp_solver* s, const double* b, double* x, double abstol, double reltol,
+                   int maxiter, sbp_result* res, double* norms, int norms_cap, void* stream);
+
+/* Matrix-free CG on (sign*A) x = b.  sign = -1 is the reference's
+ * CG_full_GPU / CG_Matrix_Free_GPU_v2 (split_matrix_free.jl:647-714), which
+ * iterate with matrix_free_A_full_GPU and so solve (-A) x = b; sign = +1 is
+ * CG_CPU on the assembled A (level_2_multigrid_new.jl:258-291).  Works on
+ * any handle. */
+int sbp_cg_solve(sbp_solver* s, const double* b, double* x, int sign, double abstol,
+                 double reltol, int maxiter, sbp_result* res, double* norms, int norms_cap,
+                 void* stream);
+
+/* One V-cycle from v = 0: v = M b.  matrix_free_Two_level_multigrid(b, A_2h;
+ * nu) (matrix_free_mg_cg.jl:143-176) for the two-level options. */
+int sbp_vcycle_apply(sbp_solver* s, const double* b, double* v, void* stream);
+
+/* ---- host-only helpers ------------------------------------------------ */
+
+/* Dense inverse of the coarse operator A on an nc x nc grid (row-major,
+ * nc^2 x nc^2), computed on the host by banded Cholesky; the solver uploads
+ * it to replace the reference's per-V-cycle host LU solve
+ * (matrix_free_mg_cg.jl:166).  `cap` is the capacity of `out` in doubles.
+ * Needs no GPU. */
+int sbp_coarse_inverse_host(int nc, double* out, long long cap);
+
+/* Message of the last SBP_ERR_CUDA / SBP_ERR_NOMEM on this host thread. */
+const char* sbp_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SBPMG_H_ */

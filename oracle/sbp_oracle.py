@@ -1,0 +1,574 @@
+"""CPU oracle for the matrix-free SBP-SAT Poisson solver path.
+
+TEST INFRASTRUCTURE ONLY.  This module restates, in numpy/scipy, the
+reference's algorithms for the hot path so that the CUDA library can be
+checked against them.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
+``cpu_baseline`` / ``--impl reference`` legs of ``bench.py`` may import it,
+and only as the checker.  The product library never calls into it.
+
+Reference files restated here (paths inside AlexandreChern/SC_2022):
+
+* ``diagonal_sbp.jl:56-147``   ``diagonal_sbp_D1`` (p=2 branch, H norm)
+* ``diagonal_sbp.jl:189-197, 414-452`` ``diagonal_sbp_D2`` (p=2: D2, S0, SN)
+* ``preconditioned_CG/level_2_multigrid_new.jl:48-123`` ``Operators_2d``
+* ``preconditioned_CG/level_2_multigrid_new.jl:125-188`` ``Assembling_matrix``
+* ``preconditioned_CG/level_2_multigrid_new.jl:190-246`` transfer matrices
+* ``preconditioned_CG/level_2_multigrid_new.jl:258-291`` ``CG_CPU``
+* ``preconditioned_CG/level_2_multigrid_new.jl:335-350`` Jacobi / Richardson
+* ``preconditioned_CG/level_2_multigrid_new.jl:358-382`` ``Two_level_multigrid``
+* ``preconditioned_CG/level_2_multigrid_new.jl:480-524`` ``mg_preconditioned_CG``
+* ``split_matrix_free.jl:32-49, 324-486`` ``matrix_free_A_full_GPU`` (the -A apply)
+* ``preconditioned_CG/matrix_free_mg_cg.jl:17-38, 80-94`` matrix-free transfers
+
+Parity pin: the reference is Julia and no Julia toolchain exists here, and
+the reference commits no golden vectors.  The oracle is pinned by the
+reference's own in-code cross checks, restated: the matrix-free -A apply
+equals the kron-assembled operator (``split_matrix_free.jl:517``), the
+matrix-free transfers equal the kron matrices
+(``matrix_free_mg_cg.jl:636-646``), plus second-order convergence of the
+discretisation error against the manufactured solution
+(``matrix_free_mg_cg.jl:464``).  Parity against reference *outputs* is
+therefore unpinned.
+
+Grid convention (the reference's, Julia column-major): a grid function on
+n x n points is a flat vector with element (i, j) at ``j*n + i``; i is the
+fast index (x in the reference's ``u(x, y')``), j the slow index.  In numpy
+a grid is held as ``U[j, i]`` (shape (n, n), C order), which has the same
+flat order.  The reference's "W/E" sides (Dirichlet) are j = 0 / j = n-1,
+its "S/N" sides (Neumann) are i = 0 / i = n-1.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+# Penalty parameters hard-coded by the reference
+# (level_2_multigrid_new.jl:145-150; split_matrix_free.jl:453-455).
+TAU_D_TIMES_H = -13.0   # tau_W = tau_E = -13/h
+TAU_N = -1.0            # tau_S = tau_N
+BETA = 1.0
+# Dirichlet SAT coefficients on the three columns next to a Dirichlet side,
+# after H-tilde scaling: (h*tau + 1.5*beta, -2*beta, 0.5*beta).
+DIRICHLET_COEF = (TAU_D_TIMES_H + 1.5 * BETA, -2.0 * BETA, 0.5 * BETA)
+
+
+# --------------------------------------------------------------------------
+# 1D SBP operators, p = 2
+# --------------------------------------------------------------------------
+def sbp_1d(n: int):
+    """1D second-order diagonal-norm SBP pieces on n points of [0, 1].
+
+    Follows ``diagonal_sbp.jl:56-61,112-146`` (D1 norm H: bhinv = [2] so
+    H = h*diag(1/2, 1, ..., 1, 1/2)) and ``diagonal_sbp.jl:191-197,414-452``
+    (D2 with the one-sided boundary rows equal to the interior stencil,
+    S0 = -BS/h on row 1, SN = BS/h on row n with BS = [3/2, -2, 1/2]).
+    Returns (D2, H, HI, BS) as scipy CSR matrices (BS = SN - S0).
+    """
+    if n < 3:
+        raise ValueError("SBP p=2 operator needs n >= 3")
+    h = 1.0 / (n - 1)
+    rows, cols, vals = [], [], []
+    for r in range(n):
+        if r == 0:
+            c = (0, 1, 2)
+        elif r == n - 1:
+            c = (n - 1, n - 2, n - 3)
+        else:
+            c = (r - 1, r, r + 1)
+        w = (1.0, -2.0, 1.0) if r in (0, n - 1) else (1.0, -2.0, 1.0)
+        rows += [r, r, r]
+        cols += list(c)
+        vals += [v / h**2 for v in w]
+    D2 = sp.csr_matrix((vals, (rows, cols)), shape=(n, n))
+    hv = np.ones(n)
+    hv[0] = hv[-1] = 0.5
+    H = sp.diags(h * hv).tocsr()
+    HI = sp.diags(1.0 / (h * hv)).tocsr()
+    bs = np.array([1.5, -2.0, 0.5]) / h
+    S0 = sp.csr_matrix((-bs, ([0, 0, 0], [0, 1, 2])), shape=(n, n))
+    SN = sp.csr_matrix((bs, ([n - 1] * 3, [n - 1, n - 2, n - 3])), shape=(n, n))
+    BS = (SN - S0).tocsr()
+    return D2, H, HI, BS
+
+
+def _e(k: int, n: int):
+    return sp.csr_matrix(([1.0], ([k], [0])), shape=(n, 1))
+
+
+@dataclass
+class Assembled:
+    """Result of :func:`assemble` (``Assembling_matrix`` restated)."""
+    n: int
+    A: sp.csr_matrix            # SPD, = -H~ (D2 + SAT)
+    H_tilde: sp.csr_matrix
+    sat_r: dict                 # side -> n^2 x n sparse map of boundary data
+    h: float = field(init=False)
+
+    def __post_init__(self):
+        self.h = 1.0 / (self.n - 1)
+
+    def rhs(self, f_ref: np.ndarray, g: dict) -> np.ndarray:
+        """b = -H~ (f_ref + sum_side SAT_side_r g_side)  (``:182-185``).
+
+        ``f_ref`` is the D2-convention source (Delta u = f_ref), flat.
+        ``g`` maps 'W','E','S','N' to length-n boundary vectors.
+        """
+        acc = np.asarray(f_ref, dtype=np.float64).ravel().copy()
+        for side in ("W", "E", "S", "N"):
+            acc += self.sat_r[side] @ np.asarray(g[side], dtype=np.float64)
+        return -(self.H_tilde @ acc)
+
+
+def assemble(n: int) -> Assembled:
+    """Restates ``Operators_2d`` + ``Assembling_matrix``
+    (``level_2_multigrid_new.jl:48-188``) for N_x = N_y = n - 1 intervals.
+
+    kron(X, I) acts on the slow index j, kron(I, X) on the fast index i.
+    """
+    D2x, H1x, HIx, BSx = sbp_1d(n)
+    D2y, H1y, HIy, BSy = D2x, H1x, HIx, BSx
+    I = sp.identity(n, format="csr")
+    e1 = _e(0, n)
+    eN = _e(n - 1, n)
+    E1 = sp.diags(e1.toarray().ravel()).tocsr()
+    EN = sp.diags(eN.toarray().ravel()).tocsr()
+
+    e_E = sp.kron(eN, I).tocsr()
+    e_W = sp.kron(e1, I).tocsr()
+    e_S = sp.kron(I, e1).tocsr()
+    e_N = sp.kron(I, eN).tocsr()
+    E_E = sp.kron(EN, I).tocsr()
+    E_W = sp.kron(E1, I).tocsr()
+    E_S = sp.kron(I, E1).tocsr()
+    E_N = sp.kron(I, EN).tocsr()
+
+    D2 = (sp.kron(D2x, I) + sp.kron(I, D2y)).tocsr()
+    HI_x = sp.kron(HIx, I).tocsr()
+    HI_y = sp.kron(I, HIy).tocsr()
+    BS_x = sp.kron(BSx, I).tocsr()
+    BS_y = sp.kron(I, BSy).tocsr()
+    H_tilde = sp.kron(H1x, H1y).tocsr()
+
+    h = 1.0 / (n - 1)
+    tau_E = tau_W = TAU_D_TIMES_H / h
+    tau_N = tau_S = TAU_N
+    beta = BETA
+
+    SAT_W = tau_W * HI_x @ E_W + beta * HI_x @ BS_x.T @ E_W
+    SAT_E = tau_E * HI_x @ E_E + beta * HI_x @ BS_x.T @ E_E
+    SAT_S = tau_S * HI_y @ E_S @ BS_y
+    SAT_N = tau_N * HI_y @ E_N @ BS_y
+
+    sat_r = {
+        "W": (tau_W * HI_x @ E_W @ e_W + beta * HI_x @ BS_x.T @ E_W @ e_W).tocsr(),
+        "E": (tau_E * HI_x @ E_E @ e_E + beta * HI_x @ BS_x.T @ E_E @ e_E).tocsr(),
+        "S": (tau_S * HI_y @ E_S @ e_S).tocsr(),
+        "N": (tau_N * HI_y @ E_N @ e_N).tocsr(),
+    }
+    A = D2 + SAT_W + SAT_E + SAT_S + SAT_N
+    A = (-(H_tilde @ A)).tocsr()
+    A.eliminate_zeros()
+    A.sort_indices()
+    return Assembled(n=n, A=A, H_tilde=H_tilde, sat_r=sat_r)
+
+
+# --------------------------------------------------------------------------
+# Manufactured problems
+# --------------------------------------------------------------------------
+def grid(n: int) -> np.ndarray:
+    return np.linspace(0.0, 1.0, n)
+
+
+def manufactured(n: int, kind: str = "reference"):
+    """Return (f_ref, g, u_exact) on n x n points, all flat (i fast).
+
+    ``kind='reference'``: u = sin(pi(x+y)), the reference's own problem
+    (``level_2_multigrid_new.jl:36-38, 169-182``).
+    ``kind='baseline'``: u = sin(pi x) cos(pi y) with -Delta u = f, mapped
+    on the reference's sides (Dirichlet at y = 0, 1 = j sides, Neumann at
+    x = 0, 1 = i sides; S/N data are the outward normal derivatives).
+    f_ref is in the reference's D2 convention (Delta u = f_ref).
+    """
+    x = grid(n)
+    X = x[None, :]   # varies along i (axis 1)
+    Y = x[:, None]   # varies along j (axis 0)
+    pi = math.pi
+    if kind == "reference":
+        U = np.sin(pi * X + pi * Y)
+        F = -2 * pi**2 * U
+        g = {"W": np.sin(pi * x), "E": -np.sin(pi * x),
+             "S": -pi * np.cos(pi * x), "N": pi * np.cos(pi * x + pi)}
+    elif kind == "baseline":
+        U = np.sin(pi * X) * np.cos(pi * Y)
+        F = -2 * pi**2 * U
+        g = {"W": np.sin(pi * x),                 # u(x, 0)
+             "E": -np.sin(pi * x),                # u(x, 1)
+             "S": -pi * np.cos(pi * x),           # -u_x(0, y)
+             "N": pi * math.cos(pi) * np.cos(pi * x)}  # u_x(1, y)
+    else:
+        raise ValueError(kind)
+    return F.ravel(), g, U.ravel()
+
+
+def h_error(asm: Assembled, x: np.ndarray, u: np.ndarray) -> float:
+    """sqrt((x-u)' H~ (x-u))  (``matrix_free_mg_cg.jl:464``)."""
+    d = np.asarray(x).ravel() - np.asarray(u).ravel()
+    return float(math.sqrt(d @ (asm.H_tilde @ d)))
+
+
+# --------------------------------------------------------------------------
+# Matrix-free -A (split_matrix_free.jl:444-486 with the SBP_* kernels)
+# --------------------------------------------------------------------------
+def neg_A_matrix_free(u: np.ndarray, n: int | None = None) -> np.ndarray:
+    """The reference's ``matrix_free_A_full_GPU`` output, odata = -A u.
+
+    Written from the per-kernel formulas: interior 5-point stencil
+    (``D2_split_naive_v2``, :32-49), Neumann rows with one-sided D2 and the
+    alpha3 = -1 penalty halved (/2) or quartered at corners (/4)
+    (``SBP_N!``/``SBP_S!``, :324-388), Dirichlet columns with one-sided D2,
+    1.5*beta*u + h*alpha1*u at the boundary point and -2u, +0.5u spread into
+    the next two columns, halved in the corner rows (``SBP_W!``/``SBP_E!``,
+    :391-429), summed as in :478-483.
+    """
+    flat = np.asarray(u, dtype=np.float64)
+    if n is None:
+        n = int(round(math.sqrt(flat.size)))
+    U = flat.reshape(n, n)          # U[j, i]
+    out = np.zeros_like(U)
+    # interior
+    out[1:-1, 1:-1] = (U[1:-1, :-2] + U[1:-1, 2:] + U[:-2, 1:-1] + U[2:, 1:-1]
+                       - 4 * U[1:-1, 1:-1])
+    a1h = TAU_D_TIMES_H
+    a3 = TAU_N
+    b = BETA
+    # --- W / E temporaries (SBP_W!, SBP_E!), interior rows i = 1..n-2 ---
+    W = np.zeros((3, n))  # W[c, i] for columns j = c
+    E = np.zeros((3, n))  # E[c, i] for columns j = n-3+c
+    ii = slice(1, n - 1)
+    W[0, ii] = (U[0, :-2] - 2 * U[0, 1:-1] + U[0, 2:]
+                + U[0, 1:-1] - 2 * U[1, 1:-1] + U[2, 1:-1]
+                + 2 * b * 1.5 * U[0, 1:-1] + 2 * a1h * U[0, 1:-1]) / 2
+    W[1, ii] = 2 * b * (-1 * U[0, 1:-1])
+    W[2, ii] = 0.5 * b * U[0, 1:-1]
+    E[2, ii] = (U[-1, :-2] - 2 * U[-1, 1:-1] + U[-1, 2:]
+                + U[-1, 1:-1] - 2 * U[-2, 1:-1] + U[-3, 1:-1]
+                + 2 * b * 1.5 * U[-1, 1:-1] + 2 * a1h * U[-1, 1:-1]) / 2
+    E[1, ii] = 2 * b * (-1 * U[-1, 1:-1])
+    E[0, ii] = 0.5 * b * U[-1, 1:-1]
+    for i in (0, n - 1):
+        W[0, i] = (2 * b * 1.5 * U[0, i] + 2 * a1h * U[0, i]) / 4
+        W[1, i] = (2 * b * (-1 * U[0, i])) / 2
+        W[2, i] = (0.5 * b * U[0, i]) / 2
+        E[2, i] = (2 * b * 1.5 * U[-1, i] + 2 * a1h * U[-1, i]) / 4
+        E[1, i] = (2 * b * (-1 * U[-1, i])) / 2
+        E[0, i] = (0.5 * b * U[-1, i]) / 2
+    # --- N / S temporaries (SBP_N!, SBP_S!): rows i = 0 and i = n-1 ---
+    Nrow = np.zeros(n)
+    Srow = np.zeros(n)
+
+    def nrow(j, edge):
+        # i = 0 row; col j; one-sided in i, interior or one-sided in j
+        li = U[j, 0] - 2 * U[j, 1] + U[j, 2]
+        pen = 2 * a3 * (1.5 * U[j, 0] - 2 * U[j, 1] + 0.5 * U[j, 2])
+        if j == 0:
+            lj = U[0, 0] - 2 * U[1, 0] + U[2, 0]
+        elif j == n - 1:
+            lj = U[n - 1, 0] - 2 * U[n - 2, 0] + U[n - 3, 0]
+        else:
+            lj = U[j - 1, 0] - 2 * U[j, 0] + U[j + 1, 0]
+        return (li + lj + pen) / (4 if edge else 2)
+
+    def srow(j, edge):
+        li = U[j, -1] - 2 * U[j, -2] + U[j, -3]
+        pen = 2 * a3 * (1.5 * U[j, -1] - 2 * U[j, -2] + 0.5 * U[j, -3])
+        if j == 0:
+            lj = U[0, -1] - 2 * U[1, -1] + U[2, -1]
+        elif j == n - 1:
+            lj = U[n - 1, -1] - 2 * U[n - 2, -1] + U[n - 3, -1]
+        else:
+            lj = U[j - 1, -1] - 2 * U[j, -1] + U[j + 1, -1]
+        return (li + lj + pen) / (4 if edge else 2)
+
+    for j in range(n):
+        edge = j in (0, n - 1)
+        Nrow[j] = nrow(j, edge)
+        Srow[j] = srow(j, edge)
+    # merge (split_matrix_free.jl:478-483): boundary ring of `out` is zero
+    out[0:3, :] += W
+    out[n - 3:n, :] += E
+    out[:, 0] += Nrow
+    out[:, n - 1] += Srow
+    return out.ravel()
+
+
+def neg_A_coefficients(n: int):
+    """Per-point description of -A used by the GPU kernels, restated from
+    the assembled operator: -A u = wi*wj*(Li u + Lj u) + wj*Neumann(i)
+    + wi*Dirichlet(j).  Returned for documentation/tests: diag(A)."""
+    wi = np.ones(n)
+    wi[0] = wi[-1] = 0.5
+    ci = np.full(n, -2.0)
+    ci[0] = ci[-1] = 1.0
+    neu = np.zeros(n)
+    neu[0] = neu[-1] = 1.5 * TAU_N
+    dir_ = np.zeros(n)
+    dir_[0] = dir_[-1] = DIRICHLET_COEF[0]
+    WJ = wi[:, None]
+    WI = wi[None, :]
+    diag_negA = (WI * WJ * (ci[None, :] + ci[:, None]) + WJ * neu[None, :]
+                 + WI * dir_[:, None])
+    return -diag_negA.ravel()
+
+
+# --------------------------------------------------------------------------
+# Transfer operators (level_2_multigrid_new.jl:190-246,
+# matrix_free_mg_cg.jl:17-38, 80-94)
+# --------------------------------------------------------------------------
+def prolongation_matrix(nc: int) -> sp.csr_matrix:
+    """1D bilinear prolongation, nc -> 2nc-1 (``:190-203``)."""
+    nf = 2 * nc - 1
+    rows, cols, vals = [], [], []
+    for r in range(nf):
+        if r % 2 == 0:
+            rows.append(r); cols.append(r // 2); vals.append(1.0)
+        else:
+            rows += [r, r]; cols += [r // 2, r // 2 + 1]; vals += [0.5, 0.5]
+    return sp.csr_matrix((vals, (rows, cols)), shape=(nf, nc))
+
+
+def restriction_matrix(nf: int) -> sp.csr_matrix:
+    """1D SBP-preserving restriction (``restriction_matrix`` :205-218):
+    boundary rows (1/2, 1/2), interior (1/4, 1/2, 1/4)."""
+    nc = (nf + 1) // 2
+    R = sp.lil_matrix((nc, nf))
+    R[0, 0] = 0.5; R[0, 1] = 0.5
+    R[nc - 1, nf - 2] = 0.5; R[nc - 1, nf - 1] = 0.5
+    for c in range(1, nc - 1):
+        R[c, 2 * c - 1] = 0.25; R[c, 2 * c] = 0.5; R[c, 2 * c + 1] = 0.25
+    return R.tocsr()
+
+
+def restriction_matrix_normal(nf: int) -> sp.csr_matrix:
+    """1D full weighting with zero padding (``restriction_matrix_normal``
+    :220-233): boundary rows (1/2, 1/4), interior (1/4, 1/2, 1/4)."""
+    nc = (nf + 1) // 2
+    R = sp.lil_matrix((nc, nf))
+    R[0, 0] = 0.5; R[0, 1] = 0.25
+    R[nc - 1, nf - 2] = 0.25; R[nc - 1, nf - 1] = 0.5
+    for c in range(1, nc - 1):
+        R[c, 2 * c - 1] = 0.25; R[c, 2 * c] = 0.5; R[c, 2 * c + 1] = 0.25
+    return R.tocsr()
+
+
+def prolongation_2d(nc: int) -> sp.csr_matrix:
+    P = prolongation_matrix(nc)
+    return sp.kron(P, P).tocsr()
+
+
+RESTRICT_KINDS = ("normal", "sbp", "galerkin")
+
+
+def restriction_2d(nf: int, kind: str = "normal") -> sp.csr_matrix:
+    """2D restriction.  'normal' is the reference's ``restriction_2d``
+    (:241-246, kron of ``restriction_matrix_normal``); 'sbp' is the kron of
+    the SBP-preserving ``restriction_matrix``; 'galerkin' is P^T, which is
+    the SBP-compatible restriction H~_2h^-1 P^T H~_h re-expressed for the
+    H~-scaled residuals this operator produces (f_2h = H~_2h R_sbp H~_h^-1 r).
+    """
+    if kind == "normal":
+        R = restriction_matrix_normal(nf)
+        return sp.kron(R, R).tocsr()
+    if kind == "sbp":
+        R = restriction_matrix(nf)
+        return sp.kron(R, R).tocsr()
+    if kind == "galerkin":
+        return prolongation_2d((nf + 1) // 2).T.tocsr()
+    raise ValueError(kind)
+
+
+def restriction_mf(r: np.ndarray, nf: int) -> np.ndarray:
+    """Matrix-free full weighting on a zero-padded copy
+    (``matrix_free_restriction_2d`` :80-94)."""
+    R = np.asarray(r, dtype=np.float64).reshape(nf, nf)
+    P = np.zeros((nf + 2, nf + 2))
+    P[1:-1, 1:-1] = R
+    nc = (nf + 1) // 2
+    c = np.arange(nc)
+    J, I = np.meshgrid(2 * c + 1, 2 * c + 1, indexing="ij")
+    out = (4 * P[J, I] + 2 * (P[J, I - 1] + P[J, I + 1] + P[J - 1, I] + P[J + 1, I])
+           + P[J - 1, I - 1] + P[J - 1, I + 1] + P[J + 1, I - 1] + P[J + 1, I + 1]) / 16
+    return out.ravel()
+
+
+def prolongation_mf(e: np.ndarray, nc: int) -> np.ndarray:
+    """Matrix-free bilinear prolongation (``matrix_free_prolongation_2d``
+    :17-38): injection at even points, 2- and 4-point averages elsewhere."""
+    E = np.asarray(e, dtype=np.float64).reshape(nc, nc)
+    nf = 2 * nc - 1
+    out = np.zeros((nf, nf))
+    out[::2, ::2] = E
+    out[::2, 1::2] = (E[:, :-1] + E[:, 1:]) / 2
+    out[1::2, ::2] = (E[:-1, :] + E[1:, :]) / 2
+    out[1::2, 1::2] = (E[:-1, :-1] + E[1:, :-1] + E[:-1, 1:] + E[1:, 1:]) / 4
+    return out.ravel()
+
+
+# --------------------------------------------------------------------------
+# Smoothers (level_2_multigrid_new.jl:335-350, matrix_free_mg_cg.jl:134-140)
+# --------------------------------------------------------------------------
+def richardson(x, A, b, maxiter=3, omega=0.15):
+    """``modified_richardson!``: x <- x + omega (b - A x)."""
+    x = np.array(x, dtype=np.float64, copy=True)
+    for _ in range(maxiter):
+        x = x + omega * (b - A @ x)
+    return x
+
+
+def jacobi(x, A, b, maxiter=3, omega=2.0 / 3.0, diag=None):
+    """``jacobi_brittany!``: x <- omega D^-1 (b - (A - D) x) + (1-omega) x,
+    i.e. x + omega D^-1 (b - A x)."""
+    x = np.array(x, dtype=np.float64, copy=True)
+    d = A.diagonal() if diag is None else diag
+    for _ in range(maxiter):
+        x = x + omega * (b - A @ x) / d
+    return x
+
+
+# --------------------------------------------------------------------------
+# Multigrid hierarchy, V-cycle, MGCG, CG
+# --------------------------------------------------------------------------
+@dataclass
+class MGOptions:
+    """Options mirrored by the C-ABI ``sbp_options`` struct."""
+    smoother: str = "jacobi"        # 'jacobi' (omega=2/3) or 'richardson' (0.15)
+    omega: float | None = None
+    nu_pre: int = 3
+    nu_post: int = 3
+    restriction: str = "galerkin"   # 'normal' | 'sbp' | 'galerkin'
+    coarse_n: int = 65              # size at which the direct solve happens
+
+    def w(self):
+        if self.omega is not None:
+            return self.omega
+        return 2.0 / 3.0 if self.smoother == "jacobi" else 0.15
+
+    @staticmethod
+    def reference_two_level(n: int) -> "MGOptions":
+        """The reference's GPU MGCG: two levels, Richardson 0.15, nu = 3,
+        full-weighting 'normal' restriction, exact coarse solve at (n+1)/2
+        (``matrix_free_mg_cg.jl:143-176, 281-324``)."""
+        return MGOptions(smoother="richardson", omega=0.15, nu_pre=3, nu_post=3,
+                         restriction="normal", coarse_n=(n + 1) // 2)
+
+
+class Hierarchy:
+    """Levels n, (n+1)/2, ... down to ``coarse_n``; each level re-discretised
+    with :func:`assemble` like ``Assembling_matrix(level-1)``
+    (``matrix_free_mg_cg.jl:455``), coarse level solved by a sparse LU
+    (``:460``, ``A_2h \\ f`` at :166)."""
+
+    def __init__(self, n: int, opts: MGOptions):
+        self.opts = opts
+        self.ns = [n]
+        while self.ns[-1] > opts.coarse_n:
+            nn = (self.ns[-1] + 1) // 2
+            if nn < 3:
+                break
+            self.ns.append(nn)
+        if self.ns[-1] != opts.coarse_n and len(self.ns) > 1:
+            raise ValueError(f"n={n} does not coarsen to coarse_n={opts.coarse_n}")
+        self.asm = [assemble(m) for m in self.ns]
+        self.A = [a.A for a in self.asm]
+        self.diag = [A.diagonal() for A in self.A]
+        self.R = [restriction_2d(m, opts.restriction) for m in self.ns[:-1]]
+        self.P = [prolongation_2d(m) for m in self.ns[1:]]
+        self.lu = spla.splu(self.A[-1].tocsc())
+
+    def smooth(self, l, v, b, iters):
+        o = self.opts
+        if o.smoother == "jacobi":
+            return jacobi(v, self.A[l], b, iters, o.w(), self.diag[l])
+        return richardson(v, self.A[l], b, iters, o.w())
+
+    def vcycle(self, b, l=0):
+        """One V-cycle from v = 0 (``Two_level_multigrid`` :358-382 for two
+        levels; recursive here)."""
+        if l == len(self.ns) - 1:
+            return self.lu.solve(np.asarray(b, dtype=np.float64))
+        v = np.zeros_like(b)
+        v = self.smooth(l, v, b, self.opts.nu_pre)
+        r = b - self.A[l] @ v
+        f = self.R[l] @ r
+        e = self.vcycle(f, l + 1)
+        v = v + self.P[l] @ e
+        v = self.smooth(l, v, b, self.opts.nu_post)
+        return v
+
+
+def mgcg(hier: Hierarchy, b, x=None, abstol=None, reltol=None, maxiter=None):
+    """``mg_preconditioned_CG`` (``level_2_multigrid_new.jl:480-524``),
+    with the V-cycle of :class:`Hierarchy` as preconditioner.  Stops when
+    ||r||_2 < abstol (abstol = reltol*||b - A x0|| if reltol given).
+    Returns (x, iters, norms)."""
+    A = hier.A[0]
+    b = np.asarray(b, dtype=np.float64)
+    x = np.zeros_like(b) if x is None else np.array(x, dtype=np.float64)
+    r = b - A @ x
+    if abstol is None:
+        reltol = math.sqrt(np.finfo(float).eps) if reltol is None else reltol
+        abstol = reltol * np.linalg.norm(r)
+    maxiter = b.size if maxiter is None else maxiter
+    z = hier.vcycle(r)
+    p = z.copy()
+    rz = r @ z
+    norms = [float(np.linalg.norm(r))]
+    it = 0
+    for _ in range(maxiter):
+        it += 1
+        Ap = A @ p
+        alpha = rz / (p @ Ap)
+        x = x + alpha * p
+        r = r - alpha * Ap
+        rs = r @ r
+        norms.append(float(math.sqrt(rs)))
+        if math.sqrt(rs) < abstol:
+            break
+        z = hier.vcycle(r)
+        rz_new = r @ z
+        beta = rz_new / rz
+        p = z + beta * p
+        rz = rz_new
+    return x, it, norms
+
+
+def cg(A, b, x=None, abstol=None, reltol=None, maxiter=None):
+    """``CG_CPU`` (``level_2_multigrid_new.jl:258-291``): textbook CG,
+    stop when ||r|| < abstol.  Returns (x, iters, norms)."""
+    b = np.asarray(b, dtype=np.float64)
+    x = np.zeros_like(b) if x is None else np.array(x, dtype=np.float64)
+    r = b - A @ x
+    if abstol is None:
+        reltol = math.sqrt(np.finfo(float).eps) if reltol is None else reltol
+        abstol = reltol * np.linalg.norm(r)
+    maxiter = b.size if maxiter is None else maxiter
+    p = r.copy()
+    rs = r @ r
+    norms = [float(math.sqrt(rs))]
+    it = 0
+    for _ in range(maxiter):
+        it += 1
+        Ap = A @ p
+        alpha = rs / (p @ Ap)
+        x = x + alpha * p
+        r = r - alpha * Ap
+        rsn = r @ r
+        norms.append(float(math.sqrt(rsn)))
+        if math.sqrt(rsn) < abstol:
+            break
+        p = r + (rsn / rs) * p
+        rs = rsn
+    return x, it, norms

@@ -1,0 +1,26 @@
+"""GB300-native matrix-free SBP-SAT Poisson solver (libsbpmg) with the
+reference's entry points: matrix_free_A_full_GPU, CG_full_GPU,
+CG_Matrix_Free_GPU_v2, matrix_free_MGCG, matrix_free_Two_level_multigrid,
+matrix_free_richardson, matrix_free_restriction_2d_GPU,
+matrix_free_prolongation_2d_GPU.
+"""
+from . import _lib
+from ._lib import SbpError
+from .matrix_free import (CG_Matrix_Free_GPU_v2, CG_full_GPU, jacobi, matrix_free_A_full_GPU,
+                          matrix_free_A_full_GPU_f32, matrix_free_MGCG,
+                          matrix_free_prolongation_2d_GPU, matrix_free_restriction_2d_GPU,
+                          matrix_free_richardson, matrix_free_Two_level_multigrid)
+from .solver import Options, SolveResult, Solver, default_options, reference_two_level_options
+
+__all__ = [
+    "CG_Matrix_Free_GPU_v2", "CG_full_GPU", "jacobi", "matrix_free_A_full_GPU",
+    "matrix_free_A_full_GPU_f32", "matrix_free_MGCG", "matrix_free_prolongation_2d_GPU",
+    "matrix_free_restriction_2d_GPU", "matrix_free_richardson",
+    "matrix_free_Two_level_multigrid", "Options", "SolveResult", "Solver", "default_options",
+    "reference_two_level_options", "SbpError", "load_library",
+]
+
+
+def load_library():
+    """Load libsbpmg.so; raises ImportError if it has not been built."""
+    return _lib.load()

@@ -1,0 +1,685 @@
+// C ABI of libsbpmg: solver handles (multigrid hierarchy, workspace, CUDA
+// graphs of one Krylov iteration) and the single-grid entry points.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/sbpmg.h"
+#include "sbp_coarse.h"
+#include "sbp_launch.h"
+
+using namespace sbp;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail_cuda(cudaError_t e, const char* what) {
+  g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+  return SBP_ERR_CUDA;
+}
+
+#define SBP_CUDA(call)                                     \
+  do {                                                     \
+    cudaError_t _e = (call);                               \
+    if (_e != cudaSuccess) return fail_cuda(_e, #call);    \
+  } while (0)
+
+bool valid_mg_n(int n) {
+  if (n < 3) return false;
+  const int m = n - 1;
+  return (m & (m - 1)) == 0;
+}
+
+template <typename T>
+Grid<T> grid(void* p, int ld) {
+  return Grid<T>{static_cast<T*>(p), ld};
+}
+template <typename T>
+Grid<const T> cgrid(const void* p, int ld) {
+  return Grid<const T>{static_cast<const T*>(p), ld};
+}
+
+struct Level {
+  int n = 0;
+  void* b = nullptr;        // right-hand side (level 0: the solver's r or r_lo)
+  void* v[2] = {nullptr, nullptr};
+  int out = 0;              // buffer holding the V-cycle result
+  bool own_b = false;
+};
+
+}  // namespace
+
+struct sbp_solver {
+  int n = 0;
+  int device = 0;
+  bool mg = false;
+  sbp_options opts{};
+  size_t esize = 8;                 // element size of the V-cycle levels
+  std::vector<Level> levels;
+  double* Ainv = nullptr;
+  // Krylov vectors (FP64, ld = n)
+  double* r = nullptr;
+  double* p[2] = {nullptr, nullptr};
+  double* Ap = nullptr;
+  float* r_lo = nullptr;            // FP32 copy of r (mixed precision)
+  SolveState* st = nullptr;
+  SolveState* st_host = nullptr;    // pinned, 2 slots
+  double* norms = nullptr;
+  int norms_cap = 0;
+  ReduceBuf rb{nullptr, nullptr};
+  long long dev_bytes = 0;
+  std::vector<void*> allocs;
+  cudaStream_t cap = nullptr;       // private stream for graph capture
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  // cached iteration graphs: [kind][parity]; kind 0 = MGCG, 1 = CG
+  cudaGraphExec_t iter_exec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  const void* iter_key_x[2] = {nullptr, nullptr};
+  int iter_key_sign[2] = {0, 0};
+  int iter_key_maxiter[2] = {0, 0};
+  // kernel launches: per captured iteration graph, and of the last solve
+  long long launches_per_iter[2] = {0, 0};
+  long long last_launches = 0;
+  long long counting = 0;          // launches enqueued since the counter reset
+};
+
+namespace {
+
+int dalloc(sbp_solver* s, void** p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    g_last_error = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+    return SBP_ERR_NOMEM;
+  }
+  s->allocs.push_back(*p);
+  s->dev_bytes += (long long)bytes;
+  return SBP_OK;
+}
+
+void destroy_graphs(sbp_solver* s) {
+  for (auto& k : s->iter_exec)
+    for (auto& g : k)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
+  s->iter_key_x[0] = s->iter_key_x[1] = nullptr;
+}
+
+// ---------------------------------------------------------------------------
+// V-cycle schedule.  Level l < last:
+//   pre:  F = first sweep from zero, fused with the second sweep when
+//         nu_pre >= 2; remaining sweeps ping-pong between v[0] and v[1];
+//   f_{l+1} = R (b - A v)            (fused residual + restriction)
+//   recurse
+//   post: first pass reads v + P e (prolongation folded into the sweep);
+//         remaining sweeps ping-pong.  On level 0 the last pass also reduces
+//         b.z into the Krylov state when `dot` is set.
+// Last level: v = Ainv b (dense FP64 GEMV).
+// ---------------------------------------------------------------------------
+template <typename T>
+cudaError_t enqueue_vcycle(sbp_solver* s, size_t l, bool dot, SolveState* st, cudaStream_t q) {
+  Level& L = s->levels[l];
+  const sbp_options& o = s->opts;
+  const int n = L.n;
+  const double om = o.omega;
+  const int sm = o.smoother;
+  cudaError_t e;
+  Grid<const T> b = cgrid<T>(L.b, n);
+  if (l + 1 == s->levels.size()) {
+    L.out = 0;
+    e = launch_coarse_gemv<T>(s->Ainv, b, grid<T>(L.v[0], n), n, st, q);
+    if (e != cudaSuccess) return e;
+    if (dot && l == 0) {
+      // single-level hierarchy: still reduce b.z for the Krylov state
+      e = launch_smooth<T>(kFieldPlain, kEpiStore, cgrid<T>(L.v[0], n), Grid<const T>{nullptr, 0},
+                           b, grid<T>(L.v[1], n), n, sm, om, 1, st, s->rb, q);
+      L.out = 1;
+    }
+    return e;
+  }
+  int cur;
+  int k;
+  if (o.nu_pre >= 2) {
+    e = launch_smooth<T>(kFieldZero, kEpiSweep, Grid<const T>{nullptr, 0},
+                         Grid<const T>{nullptr, 0}, b, grid<T>(L.v[0], n), n, sm, om, 0, st,
+                         s->rb, q);
+    k = 2;
+  } else {
+    e = launch_smooth<T>(kFieldZero, kEpiStore, Grid<const T>{nullptr, 0},
+                         Grid<const T>{nullptr, 0}, b, grid<T>(L.v[0], n), n, sm, om, 0, st,
+                         s->rb, q);
+    k = 1;
+  }
+  if (e != cudaSuccess) return e;
+  cur = 0;
+  for (; k < o.nu_pre; ++k) {
+    e = launch_smooth<T>(kFieldPlain, kEpiSweep, cgrid<T>(L.v[cur], n), Grid<const T>{nullptr, 0},
+                         b, grid<T>(L.v[1 - cur], n), n, sm, om, 0, st, s->rb, q);
+    if (e != cudaSuccess) return e;
+    cur = 1 - cur;
+  }
+  Level& C = s->levels[l + 1];
+  e = launch_resrestrict<T>(cgrid<T>(L.v[cur], n), b, grid<T>(C.b, C.n), n, o.restriction, st, q);
+  if (e != cudaSuccess) return e;
+  e = enqueue_vcycle<T>(s, l + 1, false, st, q);
+  if (e != cudaSuccess) return e;
+  Grid<const T> ec = cgrid<T>(C.v[C.out], C.n);
+  const int npost = std::max(1, o.nu_post);
+  for (int pass = 0; pass < npost; ++pass) {
+    const bool last = (pass == npost - 1);
+    const int field = (pass == 0) ? kFieldProlong : kFieldPlain;
+    const int epi = (o.nu_post == 0) ? kEpiStore : kEpiSweep;
+    e = launch_smooth<T>(field, epi, cgrid<T>(L.v[cur], n), ec, b, grid<T>(L.v[1 - cur], n), n, sm,
+                         om, (dot && last) ? 1 : 0, st, s->rb, q);
+    if (e != cudaSuccess) return e;
+    cur = 1 - cur;
+  }
+  L.out = cur;
+  return cudaSuccess;
+}
+
+// Kernel launches of one V-cycle (mirrors enqueue_vcycle).
+long long vcycle_launches(const sbp_solver* s, bool dot) {
+  const sbp_options& o = s->opts;
+  long long c = 0;
+  const size_t nl = s->levels.size();
+  for (size_t l = 0; l + 1 < nl; ++l) {
+    c += (o.nu_pre >= 2) ? 1 + (o.nu_pre - 2) : 1;
+    c += 1;                               // residual + restriction
+    c += std::max(1, o.nu_post);          // prolongation + post sweeps
+  }
+  c += 1;                                 // coarse GEMV
+  if (dot && nl == 1) c += 1;
+  return c;
+}
+
+cudaError_t enqueue_vcycle_any(sbp_solver* s, bool dot, SolveState* st, cudaStream_t q) {
+  if (s->opts.precision == SBP_PREC_MIXED) return enqueue_vcycle<float>(s, 0, dot, st, q);
+  return enqueue_vcycle<double>(s, 0, dot, st, q);
+}
+
+// z pointer of the V-cycle output on level 0 (valid after a schedule has
+// been enqueued once: the schedule is static).
+const void* vcycle_out(sbp_solver* s) {
+  Level& L = s->levels[0];
+  return L.v[L.out];
+}
+
+// One Krylov iteration: direction + operator + alpha, update + convergence,
+// then (MGCG) the V-cycle with the r.z / beta reduction.
+cudaError_t enqueue_iteration(sbp_solver* s, int kind, int parity, double* x, int sign,
+                              cudaStream_t q) {
+  const int n = s->n;
+  double* pold = s->p[parity];
+  double* pnew = s->p[1 - parity];
+  cudaError_t e;
+  const bool mixed = (kind == 0 && s->opts.precision == SBP_PREC_MIXED);
+  if (kind == 0) {
+    if (mixed)
+      e = launch_cg_dir<double, float>(cgrid<float>(vcycle_out(s), n), cgrid<double>(pold, n),
+                                       grid<double>(pnew, n), grid<double>(s->Ap, n), n, +1,
+                                       s->st, s->rb, q);
+    else
+      e = launch_cg_dir<double, double>(cgrid<double>(vcycle_out(s), n), cgrid<double>(pold, n),
+                                        grid<double>(pnew, n), grid<double>(s->Ap, n), n, +1,
+                                        s->st, s->rb, q);
+  } else {
+    e = launch_cg_dir<double, double>(cgrid<double>(s->r, n), cgrid<double>(pold, n),
+                                      grid<double>(pnew, n), grid<double>(s->Ap, n), n, sign,
+                                      s->st, s->rb, q);
+  }
+  if (e != cudaSuccess) return e;
+  e = launch_cg_update<double>(grid<double>(x, n), grid<double>(s->r, n), cgrid<double>(pnew, n),
+                               cgrid<double>(s->Ap, n),
+                               Grid<float>{mixed ? s->r_lo : nullptr, n}, n, kind == 1 ? 1 : 0,
+                               s->st, s->norms, s->rb, q);
+  if (e != cudaSuccess) return e;
+  if (kind == 0) e = enqueue_vcycle_any(s, true, s->st, q);
+  return e;
+}
+
+int ensure_norms(sbp_solver* s, int maxiter) {
+  if (maxiter + 1 <= s->norms_cap) return SBP_OK;
+  // grow (old buffer stays in allocs until destroy; norms are small)
+  void* p = nullptr;
+  const int cap = std::max(maxiter + 1, 2 * s->norms_cap);
+  int rc = dalloc(s, &p, (size_t)cap * sizeof(double));
+  if (rc) return rc;
+  s->norms = static_cast<double*>(p);
+  s->norms_cap = cap;
+  destroy_graphs(s);  // graphs captured the old pointer
+  return SBP_OK;
+}
+
+int capture_iteration(sbp_solver* s, int kind, double* x, int sign) {
+  for (int par = 0; par < 2; ++par) {
+    cudaGraph_t g = nullptr;
+    SBP_CUDA(cudaStreamBeginCapture(s->cap, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = enqueue_iteration(s, kind, par, x, sign, s->cap);
+    cudaError_t e2 = cudaStreamEndCapture(s->cap, &g);
+    if (e != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return fail_cuda(e, "enqueue_iteration (capture)");
+    }
+    if (e2 != cudaSuccess) return fail_cuda(e2, "cudaStreamEndCapture");
+    if (s->iter_exec[kind][par]) cudaGraphExecDestroy(s->iter_exec[kind][par]);
+    s->iter_exec[kind][par] = nullptr;
+    e = cudaGraphInstantiate(&s->iter_exec[kind][par], g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail_cuda(e, "cudaGraphInstantiate");
+  }
+  s->iter_key_x[kind] = x;
+  s->iter_key_sign[kind] = sign;
+  s->launches_per_iter[kind] = 2 + (kind == 0 ? vcycle_launches(s, true) : 0);
+  return SBP_OK;
+}
+
+// Shared driver of sbp_mgcg_solve (kind 0) and sbp_cg_solve (kind 1).
+int run_krylov(sbp_solver* s, int kind, const double* b, double* x, int sign, double abstol,
+               double reltol, int maxiter, sbp_result* res, double* norms_out, int norms_cap,
+               cudaStream_t q) {
+  if (!s || !b || !x) return SBP_ERR_ARGS;
+  if (maxiter < 0) return SBP_ERR_ARGS;
+  if (kind == 0 && !s->mg) return SBP_ERR_UNSUPPORTED;
+  if (abstol <= 0.0 && reltol <= 0.0) return SBP_ERR_ARGS;
+  SBP_CUDA(cudaSetDevice(s->device));
+  int rc = ensure_norms(s, maxiter);
+  if (rc) return rc;
+  const int n = s->n;
+  const bool mixed = (kind == 0 && s->opts.precision == SBP_PREC_MIXED);
+  // set-up: state, r0 = b - sign*A*x0, z0 = M r0 and rz (MGCG)
+  SBP_CUDA(launch_state_init(s->st, maxiter, q));
+  SBP_CUDA(launch_residual<double>(cgrid<double>(x, n), cgrid<double>(b, n),
+                                   grid<double>(s->r, n), Grid<float>{mixed ? s->r_lo : nullptr, n},
+                                   n, sign, s->st, s->norms, abstol, reltol, kind == 1 ? 1 : 0,
+                                   nullptr, s->rb, q));
+  if (kind == 0) SBP_CUDA(enqueue_vcycle_any(s, true, s->st, q));
+  if (s->iter_key_x[kind] != x || s->iter_key_sign[kind] != sign || !s->iter_exec[kind][0]) {
+    rc = capture_iteration(s, kind, x, sign);
+    if (rc) return rc;
+  }
+  // Iterate: keep one iteration queued ahead of the one being checked.
+  long long launches = 2 + (kind == 0 ? vcycle_launches(s, true) : 0);
+  int k = 0;
+  bool finished = false;
+  if (maxiter == 0) finished = true;
+  while (!finished) {
+    SBP_CUDA(cudaGraphLaunch(s->iter_exec[kind][k & 1], q));
+    launches += s->launches_per_iter[kind];
+    SBP_CUDA(cudaMemcpyAsync(&s->st_host[k & 1], s->st, sizeof(SolveState),
+                             cudaMemcpyDeviceToHost, q));
+    SBP_CUDA(cudaEventRecord(s->ev[k & 1], q));
+    if (k >= 1) {
+      SBP_CUDA(cudaEventSynchronize(s->ev[(k - 1) & 1]));
+      if (s->st_host[(k - 1) & 1].done) finished = true;
+    }
+    ++k;
+    if (k > maxiter + 2) finished = true;  // safety net; kernels stop at maxiter
+  }
+  SBP_CUDA(cudaMemcpyAsync(&s->st_host[0], s->st, sizeof(SolveState), cudaMemcpyDeviceToHost, q));
+  SBP_CUDA(cudaStreamSynchronize(q));
+  const SolveState fs = s->st_host[0];
+  s->last_launches = launches;
+  const int iters = fs.iter;
+  if (norms_out && norms_cap > 0) {
+    const int cnt = std::min(norms_cap, iters + 1);
+    SBP_CUDA(cudaMemcpy(norms_out, s->norms, (size_t)cnt * sizeof(double),
+                        cudaMemcpyDeviceToHost));
+  }
+  int status;
+  if (fs.done == kDoneConverged)
+    status = SBP_OK;
+  else if (fs.done == kDoneBreakdown)
+    status = SBP_ERR_BREAKDOWN;
+  else
+    status = SBP_ERR_MAXITER;
+  if (res) {
+    res->iters = iters;
+    res->status = status;
+    res->initial_norm = std::sqrt(fs.rr0);
+    res->final_norm = std::sqrt(fs.rr);
+    res->threshold = std::sqrt(fs.thresh2);
+  }
+  return status;
+}
+
+// Stream-ordered scratch for the single-grid reducing entry points.
+struct TempReduce {
+  ReduceBuf rb{nullptr, nullptr};
+  double* out = nullptr;
+  void* base = nullptr;
+  cudaStream_t q = nullptr;
+  int alloc(int n, cudaStream_t stream) {
+    q = stream;
+    const size_t parts = (size_t)max_reduce_ctas(n);
+    const size_t bytes = parts * sizeof(double) + 2 * sizeof(double);
+    SBP_CUDA(cudaMallocAsync(&base, bytes, q));
+    rb.partials = static_cast<double*>(base);
+    out = rb.partials + parts;
+    rb.ticket = reinterpret_cast<unsigned*>(out + 1);
+    SBP_CUDA(cudaMemsetAsync(rb.ticket, 0, sizeof(unsigned), q));
+    return SBP_OK;
+  }
+  ~TempReduce() {
+    if (base) cudaFreeAsync(base, q);
+  }
+};
+
+int smooth_sweeps(double* v, double* tmp, const double* b, int n, int iters, double omega,
+                  int smoother, cudaStream_t q) {
+  if (!v || !tmp || !b || n < 3 || iters < 0) return SBP_ERR_ARGS;
+  double* bufs[2] = {v, tmp};
+  int cur = 0;
+  ReduceBuf none{nullptr, nullptr};
+  for (int k = 0; k < iters; ++k) {
+    SBP_CUDA(launch_smooth<double>(kFieldPlain, kEpiSweep, cgrid<double>(bufs[cur], n),
+                                   Grid<const double>{nullptr, 0}, cgrid<double>(b, n),
+                                   grid<double>(bufs[1 - cur], n), n, smoother, omega, 0,
+                                   nullptr, none, q));
+    cur = 1 - cur;
+  }
+  // leave the result in both buffers, as the reference's in-place loop does
+  SBP_CUDA(cudaMemcpyAsync(bufs[1 - cur], bufs[cur], (size_t)n * n * sizeof(double),
+                           cudaMemcpyDeviceToDevice, q));
+  return SBP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sbp_version(void) { return 100; }
+
+const char* sbp_last_error(void) { return g_last_error.c_str(); }
+
+int sbp_coarse_inverse_host(int nc, double* out, long long cap) {
+  if (!out || !valid_mg_n(nc) || nc > 129) return SBP_ERR_ARGS;
+  const long long N = (long long)nc * nc;
+  if (cap < N * N) return SBP_ERR_ARGS;
+  try {
+    auto X = coarse_inverse(nc);
+    std::memcpy(out, X->data(), (size_t)(N * N) * sizeof(double));
+  } catch (const std::exception& ex) {
+    g_last_error = ex.what();
+    return SBP_ERR_CUDA;
+  }
+  return SBP_OK;
+}
+
+const char* sbp_status_string(int status) {
+  switch (status) {
+    case SBP_OK: return "ok";
+    case SBP_ERR_ARGS: return "invalid argument";
+    case SBP_ERR_CUDA: return g_last_error.empty() ? "CUDA error" : g_last_error.c_str();
+    case SBP_ERR_NOMEM: return "out of memory";
+    case SBP_ERR_MAXITER: return "maximum iterations reached";
+    case SBP_ERR_BREAKDOWN: return "breakdown (p'Ap == 0 or non-finite residual)";
+    case SBP_ERR_UNSUPPORTED: return "unsupported option combination";
+    default: return "unknown status";
+  }
+}
+
+void sbp_options_default(sbp_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->smoother = SBP_SMOOTH_JACOBI;
+  o->omega = 2.0 / 3.0;
+  o->nu_pre = 3;
+  o->nu_post = 3;
+  o->restriction = SBP_RESTRICT_GALERKIN;
+  o->coarse_n = 65;
+  o->precision = SBP_PREC_FP64;
+}
+
+void sbp_options_reference_two_level(sbp_options* o, int n) {
+  if (!o) return;
+  sbp_options_default(o);
+  o->smoother = SBP_SMOOTH_RICHARDSON;
+  o->omega = 0.15;
+  o->nu_pre = 3;
+  o->nu_post = 3;
+  o->restriction = SBP_RESTRICT_NORMAL;
+  o->coarse_n = (n + 1) / 2;
+}
+
+int sbp_apply_f64(const double* u, double* out, int n, int sign, void* stream) {
+  if (!u || !out || n < 3 || (sign != 1 && sign != -1)) return SBP_ERR_ARGS;
+  ReduceBuf none{nullptr, nullptr};
+  SBP_CUDA(launch_apply<double>(cgrid<double>(u, n), grid<double>(out, n), n, sign, none, nullptr,
+                                (cudaStream_t)stream));
+  return SBP_OK;
+}
+
+int sbp_apply_f32(const float* u, float* out, int n, int sign, void* stream) {
+  if (!u || !out || n < 3 || (sign != 1 && sign != -1)) return SBP_ERR_ARGS;
+  ReduceBuf none{nullptr, nullptr};
+  SBP_CUDA(launch_apply<float>(cgrid<float>(u, n), grid<float>(out, n), n, sign, none, nullptr,
+                               (cudaStream_t)stream));
+  return SBP_OK;
+}
+
+int sbp_apply_dot_f64(const double* u, double* out, int n, int sign, double* dot, void* stream) {
+  if (!u || !out || !dot || n < 3 || (sign != 1 && sign != -1)) return SBP_ERR_ARGS;
+  cudaStream_t q = (cudaStream_t)stream;
+  TempReduce t;
+  int rc = t.alloc(n, q);
+  if (rc) return rc;
+  SBP_CUDA(launch_apply<double>(cgrid<double>(u, n), grid<double>(out, n), n, sign, t.rb, dot, q));
+  return SBP_OK;
+}
+
+int sbp_residual_norm_f64(const double* x, const double* b, int n, int sign, double* norm_host,
+                          void* stream) {
+  if (!x || !b || !norm_host || n < 3 || (sign != 1 && sign != -1)) return SBP_ERR_ARGS;
+  cudaStream_t q = (cudaStream_t)stream;
+  TempReduce t;
+  int rc = t.alloc(n, q);
+  if (rc) return rc;
+  double* r = nullptr;
+  SBP_CUDA(cudaMallocAsync((void**)&r, (size_t)n * n * sizeof(double), q));
+  cudaError_t e = launch_residual<double>(cgrid<double>(x, n), cgrid<double>(b, n),
+                                          grid<double>(r, n), Grid<float>{nullptr, n}, n, sign,
+                                          nullptr, nullptr, 0.0, 0.0, 0, t.out, t.rb, q);
+  double v = 0.0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&v, t.out, sizeof(double), cudaMemcpyDeviceToHost, q);
+  cudaFreeAsync(r, q);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(q);
+  if (e != cudaSuccess) return fail_cuda(e, "sbp_residual_norm_f64");
+  *norm_host = std::sqrt(v);
+  return SBP_OK;
+}
+
+int sbp_restrict_f64(const double* fine, double* coarse, int n_fine, int kind, void* stream) {
+  if (!fine || !coarse || n_fine < 3 || (n_fine % 2) == 0 || kind < 0 || kind > 2)
+    return SBP_ERR_ARGS;
+  const int nc = (n_fine + 1) / 2;
+  SBP_CUDA(launch_resrestrict<double>(Grid<const double>{nullptr, 0}, cgrid<double>(fine, n_fine),
+                                      grid<double>(coarse, nc), n_fine, kind, nullptr,
+                                      (cudaStream_t)stream));
+  return SBP_OK;
+}
+
+int sbp_prolong_f64(const double* coarse, double* fine, int n_coarse, int accumulate,
+                    void* stream) {
+  if (!coarse || !fine || n_coarse < 2) return SBP_ERR_ARGS;
+  SBP_CUDA(launch_prolong<double>(cgrid<double>(coarse, n_coarse),
+                                  grid<double>(fine, 2 * n_coarse - 1), n_coarse, accumulate,
+                                  nullptr, (cudaStream_t)stream));
+  return SBP_OK;
+}
+
+int sbp_richardson_f64(double* v, double* tmp, const double* b, int n, int iters, double omega,
+                       void* stream) {
+  return smooth_sweeps(v, tmp, b, n, iters, omega, SBP_SMOOTH_RICHARDSON, (cudaStream_t)stream);
+}
+
+int sbp_jacobi_f64(double* v, double* tmp, const double* b, int n, int iters, double omega,
+                   void* stream) {
+  return smooth_sweeps(v, tmp, b, n, iters, omega, SBP_SMOOTH_JACOBI, (cudaStream_t)stream);
+}
+
+int sbp_rhs_f64(const double* f, const double* gW, const double* gE, const double* gS,
+                const double* gN, double* b, int n, double fsign, void* stream) {
+  if (!f || !gW || !gE || !gS || !gN || !b || n < 3) return SBP_ERR_ARGS;
+  SBP_CUDA(launch_rhs(cgrid<double>(f, n), gW, gE, gS, gN, grid<double>(b, n), n, fsign,
+                      (cudaStream_t)stream));
+  return SBP_OK;
+}
+
+int sbp_rhs_adjoint_f64(const double* lam, double* df, double* dgW, double* dgE, double* dgS,
+                        double* dgN, int n, double fsign, void* stream) {
+  if (!lam || n < 3) return SBP_ERR_ARGS;
+  SBP_CUDA(launch_rhs_adjoint(cgrid<double>(lam, n), grid<double>(df, n), dgW, dgE, dgS, dgN, n,
+                              fsign, (cudaStream_t)stream));
+  return SBP_OK;
+}
+
+int sbp_solver_create(sbp_solver** out, int n, const sbp_options* opts) {
+  if (!out) return SBP_ERR_ARGS;
+  *out = nullptr;
+  if (n < 3) return SBP_ERR_ARGS;
+  sbp_solver* s = new (std::nothrow) sbp_solver();
+  if (!s) return SBP_ERR_NOMEM;
+  std::unique_ptr<sbp_solver, int (*)(sbp_solver*)> guard(s, sbp_solver_destroy);
+  s->n = n;
+  SBP_CUDA(cudaGetDevice(&s->device));
+  if (opts) {
+    s->mg = true;
+    s->opts = *opts;
+    sbp_options& o = s->opts;
+    if (o.omega <= 0.0) o.omega = (o.smoother == SBP_SMOOTH_JACOBI) ? 2.0 / 3.0 : 0.15;
+    if (!valid_mg_n(n) || !valid_mg_n(o.coarse_n) || o.coarse_n > n) return SBP_ERR_ARGS;
+    if (o.coarse_n > 65) return SBP_ERR_UNSUPPORTED;  // dense coarse inverse limit
+    if (o.nu_pre < 1 || o.nu_post < 0 || o.nu_pre > 64 || o.nu_post > 64) return SBP_ERR_UNSUPPORTED;
+    if (o.smoother != SBP_SMOOTH_JACOBI && o.smoother != SBP_SMOOTH_RICHARDSON) return SBP_ERR_ARGS;
+    if (o.restriction < 0 || o.restriction > 2) return SBP_ERR_ARGS;
+    if (o.precision != SBP_PREC_FP64 && o.precision != SBP_PREC_MIXED) return SBP_ERR_ARGS;
+    s->esize = (o.precision == SBP_PREC_MIXED) ? sizeof(float) : sizeof(double);
+  }
+  const size_t nn = (size_t)n * n;
+  int rc;
+  void* p;
+  rc = dalloc(s, &p, nn * 8); if (rc) return rc; s->r = (double*)p;
+  rc = dalloc(s, &p, nn * 8); if (rc) return rc; s->p[0] = (double*)p;
+  rc = dalloc(s, &p, nn * 8); if (rc) return rc; s->p[1] = (double*)p;
+  rc = dalloc(s, &p, nn * 8); if (rc) return rc; s->Ap = (double*)p;
+  rc = dalloc(s, &p, sizeof(SolveState)); if (rc) return rc; s->st = (SolveState*)p;
+  const size_t parts = (size_t)max_reduce_ctas(n) + 64;
+  rc = dalloc(s, &p, parts * sizeof(double)); if (rc) return rc; s->rb.partials = (double*)p;
+  rc = dalloc(s, &p, 64); if (rc) return rc; s->rb.ticket = (unsigned*)p;
+  SBP_CUDA(cudaMemset(s->rb.ticket, 0, 64));
+  SBP_CUDA(cudaMemset(s->p[0], 0, nn * 8));
+  SBP_CUDA(cudaMemset(s->p[1], 0, nn * 8));
+  SBP_CUDA(cudaMallocHost((void**)&s->st_host, 2 * sizeof(SolveState)));
+  SBP_CUDA(cudaStreamCreateWithFlags(&s->cap, cudaStreamNonBlocking));
+  SBP_CUDA(cudaEventCreateWithFlags(&s->ev[0], cudaEventDisableTiming));
+  SBP_CUDA(cudaEventCreateWithFlags(&s->ev[1], cudaEventDisableTiming));
+  rc = ensure_norms(s, 1024);
+  if (rc) return rc;
+  if (s->mg) {
+    const bool mixed = s->opts.precision == SBP_PREC_MIXED;
+    if (mixed) {
+      rc = dalloc(s, &p, nn * sizeof(float)); if (rc) return rc; s->r_lo = (float*)p;
+    }
+    int m = n;
+    while (true) {
+      Level L;
+      L.n = m;
+      const size_t bytes = (size_t)m * m * s->esize;
+      if (s->levels.empty()) {
+        L.b = mixed ? (void*)s->r_lo : (void*)s->r;
+      } else {
+        rc = dalloc(s, &L.b, bytes); if (rc) return rc;
+        L.own_b = true;
+      }
+      rc = dalloc(s, &L.v[0], bytes); if (rc) return rc;
+      rc = dalloc(s, &L.v[1], bytes); if (rc) return rc;
+      SBP_CUDA(cudaMemset(L.v[0], 0, bytes));
+      SBP_CUDA(cudaMemset(L.v[1], 0, bytes));
+      s->levels.push_back(L);
+      if (m == s->opts.coarse_n) break;
+      m = (m + 1) / 2;
+    }
+    const int nc = s->opts.coarse_n;
+    std::shared_ptr<const std::vector<double>> X;
+    try {
+      X = coarse_inverse(nc);
+    } catch (const std::exception& ex) {
+      g_last_error = ex.what();
+      return SBP_ERR_CUDA;
+    }
+    const size_t ab = X->size() * sizeof(double);
+    rc = dalloc(s, &p, ab); if (rc) return rc; s->Ainv = (double*)p;
+    SBP_CUDA(cudaMemcpy(s->Ainv, X->data(), ab, cudaMemcpyHostToDevice));
+  }
+  SBP_CUDA(cudaDeviceSynchronize());
+  guard.release();
+  *out = s;
+  return SBP_OK;
+}
+
+int sbp_solver_destroy(sbp_solver* s) {
+  if (!s) return SBP_OK;
+  cudaSetDevice(s->device);
+  destroy_graphs(s);
+  for (void* p : s->allocs) cudaFree(p);
+  if (s->st_host) cudaFreeHost(s->st_host);
+  if (s->cap) cudaStreamDestroy(s->cap);
+  for (auto& e : s->ev)
+    if (e) cudaEventDestroy(e);
+  delete s;
+  return SBP_OK;
+}
+
+int sbp_solver_levels(const sbp_solver* s) {
+  if (!s) return SBP_ERR_ARGS;
+  return s->mg ? (int)s->levels.size() : 1;
+}
+
+long long sbp_solver_device_bytes(const sbp_solver* s) { return s ? s->dev_bytes : 0; }
+
+long long sbp_solver_last_launches(const sbp_solver* s) { return s ? s->last_launches : 0; }
+
+int sbp_mgcg_solve(sbp_solver* s, const double* b, double* x, double abstol, double reltol,
+                   int maxiter, sbp_result* res, double* norms, int norms_cap, void* stream) {
+  return run_krylov(s, 0, b, x, +1, abstol, reltol, maxiter, res, norms, norms_cap,
+                    (cudaStream_t)stream);
+}
+
+int sbp_cg_solve(sbp_solver* s, const double* b, double* x, int sign, double abstol,
+                 double reltol, int maxiter, sbp_result* res, double* norms, int norms_cap,
+                 void* stream) {
+  if (sign != 1 && sign != -1) return SBP_ERR_ARGS;
+  return run_krylov(s, 1, b, x, sign, abstol, reltol, maxiter, res, norms, norms_cap,
+                    (cudaStream_t)stream);
+}
+
+int sbp_vcycle_apply(sbp_solver* s, const double* b, double* v, void* stream) {
+  if (!s || !b || !v) return SBP_ERR_ARGS;
+  if (!s->mg) return SBP_ERR_UNSUPPORTED;
+  cudaStream_t q = (cudaStream_t)stream;
+  SBP_CUDA(cudaSetDevice(s->device));
+  const int n = s->n;
+  if (s->opts.precision == SBP_PREC_MIXED) {
+    SBP_CUDA((launch_copy<double, float>(cgrid<double>(b, n), grid<float>(s->r_lo, n), n, q)));
+    SBP_CUDA(enqueue_vcycle<float>(s, 0, false, nullptr, q));
+    SBP_CUDA((launch_copy<float, double>(cgrid<float>(vcycle_out(s), n), grid<double>(v, n), n, q)));
+  } else {
+    SBP_CUDA(cudaMemcpyAsync(s->r, b, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToDevice, q));
+    SBP_CUDA(enqueue_vcycle<double>(s, 0, false, nullptr, q));
+    SBP_CUDA(cudaMemcpyAsync(v, vcycle_out(s), (size_t)n * n * sizeof(double),
+                             cudaMemcpyDeviceToDevice, q));
+  }
+  return SBP_OK;
+}
+
+}  // extern "C"

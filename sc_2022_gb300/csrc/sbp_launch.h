@@ -1,0 +1,100 @@
+// Host-side launch wrappers for the SBP-SAT kernels (defined in
+// sbp_kernels.cu).  All launches are asynchronous on `s`; none allocates.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "sbp_common.cuh"
+
+namespace sbp {
+
+// Upper bound on the CTAs any reducing launch uses for an n x n grid; the
+// partials buffer of a ReduceBuf must hold this many doubles.
+int max_reduce_ctas(int n);
+
+// out = sign * (-A) u.  If dot_out != nullptr also writes sum(u .* out)
+// to *dot_out (device), using `rb` as scratch.
+template <typename T>
+cudaError_t launch_apply(Grid<const T> u, Grid<T> out, int n, int sign, ReduceBuf rb,
+                         double* dot_out, cudaStream_t s);
+
+// r = b - opsign*A*x (and rlo = float(r) if rlo.p); sum(r.*r) goes to
+// *out2 (if non-null) and, if st != nullptr, initialises the Krylov state:
+// rr0, rr, thresh2 (abstol^2 if abstol > 0 else reltol^2*rr0), norms[0],
+// iter = 0, done, and rz = rr0 when `plain`.
+template <typename T>
+cudaError_t launch_residual(Grid<const T> x, Grid<const T> b, Grid<T> r, Grid<float> rlo, int n,
+                            int opsign, SolveState* st, double* norms, double abstol,
+                            double reltol, int plain, double* out2, ReduceBuf rb,
+                            cudaStream_t s);
+
+// p_new = z + beta*p_old (p_new = z on the first iteration), Ap = opsign*A*p_new,
+// pAp = p_new.Ap, alpha = rz / pAp.
+template <typename T, typename Tz>
+cudaError_t launch_cg_dir(Grid<const Tz> z, Grid<const T> pold, Grid<T> pnew, Grid<T> Ap, int n,
+                          int opsign, SolveState* st, ReduceBuf rb, cudaStream_t s);
+
+// x += alpha p, r -= alpha Ap, rlo = float(r) (if rlo.p), rr = r.r,
+// iter += 1, norms[iter] = sqrt(rr), convergence / max-iteration test.
+// `plain`: unpreconditioned CG, also beta = rr/rz and rz = rr.
+template <typename T>
+cudaError_t launch_cg_update(Grid<T> x, Grid<T> r, Grid<const T> p, Grid<const T> Ap,
+                             Grid<float> rlo, int n, int plain, SolveState* st, double* norms,
+                             ReduceBuf rb, cudaStream_t s);
+
+// One smoothing pass on level n.  The stencil input ("field") is
+//   kFieldPlain:   vin
+//   kFieldZero:    the first sweep from v = 0 (omega D^-1 b or omega b)
+//   kFieldProlong: vin + P e  (e on the (n+1)/2 grid)
+// and the output is vout = F + omega M (b - A F) (sweep) or vout = F (store),
+// M = D^-1 (Jacobi) or I (Richardson).  With dot != 0 the pass also reduces
+// b.vout into the Krylov state: beta = b.vout / rz (after the first
+// iteration), rz = b.vout.
+enum FieldKind : int { kFieldPlain = 0, kFieldZero = 1, kFieldProlong = 2 };
+enum EpiKind : int { kEpiSweep = 0, kEpiStore = 1 };
+template <typename T>
+cudaError_t launch_smooth(int field, int epi, Grid<const T> vin, Grid<const T> e, Grid<const T> b,
+                          Grid<T> vout, int n, int smoother, double omega, int dot,
+                          SolveState* st, ReduceBuf rb, cudaStream_t s);
+
+// f = R (b - A v) on the (nf+1)/2 grid (v == nullptr: f = R b).
+template <typename T>
+cudaError_t launch_resrestrict(Grid<const T> v, Grid<const T> b, Grid<T> f, int nf, int kind,
+                               const SolveState* st, cudaStream_t s);
+
+// out = P e  (accumulate: out += P e), e on nc x nc, out on (2nc-1)^2.
+template <typename T>
+cudaError_t launch_prolong(Grid<const T> e, Grid<T> out, int nc, int accumulate,
+                           const SolveState* st, cudaStream_t s);
+
+// e = Ainv f with Ainv the dense nc^2 x nc^2 inverse of the coarse operator
+// (FP64 regardless of T).
+template <typename T>
+cudaError_t launch_coarse_gemv(const double* Ainv, Grid<const T> f, Grid<T> e, int nc,
+                               const SolveState* st, cudaStream_t s);
+
+// out = convert(in) on an n x n grid.
+template <typename Tin, typename Tout>
+cudaError_t launch_copy(Grid<const Tin> in, Grid<Tout> out, int n, cudaStream_t s);
+
+// *out = sum(a .* b) on an n x n grid.
+template <typename T>
+cudaError_t launch_dot(Grid<const T> a, Grid<const T> b, int n, double* out, ReduceBuf rb,
+                       cudaStream_t s);
+
+// Krylov state reset (iter = done = 0, maxiter) before a solve.
+cudaError_t launch_state_init(SolveState* st, int maxiter, cudaStream_t s);
+
+// b = -H~ (fsign*f + SAT_W gW + SAT_E gE + SAT_S gS + SAT_N gN), the right-hand
+// side of Assembling_matrix (level_2_multigrid_new.jl:169-185) with f in
+// the Delta u = f convention times fsign.
+cudaError_t launch_rhs(Grid<const double> f, const double* gW, const double* gE,
+                       const double* gS, const double* gN, Grid<double> b, int n, double fsign,
+                       cudaStream_t s);
+
+// Transpose of launch_rhs's linear map applied to lambda: gradients of
+// lambda.b with respect to f and the four boundary vectors.
+cudaError_t launch_rhs_adjoint(Grid<const double> lam, Grid<double> df, double* dgW, double* dgE,
+                               double* dgS, double* dgN, int n, double fsign, cudaStream_t s);
+
+}  // namespace sbp

@@ -1,0 +1,83 @@
+"""CPU tests of the C ABI: the library loads, exports every function that
+include/sbpmg.h declares, argument checks reject bad input before touching
+the GPU, and the host-side coarse inverse is exact."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import sbp_oracle as o
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_functions():
+    text = (ROOT / "include" / "sbpmg.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"\b(sbp_[a-z0-9_]+)\s*\(", text)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from sc_2022_gb300 import _lib
+    return _lib.load()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    names = declared_functions()
+    assert len(names) >= 20
+    for name in names:
+        assert hasattr(lib, name), f"libsbpmg.so does not export {name}"
+
+
+def test_python_binding_covers_header():
+    from sc_2022_gb300 import _lib
+    assert set(declared_functions()) == set(_lib.SIGNATURES)
+
+
+def test_options(lib):
+    from sc_2022_gb300 import _lib
+    o1 = _lib.sbp_options()
+    lib.sbp_options_default(C.byref(o1))
+    assert (o1.smoother, o1.nu_pre, o1.nu_post, o1.restriction, o1.coarse_n, o1.precision) == (
+        _lib.SBP_SMOOTH_JACOBI, 3, 3, _lib.SBP_RESTRICT_GALERKIN, 65, _lib.SBP_PREC_FP64)
+    assert abs(o1.omega - 2 / 3) < 1e-15
+    o2 = _lib.sbp_options()
+    lib.sbp_options_reference_two_level(C.byref(o2), 129)
+    assert (o2.smoother, o2.restriction, o2.coarse_n) == (_lib.SBP_SMOOTH_RICHARDSON,
+                                                          _lib.SBP_RESTRICT_NORMAL, 65)
+    assert o2.omega == 0.15
+
+
+def test_argument_errors_without_gpu(lib):
+    from sc_2022_gb300 import _lib
+    assert lib.sbp_apply_f64(None, None, 5, -1, None) == _lib.SBP_ERR_ARGS
+    assert lib.sbp_apply_f64(C.c_void_p(8), C.c_void_p(8), 2, -1, None) == _lib.SBP_ERR_ARGS
+    assert lib.sbp_apply_f64(C.c_void_p(8), C.c_void_p(8), 5, 3, None) == _lib.SBP_ERR_ARGS
+    assert lib.sbp_restrict_f64(C.c_void_p(8), C.c_void_p(8), 8, 0, None) == _lib.SBP_ERR_ARGS
+    assert lib.sbp_restrict_f64(C.c_void_p(8), C.c_void_p(8), 9, 7, None) == _lib.SBP_ERR_ARGS
+    h = C.c_void_p()
+    assert lib.sbp_solver_create(C.byref(h), 2, None) == _lib.SBP_ERR_ARGS
+    assert lib.sbp_mgcg_solve(None, None, None, 0, 0, 1, None, None, 0, None) == _lib.SBP_ERR_ARGS
+    assert lib.sbp_status_string(_lib.SBP_ERR_MAXITER) == b"maximum iterations reached"
+
+
+@pytest.mark.parametrize("nc", [5, 17, 33])
+def test_coarse_inverse_host(lib, nc):
+    N = nc * nc
+    X = np.zeros(N * N)
+    rc = lib.sbp_coarse_inverse_host(nc, X.ctypes.data_as(C.POINTER(C.c_double)), N * N)
+    assert rc == 0
+    A = o.assemble(nc).A.toarray()
+    X = X.reshape(N, N)
+    assert np.abs(X - X.T).max() == 0.0
+    assert np.abs(X @ A - np.eye(N)).max() < 1e-11
+
+
+def test_coarse_inverse_rejects_bad_size(lib):
+    X = np.zeros(10)
+    assert lib.sbp_coarse_inverse_host(6, X.ctypes.data_as(C.POINTER(C.c_double)), 10) < 0
+    assert lib.sbp_coarse_inverse_host(5, X.ctypes.data_as(C.POINTER(C.c_double)), 10) < 0

@@ -1,0 +1,196 @@
+"""GPU parity of the single-grid operators (through the C ABI) against the
+CPU oracle and the golden fixtures."""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import sbp_oracle as o
+
+pytestmark = pytest.mark.gpu
+
+APPLY_RTOL = 1e-13   # FP64 operator apply, relative 2-norm
+
+
+def dev(a, dtype=torch.float64):
+    return torch.tensor(np.asarray(a), dtype=dtype, device="cuda").contiguous()
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.detach().cpu().numpy().ravel().astype(np.float64)
+
+
+def relerr(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.mark.parametrize("n", [3, 5, 9, 17, 33])
+def test_apply_golden(sbp, golden, n):
+    u = dev(golden[f"apply_u_{n}"])
+    out = torch.empty_like(u)
+    sbp.matrix_free_A_full_GPU(u, out)
+    assert relerr(host(out), golden[f"apply_negAu_{n}"]) < APPLY_RTOL
+
+
+@pytest.mark.parametrize("n", [65, 129, 257, 513, 1025])
+def test_apply_vs_assembled(sbp, n):
+    rng = np.random.default_rng(n)
+    u = rng.standard_normal(n * n)
+    A = o.assemble(n).A
+    ud = dev(u)
+    out = torch.empty_like(ud)
+    lib = sbp.load_library()
+    for sign in (-1, 1):
+        rc = lib.sbp_apply_f64(C.c_void_p(ud.data_ptr()), C.c_void_p(out.data_ptr()), n, sign,
+                               None)
+        assert rc == 0
+        assert relerr(host(out), sign * (A @ u)) < APPLY_RTOL
+
+
+def test_apply_large_linearity(sbp):
+    # size-independent property at the benchmark size: A(a u + b v) = a Au + b Av
+    n = 4097
+    g = torch.Generator(device="cuda").manual_seed(1)
+    u = torch.randn(n * n, generator=g, device="cuda", dtype=torch.float64)
+    v = torch.randn(n * n, generator=g, device="cuda", dtype=torch.float64)
+    au, av, aw = (torch.empty_like(u) for _ in range(3))
+    sbp.matrix_free_A_full_GPU(u, au)
+    sbp.matrix_free_A_full_GPU(v, av)
+    sbp.matrix_free_A_full_GPU(2.0 * u - 3.0 * v, aw)
+    torch.cuda.synchronize()
+    d = (aw - (2.0 * au - 3.0 * av)).norm() / aw.norm()
+    assert d.item() < 1e-14
+    # symmetry u.Av == v.Au
+    s1 = torch.dot(u, av).item()
+    s2 = torch.dot(v, au).item()
+    assert abs(s1 - s2) <= 1e-12 * (abs(s1) + 1e-300) * 100
+
+
+@pytest.mark.parametrize("n", [9, 65, 1025])
+def test_apply_f32(sbp, n):
+    rng = np.random.default_rng(7)
+    u = rng.standard_normal(n * n).astype(np.float32)
+    A = o.assemble(n).A
+    ud = dev(u, torch.float32)
+    out = torch.empty_like(ud)
+    sbp.matrix_free_A_full_GPU_f32(ud, out)
+    ref = -(A @ u.astype(np.float64))
+    assert relerr(host(out), ref) < 1e-6
+
+
+@pytest.mark.parametrize("n", [5, 33, 257])
+def test_apply_dot(sbp, n):
+    rng = np.random.default_rng(3)
+    u = rng.standard_normal(n * n)
+    A = o.assemble(n).A
+    ud = dev(u)
+    out = torch.empty_like(ud)
+    dot = torch.zeros(1, dtype=torch.float64, device="cuda")
+    lib = sbp.load_library()
+    rc = lib.sbp_apply_dot_f64(C.c_void_p(ud.data_ptr()), C.c_void_p(out.data_ptr()), n, 1,
+                               C.c_void_p(dot.data_ptr()), None)
+    assert rc == 0
+    ref = u @ (A @ u)
+    assert abs(host(dot)[0] - ref) <= 1e-12 * abs(ref)
+    assert relerr(host(out), A @ u) < APPLY_RTOL
+
+
+@pytest.mark.parametrize("n", [5, 9, 17, 33])
+def test_restrict_golden(sbp, golden, n):
+    lib = sbp.load_library()
+    r = dev(golden[f"restrict_in_{n}"])
+    nc = (n + 1) // 2
+    f = torch.empty(nc * nc, dtype=torch.float64, device="cuda")
+    for k, kind in enumerate(o.RESTRICT_KINDS):
+        assert lib.sbp_restrict_f64(C.c_void_p(r.data_ptr()), C.c_void_p(f.data_ptr()), n, k,
+                                    None) == 0
+        np.testing.assert_allclose(host(f), golden[f"restrict_{kind}_{n}"], rtol=0, atol=1e-14)
+    # the reference's entry point (NORMAL)
+    sbp.matrix_free_restriction_2d_GPU(r, f)
+    np.testing.assert_allclose(host(f), golden[f"restrict_normal_{n}"], rtol=0, atol=1e-14)
+
+
+@pytest.mark.parametrize("nc", [3, 5, 9, 17])
+def test_prolong_golden(sbp, golden, nc):
+    e = dev(golden[f"prolong_in_{nc}"])
+    nf = 2 * nc - 1
+    out = torch.full((nf * nf,), float("nan"), dtype=torch.float64, device="cuda")
+    sbp.matrix_free_prolongation_2d_GPU(e, out)
+    np.testing.assert_allclose(host(out), golden[f"prolong_{nc}"], rtol=0, atol=1e-15)
+    base = torch.ones_like(out)
+    sbp.matrix_free_prolongation_2d_GPU(e, base, accumulate=True)
+    np.testing.assert_allclose(host(base), golden[f"prolong_{nc}"] + 1.0, rtol=0, atol=1e-14)
+
+
+@pytest.mark.parametrize("n", [1025, 4097])
+def test_restrict_prolong_adjoint_large(sbp, n):
+    # <P e, r> == <e, P^T r> with P^T = GALERKIN restriction, at full size
+    lib = sbp.load_library()
+    nc = (n + 1) // 2
+    g = torch.Generator(device="cuda").manual_seed(5)
+    r = torch.randn(n * n, generator=g, device="cuda", dtype=torch.float64)
+    e = torch.randn(nc * nc, generator=g, device="cuda", dtype=torch.float64)
+    pe = torch.empty_like(r)
+    rt = torch.empty_like(e)
+    sbp.matrix_free_prolongation_2d_GPU(e, pe)
+    assert lib.sbp_restrict_f64(C.c_void_p(r.data_ptr()), C.c_void_p(rt.data_ptr()), n, 2,
+                                None) == 0
+    torch.cuda.synchronize()
+    a, b = torch.dot(pe, r).item(), torch.dot(e, rt).item()
+    assert abs(a - b) <= 1e-11 * (abs(a) + abs(b))
+
+
+@pytest.mark.parametrize("smoother", ["richardson", "jacobi"])
+def test_smoothers(sbp, smoother):
+    n = 33
+    a = o.assemble(n)
+    rng = np.random.default_rng(11)
+    v0 = rng.standard_normal(n * n)
+    b = rng.standard_normal(n * n)
+    vd, td, bd = dev(v0), torch.empty(n * n, dtype=torch.float64, device="cuda"), dev(b)
+    if smoother == "richardson":
+        sbp.matrix_free_richardson(vd, td, bd, maxiter=3, omega=0.15)
+        ref = o.richardson(v0, a.A, b, 3, 0.15)
+    else:
+        sbp.jacobi(vd, td, bd, maxiter=4, omega=2 / 3)
+        ref = o.jacobi(v0, a.A, b, 4, 2 / 3)
+    assert relerr(host(vd), ref) < 1e-13
+    assert relerr(host(td), ref) < 1e-13
+
+
+@pytest.mark.parametrize("n", [9, 17, 33])
+def test_rhs_golden(sbp, golden, n):
+    from sc_2022_gb300 import problems
+    g = {k: golden[f"rhs_g{k}_{n}"] for k in "WESN"}
+    b = problems.assemble_rhs(golden[f"rhs_f_{n}"], g)
+    np.testing.assert_allclose(host(b), golden[f"rhs_b_{n}"], rtol=0, atol=1e-13)
+
+
+def test_rhs_adjoint_dot_identity(sbp):
+    from sc_2022_gb300 import problems
+    n = 257
+    rng = np.random.default_rng(2)
+    f = rng.standard_normal(n * n)
+    g = {k: rng.standard_normal(n) for k in "WESN"}
+    lam = dev(rng.standard_normal(n * n))
+    b = problems.assemble_rhs(f, g)
+    df, dg = problems.rhs_adjoint(lam)
+    lhs = torch.dot(lam.ravel(), b.ravel()).item()
+    rhs = float(host(df) @ f) + sum(float(host(dg[k]) @ g[k]) for k in "WESN")
+    assert abs(lhs - rhs) <= 1e-12 * (abs(lhs) + 1.0)
+
+
+def test_residual_norm(sbp):
+    n = 65
+    a = o.assemble(n)
+    rng = np.random.default_rng(4)
+    x, b = rng.standard_normal(n * n), rng.standard_normal(n * n)
+    lib = sbp.load_library()
+    out = C.c_double()
+    xd, bd = dev(x), dev(b)
+    assert lib.sbp_residual_norm_f64(C.c_void_p(xd.data_ptr()), C.c_void_p(bd.data_ptr()), n, 1,
+                                     C.byref(out), None) == 0
+    ref = np.linalg.norm(b - a.A @ x)
+    assert abs(out.value - ref) <= 1e-12 * ref

@@ -1,0 +1,188 @@
+"""GPU parity of the CG / MGCG solvers against the CPU oracle."""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import sbp_oracle as o
+
+pytestmark = pytest.mark.gpu
+
+SQRT_EPS = math.sqrt(np.finfo(float).eps)
+
+
+def dev(a):
+    return torch.tensor(np.asarray(a), dtype=torch.float64, device="cuda").contiguous()
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.detach().cpu().numpy().ravel()
+
+
+def relerr(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def ref_problem(n, kind="reference"):
+    a = o.assemble(n)
+    F, g, U = o.manufactured(n, kind)
+    return a, a.rhs(F, g), U
+
+
+def test_cg_matches_oracle(sbp, golden):
+    n = 33
+    b = golden["ref33_b"]
+    s = sbp.Solver(n)
+    x = torch.zeros(n * n, dtype=torch.float64, device="cuda")
+    res = s.cg(dev(b), x, sign=1, abstol=np.linalg.norm(b) * SQRT_EPS)
+    ref = golden["ref33_cg_norms"]
+    assert res.converged and res.iters == len(ref) - 1
+    np.testing.assert_allclose(res.norms, ref, rtol=1e-6)
+    assert relerr(host(x), golden["ref33_cg_x"]) < 1e-10
+
+
+def test_cg_full_gpu_reference_semantics(sbp):
+    # CG_full_GPU iterates with matrix_free_A_full_GPU (-A): solves (-A) x = b
+    n = 65
+    a, b, _ = ref_problem(n)
+    x = torch.zeros(n * n, dtype=torch.float64, device="cuda")
+    abstol = np.linalg.norm(b) * SQRT_EPS
+    iters, tol, last = sbp.CG_full_GPU(dev(b), x, abstol=abstol)
+    xr, itr, nr = o.cg(-a.A, b, abstol=abstol)
+    assert iters == itr and tol == abstol
+    assert last == pytest.approx(nr[-2], rel=1e-6)
+    assert relerr(host(x), xr) < 1e-9
+
+
+@pytest.mark.parametrize("n,expect", [(33, 18), (65, 19), (129, 18)])
+def test_mgcg_reference_two_level(sbp, n, expect):
+    a, b, U = ref_problem(n)
+    hier = o.Hierarchy(n, o.MGOptions.reference_two_level(n))
+    xr, itr, nr = o.mgcg(hier, b)
+    x = torch.zeros(n * n, dtype=torch.float64, device="cuda")
+    abstol = np.linalg.norm(b) * SQRT_EPS
+    iters, norms, xo = sbp.matrix_free_MGCG(dev(b), x, abstol=abstol)
+    assert iters == itr == expect
+    np.testing.assert_allclose(norms, nr, rtol=1e-8)
+    assert relerr(host(x), xr) < 1e-10
+
+
+def test_two_level_vcycle_matches(sbp):
+    n = 65
+    a, b, _ = ref_problem(n)
+    hier = o.Hierarchy(n, o.MGOptions.reference_two_level(n))
+    z_ref = hier.vcycle(b)
+    v, resnorm = sbp.matrix_free_Two_level_multigrid(dev(b))
+    assert relerr(host(v), z_ref) < 1e-12
+    assert resnorm == pytest.approx(np.linalg.norm(a.A @ z_ref - b), rel=1e-9)
+
+
+def test_vcycle_mgcg_golden(sbp, golden):
+    n = 65
+    b = golden["base65_b"]
+    opts = sbp.default_options()
+    opts.coarse_n = 17
+    s = sbp.Solver(n, opts)
+    assert s.levels == 3
+    z = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    s.vcycle(dev(b), z)
+    assert relerr(host(z), golden["base65_vcycle17_z"]) < 1e-12
+    x = torch.zeros_like(z)
+    res = s.mgcg(dev(b), x, reltol=1e-10)
+    ref = golden["base65_vcycle17_norms"]
+    assert res.converged and res.iters == len(ref) - 1
+    np.testing.assert_allclose(res.norms, ref, rtol=1e-7)
+    assert relerr(host(x), golden["base65_vcycle17_x"]) < 1e-10
+
+
+@pytest.mark.parametrize("n", [129, 257, 513])
+def test_mgcg_vcycle_default(sbp, n):
+    a, b, U = ref_problem(n, "baseline")
+    hier = o.Hierarchy(n, o.MGOptions(coarse_n=65))
+    xr, itr, nr = o.mgcg(hier, b, reltol=1e-10)
+    s = sbp.Solver(n, sbp.default_options())
+    x = torch.zeros(n * n, dtype=torch.float64, device="cuda")
+    res = s.mgcg(dev(b), x, reltol=1e-10)
+    assert res.converged and res.iters == itr
+    np.testing.assert_allclose(res.norms, nr, rtol=1e-6)
+    assert relerr(host(x), xr) < 1e-10
+
+
+@pytest.mark.parametrize("n", [257, 1025])
+def test_mgcg_mixed_precision(sbp, n):
+    from sc_2022_gb300 import _lib
+    a, b, U = ref_problem(n, "baseline")
+    bd = dev(b)
+    s64 = sbp.Solver(n, sbp.default_options())
+    x64 = torch.zeros_like(bd)
+    r64 = s64.mgcg(bd, x64, reltol=1e-10)
+    s32 = sbp.Solver(n, sbp.default_options(_lib.SBP_PREC_MIXED))
+    x32 = torch.zeros_like(bd)
+    r32 = s32.mgcg(bd, x32, reltol=1e-10)
+    assert r64.converged and r32.converged
+    assert r32.iters <= r64.iters + 2
+    # true FP64 residual of the mixed solution
+    import ctypes as C
+    lib = sbp.load_library()
+    out = C.c_double()
+    assert lib.sbp_residual_norm_f64(C.c_void_p(x32.data_ptr()), C.c_void_p(bd.data_ptr()), n, 1,
+                                     C.byref(out), None) == 0
+    assert out.value <= 2e-10 * np.linalg.norm(b)
+    assert relerr(host(x32), host(x64)) < 1e-8
+
+
+def test_mgcg_large_discretisation_error(sbp):
+    # N = 4097 and 2049: MGCG to 1e-10 and second-order H-error of the
+    # manufactured solution (size-independent property of the full solve)
+    from sc_2022_gb300 import problems
+    errs = {}
+    for n in (2049, 4097):
+        f, g, U = problems.manufactured(n, "baseline")
+        bd = problems.assemble_rhs(f, g)
+        s = sbp.Solver(n, sbp.default_options())
+        x = torch.zeros_like(bd)
+        res = s.mgcg(bd, x, reltol=1e-10)
+        assert res.converged and res.iters <= 10
+        d = host(x) - U.ravel()
+        h = 1.0 / (n - 1)
+        w = np.ones(n)
+        w[0] = w[-1] = 0.5
+        W = (h * h) * np.outer(w, w).ravel()
+        errs[n] = math.sqrt(float(d @ (W * d)))
+        s.close()
+    assert 3.8 < errs[2049] / errs[4097] < 4.2
+
+
+def test_status_codes(sbp):
+    from sc_2022_gb300 import _lib
+    n = 65
+    a, b, _ = ref_problem(n)
+    s = sbp.Solver(n, sbp.default_options())
+    x = torch.zeros(n * n, dtype=torch.float64, device="cuda")
+    res = s.mgcg(dev(b), x, reltol=1e-14, maxiter=2)
+    assert res.status == _lib.SBP_ERR_MAXITER and res.iters == 2
+    bad = b.copy()
+    bad[100] = np.nan
+    x.zero_()
+    res = s.mgcg(dev(bad), x, reltol=1e-10)
+    assert res.status == _lib.SBP_ERR_BREAKDOWN
+    x.zero_()
+    res = s.mgcg(torch.zeros(n * n, dtype=torch.float64, device="cuda"), x, reltol=1e-10)
+    assert res.converged and res.iters == 0
+    with pytest.raises(sbp.SbpError):
+        s.mgcg(dev(b), x, reltol=1e-14, maxiter=2, raise_on_fail=True)
+
+
+def test_deterministic(sbp):
+    n = 257
+    a, b, _ = ref_problem(n, "baseline")
+    s = sbp.Solver(n, sbp.default_options())
+    runs = []
+    for _ in range(2):
+        x = torch.zeros(n * n, dtype=torch.float64, device="cuda")
+        res = s.mgcg(dev(b), x, reltol=1e-10)
+        runs.append((res.norms, host(x)))
+    assert runs[0][0] == runs[1][0]
+    assert np.array_equal(runs[0][1], runs[1][1])

@@ -1,0 +1,164 @@
+"""CPU tests: the oracle pinned against the golden fixtures and against the
+reference's own cross checks (matrix-free == assembled, transfers == kron
+matrices, second-order discretisation error, iteration counts)."""
+import math
+
+import numpy as np
+import pytest
+import scipy.sparse.linalg as spla
+
+from oracle import cpu_path
+from oracle import sbp_oracle as o
+
+
+@pytest.mark.parametrize("n", [3, 5, 9, 17, 33])
+def test_apply_golden(golden, n):
+    u = golden[f"apply_u_{n}"]
+    np.testing.assert_allclose(o.neg_A_matrix_free(u, n), golden[f"apply_negAu_{n}"],
+                               rtol=0, atol=1e-13)
+    np.testing.assert_array_equal(o.assemble(n).A.diagonal(), golden[f"diagA_{n}"])
+
+
+@pytest.mark.parametrize("n", [3, 5, 9, 17, 33, 65])
+def test_matrix_free_equals_assembled(n):
+    # split_matrix_free.jl:517 compares the matrix-free apply variants;
+    # here the matrix-free formula against the kron-assembled A.
+    a = o.assemble(n)
+    u = np.random.default_rng(n).standard_normal(n * n)
+    mf = o.neg_A_matrix_free(u, n)
+    ref = -(a.A @ u)
+    assert np.linalg.norm(mf - ref) <= 1e-14 * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("n", [5, 9, 17, 33])
+def test_operator_symmetric_positive_definite(n):
+    A = o.assemble(n).A
+    assert abs(A - A.T).max() == 0.0
+    lam = np.linalg.eigvalsh(A.toarray())
+    assert lam.min() > 0
+    np.testing.assert_array_equal(A.diagonal(), o.neg_A_coefficients(n))
+
+
+def test_diagonal_values():
+    d = o.assemble(9).A.diagonal().reshape(9, 9)
+    assert d[4, 4] == 4.0 and d[4, 0] == 2.0 and d[0, 4] == 12.0 and d[0, 0] == 6.0
+
+
+@pytest.mark.parametrize("n", [5, 9, 17, 33])
+def test_transfers_golden_and_kron(golden, n):
+    r = golden[f"restrict_in_{n}"]
+    for kind in o.RESTRICT_KINDS:
+        np.testing.assert_allclose(o.restriction_2d(n, kind) @ r, golden[f"restrict_{kind}_{n}"],
+                                   rtol=0, atol=1e-14)
+    # matrix_free_mg_cg.jl:636-646: matrix-free transfers == kron matrices
+    np.testing.assert_allclose(o.restriction_mf(r, n), o.restriction_2d(n, "normal") @ r,
+                               rtol=0, atol=1e-14)
+    nc = (n + 1) // 2
+    e = golden[f"prolong_in_{nc}"]
+    np.testing.assert_allclose(o.prolongation_mf(e, nc), golden[f"prolong_{nc}"], rtol=0,
+                               atol=1e-14)
+    np.testing.assert_allclose(o.prolongation_2d(nc) @ e, golden[f"prolong_{nc}"], rtol=0,
+                               atol=1e-14)
+
+
+def test_galerkin_is_P_transpose_and_4x_normal():
+    n = 17
+    G = o.restriction_2d(n, "galerkin")
+    Nn = o.restriction_2d(n, "normal")
+    assert abs(G - 4 * Nn).max() < 1e-15
+    assert abs(G - o.prolongation_2d(9).T).max() < 1e-15
+
+
+@pytest.mark.parametrize("n", [9, 17, 33])
+def test_rhs_golden(golden, n):
+    a = o.assemble(n)
+    g = {k: golden[f"rhs_g{k}_{n}"] for k in "WESN"}
+    np.testing.assert_allclose(a.rhs(golden[f"rhs_f_{n}"], g), golden[f"rhs_b_{n}"], rtol=0,
+                               atol=1e-13)
+
+
+def test_discretisation_error_second_order():
+    # matrix_free_mg_cg.jl:464 error measure; values match the probe of the
+    # reference problem u = sin(pi(x+y)) (7.09e-3, 4.32e-4, 1.08e-4, 2.70e-5).
+    errs = {}
+    for n in (9, 33, 65, 129):
+        a = o.assemble(n)
+        F, g, U = o.manufactured(n, "reference")
+        x = spla.spsolve(a.A.tocsc(), a.rhs(F, g))
+        errs[n] = o.h_error(a, x, U)
+    assert errs[9] == pytest.approx(7.087e-3, rel=2e-3)
+    assert errs[33] == pytest.approx(4.319e-4, rel=2e-3)
+    assert errs[65] == pytest.approx(1.079e-4, rel=2e-3)
+    assert errs[129] == pytest.approx(2.697e-5, rel=2e-3)
+    assert 3.9 < errs[65] / errs[129] < 4.1
+    # the baseline problem u = sin(pi x) cos(pi y) converges at the same rate
+    eb = []
+    for n in (33, 65, 129):
+        a = o.assemble(n)
+        F, g, U = o.manufactured(n, "baseline")
+        eb.append(o.h_error(a, spla.spsolve(a.A.tocsc(), a.rhs(F, g)), U))
+    assert 3.9 < eb[0] / eb[1] < 4.1 and 3.9 < eb[1] / eb[2] < 4.1
+
+
+@pytest.mark.parametrize("n,expect_mg,expect_cg", [(33, 18, 96), (65, 19, 187), (129, 18, 368)])
+def test_reference_iteration_counts(n, expect_mg, expect_cg):
+    a = o.assemble(n)
+    F, g, U = o.manufactured(n, "reference")
+    b = a.rhs(F, g)
+    hier = o.Hierarchy(n, o.MGOptions.reference_two_level(n))
+    _, it, _ = o.mgcg(hier, b)
+    _, itc, _ = o.cg(a.A, b)
+    assert it == expect_mg
+    assert itc == expect_cg
+
+
+def test_solver_histories_golden(golden):
+    n = 33
+    a = o.assemble(n)
+    b = golden["ref33_b"]
+    hier = o.Hierarchy(n, o.MGOptions.reference_two_level(n))
+    x, it, norms = o.mgcg(hier, b)
+    np.testing.assert_allclose(norms, golden["ref33_mgcg2_norms"], rtol=1e-10)
+    x, it, norms = o.cg(a.A, b)
+    np.testing.assert_allclose(norms, golden["ref33_cg_norms"], rtol=1e-8)
+    n = 65
+    hier = o.Hierarchy(n, o.MGOptions(coarse_n=17))
+    x, it, norms = o.mgcg(hier, golden["base65_b"], reltol=1e-10)
+    np.testing.assert_allclose(norms, golden["base65_vcycle17_norms"], rtol=1e-9)
+
+
+@pytest.mark.parametrize("n", [5, 17, 65])
+def test_c_oracle_matches_python_oracle(n):
+    m = cpu_path.CpuMG(n, plain=True)
+    assert abs(m.csr() - o.assemble(n).A).max() == 0.0
+
+
+def test_c_oracle_mgcg_matches():
+    n = 65
+    a = o.assemble(n)
+    F, g, U = o.manufactured(n, "baseline")
+    b = a.rhs(F, g)
+    hier = o.Hierarchy(n, o.MGOptions(coarse_n=17))
+    xo, ito, no = o.mgcg(hier, b, reltol=1e-10)
+    m = cpu_path.CpuMG(n, coarse_n=17)
+    x, it, norms = m.mgcg(b, np.zeros_like(b), 1e-10 * np.linalg.norm(b))
+    assert it == ito
+    np.testing.assert_allclose(norms, no, rtol=1e-9)
+    assert np.linalg.norm(x - xo) <= 1e-12 * np.linalg.norm(xo)
+    m2 = cpu_path.CpuMG(33, smoother="richardson", restriction="normal", coarse_n=17)
+    a = o.assemble(33)
+    F, g, U = o.manufactured(33, "reference")
+    b = a.rhs(F, g)
+    _, it, _ = m2.mgcg(b, np.zeros_like(b), np.linalg.norm(b) * math.sqrt(np.finfo(float).eps))
+    assert it == 18
+
+
+def test_vcycle_galerkin_h_independent():
+    its = []
+    for n in (65, 129, 257):
+        a = o.assemble(n)
+        F, g, U = o.manufactured(n, "baseline")
+        hier = o.Hierarchy(n, o.MGOptions(coarse_n=17))
+        _, it, _ = o.mgcg(hier, a.rhs(F, g), reltol=1e-10)
+        its.append(it)
+    assert max(its) <= 8 and max(its) - min(its) <= 1
