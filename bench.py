@@ -44,6 +44,9 @@ def parse_args():
     p.add_argument("--n", type=int, default=4097)
     p.add_argument("--apply-iters", type=int, default=50)
     p.add_argument("--cpu-baseline", type=int, default=1, help="time the CPU baseline leg")
+    p.add_argument("--mode", choices=["full", "apply", "solve-fp64", "solve-mixed"],
+                   default="full", help="profiling modes run one part only and print a "
+                   "short line (not the benchmark line)")
     return p.parse_args()
 
 
@@ -361,8 +364,48 @@ def run_ours(args, d: Dist):
     s64.close()
 
 
+def run_part(args):
+    """Profiling helper: one part of the benchmark on a single GPU."""
+    import ctypes as C
+
+    import torch
+
+    import sc_2022_gb300 as sbp
+    from sc_2022_gb300 import _lib, problems
+    n = args.n
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    lib = sbp.load_library()
+    if args.mode == "apply":
+        gen = torch.Generator(device=dev).manual_seed(0)
+        us = [torch.randn(n * n, generator=gen, device=dev, dtype=torch.float64) for _ in range(2)]
+        outs = [torch.empty_like(us[0]) for _ in range(2)]
+        for k in range(args.warmup + args.steps):
+            rc = lib.sbp_apply_f64(C.c_void_p(us[k % 2].data_ptr()),
+                                   C.c_void_p(outs[k % 2].data_ptr()), n, -1, sp)
+            assert rc == 0
+        torch.cuda.synchronize()
+        print(json.dumps({"mode": "apply", "n": n, "launches": args.warmup + args.steps}))
+        return
+    prec = _lib.SBP_PREC_MIXED if args.mode == "solve-mixed" else _lib.SBP_PREC_FP64
+    f, g, _ = problems.manufactured(n, "baseline")
+    b = problems.assemble_rhs(f, g, device=dev).reshape(-1)
+    s = sbp.Solver(n, sbp.default_options(prec))
+    x = torch.zeros_like(b)
+    for _ in range(args.warmup + args.steps):
+        x.zero_()
+        r = s.mgcg(b, x, reltol=1e-10)
+    torch.cuda.synchronize()
+    print(json.dumps({"mode": args.mode, "n": n, "iters": r.iters, "converged": r.converged,
+                      "launches_per_solve": s.last_launches}))
+
+
 def main():
     args = parse_args()
+    if args.mode != "full":
+        run_part(args)
+        return
     d = Dist(args.gpus)
     try:
         if args.impl == "reference":

@@ -1,6 +1,9 @@
 // SBP-SAT Poisson kernels for sm_103a: operator apply, fused CG updates,
 // multigrid smoothing / transfer / coarse solve, right-hand-side assembly.
 #include <math.h>
+#include <stdint.h>
+
+#include <algorithm>
 
 #include "sbp_kernels.cuh"
 #include "sbp_launch.h"
@@ -9,12 +12,15 @@ namespace sbp {
 
 // Output tile of the stencil kernels: 64 points along the contiguous index
 // i (two 256-byte FP64 rows per warp pass) by 32 along j.  The staged tile
-// with halo is at most 67 x 37 = 19.8 KB in FP64, so eleven CTAs fit on an
-// SM by shared memory (eight by threads).
+// with halo is at most 67 x 37 = 19.8 KB in FP64.
 constexpr int TI = 64;
 constexpr int TJ = 32;
 using TileT = Tile<TI, TJ>;
 constexpr int kSmemPts = TileT::SI * TileT::SJ;
+constexpr int kIntPts = (TI + 1) * (TJ + 1);     // interior-staged operand
+// Coarse region under a fine tile (prolongation operand).
+constexpr int EP = TI / 2 + 4;
+constexpr int EJ = TJ / 2 + 6;
 
 // Coarse tile of the fused residual + restriction kernel.
 constexpr int RTI = 32;
@@ -27,14 +33,22 @@ constexpr int RRJ = RVJ - 2;
 // Coarse dense solve: rows of Ainv per warp.
 constexpr int kGemvRowsPerWarp = 2;
 
+// Flat (pointwise) kernels: CTAs per launch cap (152 SMs x 8).
+constexpr int kFlatCtas = 1216;
+
 static inline dim3 tile_grid(int n) { return dim3(ntiles(n, TI), ntiles(n, TJ)); }
+
+static inline int flat_grid(long long N, int per) {
+  const long long want = (N + (long long)kThreads * per - 1) / ((long long)kThreads * per);
+  return (int)std::max(1LL, std::min<long long>(want, kFlatCtas));
+}
 
 int max_reduce_ctas(int n) {
   const dim3 g = tile_grid(n);
-  return (int)(g.x * g.y);
+  return std::max((int)(g.x * g.y), kFlatCtas);
 }
 
-// Visit the points of a tile without shared memory (pointwise kernels).
+// Visit the points of a tile without shared memory (pointwise 2D kernels).
 template <typename Fn>
 __device__ __forceinline__ void for_points(const TileT& t, Fn&& fn) {
   const int lane = threadIdx.x & 31;
@@ -54,10 +68,11 @@ __global__ void __launch_bounds__(kThreads) k_apply(Grid<const T> u, Grid<T> out
   __shared__ T s[kSmemPts];
   TileT t;
   t.init(blockIdx.x, blockIdx.y, n);
-  stage_tile(s, t, n, FieldPlain<T>{u});
+  stage_tile_async(s, t, u, n);
+  cp_async_wait_all();
   __syncthreads();
   double acc = 0.0;
-  for_tile_points(s, t, [&](int i, int j, const SAcc<T>& a) {
+  for_tile_points(s, t, [&](int i, int j, const SAcc<T>& a, int) {
     const T v = sign * negA<T>(a, i, j, n);
     out.at(i, j) = v;
     if (DOT) acc += (double)a(0, 0) * (double)v;
@@ -68,10 +83,11 @@ __global__ void __launch_bounds__(kThreads) k_apply(Grid<const T> u, Grid<T> out
 template <typename T>
 cudaError_t launch_apply(Grid<const T> u, Grid<T> out, int n, int sign, ReduceBuf rb,
                          double* dot_out, cudaStream_t s) {
+  // the kernel writes s * (-A u); out = sign * A u needs s = -sign
   if (dot_out)
-    k_apply<T, true><<<tile_grid(n), kThreads, 0, s>>>(u, out, n, T(sign), rb, dot_out);
+    k_apply<T, true><<<tile_grid(n), kThreads, 0, s>>>(u, out, n, T(-sign), rb, dot_out);
   else
-    k_apply<T, false><<<tile_grid(n), kThreads, 0, s>>>(u, out, n, T(sign), rb, nullptr);
+    k_apply<T, false><<<tile_grid(n), kThreads, 0, s>>>(u, out, n, T(-sign), rb, nullptr);
   return cudaGetLastError();
 }
 
@@ -92,13 +108,16 @@ __global__ void __launch_bounds__(kThreads)
     k_residual(Grid<const T> x, Grid<const T> b, Grid<T> r, Grid<float> rlo, int n, T opsign,
                ResFin rf, ReduceBuf rb) {
   __shared__ T s[kSmemPts];
+  __shared__ T sb[kIntPts];
   TileT t;
   t.init(blockIdx.x, blockIdx.y, n);
-  stage_tile(s, t, n, FieldPlain<T>{x});
+  stage_tile_async(s, t, x, n);
+  stage_interior_async(sb, t, b, n);
+  cp_async_wait_all();
   __syncthreads();
   double acc = 0.0;
-  for_tile_points(s, t, [&](int i, int j, const SAcc<T>& a) {
-    const T rv = __ldg(&b.at(i, j)) + opsign * negA<T>(a, i, j, n);
+  for_tile_points(s, t, [&](int i, int j, const SAcc<T>& a, int k) {
+    const T rv = sb[k] + opsign * negA<T>(a, i, j, n);
     r.at(i, j) = rv;
     if (rlo.p) rlo.at(i, j) = (float)rv;
     acc += (double)rv * (double)rv;
@@ -144,13 +163,30 @@ __global__ void __launch_bounds__(kThreads)
              SolveState* st, ReduceBuf rb) {
   if (st->done) return;
   __shared__ T s[kSmemPts];
+  __shared__ Tz sz[kSmemPts];
   TileT t;
   t.init(blockIdx.x, blockIdx.y, n);
   const bool first = (st->iter == 0);
-  stage_tile(s, t, n, FieldDir<T, Tz>{z, pold, T(st->beta), first});
+  const T beta = T(st->beta);
+  stage_tile_async(sz, t, z, n);
+  if (!first) stage_tile_async(s, t, pold, n);
+  cp_async_wait_all();
+  __syncthreads();
+  {
+    constexpr int SI = TileT::SI;
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    const int ei = t.i_hi - t.i_lo + 2;
+    const int ej = t.j_hi - t.j_lo + t.hl + t.hr;
+    for (int c = w; c < ej; c += kWarps)
+      for (int r = lane; r < ei; r += 32) {
+        const int q = c * SI + r;
+        s[q] = first ? T(sz[q]) : T(sz[q]) + beta * s[q];
+      }
+  }
   __syncthreads();
   double acc = 0.0;
-  for_tile_points(s, t, [&](int i, int j, const SAcc<T>& a) {
+  for_tile_points(s, t, [&](int i, int j, const SAcc<T>& a, int) {
     const T pv = a(0, 0);
     const T ap = -opsign * negA<T>(a, i, j, n);
     pnew.at(i, j) = pv;
@@ -174,28 +210,54 @@ cudaError_t launch_cg_dir(Grid<const Tz> z, Grid<const T> pold, Grid<T> pnew, Gr
 }
 
 // ---------------------------------------------------------------------------
-// CG update: x += alpha p; r -= alpha Ap; ||r||^2; convergence test.
+// CG update (pointwise, flat, 16-byte vectors): x += alpha p; r -= alpha Ap;
+// ||r||^2; convergence test.  All solver arrays are contiguous n*n.
 // ---------------------------------------------------------------------------
-template <typename T>
+__device__ __forceinline__ void cg_update_pt(double& x, double& r, double p, double ap,
+                                             double alpha, double& acc) {
+  x += alpha * p;
+  r -= alpha * ap;
+  acc += r * r;
+}
+
+template <bool VEC>
 __global__ void __launch_bounds__(kThreads)
-    k_cg_update(Grid<T> x, Grid<T> r, Grid<const T> p, Grid<const T> Ap, Grid<float> rlo, int n,
-                int plain, SolveState* st, double* norms, ReduceBuf rb) {
+    k_cg_update(double* __restrict__ x, double* __restrict__ r, const double* __restrict__ p,
+                const double* __restrict__ Ap, float* __restrict__ rlo, long long N, int plain,
+                SolveState* st, double* norms, ReduceBuf rb) {
   if (st->done) return;
-  TileT t;
-  t.init(blockIdx.x, blockIdx.y, n);
-  const T alpha = T(st->alpha);
+  const double alpha = st->alpha;
   double acc = 0.0;
-  for_points(t, [&](int i, int j) {
-    const T pv = __ldg(&p.at(i, j));
-    const T apv = __ldg(&Ap.at(i, j));
-    const T xv = x.at(i, j);
-    const T rv0 = r.at(i, j);
-    const T rv = rv0 - alpha * apv;
-    x.at(i, j) = xv + alpha * pv;
-    r.at(i, j) = rv;
-    if (rlo.p) rlo.at(i, j) = (float)rv;
-    acc += (double)rv * (double)rv;
-  });
+  const long long tid = (long long)blockIdx.x * kThreads + threadIdx.x;
+  const long long stride = (long long)gridDim.x * kThreads;
+  long long done_to = 0;
+  if (VEC) {
+    const long long nv = N / 2;
+    double2* x2 = reinterpret_cast<double2*>(x);
+    double2* r2 = reinterpret_cast<double2*>(r);
+    const double2* p2 = reinterpret_cast<const double2*>(p);
+    const double2* a2 = reinterpret_cast<const double2*>(Ap);
+#pragma unroll 2
+    for (long long k = tid; k < nv; k += stride) {
+      const double2 pv = __ldg(p2 + k);
+      const double2 av = __ldg(a2 + k);
+      double2 xv = x2[k];
+      double2 rv = r2[k];
+      cg_update_pt(xv.x, rv.x, pv.x, av.x, alpha, acc);
+      cg_update_pt(xv.y, rv.y, pv.y, av.y, alpha, acc);
+      x2[k] = xv;
+      r2[k] = rv;
+      if (rlo) reinterpret_cast<float2*>(rlo)[k] = make_float2((float)rv.x, (float)rv.y);
+    }
+    done_to = 2 * nv;
+  }
+  for (long long k = done_to + tid; k < N; k += stride) {
+    double xv = x[k], rv = r[k];
+    cg_update_pt(xv, rv, p[k], Ap[k], alpha, acc);
+    x[k] = xv;
+    r[k] = rv;
+    if (rlo) rlo[k] = (float)rv;
+  }
   grid_reduce(acc, rb, [&](double tot) {
     const int it = st->iter + 1;
     st->iter = it;
@@ -214,11 +276,22 @@ __global__ void __launch_bounds__(kThreads)
   });
 }
 
+static inline bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
 template <typename T>
 cudaError_t launch_cg_update(Grid<T> x, Grid<T> r, Grid<const T> p, Grid<const T> Ap,
                              Grid<float> rlo, int n, int plain, SolveState* st, double* norms,
                              ReduceBuf rb, cudaStream_t s) {
-  k_cg_update<T><<<tile_grid(n), kThreads, 0, s>>>(x, r, p, Ap, rlo, n, plain, st, norms, rb);
+  static_assert(sizeof(T) == 8, "the Krylov vectors are FP64");
+  if (x.ld != n || r.ld != n || p.ld != n || Ap.ld != n) return cudaErrorInvalidValue;
+  const long long N = (long long)n * n;
+  const bool vec = aligned16(x.p) && aligned16(r.p) && aligned16(p.p) && aligned16(Ap.p) &&
+                   (!rlo.p || ((uintptr_t)rlo.p & 7u) == 0);
+  const int g = flat_grid(N, vec ? 4 : 2);
+  if (vec)
+    k_cg_update<true><<<g, kThreads, 0, s>>>(x.p, r.p, p.p, Ap.p, rlo.p, N, plain, st, norms, rb);
+  else
+    k_cg_update<false><<<g, kThreads, 0, s>>>(x.p, r.p, p.p, Ap.p, rlo.p, N, plain, st, norms, rb);
   return cudaGetLastError();
 }
 
@@ -231,27 +304,52 @@ __global__ void __launch_bounds__(kThreads)
              int smoother, T omega, SolveState* st, ReduceBuf rb) {
   if (st && st->done) return;
   __shared__ T s[kSmemPts];
+  __shared__ T sb[kIntPts];
+  __shared__ T se[FIELD == kFieldProlong ? EP * EJ : 1];
   TileT t;
   t.init(blockIdx.x, blockIdx.y, n);
-  if (FIELD == kFieldPlain) {
-    stage_tile(s, t, n, FieldPlain<T>{vin});
-  } else if (FIELD == kFieldZero) {
-    stage_tile(s, t, n, FieldZeroSweep<T>{b, n, omega, smoother});
-  } else {
-    stage_tile(s, t, n, FieldProlong<T>{vin, e});
-  }
-  __syncthreads();
-  double acc = 0.0;
   const bool jac = (smoother == kSmoothJacobi);
-  for_tile_points(s, t, [&](int i, int j, const SAcc<T>& a) {
-    const T f = a(0, 0);
-    T vn = f;
+  const bool need_b = (EPI == kEpiSweep) || DOT;
+  int I0 = 0, J0 = 0;
+  if (FIELD == kFieldZero) {
+    stage_tile_async(s, t, b, n);
+  } else {
+    stage_tile_async(s, t, vin, n);
+    if (need_b) stage_interior_async(sb, t, b, n);
+  }
+  if (FIELD == kFieldProlong) {
+    const int nc = (n + 1) / 2;
+    I0 = (t.i_lo - 1) >> 1;
+    J0 = (t.j_lo - t.hl) >> 1;
+    const int ei = (t.i_hi >> 1) - I0 + 2;
+    const int ej = ((t.j_hi + t.hr - 1) >> 1) - J0 + 2;
+    stage_async<EP>(se, e, I0, J0, ei, ej, nc);
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  if (FIELD == kFieldProlong) {
+    transform_staged(s, t, n, [&](int i, int j, T& v) { v += prolong_smem<EP>(se, I0, J0, i, j); });
+    __syncthreads();
+  }
+  double acc = 0.0;
+  constexpr int SI = TileT::SI;
+  for_tile_points(s, t, [&](int i, int j, const SAcc<T>& a, int k) {
+    T f, na;
     T bb = T(0);
-    if (EPI == kEpiSweep || DOT) bb = __ldg(&b.at(i, j));
+    if (FIELD == kFieldZero) {
+      SAccZero<T> z{a.s, SI, i, j, n, omega, jac};
+      f = z(0, 0);
+      bb = a(0, 0);
+      na = (EPI == kEpiSweep) ? negA<T>(z, i, j, n) : T(0);
+    } else {
+      f = a(0, 0);
+      if (need_b) bb = sb[k];
+      na = (EPI == kEpiSweep) ? negA<T>(a, i, j, n) : T(0);
+    }
+    T vn = f;
     if (EPI == kEpiSweep) {
-      const T res = bb + negA<T>(a, i, j, n);
       const T m = jac ? omega * inv_diagA<T>(i, j, n) : omega;
-      vn = f + m * res;
+      vn = f + m * (bb + na);
     }
     vout.at(i, j) = vn;
     if (DOT) acc += (double)bb * (double)vn;
@@ -322,8 +420,9 @@ __global__ void __launch_bounds__(kThreads)
   const int rj0 = 2 * t.j_lo - 1;
   const int rei = 2 * m + 1;
   const int rej = 2 * mp + 1;
-  stage_region<RRI, RRJ>(sr, ri0, rj0, rei, rej, nf, FieldPlain<T>{b});
-  if (v.p) stage_region<RVI, RVJ>(sv, ri0 - 1, rj0 - 1, rei + 2, rej + 2, nf, FieldPlain<T>{v});
+  stage_async<RRI>(sr, b, ri0, rj0, rei, rej, nf);
+  if (v.p) stage_async<RVI>(sv, v, ri0 - 1, rj0 - 1, rei + 2, rej + 2, nf);
+  cp_async_wait_all();
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
@@ -443,37 +542,41 @@ cudaError_t launch_coarse_gemv(const double* Ainv, Grid<const T> f, Grid<T> e, i
 }
 
 // ---------------------------------------------------------------------------
-// Copy / convert, dot, state init.
+// Copy / convert and dot (pointwise, flat over contiguous n*n arrays).
 // ---------------------------------------------------------------------------
 template <typename Tin, typename Tout>
-__global__ void __launch_bounds__(kThreads) k_copy(Grid<const Tin> in, Grid<Tout> out, int n) {
-  TileT t;
-  t.init(blockIdx.x, blockIdx.y, n);
-  for_points(t, [&](int i, int j) { out.at(i, j) = (Tout)__ldg(&in.at(i, j)); });
+__global__ void __launch_bounds__(kThreads)
+    k_copy(const Tin* __restrict__ in, Tout* __restrict__ out, long long N) {
+  const long long stride = (long long)gridDim.x * kThreads;
+  for (long long k = (long long)blockIdx.x * kThreads + threadIdx.x; k < N; k += stride)
+    out[k] = (Tout)__ldg(in + k);
 }
 
 template <typename Tin, typename Tout>
 cudaError_t launch_copy(Grid<const Tin> in, Grid<Tout> out, int n, cudaStream_t s) {
-  k_copy<Tin, Tout><<<tile_grid(n), kThreads, 0, s>>>(in, out, n);
+  if (in.ld != n || out.ld != n) return cudaErrorInvalidValue;
+  const long long N = (long long)n * n;
+  k_copy<Tin, Tout><<<flat_grid(N, 4), kThreads, 0, s>>>(in.p, out.p, N);
   return cudaGetLastError();
 }
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-    k_dot(Grid<const T> a, Grid<const T> b, int n, double* out, ReduceBuf rb) {
-  TileT t;
-  t.init(blockIdx.x, blockIdx.y, n);
+    k_dot(const T* __restrict__ a, const T* __restrict__ b, long long N, double* out,
+          ReduceBuf rb) {
   double acc = 0.0;
-  for_points(t, [&](int i, int j) {
-    acc += (double)__ldg(&a.at(i, j)) * (double)__ldg(&b.at(i, j));
-  });
+  const long long stride = (long long)gridDim.x * kThreads;
+  for (long long k = (long long)blockIdx.x * kThreads + threadIdx.x; k < N; k += stride)
+    acc += (double)__ldg(a + k) * (double)__ldg(b + k);
   grid_reduce(acc, rb, [&](double tot) { *out = tot; });
 }
 
 template <typename T>
 cudaError_t launch_dot(Grid<const T> a, Grid<const T> b, int n, double* out, ReduceBuf rb,
                        cudaStream_t s) {
-  k_dot<T><<<tile_grid(n), kThreads, 0, s>>>(a, b, n, out, rb);
+  if (a.ld != n || b.ld != n) return cudaErrorInvalidValue;
+  const long long N = (long long)n * n;
+  k_dot<T><<<flat_grid(N, 4), kThreads, 0, s>>>(a.p, b.p, N, out, rb);
   return cudaGetLastError();
 }
 

@@ -59,50 +59,84 @@ struct SAcc {
   __device__ __forceinline__ T operator()(int di, int dj) const { return s[dj * si + di]; }
 };
 
-// Stage field values f(i, j) of the region [i0, i0+ei) x [j0, j0+ej) into s
-// (row pitch MAXI).  Loads are fully unrolled into registers first so every
-// thread has all of its loads in flight before the first shared store.
-// Points outside the n x n domain are set to zero.
-template <int MAXI, int MAXJ, typename T, typename F>
-__device__ __forceinline__ void stage_region(T* s, int i0, int j0, int ei, int ej, int n,
-                                             const F& f) {
-  constexpr int NR = (MAXI + 31) / 32;
-  constexpr int NC = (MAXJ + kWarps - 1) / kWarps;
+// ---------------------------------------------------------------------------
+// Asynchronous staging.  cp.async copies global -> shared without passing
+// through registers, so every element a CTA stages is in flight at once
+// (the staged tile of one CTA is ~20 KB; with several CTAs per SM this keeps
+// well over the ~40 KB per SM that HBM latency x bandwidth requires).  It
+// needs only element alignment, so it works on the caller's column-major
+// arrays whatever their leading dimension (n = 2^k + 1 is odd, so columns
+// are not 16-byte aligned and TMA tensor copies could not address them).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async_elem(double* sdst, const double* gsrc) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(sdst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_elem(float* sdst, const float* gsrc) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(sdst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gsrc) : "memory");
+}
+// Wait for this thread's copies; a __syncthreads() must follow before other
+// threads read the staged data.
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;\n" ::: "memory");
+}
+
+// Stage the raw values of g over [i0, i0+ei) x [j0, j0+ej) into s with row
+// pitch P; points outside the n x n domain are zero-filled.
+template <int P, typename T>
+__device__ __forceinline__ void stage_async(T* s, Grid<const T> g, int i0, int j0, int ei, int ej,
+                                            int n) {
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
-  T buf[NC][NR];
-#pragma unroll
-  for (int a = 0; a < NC; ++a) {
-#pragma unroll
-    for (int b = 0; b < NR; ++b) {
-      const int c = w + a * kWarps;
-      const int r = lane + b * 32;
+  for (int c = w; c < ej; c += kWarps) {
+    const int j = j0 + c;
+    const bool jok = (j >= 0 && j < n);
+    for (int r = lane; r < ei; r += 32) {
       const int i = i0 + r;
-      const int j = j0 + c;
-      const bool ok = (c < ej) && (r < ei) && (i >= 0) && (i < n) && (j >= 0) && (j < n);
-      buf[a][b] = ok ? f(i, j) : T(0);
-    }
-  }
-#pragma unroll
-  for (int a = 0; a < NC; ++a) {
-#pragma unroll
-    for (int b = 0; b < NR; ++b) {
-      const int c = w + a * kWarps;
-      const int r = lane + b * 32;
-      if (c < ej && r < ei) s[c * MAXI + r] = buf[a][b];
+      if (jok && i >= 0 && i < n)
+        cp_async_elem(&s[c * P + r], &g.at(i, j));
+      else
+        s[c * P + r] = T(0);
     }
   }
 }
 
-// Stage a tile plus its halo.
-template <int TI, int TJ, typename T, typename F>
-__device__ __forceinline__ void stage_tile(T* s, const Tile<TI, TJ>& t, int n, const F& f) {
-  stage_region<Tile<TI, TJ>::SI, Tile<TI, TJ>::SJ>(s, t.i_lo - 1, t.j_lo - t.hl,
-                                                   t.i_hi - t.i_lo + 2,
-                                                   t.j_hi - t.j_lo + t.hl + t.hr, n, f);
+// Stage a tile plus its halo (pitch Tile::SI).
+template <int TI, int TJ, typename T>
+__device__ __forceinline__ void stage_tile_async(T* s, const Tile<TI, TJ>& t, Grid<const T> g,
+                                                 int n) {
+  stage_async<Tile<TI, TJ>::SI>(s, g, t.i_lo - 1, t.j_lo - t.hl, t.i_hi - t.i_lo + 2,
+                                t.j_hi - t.j_lo + t.hl + t.hr, n);
 }
 
-// Visit every output point of the tile: fn(i, j, SAcc centred on (i, j)).
+// Stage only the tile's own points (pitch TI + 1), for pointwise operands.
+template <int TI, int TJ, typename T>
+__device__ __forceinline__ void stage_interior_async(T* s, const Tile<TI, TJ>& t,
+                                                     Grid<const T> g, int n) {
+  stage_async<TI + 1>(s, g, t.i_lo, t.j_lo, t.i_hi - t.i_lo, t.j_hi - t.j_lo, n);
+}
+
+// Apply fn(i, j, value&) to every staged point of a tile (halo included).
+template <int TI, int TJ, typename T, typename Fn>
+__device__ __forceinline__ void transform_staged(T* s, const Tile<TI, TJ>& t, int n, Fn&& fn) {
+  constexpr int SI = Tile<TI, TJ>::SI;
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  const int ei = t.i_hi - t.i_lo + 2;
+  const int ej = t.j_hi - t.j_lo + t.hl + t.hr;
+  for (int c = w; c < ej; c += kWarps) {
+    const int j = t.j_lo - t.hl + c;
+    if (j < 0 || j >= n) continue;
+    for (int r = lane; r < ei; r += 32) {
+      const int i = t.i_lo - 1 + r;
+      if (i >= 0 && i < n) fn(i, j, s[c * SI + r]);
+    }
+  }
+}
+
+// Visit every output point of the tile: fn(i, j, SAcc centred on (i, j),
+// k) with k the point's index in an interior-staged array (pitch TI + 1).
 template <int TI, int TJ, typename T, typename Fn>
 __device__ __forceinline__ void for_tile_points(const T* s, const Tile<TI, TJ>& t, Fn&& fn) {
   constexpr int SI = Tile<TI, TJ>::SI;
@@ -113,7 +147,7 @@ __device__ __forceinline__ void for_tile_points(const T* s, const Tile<TI, TJ>& 
   for (int c = w; c < mj; c += kWarps) {
     for (int r = lane; r < mi; r += 32) {
       SAcc<T> acc{s + (c + t.hl) * SI + (r + 1), SI};
-      fn(t.i_lo + r, t.j_lo + c, acc);
+      fn(t.i_lo + r, t.j_lo + c, acc, c * (TI + 1) + r);
     }
   }
 }
@@ -173,45 +207,10 @@ __device__ __forceinline__ void grid_reduce(double v, const ReduceBuf& red, Fin&
 __device__ __forceinline__ bool finite_d(double x) { return isfinite(x); }
 
 // ---------------------------------------------------------------------------
-// Fields (stencil inputs computed while staging).
+// Multigrid transfer helpers.
 // ---------------------------------------------------------------------------
-template <typename T>
-struct FieldPlain {
-  Grid<const T> u;
-  __device__ __forceinline__ T operator()(int i, int j) const { return __ldg(&u.at(i, j)); }
-};
-
-// CG search direction: p = z + beta * p_old (beta from the device state;
-// first iteration p = z).
-template <typename T, typename Tz>
-struct FieldDir {
-  Grid<const Tz> z;
-  Grid<const T> pold;
-  T beta;
-  bool first;
-  __device__ __forceinline__ T operator()(int i, int j) const {
-    const T zz = T(__ldg(&z.at(i, j)));
-    return first ? zz : zz + beta * __ldg(&pold.at(i, j));
-  }
-};
-
-// First smoothing sweep from v = 0: v1 = omega * D^-1 * b (Jacobi) or
-// omega * b (Richardson).
-template <typename T>
-struct FieldZeroSweep {
-  Grid<const T> b;
-  int n;
-  T omega;
-  int smoother;
-  __device__ __forceinline__ T operator()(int i, int j) const {
-    const T bb = __ldg(&b.at(i, j));
-    if (smoother == kSmoothJacobi) return omega * bb * inv_diagA<T>(i, j, n);
-    return omega * bb;
-  }
-};
-
 // Bilinear prolongation of the coarse correction e (nc x nc) to fine point
-// (i, j) (prolongation_2D_kernel, matrix_free_mg_cg.jl:41-67).
+// (i, j) from global memory (prolongation_2D_kernel, matrix_free_mg_cg.jl:41-67).
 template <typename T>
 __device__ __forceinline__ T prolong_at(const Grid<const T>& e, int i, int j) {
   const int i0 = i >> 1, j0 = j >> 1;
@@ -226,13 +225,33 @@ __device__ __forceinline__ T prolong_at(const Grid<const T>& e, int i, int j) {
   return v * scale;
 }
 
-// v + P e: the coarse-grid correction folded into the following sweep.
+// The same from a staged coarse region with origin (I0, J0) and pitch EP.
+template <int EP, typename T>
+__device__ __forceinline__ T prolong_smem(const T* se, int I0, int J0, int i, int j) {
+  const T* q = se + ((j >> 1) - J0) * EP + ((i >> 1) - I0);
+  const bool oi = i & 1, oj = j & 1;
+  T v = q[0];
+  if (oi) v += q[1];
+  if (oj) {
+    v += q[EP];
+    if (oi) v += q[EP + 1];
+  }
+  const T scale = (oi && oj) ? T(0.25) : ((oi || oj) ? T(0.5) : T(1));
+  return v * scale;
+}
+
+// Accessor for the first smoothing sweep from v = 0: the field is
+// omega * D^-1 * b (Jacobi) or omega * b (Richardson), formed from the staged
+// b at each neighbour the stencil reads.
 template <typename T>
-struct FieldProlong {
-  Grid<const T> v;
-  Grid<const T> e;
-  __device__ __forceinline__ T operator()(int i, int j) const {
-    return __ldg(&v.at(i, j)) + prolong_at(e, i, j);
+struct SAccZero {
+  const T* s;
+  int si, i, j, n;
+  T omega;
+  bool jac;
+  __device__ __forceinline__ T operator()(int di, int dj) const {
+    const T v = s[dj * si + di] * omega;
+    return jac ? v * inv_diagA<T>(i + di, j + dj, n) : v;
   }
 };
 
