@@ -111,13 +111,28 @@ __host__ __device__ __forceinline__ R inv_diagA(int i, int j, int n) {
 // coarse index c.  normal = restriction_matrix_normal (boundary 1/2, 1/4),
 // sbp = restriction_matrix (boundary 1/2, 1/2), galerkin = P^T = 2*normal
 // (level_2_multigrid_new.jl:205-233).
-__host__ __device__ __forceinline__ double restrict_w1(int kind, int c, int nc, int a) {
-  if ((c == 0 && a < 0) || (c == nc - 1 && a > 0)) return 0.0;
+// Computed in the kernel's own precision R: every weight is a power of two.
+template <typename R = double>
+__host__ __device__ __forceinline__ R restrict_w1(int kind, int c, int nc, int a) {
+  if ((c == 0 && a < 0) || (c == nc - 1 && a > 0)) return R(0);
   const bool edge = (c == 0 || c == nc - 1);
-  double w = (a == 0) ? 0.5 : 0.25;
-  if (kind == kRestrictSbp && edge && a != 0) w = 0.5;
-  if (kind == kRestrictGalerkin) w *= 2.0;
-  return w;
+  const bool gal = (kind == kRestrictGalerkin);
+  if (a == 0) return gal ? R(1) : R(0.5);
+  if (kind == kRestrictSbp && edge) return R(0.5);
+  return gal ? R(0.5) : R(0.25);
+}
+
+// sign * (A u)(i, j) with the sign folded into the stencil's final FMA (no
+// separate multiply: on GB300 every FP64 instruction counts).
+template <typename R, typename U>
+__host__ __device__ __forceinline__ R signedA(const U& u, int i, int j, int n, int sign) {
+  if (i > 0 && i < n - 1 && j > 2 && j < n - 3) {
+    const R c = u(0, 0);
+    const R sum = (u(-1, 0) + u(1, 0)) + (u(0, -1) + u(0, 1));
+    return sign > 0 ? fma(R(4), c, -sum) : fma(R(-4), c, sum);
+  }
+  const R v = negA<R>(u, i, j, n);
+  return sign > 0 ? -v : v;
 }
 
 // ---------------------------------------------------------------------------

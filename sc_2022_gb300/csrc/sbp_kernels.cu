@@ -63,7 +63,7 @@ __device__ __forceinline__ void for_points(const TileT& t, Fn&& fn) {
 // Operator apply: out = sign * (-A) u, optional fused dot u.out.
 // ---------------------------------------------------------------------------
 template <typename T, bool DOT>
-__global__ void __launch_bounds__(kThreads) k_apply(Grid<const T> u, Grid<T> out, int n, T sign,
+__global__ void __launch_bounds__(kThreads) k_apply(Grid<const T> u, Grid<T> out, int n, int sign,
                                                     ReduceBuf rb, double* dot_out) {
   __shared__ T s[kSmemPts];
   TileT t;
@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(kThreads) k_apply(Grid<const T> u, Grid<T> out
   __syncthreads();
   double acc = 0.0;
   for_tile_points(s, t, [&](int i, int j, const SAcc<T>& a, int) {
-    const T v = sign * negA<T>(a, i, j, n);
+    const T v = signedA<T>(a, i, j, n, sign);
     out.at(i, j) = v;
     if (DOT) acc += (double)a(0, 0) * (double)v;
   });
@@ -83,11 +83,10 @@ __global__ void __launch_bounds__(kThreads) k_apply(Grid<const T> u, Grid<T> out
 template <typename T>
 cudaError_t launch_apply(Grid<const T> u, Grid<T> out, int n, int sign, ReduceBuf rb,
                          double* dot_out, cudaStream_t s) {
-  // the kernel writes s * (-A u); out = sign * A u needs s = -sign
   if (dot_out)
-    k_apply<T, true><<<tile_grid(n), kThreads, 0, s>>>(u, out, n, T(-sign), rb, dot_out);
+    k_apply<T, true><<<tile_grid(n), kThreads, 0, s>>>(u, out, n, sign, rb, dot_out);
   else
-    k_apply<T, false><<<tile_grid(n), kThreads, 0, s>>>(u, out, n, T(-sign), rb, nullptr);
+    k_apply<T, false><<<tile_grid(n), kThreads, 0, s>>>(u, out, n, sign, rb, nullptr);
   return cudaGetLastError();
 }
 
@@ -105,7 +104,7 @@ struct ResFin {
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-    k_residual(Grid<const T> x, Grid<const T> b, Grid<T> r, Grid<float> rlo, int n, T opsign,
+    k_residual(Grid<const T> x, Grid<const T> b, Grid<T> r, Grid<float> rlo, int n, int opsign,
                ResFin rf, ReduceBuf rb) {
   __shared__ T s[kSmemPts];
   __shared__ T sb[kIntPts];
@@ -117,7 +116,7 @@ __global__ void __launch_bounds__(kThreads)
   __syncthreads();
   double acc = 0.0;
   for_tile_points(s, t, [&](int i, int j, const SAcc<T>& a, int k) {
-    const T rv = sb[k] + opsign * negA<T>(a, i, j, n);
+    const T rv = sb[k] + signedA<T>(a, i, j, n, -opsign);
     r.at(i, j) = rv;
     if (rlo.p) rlo.at(i, j) = (float)rv;
     acc += (double)rv * (double)rv;
@@ -150,7 +149,7 @@ cudaError_t launch_residual(Grid<const T> x, Grid<const T> b, Grid<T> r, Grid<fl
                             double reltol, int plain, double* out2, ReduceBuf rb,
                             cudaStream_t s) {
   ResFin rf{st, norms, abstol, reltol, plain, out2};
-  k_residual<T><<<tile_grid(n), kThreads, 0, s>>>(x, b, r, rlo, n, T(opsign), rf, rb);
+  k_residual<T><<<tile_grid(n), kThreads, 0, s>>>(x, b, r, rlo, n, opsign, rf, rb);
   return cudaGetLastError();
 }
 
@@ -159,7 +158,7 @@ cudaError_t launch_residual(Grid<const T> x, Grid<const T> b, Grid<T> r, Grid<fl
 // ---------------------------------------------------------------------------
 template <typename T, typename Tz>
 __global__ void __launch_bounds__(kThreads)
-    k_cg_dir(Grid<const Tz> z, Grid<const T> pold, Grid<T> pnew, Grid<T> Ap, int n, T opsign,
+    k_cg_dir(Grid<const Tz> z, Grid<const T> pold, Grid<T> pnew, Grid<T> Ap, int n, int opsign,
              SolveState* st, ReduceBuf rb) {
   if (st->done) return;
   __shared__ T s[kSmemPts];
@@ -188,7 +187,7 @@ __global__ void __launch_bounds__(kThreads)
   double acc = 0.0;
   for_tile_points(s, t, [&](int i, int j, const SAcc<T>& a, int) {
     const T pv = a(0, 0);
-    const T ap = -opsign * negA<T>(a, i, j, n);
+    const T ap = signedA<T>(a, i, j, n, opsign);
     pnew.at(i, j) = pv;
     Ap.at(i, j) = ap;
     acc += (double)pv * (double)ap;
@@ -205,7 +204,7 @@ __global__ void __launch_bounds__(kThreads)
 template <typename T, typename Tz>
 cudaError_t launch_cg_dir(Grid<const Tz> z, Grid<const T> pold, Grid<T> pnew, Grid<T> Ap, int n,
                           int opsign, SolveState* st, ReduceBuf rb, cudaStream_t s) {
-  k_cg_dir<T, Tz><<<tile_grid(n), kThreads, 0, s>>>(z, pold, pnew, Ap, n, T(opsign), st, rb);
+  k_cg_dir<T, Tz><<<tile_grid(n), kThreads, 0, s>>>(z, pold, pnew, Ap, n, opsign, st, rb);
   return cudaGetLastError();
 }
 
@@ -313,6 +312,7 @@ __global__ void __launch_bounds__(kThreads)
   int I0 = 0, J0 = 0;
   if (FIELD == kFieldZero) {
     stage_tile_async(s, t, b, n);
+    if (need_b) stage_interior_async(sb, t, b, n);
   } else {
     stage_tile_async(s, t, vin, n);
     if (need_b) stage_interior_async(sb, t, b, n);
@@ -330,26 +330,21 @@ __global__ void __launch_bounds__(kThreads)
   if (FIELD == kFieldProlong) {
     transform_staged(s, t, n, [&](int i, int j, T& v) { v += prolong_smem<EP>(se, I0, J0, i, j); });
     __syncthreads();
+  } else if (FIELD == kFieldZero) {
+    // first sweep from zero, once per staged point: v1 = omega D^-1 b
+    transform_staged(s, t, n, [&](int i, int j, T& v) {
+      v *= jac ? omega * inv_diagA<T>(i, j, n) : omega;
+    });
+    __syncthreads();
   }
   double acc = 0.0;
-  constexpr int SI = TileT::SI;
   for_tile_points(s, t, [&](int i, int j, const SAcc<T>& a, int k) {
-    T f, na;
-    T bb = T(0);
-    if (FIELD == kFieldZero) {
-      SAccZero<T> z{a.s, SI, i, j, n, omega, jac};
-      f = z(0, 0);
-      bb = a(0, 0);
-      na = (EPI == kEpiSweep) ? negA<T>(z, i, j, n) : T(0);
-    } else {
-      f = a(0, 0);
-      if (need_b) bb = sb[k];
-      na = (EPI == kEpiSweep) ? negA<T>(a, i, j, n) : T(0);
-    }
+    const T f = a(0, 0);
+    const T bb = need_b ? sb[k] : T(0);
     T vn = f;
     if (EPI == kEpiSweep) {
       const T m = jac ? omega * inv_diagA<T>(i, j, n) : omega;
-      vn = f + m * (bb + na);
+      vn = fma(m, bb + negA<T>(a, i, j, n), f);
     }
     vout.at(i, j) = vn;
     if (DOT) acc += (double)bb * (double)vn;
@@ -446,10 +441,10 @@ __global__ void __launch_bounds__(kThreads)
       T acc = T(0);
 #pragma unroll
       for (int bj = -1; bj <= 1; ++bj) {
-        const T wj = T(restrict_w1(kind, J, nc, bj));
+        const T wj = restrict_w1<T>(kind, J, nc, bj);
 #pragma unroll
         for (int ai = -1; ai <= 1; ++ai) {
-          const T wi = T(restrict_w1(kind, I, nc, ai));
+          const T wi = restrict_w1<T>(kind, I, nc, ai);
           acc += wi * wj * sr[(2 * c + 1 + bj) * RRI + (2 * r + 1 + ai)];
         }
       }

@@ -240,19 +240,4 @@ __device__ __forceinline__ T prolong_smem(const T* se, int I0, int J0, int i, in
   return v * scale;
 }
 
-// Accessor for the first smoothing sweep from v = 0: the field is
-// omega * D^-1 * b (Jacobi) or omega * b (Richardson), formed from the staged
-// b at each neighbour the stencil reads.
-template <typename T>
-struct SAccZero {
-  const T* s;
-  int si, i, j, n;
-  T omega;
-  bool jac;
-  __device__ __forceinline__ T operator()(int di, int dj) const {
-    const T v = s[dj * si + di] * omega;
-    return jac ? v * inv_diagA<T>(i + di, j + dj, n) : v;
-  }
-};
-
 }  // namespace sbp
