@@ -552,6 +552,7 @@ int sbp_solver_create(sbp_solver** out, int n, const sbp_options* opts) {
   std::unique_ptr<sbp_solver, int (*)(sbp_solver*)> guard(s, sbp_solver_destroy);
   s->n = n;
   SBP_CUDA(cudaGetDevice(&s->device));
+  SBP_CUDA(prepare_kernels());
   if (opts) {
     s->mg = true;
     s->opts = *opts;

@@ -12,7 +12,7 @@ namespace sbp {
 
 // Output tile of the stencil kernels: 64 points along the contiguous index
 // i (two 256-byte FP64 rows per warp pass) by 32 along j.  The staged tile
-// with halo is at most 67 x 37 = 19.8 KB in FP64.
+// with halo is at most 67 x 37 points.
 constexpr int TI = 64;
 constexpr int TJ = 32;
 using TileT = Tile<TI, TJ>;
@@ -33,8 +33,12 @@ constexpr int RRJ = RVJ - 2;
 // Coarse dense solve: rows of Ainv per warp.
 constexpr int kGemvRowsPerWarp = 2;
 
-// Flat (pointwise) kernels: CTAs per launch cap (152 SMs x 8).
+// Flat (pointwise) kernels: CTAs per launch cap.
 constexpr int kFlatCtas = 1216;
+// Upper bound on the CTAs of a persistent launch (SMs x resident CTAs).
+constexpr int kMaxPersistCtas = 4096;
+
+__host__ __device__ constexpr int align16(int b) { return (b + 15) & ~15; }
 
 static inline dim3 tile_grid(int n) { return dim3(ntiles(n, TI), ntiles(n, TJ)); }
 
@@ -45,7 +49,19 @@ static inline int flat_grid(long long N, int per) {
 
 int max_reduce_ctas(int n) {
   const dim3 g = tile_grid(n);
-  return std::max((int)(g.x * g.y), kFlatCtas);
+  return std::max((int)(g.x * g.y), kMaxPersistCtas);
+}
+
+static int sm_count() {
+  static int cache[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+  if (cache[dev] == 0) {
+    int c = 0;
+    cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev);
+    cache[dev] = c > 0 ? c : 152;
+  }
+  return cache[dev];
 }
 
 // Visit the points of a tile without shared memory (pointwise 2D kernels).
@@ -59,35 +75,113 @@ __device__ __forceinline__ void for_points(const TileT& t, Fn&& fn) {
     for (int r = lane; r < mi; r += 32) fn(t.i_lo + r, t.j_lo + c);
 }
 
+template <int A, int B>
+__device__ __forceinline__ Tile<A, B> tile_at(int id, int ntx, int n) {
+  Tile<A, B> t;
+  t.init(id % ntx, id / ntx, n);
+  return t;
+}
+
 // ---------------------------------------------------------------------------
-// Operator apply: out = sign * (-A) u, optional fused dot u.out.
+// Persistent, double-buffered tile pipeline.  A CTA walks tiles blockIdx.x,
+// blockIdx.x + gridDim.x, ...; while it computes tile k from one shared
+// buffer, cp.async is already fetching tile k+1 into the other, so HBM
+// latency overlaps compute instead of stalling every tile.  The grid is one
+// wave (SMs x resident CTAs), so neighbouring CTAs work on neighbouring tiles
+// and halo re-reads hit L2.
+//
+// A Job provides: kStage (bytes of one buffer), kReduce, Acc (accumulator),
+// prepare() (reads device state; true = skip the launch), tiles(),
+// stage(buf, tile), compute(buf, tile, acc) and finish(total).
+// ---------------------------------------------------------------------------
+template <class Job>
+__global__ void __launch_bounds__(kThreads) k_persist(const Job job_in) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  Job job = job_in;
+  if (job.prepare()) return;
+  const int total = job.tiles();
+  unsigned char* const buf0 = smem;
+  unsigned char* const buf1 = smem + Job::kStage;
+  typename Job::Acc acc;
+  int tile = blockIdx.x;
+  if (tile < total) job.stage(buf0, tile);
+  cp_async_commit();
+  for (int k = 0; tile < total; ++k, tile += gridDim.x) {
+    const int next = tile + gridDim.x;
+    if (next < total) job.stage((k & 1) ? buf0 : buf1, next);
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();
+    job.compute((k & 1) ? buf1 : buf0, tile, acc);
+    __syncthreads();
+  }
+  cp_async_wait<0>();
+  if (Job::kReduce) grid_reduce(acc.value(), job.rb, [&](double tot) { job.finish(tot); });
+}
+
+template <class Job>
+static int persist_ctas_per_sm() {
+  static const int v = [] {
+    const int smem = 2 * Job::kStage;
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute(k_persist<Job>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_persist<Job>, kThreads, smem) !=
+            cudaSuccess ||
+        b < 1)
+      b = 1;
+    return b;
+  }();
+  return v;
+}
+
+template <class Job>
+static cudaError_t launch_persist(const Job& job, int total, cudaStream_t s) {
+  const int cap = std::min(kMaxPersistCtas, sm_count() * persist_ctas_per_sm<Job>());
+  const int grid = std::max(1, std::min(total, cap));
+  k_persist<Job><<<grid, kThreads, 2 * Job::kStage, s>>>(job);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Operator apply: out = sign * A u, optional fused dot u.out.
 // ---------------------------------------------------------------------------
 template <typename T, bool DOT>
-__global__ void __launch_bounds__(kThreads) k_apply(Grid<const T> u, Grid<T> out, int n, int sign,
-                                                    ReduceBuf rb, double* dot_out) {
-  __shared__ T s[kSmemPts];
-  TileT t;
-  t.init(blockIdx.x, blockIdx.y, n);
-  stage_tile_async(s, t, u, n);
-  cp_async_wait_all();
-  __syncthreads();
-  double acc = 0.0;
-  for_tile_points(s, t, [&](int i, int j, const SAcc<T>& a, int) {
-    const T v = signedA<T>(a, i, j, n, sign);
-    out.at(i, j) = v;
-    if (DOT) acc += (double)a(0, 0) * (double)v;
-  });
-  if (DOT) grid_reduce(acc, rb, [&](double tot) { *dot_out = tot; });
-}
+struct ApplyJob {
+  static constexpr int kStage = align16(sizeof(T) * kSmemPts);
+  static constexpr bool kReduce = DOT;
+  using Acc = DotAcc<T>;
+  Grid<const T> u;
+  Grid<T> out;
+  int n, ntx, ntot, sign;
+  ReduceBuf rb;
+  double* dot_out;
+  __device__ bool prepare() { return false; }
+  __device__ int tiles() const { return ntot; }
+  __device__ void stage(unsigned char* buf, int id) const {
+    stage_tile_async(reinterpret_cast<T*>(buf), tile_at<TI, TJ>(id, ntx, n), u, n);
+  }
+  __device__ void compute(unsigned char* buf, int id, Acc& acc) const {
+    const TileT t = tile_at<TI, TJ>(id, ntx, n);
+    for_tile_points(reinterpret_cast<T*>(buf), t, [&](int i, int j, const SAcc<T>& a, int) {
+      const T v = signedA<T>(a, i, j, n, sign);
+      out.at(i, j) = v;
+      if (DOT) acc.add_prod(a(0, 0), v);
+    });
+  }
+  __device__ void finish(double tot) const { *dot_out = tot; }
+};
 
 template <typename T>
 cudaError_t launch_apply(Grid<const T> u, Grid<T> out, int n, int sign, ReduceBuf rb,
                          double* dot_out, cudaStream_t s) {
+  const dim3 g = tile_grid(n);
+  const int total = (int)(g.x * g.y);
   if (dot_out)
-    k_apply<T, true><<<tile_grid(n), kThreads, 0, s>>>(u, out, n, sign, rb, dot_out);
-  else
-    k_apply<T, false><<<tile_grid(n), kThreads, 0, s>>>(u, out, n, sign, rb, nullptr);
-  return cudaGetLastError();
+    return launch_persist(ApplyJob<T, true>{u, out, n, (int)g.x, total, sign, rb, dot_out}, total,
+                          s);
+  return launch_persist(ApplyJob<T, false>{u, out, n, (int)g.x, total, sign, rb, nullptr}, total,
+                        s);
 }
 
 // ---------------------------------------------------------------------------
@@ -103,109 +197,142 @@ struct ResFin {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads)
-    k_residual(Grid<const T> x, Grid<const T> b, Grid<T> r, Grid<float> rlo, int n, int opsign,
-               ResFin rf, ReduceBuf rb) {
-  __shared__ T s[kSmemPts];
-  __shared__ T sb[kIntPts];
-  TileT t;
-  t.init(blockIdx.x, blockIdx.y, n);
-  stage_tile_async(s, t, x, n);
-  stage_interior_async(sb, t, b, n);
-  cp_async_wait_all();
-  __syncthreads();
-  double acc = 0.0;
-  for_tile_points(s, t, [&](int i, int j, const SAcc<T>& a, int k) {
-    const T rv = sb[k] + signedA<T>(a, i, j, n, -opsign);
-    r.at(i, j) = rv;
-    if (rlo.p) rlo.at(i, j) = (float)rv;
-    acc += (double)rv * (double)rv;
-  });
-  grid_reduce(acc, rb, [&](double tot) {
+struct ResidualJob {
+  static constexpr int kStage = align16(sizeof(T) * (kSmemPts + kIntPts));
+  static constexpr bool kReduce = true;
+  using Acc = DotAcc<double>;
+  Grid<const T> x, b;
+  Grid<T> r;
+  Grid<float> rlo;
+  int n, ntx, ntot, opsign;
+  ResFin rf;
+  ReduceBuf rb;
+  __device__ bool prepare() { return false; }
+  __device__ int tiles() const { return ntot; }
+  __device__ void stage(unsigned char* buf, int id) const {
+    const TileT t = tile_at<TI, TJ>(id, ntx, n);
+    T* s = reinterpret_cast<T*>(buf);
+    stage_tile_async(s, t, x, n);
+    stage_interior_async(s + kSmemPts, t, b, n);
+  }
+  __device__ void compute(unsigned char* buf, int id, Acc& acc) const {
+    const TileT t = tile_at<TI, TJ>(id, ntx, n);
+    const T* s = reinterpret_cast<const T*>(buf);
+    const T* sb = s + kSmemPts;
+    for_tile_points(s, t, [&](int i, int j, const SAcc<T>& a, int k) {
+      const T rv = sb[k] + signedA<T>(a, i, j, n, -opsign);
+      r.at(i, j) = rv;
+      if (rlo.p) rlo.at(i, j) = convert<float>(rv);
+      acc.add_prod((double)rv, (double)rv);
+    });
+  }
+  __device__ void finish(double tot) const {
     if (rf.out2) *rf.out2 = tot;
     SolveState* st = rf.st;
-    if (st) {
-      st->rr0 = tot;
-      st->rr = tot;
-      st->thresh2 = rf.abstol > 0.0 ? rf.abstol * rf.abstol : rf.reltol * rf.reltol * tot;
-      st->iter = 0;
-      st->beta = 0.0;
-      st->alpha = 0.0;
-      if (rf.plain) st->rz = tot;
-      if (rf.norms) rf.norms[0] = sqrt(tot);
-      if (!isfinite(tot))
-        st->done = kDoneBreakdown;
-      else if (tot < st->thresh2 || tot == 0.0)
-        st->done = kDoneConverged;
-      else
-        st->done = 0;
-    }
-  });
-}
+    if (!st) return;
+    st->rr0 = tot;
+    st->rr = tot;
+    st->thresh2 = rf.abstol > 0.0 ? rf.abstol * rf.abstol : rf.reltol * rf.reltol * tot;
+    st->iter = 0;
+    st->beta = 0.0;
+    st->alpha = 0.0;
+    if (rf.plain) st->rz = tot;
+    if (rf.norms) rf.norms[0] = sqrt(tot);
+    if (!isfinite(tot))
+      st->done = kDoneBreakdown;
+    else if (tot < st->thresh2 || tot == 0.0)
+      st->done = kDoneConverged;
+    else
+      st->done = 0;
+  }
+};
 
 template <typename T>
 cudaError_t launch_residual(Grid<const T> x, Grid<const T> b, Grid<T> r, Grid<float> rlo, int n,
                             int opsign, SolveState* st, double* norms, double abstol,
                             double reltol, int plain, double* out2, ReduceBuf rb,
                             cudaStream_t s) {
+  const dim3 g = tile_grid(n);
+  const int total = (int)(g.x * g.y);
   ResFin rf{st, norms, abstol, reltol, plain, out2};
-  k_residual<T><<<tile_grid(n), kThreads, 0, s>>>(x, b, r, rlo, n, opsign, rf, rb);
-  return cudaGetLastError();
+  return launch_persist(ResidualJob<T>{x, b, r, rlo, n, (int)g.x, total, opsign, rf, rb}, total,
+                        s);
 }
 
 // ---------------------------------------------------------------------------
 // CG direction + operator + p.Ap  (one HBM pass: reads z, p_old; writes p, Ap)
 // ---------------------------------------------------------------------------
 template <typename T, typename Tz>
-__global__ void __launch_bounds__(kThreads)
-    k_cg_dir(Grid<const Tz> z, Grid<const T> pold, Grid<T> pnew, Grid<T> Ap, int n, int opsign,
-             SolveState* st, ReduceBuf rb) {
-  if (st->done) return;
-  __shared__ T s[kSmemPts];
-  __shared__ Tz sz[kSmemPts];
-  TileT t;
-  t.init(blockIdx.x, blockIdx.y, n);
-  const bool first = (st->iter == 0);
-  const T beta = T(st->beta);
-  stage_tile_async(sz, t, z, n);
-  if (!first) stage_tile_async(s, t, pold, n);
-  cp_async_wait_all();
-  __syncthreads();
-  {
-    constexpr int SI = TileT::SI;
-    const int lane = threadIdx.x & 31;
-    const int w = threadIdx.x >> 5;
-    const int ei = t.i_hi - t.i_lo + 2;
-    const int ej = t.j_hi - t.j_lo + t.hl + t.hr;
-    for (int c = w; c < ej; c += kWarps)
-      for (int r = lane; r < ei; r += 32) {
-        const int q = c * SI + r;
-        s[q] = first ? T(sz[q]) : T(sz[q]) + beta * s[q];
-      }
+struct CgDirJob {
+  static constexpr int kOffZ = align16(sizeof(T) * kSmemPts);
+  static constexpr int kStage = kOffZ + align16(sizeof(Tz) * kSmemPts);
+  static constexpr bool kReduce = true;
+  using Acc = DotAcc<double>;
+  Grid<const Tz> z;
+  Grid<const T> pold;
+  Grid<T> pnew, Ap;
+  int n, ntx, ntot, opsign;
+  SolveState* st;
+  ReduceBuf rb;
+  bool first;
+  T beta;
+  __device__ bool prepare() {
+    if (st->done) return true;
+    first = (st->iter == 0);
+    beta = T(st->beta);
+    return false;
   }
-  __syncthreads();
-  double acc = 0.0;
-  for_tile_points(s, t, [&](int i, int j, const SAcc<T>& a, int) {
-    const T pv = a(0, 0);
-    const T ap = signedA<T>(a, i, j, n, opsign);
-    pnew.at(i, j) = pv;
-    Ap.at(i, j) = ap;
-    acc += (double)pv * (double)ap;
-  });
-  grid_reduce(acc, rb, [&](double tot) {
+  __device__ int tiles() const { return ntot; }
+  __device__ void stage(unsigned char* buf, int id) const {
+    const TileT t = tile_at<TI, TJ>(id, ntx, n);
+    T* s = reinterpret_cast<T*>(buf);
+    Tz* sz = reinterpret_cast<Tz*>(buf + kOffZ);
+    stage_tile_async(sz, t, z, n);
+    if (!first) stage_tile_async(s, t, pold, n);
+  }
+  __device__ void compute(unsigned char* buf, int id, Acc& acc) const {
+    const TileT t = tile_at<TI, TJ>(id, ntx, n);
+    T* s = reinterpret_cast<T*>(buf);
+    const Tz* sz = reinterpret_cast<const Tz*>(buf + kOffZ);
+    {
+      constexpr int SI = TileT::SI;
+      const int lane = threadIdx.x & 31;
+      const int w = threadIdx.x >> 5;
+      const int ei = t.i_hi - t.i_lo + 2;
+      const int ej = t.j_hi - t.j_lo + t.hl + t.hr;
+      for (int c = w; c < ej; c += kWarps)
+        for (int r = lane; r < ei; r += 32) {
+          const int q = c * SI + r;
+          const T zz = convert<T>(sz[q]);
+          s[q] = first ? zz : fma(beta, s[q], zz);
+        }
+    }
+    __syncthreads();
+    for_tile_points(s, t, [&](int i, int j, const SAcc<T>& a, int) {
+      const T pv = a(0, 0);
+      const T ap = signedA<T>(a, i, j, n, opsign);
+      pnew.at(i, j) = pv;
+      Ap.at(i, j) = ap;
+      acc.add_prod(pv, ap);
+    });
+  }
+  __device__ void finish(double tot) const {
     st->pAp = tot;
     if (!isfinite(tot) || tot == 0.0)
       st->done = kDoneBreakdown;
     else
       st->alpha = st->rz / tot;
-  });
-}
+  }
+};
 
 template <typename T, typename Tz>
 cudaError_t launch_cg_dir(Grid<const Tz> z, Grid<const T> pold, Grid<T> pnew, Grid<T> Ap, int n,
                           int opsign, SolveState* st, ReduceBuf rb, cudaStream_t s) {
-  k_cg_dir<T, Tz><<<tile_grid(n), kThreads, 0, s>>>(z, pold, pnew, Ap, n, opsign, st, rb);
-  return cudaGetLastError();
+  const dim3 g = tile_grid(n);
+  const int total = (int)(g.x * g.y);
+  return launch_persist(
+      CgDirJob<T, Tz>{z, pold, pnew, Ap, n, (int)g.x, total, opsign, st, rb, false, T(0)}, total,
+      s);
 }
 
 // ---------------------------------------------------------------------------
@@ -214,9 +341,9 @@ cudaError_t launch_cg_dir(Grid<const Tz> z, Grid<const T> pold, Grid<T> pnew, Gr
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void cg_update_pt(double& x, double& r, double p, double ap,
                                              double alpha, double& acc) {
-  x += alpha * p;
-  r -= alpha * ap;
-  acc += r * r;
+  x = fma(alpha, p, x);
+  r = fma(-alpha, ap, r);
+  acc = fma(r, r, acc);
 }
 
 template <bool VEC>
@@ -246,7 +373,7 @@ __global__ void __launch_bounds__(kThreads)
       cg_update_pt(xv.y, rv.y, pv.y, av.y, alpha, acc);
       x2[k] = xv;
       r2[k] = rv;
-      if (rlo) reinterpret_cast<float2*>(rlo)[k] = make_float2((float)rv.x, (float)rv.y);
+      if (rlo) reinterpret_cast<float2*>(rlo)[k] = make_float2(f64_to_f32(rv.x), f64_to_f32(rv.y));
     }
     done_to = 2 * nv;
   }
@@ -255,7 +382,7 @@ __global__ void __launch_bounds__(kThreads)
     cg_update_pt(xv, rv, p[k], Ap[k], alpha, acc);
     x[k] = xv;
     r[k] = rv;
-    if (rlo) rlo[k] = (float)rv;
+    if (rlo) rlo[k] = f64_to_f32(rv);
   }
   grid_reduce(acc, rb, [&](double tot) {
     const int it = st->iter + 1;
@@ -298,81 +425,90 @@ cudaError_t launch_cg_update(Grid<T> x, Grid<T> r, Grid<const T> p, Grid<const T
 // Smoothing pass (Jacobi / Richardson) with the field variants.
 // ---------------------------------------------------------------------------
 template <typename T, int FIELD, int EPI, bool DOT>
-__global__ void __launch_bounds__(kThreads)
-    k_smooth(Grid<const T> vin, Grid<const T> e, Grid<const T> b, Grid<T> vout, int n,
-             int smoother, T omega, SolveState* st, ReduceBuf rb) {
-  if (st && st->done) return;
-  __shared__ T s[kSmemPts];
-  __shared__ T sb[kIntPts];
-  __shared__ T se[FIELD == kFieldProlong ? EP * EJ : 1];
-  TileT t;
-  t.init(blockIdx.x, blockIdx.y, n);
-  const bool jac = (smoother == kSmoothJacobi);
-  const bool need_b = (EPI == kEpiSweep) || DOT;
-  int I0 = 0, J0 = 0;
-  if (FIELD == kFieldZero) {
-    stage_tile_async(s, t, b, n);
-    if (need_b) stage_interior_async(sb, t, b, n);
-  } else {
-    stage_tile_async(s, t, vin, n);
-    if (need_b) stage_interior_async(sb, t, b, n);
-  }
-  if (FIELD == kFieldProlong) {
-    const int nc = (n + 1) / 2;
-    I0 = (t.i_lo - 1) >> 1;
-    J0 = (t.j_lo - t.hl) >> 1;
-    const int ei = (t.i_hi >> 1) - I0 + 2;
-    const int ej = ((t.j_hi + t.hr - 1) >> 1) - J0 + 2;
-    stage_async<EP>(se, e, I0, J0, ei, ej, nc);
-  }
-  cp_async_wait_all();
-  __syncthreads();
-  if (FIELD == kFieldProlong) {
-    transform_staged(s, t, n, [&](int i, int j, T& v) { v += prolong_smem<EP>(se, I0, J0, i, j); });
-    __syncthreads();
-  } else if (FIELD == kFieldZero) {
-    // first sweep from zero, once per staged point: v1 = omega D^-1 b
-    transform_staged(s, t, n, [&](int i, int j, T& v) {
-      v *= jac ? omega * inv_diagA<T>(i, j, n) : omega;
-    });
-    __syncthreads();
-  }
-  double acc = 0.0;
-  for_tile_points(s, t, [&](int i, int j, const SAcc<T>& a, int k) {
-    const T f = a(0, 0);
-    const T bb = need_b ? sb[k] : T(0);
-    T vn = f;
-    if (EPI == kEpiSweep) {
-      const T m = jac ? omega * inv_diagA<T>(i, j, n) : omega;
-      vn = fma(m, bb + negA<T>(a, i, j, n), f);
+struct SmoothJob {
+  static constexpr bool kNeedB = (EPI == kEpiSweep) || DOT;
+  static constexpr int kOffB = align16(sizeof(T) * kSmemPts);
+  static constexpr int kOffE = kOffB + (kNeedB ? align16(sizeof(T) * kIntPts) : 0);
+  static constexpr int kStage = kOffE + (FIELD == kFieldProlong ? align16(sizeof(T) * EP * EJ) : 0);
+  static constexpr bool kReduce = DOT;
+  using Acc = DotAcc<T>;
+  Grid<const T> vin, e, b;
+  Grid<T> vout;
+  int n, ntx, ntot, smoother;
+  T omega;
+  SolveState* st;
+  ReduceBuf rb;
+  __device__ bool prepare() { return st && st->done; }
+  __device__ int tiles() const { return ntot; }
+  __device__ void stage(unsigned char* buf, int id) const {
+    const TileT t = tile_at<TI, TJ>(id, ntx, n);
+    T* s = reinterpret_cast<T*>(buf);
+    stage_tile_async(s, t, FIELD == kFieldZero ? b : vin, n);
+    if (kNeedB) stage_interior_async(reinterpret_cast<T*>(buf + kOffB), t, b, n);
+    if (FIELD == kFieldProlong) {
+      const int nc = (n + 1) / 2;
+      const int I0 = (t.i_lo - 1) >> 1;
+      const int J0 = (t.j_lo - t.hl) >> 1;
+      const int ei = (t.i_hi >> 1) - I0 + 2;
+      const int ej = ((t.j_hi + t.hr - 1) >> 1) - J0 + 2;
+      stage_async<EP>(reinterpret_cast<T*>(buf + kOffE), e, I0, J0, ei, ej, nc);
     }
-    vout.at(i, j) = vn;
-    if (DOT) acc += (double)bb * (double)vn;
-  });
-  if (DOT) {
-    grid_reduce(acc, rb, [&](double tot) {
-      if (!isfinite(tot)) {
-        st->done = kDoneBreakdown;
-      } else {
-        st->rz_new = tot;
-        if (st->iter > 0) st->beta = tot / st->rz;
-        st->rz = tot;
+  }
+  __device__ void compute(unsigned char* buf, int id, Acc& acc) const {
+    const TileT t = tile_at<TI, TJ>(id, ntx, n);
+    T* s = reinterpret_cast<T*>(buf);
+    const T* sb = reinterpret_cast<const T*>(buf + kOffB);
+    const bool jac = (smoother == kSmoothJacobi);
+    if (FIELD == kFieldProlong) {
+      const T* se = reinterpret_cast<const T*>(buf + kOffE);
+      const int I0 = (t.i_lo - 1) >> 1;
+      const int J0 = (t.j_lo - t.hl) >> 1;
+      transform_staged(s, t, n,
+                       [&](int i, int j, T& v) { v += prolong_smem<EP>(se, I0, J0, i, j); });
+      __syncthreads();
+    } else if (FIELD == kFieldZero) {
+      // first sweep from zero, once per staged point: v1 = omega D^-1 b
+      transform_staged(s, t, n, [&](int i, int j, T& v) {
+        v *= jac ? omega * inv_diagA<T>(i, j, n) : omega;
+      });
+      __syncthreads();
+    }
+    for_tile_points(s, t, [&](int i, int j, const SAcc<T>& a, int k) {
+      const T f = a(0, 0);
+      const T bb = kNeedB ? sb[k] : T(0);
+      T vn = f;
+      if (EPI == kEpiSweep) {
+        const T m = jac ? omega * inv_diagA<T>(i, j, n) : omega;
+        vn = fma(m, bb + negA<T>(a, i, j, n), f);
       }
+      vout.at(i, j) = vn;
+      if (DOT) acc.add_prod(bb, vn);
     });
   }
-}
+  __device__ void finish(double tot) const {
+    if (!isfinite(tot)) {
+      st->done = kDoneBreakdown;
+    } else {
+      st->rz_new = tot;
+      if (st->iter > 0) st->beta = tot / st->rz;
+      st->rz = tot;
+    }
+  }
+};
 
 template <typename T, int FIELD, int EPI>
 static cudaError_t launch_smooth_fe(Grid<const T> vin, Grid<const T> e, Grid<const T> b,
                                     Grid<T> vout, int n, int smoother, double omega, int dot,
                                     SolveState* st, ReduceBuf rb, cudaStream_t s) {
+  const dim3 g = tile_grid(n);
+  const int total = (int)(g.x * g.y);
   if (dot)
-    k_smooth<T, FIELD, EPI, true><<<tile_grid(n), kThreads, 0, s>>>(vin, e, b, vout, n, smoother,
-                                                                    T(omega), st, rb);
-  else
-    k_smooth<T, FIELD, EPI, false><<<tile_grid(n), kThreads, 0, s>>>(vin, e, b, vout, n, smoother,
-                                                                     T(omega), st, rb);
-  return cudaGetLastError();
+    return launch_persist(SmoothJob<T, FIELD, EPI, true>{vin, e, b, vout, n, (int)g.x, total,
+                                                         smoother, T(omega), st, rb},
+                          total, s);
+  return launch_persist(SmoothJob<T, FIELD, EPI, false>{vin, e, b, vout, n, (int)g.x, total,
+                                                        smoother, T(omega), st, rb},
+                        total, s);
 }
 
 template <typename T>
@@ -400,65 +536,108 @@ cudaError_t launch_smooth(int field, int epi, Grid<const T> vin, Grid<const T> e
 // restriction weights.  One HBM pass over v and b, a quarter-size write.
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(kThreads)
-    k_resrestrict(Grid<const T> v, Grid<const T> b, Grid<T> f, int nf, int kind,
-                  const SolveState* st) {
-  if (st && st->done) return;
-  __shared__ T sv[RVI * RVJ];
-  __shared__ T sr[RRI * RRJ];
-  const int nc = (nf + 1) / 2;
-  Tile<RTI, RTJ> t;
-  t.init(blockIdx.x, blockIdx.y, nc);
-  const int m = t.i_hi - t.i_lo;
-  const int mp = t.j_hi - t.j_lo;
-  const int ri0 = 2 * t.i_lo - 1;
-  const int rj0 = 2 * t.j_lo - 1;
-  const int rei = 2 * m + 1;
-  const int rej = 2 * mp + 1;
-  stage_async<RRI>(sr, b, ri0, rj0, rei, rej, nf);
-  if (v.p) stage_async<RVI>(sv, v, ri0 - 1, rj0 - 1, rei + 2, rej + 2, nf);
-  cp_async_wait_all();
-  __syncthreads();
-  const int lane = threadIdx.x & 31;
-  const int w = threadIdx.x >> 5;
-  if (v.p) {
-    for (int c = w; c < rej; c += kWarps) {
-      const int j = rj0 + c;
-      if (j < 0 || j >= nf) continue;
-      for (int r = lane; r < rei; r += 32) {
-        const int i = ri0 + r;
-        if (i < 0 || i >= nf) continue;
-        SAcc<T> a{sv + (c + 1) * RVI + (r + 1), RVI};
-        sr[c * RRI + r] += negA<T>(a, i, j, nf);
-      }
-    }
-    __syncthreads();
+struct ResRestrictJob {
+  static constexpr int kOffV = align16(sizeof(T) * RRI * RRJ);
+  static constexpr int kStage = kOffV + align16(sizeof(T) * RVI * RVJ);
+  static constexpr bool kReduce = false;
+  using Acc = DotAcc<double>;
+  Grid<const T> v, b;
+  Grid<T> f;
+  int nf, nc, ntx, ntot, kind;
+  const SolveState* st;
+  ReduceBuf rb;
+  __device__ bool prepare() { return st && st->done; }
+  __device__ int tiles() const { return ntot; }
+  __device__ void stage(unsigned char* buf, int id) const {
+    const Tile<RTI, RTJ> t = tile_at<RTI, RTJ>(id, ntx, nc);
+    const int m = t.i_hi - t.i_lo, mp = t.j_hi - t.j_lo;
+    const int ri0 = 2 * t.i_lo - 1, rj0 = 2 * t.j_lo - 1;
+    stage_async<RRI>(reinterpret_cast<T*>(buf), b, ri0, rj0, 2 * m + 1, 2 * mp + 1, nf);
+    if (v.p)
+      stage_async<RVI>(reinterpret_cast<T*>(buf + kOffV), v, ri0 - 1, rj0 - 1, 2 * m + 3,
+                       2 * mp + 3, nf);
   }
-  for (int c = w; c < mp; c += kWarps) {
-    const int J = t.j_lo + c;
-    for (int r = lane; r < m; r += 32) {
-      const int I = t.i_lo + r;
-      T acc = T(0);
-#pragma unroll
-      for (int bj = -1; bj <= 1; ++bj) {
-        const T wj = restrict_w1<T>(kind, J, nc, bj);
-#pragma unroll
-        for (int ai = -1; ai <= 1; ++ai) {
-          const T wi = restrict_w1<T>(kind, I, nc, ai);
-          acc += wi * wj * sr[(2 * c + 1 + bj) * RRI + (2 * r + 1 + ai)];
+  __device__ void compute(unsigned char* buf, int id, Acc&) const {
+    const Tile<RTI, RTJ> t = tile_at<RTI, RTJ>(id, ntx, nc);
+    T* sr = reinterpret_cast<T*>(buf);
+    const T* sv = reinterpret_cast<const T*>(buf + kOffV);
+    const int m = t.i_hi - t.i_lo, mp = t.j_hi - t.j_lo;
+    const int ri0 = 2 * t.i_lo - 1, rj0 = 2 * t.j_lo - 1;
+    const int rei = 2 * m + 1, rej = 2 * mp + 1;
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    if (v.p) {
+      for (int c = w; c < rej; c += kWarps) {
+        const int j = rj0 + c;
+        if (j < 0 || j >= nf) continue;
+        for (int r = lane; r < rei; r += 32) {
+          const int i = ri0 + r;
+          if (i < 0 || i >= nf) continue;
+          SAcc<T> a{sv + (c + 1) * RVI + (r + 1), RVI};
+          sr[c * RRI + r] += negA<T>(a, i, j, nf);
         }
       }
-      f.at(I, J) = acc;
+      __syncthreads();
+    }
+    for (int c = w; c < mp; c += kWarps) {
+      const int J = t.j_lo + c;
+      for (int r = lane; r < m; r += 32) {
+        const int I = t.i_lo + r;
+        T acc = T(0);
+#pragma unroll
+        for (int bj = -1; bj <= 1; ++bj) {
+          const T wj = restrict_w1<T>(kind, J, nc, bj);
+#pragma unroll
+          for (int ai = -1; ai <= 1; ++ai) {
+            const T wi = restrict_w1<T>(kind, I, nc, ai);
+            acc = fma(wi * wj, sr[(2 * c + 1 + bj) * RRI + (2 * r + 1 + ai)], acc);
+          }
+        }
+        f.at(I, J) = acc;
+      }
     }
   }
-}
+  __device__ void finish(double) const {}
+};
 
 template <typename T>
 cudaError_t launch_resrestrict(Grid<const T> v, Grid<const T> b, Grid<T> f, int nf, int kind,
                                const SolveState* st, cudaStream_t s) {
   const int nc = (nf + 1) / 2;
-  const dim3 g(ntiles(nc, RTI), ntiles(nc, RTJ));
-  k_resrestrict<T><<<g, kThreads, 0, s>>>(v, b, f, nf, kind, st);
+  const int ntx = ntiles(nc, RTI), nty = ntiles(nc, RTJ);
+  const int total = ntx * nty;
+  return launch_persist(ResRestrictJob<T>{v, b, f, nf, nc, ntx, total, kind, st, ReduceBuf{}},
+                        total, s);
+}
+
+// Resolve the launch configuration of every persistent kernel up front
+// (shared-memory attribute and occupancy), outside any stream capture.
+template <typename T>
+static void prepare_precision() {
+  persist_ctas_per_sm<ApplyJob<T, false>>();
+  persist_ctas_per_sm<ApplyJob<T, true>>();
+  persist_ctas_per_sm<ResidualJob<T>>();
+  persist_ctas_per_sm<ResRestrictJob<T>>();
+  persist_ctas_per_sm<SmoothJob<T, kFieldPlain, kEpiSweep, false>>();
+  persist_ctas_per_sm<SmoothJob<T, kFieldPlain, kEpiSweep, true>>();
+  persist_ctas_per_sm<SmoothJob<T, kFieldPlain, kEpiStore, false>>();
+  persist_ctas_per_sm<SmoothJob<T, kFieldPlain, kEpiStore, true>>();
+  persist_ctas_per_sm<SmoothJob<T, kFieldZero, kEpiSweep, false>>();
+  persist_ctas_per_sm<SmoothJob<T, kFieldZero, kEpiSweep, true>>();
+  persist_ctas_per_sm<SmoothJob<T, kFieldZero, kEpiStore, false>>();
+  persist_ctas_per_sm<SmoothJob<T, kFieldZero, kEpiStore, true>>();
+  persist_ctas_per_sm<SmoothJob<T, kFieldProlong, kEpiSweep, false>>();
+  persist_ctas_per_sm<SmoothJob<T, kFieldProlong, kEpiSweep, true>>();
+  persist_ctas_per_sm<SmoothJob<T, kFieldProlong, kEpiStore, false>>();
+  persist_ctas_per_sm<SmoothJob<T, kFieldProlong, kEpiStore, true>>();
+}
+
+cudaError_t prepare_kernels() {
+  sm_count();
+  prepare_precision<double>();
+  prepare_precision<float>();
+  persist_ctas_per_sm<CgDirJob<double, double>>();
+  persist_ctas_per_sm<CgDirJob<double, float>>();
   return cudaGetLastError();
 }
 
@@ -498,7 +677,7 @@ __global__ void __launch_bounds__(kThreads)
   for (int k = threadIdx.x; k < N; k += kThreads) {
     const int j = k / nc;
     const int i = k - j * nc;
-    sf[k] = (double)f.at(i, j);
+    sf[k] = convert<double>(f.at(i, j));
   }
   __syncthreads();
   const int lane = threadIdx.x & 31;
@@ -515,7 +694,7 @@ __global__ void __launch_bounds__(kThreads)
     if (lane == 0) {
       const int j = row / nc;
       const int i = row - j * nc;
-      e.at(i, j) = (T)acc;
+      e.at(i, j) = convert<T>(acc);
     }
   }
 }

@@ -81,6 +81,88 @@ __device__ __forceinline__ void cp_async_elem(float* sdst, const float* gsrc) {
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;\n" ::: "memory");
 }
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+// Wait until at most N of this thread's committed groups are still pending.
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// ---------------------------------------------------------------------------
+// float <-> double with integer instructions only.  On GB300 the FP64 pipe
+// issues about two lanes per clock per SM, and the hardware conversions run
+// there too; the solver's conversions (r -> FP32 for the V-cycle, z -> FP64
+// for the Krylov direction) are pure bit moves on the integer pipe instead.
+// Float denormals map to signed zero and double values below the float
+// normal range flush to signed zero (both far below any residual the solver
+// produces); Inf/NaN map to Inf/NaN (double -> float: to Inf).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double f32_to_f64(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned sign = u & 0x80000000u;
+  const unsigned e = (u >> 23) & 0xFFu;
+  const unsigned m = u & 0x7FFFFFu;
+  unsigned hi = sign;
+  if (e == 0xFFu)
+    hi |= 0x7FF00000u | (m >> 3);
+  else if (e != 0u)
+    hi |= ((e + 896u) << 20) | (m >> 3);
+  const unsigned lo = (e == 0u) ? 0u : (m << 29);
+  return __hiloint2double((int)hi, (int)lo);
+}
+__device__ __forceinline__ float f64_to_f32(double d) {
+  const unsigned hi = (unsigned)__double2hiint(d);
+  const unsigned lo = (unsigned)__double2loint(d);
+  const unsigned sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7FFu) - 896;           // float biased exponent
+  const unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);  // top 23 mantissa bits
+  const unsigned rnd = (lo >> 28) & 1u;                    // round half away
+  unsigned f;
+  if (e <= 0)
+    f = sign;
+  else if (e >= 255)
+    f = sign | 0x7F800000u;
+  else
+    f = sign | (((unsigned)e << 23) + m + rnd);            // a carry rounds up the exponent
+  return __uint_as_float(f);
+}
+template <typename To, typename From>
+__device__ __forceinline__ To convert(From v) { return (To)v; }
+template <>
+__device__ __forceinline__ double convert<double, float>(float v) { return f32_to_f64(v); }
+template <>
+__device__ __forceinline__ float convert<float, double>(double v) { return f64_to_f32(v); }
+
+// ---------------------------------------------------------------------------
+// Dot-product accumulators.  FP64 data: an FP64 FMA per term.  FP32 data:
+// each product is split exactly into p + e (FMA) and summed with a
+// compensated (TwoSum) float-float accumulator, converted to FP64 once per
+// thread -- FP64-quality accumulation without FP64 instructions per term.
+// ---------------------------------------------------------------------------
+template <typename T>
+struct DotAcc;
+template <>
+struct DotAcc<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add_prod(double a, double b) { s = fma(a, b, s); }
+  __device__ __forceinline__ double value() const { return s; }
+};
+template <>
+struct DotAcc<float> {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add_prod(float a, float b) {
+    const float p = a * b;
+    const float e = fmaf(a, b, -p);
+    const float s = hi + p;
+    const float bb = s - hi;
+    const float err = (hi - (s - bb)) + (p - bb);
+    hi = s;
+    lo += err + e;
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
 
 // Stage the raw values of g over [i0, i0+ei) x [j0, j0+ej) into s with row
 // pitch P; points outside the n x n domain are zero-filled.

@@ -82,6 +82,10 @@ template <typename T>
 cudaError_t launch_dot(Grid<const T> a, Grid<const T> b, int n, double* out, ReduceBuf rb,
                        cudaStream_t s);
 
+// Resolve the launch configuration of every persistent kernel on the current
+// device; call once outside stream capture (solver creation does).
+cudaError_t prepare_kernels();
+
 // Krylov state reset (iter = done = 0, maxiter) before a solve.
 cudaError_t launch_state_init(SolveState* st, int maxiter, cudaStream_t s);
 
