@@ -50,8 +50,10 @@ Grid<const T> cgrid(const void* p, int ld) {
 
 struct Level {
   int n = 0;
+  int ld = 0;               // padded leading dimension (16-byte aligned columns)
   void* b = nullptr;        // right-hand side (level 0: the solver's r or r_lo)
   void* v[2] = {nullptr, nullptr};
+  Operand ob, ov[2];        // TMA operands of b and v
   int out = 0;              // buffer holding the V-cycle result
   bool own_b = false;
 };
@@ -66,11 +68,14 @@ struct sbp_solver {
   size_t esize = 8;                 // element size of the V-cycle levels
   std::vector<Level> levels;
   double* Ainv = nullptr;
-  // Krylov vectors (FP64, ld = n)
+  // Krylov vectors (FP64, padded leading dimension ld; padding stays zero)
+  int ld = 0;
+  double* x = nullptr;              // the iterate (the caller's x is copied in and out)
   double* r = nullptr;
   double* p[2] = {nullptr, nullptr};
   double* Ap = nullptr;
   float* r_lo = nullptr;            // FP32 copy of r (mixed precision)
+  Operand ox, orr, op[2], orlo;
   SolveState* st = nullptr;
   SolveState* st_host = nullptr;    // pinned, 2 slots
   double* norms = nullptr;
@@ -82,7 +87,7 @@ struct sbp_solver {
   cudaEvent_t ev[2] = {nullptr, nullptr};
   // cached iteration graphs: [kind][parity]; kind 0 = MGCG, 1 = CG
   cudaGraphExec_t iter_exec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
-  const void* iter_key_x[2] = {nullptr, nullptr};
+  bool iter_valid[2] = {false, false};
   int iter_key_sign[2] = {0, 0};
   int iter_key_maxiter[2] = {0, 0};
   // kernel launches: per captured iteration graph, and of the last solve
@@ -111,7 +116,7 @@ void destroy_graphs(sbp_solver* s) {
         cudaGraphExecDestroy(g);
         g = nullptr;
       }
-  s->iter_key_x[0] = s->iter_key_x[1] = nullptr;
+  s->iter_valid[0] = s->iter_valid[1] = false;
 }
 
 // ---------------------------------------------------------------------------
@@ -132,54 +137,45 @@ cudaError_t enqueue_vcycle(sbp_solver* s, size_t l, bool dot, SolveState* st, cu
   const int n = L.n;
   const double om = o.omega;
   const int sm = o.smoother;
+  const Operand none;
   cudaError_t e;
-  Grid<const T> b = cgrid<T>(L.b, n);
   if (l + 1 == s->levels.size()) {
     L.out = 0;
-    e = launch_coarse_gemv<T>(s->Ainv, b, grid<T>(L.v[0], n), n, st, q);
+    e = launch_coarse_gemv<T>(s->Ainv, cgrid<T>(L.b, L.ld), grid<T>(L.v[0], L.ld), n, st, q);
     if (e != cudaSuccess) return e;
     if (dot && l == 0) {
       // single-level hierarchy: still reduce b.z for the Krylov state
-      e = launch_smooth<T>(kFieldPlain, kEpiStore, cgrid<T>(L.v[0], n), Grid<const T>{nullptr, 0},
-                           b, grid<T>(L.v[1], n), n, sm, om, 1, st, s->rb, q);
+      e = launch_smooth_op<T>(kFieldPlain, kEpiStore, L.ov[0], none, L.ob, grid<T>(L.v[1], L.ld),
+                              n, sm, om, 1, st, s->rb, q);
       L.out = 1;
     }
     return e;
   }
-  int cur;
   int k;
-  if (o.nu_pre >= 2) {
-    e = launch_smooth<T>(kFieldZero, kEpiSweep, Grid<const T>{nullptr, 0},
-                         Grid<const T>{nullptr, 0}, b, grid<T>(L.v[0], n), n, sm, om, 0, st,
-                         s->rb, q);
-    k = 2;
-  } else {
-    e = launch_smooth<T>(kFieldZero, kEpiStore, Grid<const T>{nullptr, 0},
-                         Grid<const T>{nullptr, 0}, b, grid<T>(L.v[0], n), n, sm, om, 0, st,
-                         s->rb, q);
-    k = 1;
-  }
+  e = launch_smooth_op<T>(kFieldZero, o.nu_pre >= 2 ? kEpiSweep : kEpiStore, none, none, L.ob,
+                          grid<T>(L.v[0], L.ld), n, sm, om, 0, st, s->rb, q);
+  k = o.nu_pre >= 2 ? 2 : 1;
   if (e != cudaSuccess) return e;
-  cur = 0;
+  int cur = 0;
   for (; k < o.nu_pre; ++k) {
-    e = launch_smooth<T>(kFieldPlain, kEpiSweep, cgrid<T>(L.v[cur], n), Grid<const T>{nullptr, 0},
-                         b, grid<T>(L.v[1 - cur], n), n, sm, om, 0, st, s->rb, q);
+    e = launch_smooth_op<T>(kFieldPlain, kEpiSweep, L.ov[cur], none, L.ob,
+                            grid<T>(L.v[1 - cur], L.ld), n, sm, om, 0, st, s->rb, q);
     if (e != cudaSuccess) return e;
     cur = 1 - cur;
   }
   Level& C = s->levels[l + 1];
-  e = launch_resrestrict<T>(cgrid<T>(L.v[cur], n), b, grid<T>(C.b, C.n), n, o.restriction, st, q);
+  e = launch_resrestrict_op<T>(&L.ov[cur], L.ob, grid<T>(C.b, C.ld), n, o.restriction, st, q);
   if (e != cudaSuccess) return e;
   e = enqueue_vcycle<T>(s, l + 1, false, st, q);
   if (e != cudaSuccess) return e;
-  Grid<const T> ec = cgrid<T>(C.v[C.out], C.n);
+  const Operand& ec = C.ov[C.out];
   const int npost = std::max(1, o.nu_post);
   for (int pass = 0; pass < npost; ++pass) {
     const bool last = (pass == npost - 1);
     const int field = (pass == 0) ? kFieldProlong : kFieldPlain;
     const int epi = (o.nu_post == 0) ? kEpiStore : kEpiSweep;
-    e = launch_smooth<T>(field, epi, cgrid<T>(L.v[cur], n), ec, b, grid<T>(L.v[1 - cur], n), n, sm,
-                         om, (dot && last) ? 1 : 0, st, s->rb, q);
+    e = launch_smooth_op<T>(field, epi, L.ov[cur], ec, L.ob, grid<T>(L.v[1 - cur], L.ld), n, sm,
+                            om, (dot && last) ? 1 : 0, st, s->rb, q);
     if (e != cudaSuccess) return e;
     cur = 1 - cur;
   }
@@ -207,40 +203,39 @@ cudaError_t enqueue_vcycle_any(sbp_solver* s, bool dot, SolveState* st, cudaStre
   return enqueue_vcycle<double>(s, 0, dot, st, q);
 }
 
-// z pointer of the V-cycle output on level 0 (valid after a schedule has
-// been enqueued once: the schedule is static).
+// V-cycle output on level 0 (valid after a schedule has been enqueued once:
+// the schedule is static).
 const void* vcycle_out(sbp_solver* s) {
   Level& L = s->levels[0];
   return L.v[L.out];
 }
+const Operand& vcycle_out_op(sbp_solver* s) {
+  Level& L = s->levels[0];
+  return L.ov[L.out];
+}
 
 // One Krylov iteration: direction + operator + alpha, update + convergence,
 // then (MGCG) the V-cycle with the r.z / beta reduction.
-cudaError_t enqueue_iteration(sbp_solver* s, int kind, int parity, double* x, int sign,
-                              cudaStream_t q) {
-  const int n = s->n;
-  double* pold = s->p[parity];
+cudaError_t enqueue_iteration(sbp_solver* s, int kind, int parity, int sign, cudaStream_t q) {
+  const int n = s->n, ld = s->ld;
   double* pnew = s->p[1 - parity];
   cudaError_t e;
   const bool mixed = (kind == 0 && s->opts.precision == SBP_PREC_MIXED);
   if (kind == 0) {
     if (mixed)
-      e = launch_cg_dir<double, float>(cgrid<float>(vcycle_out(s), n), cgrid<double>(pold, n),
-                                       grid<double>(pnew, n), grid<double>(s->Ap, n), n, +1,
-                                       s->st, s->rb, q);
+      e = launch_cg_dir_op<double, float>(vcycle_out_op(s), s->op[parity], grid<double>(pnew, ld),
+                                          grid<double>(s->Ap, ld), n, +1, s->st, s->rb, q);
     else
-      e = launch_cg_dir<double, double>(cgrid<double>(vcycle_out(s), n), cgrid<double>(pold, n),
-                                        grid<double>(pnew, n), grid<double>(s->Ap, n), n, +1,
-                                        s->st, s->rb, q);
+      e = launch_cg_dir_op<double, double>(vcycle_out_op(s), s->op[parity], grid<double>(pnew, ld),
+                                           grid<double>(s->Ap, ld), n, +1, s->st, s->rb, q);
   } else {
-    e = launch_cg_dir<double, double>(cgrid<double>(s->r, n), cgrid<double>(pold, n),
-                                      grid<double>(pnew, n), grid<double>(s->Ap, n), n, sign,
-                                      s->st, s->rb, q);
+    e = launch_cg_dir_op<double, double>(s->orr, s->op[parity], grid<double>(pnew, ld),
+                                         grid<double>(s->Ap, ld), n, sign, s->st, s->rb, q);
   }
   if (e != cudaSuccess) return e;
-  e = launch_cg_update<double>(grid<double>(x, n), grid<double>(s->r, n), cgrid<double>(pnew, n),
-                               cgrid<double>(s->Ap, n),
-                               Grid<float>{mixed ? s->r_lo : nullptr, n}, n, kind == 1 ? 1 : 0,
+  e = launch_cg_update<double>(grid<double>(s->x, ld), grid<double>(s->r, ld),
+                               cgrid<double>(pnew, ld), cgrid<double>(s->Ap, ld),
+                               Grid<float>{mixed ? s->r_lo : nullptr, ld}, n, kind == 1 ? 1 : 0,
                                s->st, s->norms, s->rb, q);
   if (e != cudaSuccess) return e;
   if (kind == 0) e = enqueue_vcycle_any(s, true, s->st, q);
@@ -260,11 +255,11 @@ int ensure_norms(sbp_solver* s, int maxiter) {
   return SBP_OK;
 }
 
-int capture_iteration(sbp_solver* s, int kind, double* x, int sign) {
+int capture_iteration(sbp_solver* s, int kind, int sign) {
   for (int par = 0; par < 2; ++par) {
     cudaGraph_t g = nullptr;
     SBP_CUDA(cudaStreamBeginCapture(s->cap, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e = enqueue_iteration(s, kind, par, x, sign, s->cap);
+    cudaError_t e = enqueue_iteration(s, kind, par, sign, s->cap);
     cudaError_t e2 = cudaStreamEndCapture(s->cap, &g);
     if (e != cudaSuccess) {
       if (g) cudaGraphDestroy(g);
@@ -277,7 +272,7 @@ int capture_iteration(sbp_solver* s, int kind, double* x, int sign) {
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail_cuda(e, "cudaGraphInstantiate");
   }
-  s->iter_key_x[kind] = x;
+  s->iter_valid[kind] = true;
   s->iter_key_sign[kind] = sign;
   s->launches_per_iter[kind] = 2 + (kind == 0 ? vcycle_launches(s, true) : 0);
   return SBP_OK;
@@ -296,15 +291,24 @@ int run_krylov(sbp_solver* s, int kind, const double* b, double* x, int sign, do
   if (rc) return rc;
   const int n = s->n;
   const bool mixed = (kind == 0 && s->opts.precision == SBP_PREC_MIXED);
-  // set-up: state, r0 = b - sign*A*x0, z0 = M r0 and rz (MGCG)
+  const int ld = s->ld;
+  // set-up: the caller's x into the padded iterate, state, r0 = b - sign*A*x0,
+  // z0 = M r0 and rz (MGCG)
+  SBP_CUDA(cudaMemcpy2DAsync(s->x, (size_t)ld * sizeof(double), x, (size_t)n * sizeof(double),
+                             (size_t)n * sizeof(double), n, cudaMemcpyDeviceToDevice, q));
   SBP_CUDA(launch_state_init(s->st, maxiter, q));
-  SBP_CUDA(launch_residual<double>(cgrid<double>(x, n), cgrid<double>(b, n),
-                                   grid<double>(s->r, n), Grid<float>{mixed ? s->r_lo : nullptr, n},
-                                   n, sign, s->st, s->norms, abstol, reltol, kind == 1 ? 1 : 0,
-                                   nullptr, s->rb, q));
+  Operand ob;
+  ob.p = b;
+  ob.n = n;
+  ob.ld = n;
+  ob.tma = false;
+  SBP_CUDA(launch_residual_op<double>(s->ox, ob, grid<double>(s->r, ld),
+                                      Grid<float>{mixed ? s->r_lo : nullptr, ld}, n, sign, s->st,
+                                      s->norms, abstol, reltol, kind == 1 ? 1 : 0, nullptr, s->rb,
+                                      q));
   if (kind == 0) SBP_CUDA(enqueue_vcycle_any(s, true, s->st, q));
-  if (s->iter_key_x[kind] != x || s->iter_key_sign[kind] != sign || !s->iter_exec[kind][0]) {
-    rc = capture_iteration(s, kind, x, sign);
+  if (!s->iter_valid[kind] || s->iter_key_sign[kind] != sign || !s->iter_exec[kind][0]) {
+    rc = capture_iteration(s, kind, sign);
     if (rc) return rc;
   }
   // Iterate: keep one iteration queued ahead of the one being checked.
@@ -325,8 +329,14 @@ int run_krylov(sbp_solver* s, int kind, const double* b, double* x, int sign, do
     ++k;
     if (k > maxiter + 2) finished = true;  // safety net; kernels stop at maxiter
   }
+  SBP_CUDA(cudaMemcpy2DAsync(x, (size_t)n * sizeof(double), s->x, (size_t)ld * sizeof(double),
+                             (size_t)n * sizeof(double), n, cudaMemcpyDeviceToDevice, q));
   SBP_CUDA(cudaMemcpyAsync(&s->st_host[0], s->st, sizeof(SolveState), cudaMemcpyDeviceToHost, q));
   SBP_CUDA(cudaStreamSynchronize(q));
+  if (read_device_fault() != 0u) {
+    g_last_error = "a kernel's bounded wait on an asynchronous copy gave up";
+    return SBP_ERR_CUDA;
+  }
   const SolveState fs = s->st_host[0];
   s->last_launches = launches;
   const int iters = fs.iter;
@@ -566,20 +576,25 @@ int sbp_solver_create(sbp_solver** out, int n, const sbp_options* opts) {
     if (o.precision != SBP_PREC_FP64 && o.precision != SBP_PREC_MIXED) return SBP_ERR_ARGS;
     s->esize = (o.precision == SBP_PREC_MIXED) ? sizeof(float) : sizeof(double);
   }
-  const size_t nn = (size_t)n * n;
+  s->ld = padded_ld(n);
+  const size_t nn = (size_t)s->ld * n;
   int rc;
   void* p;
+  rc = dalloc(s, &p, nn * 8); if (rc) return rc; s->x = (double*)p;
   rc = dalloc(s, &p, nn * 8); if (rc) return rc; s->r = (double*)p;
   rc = dalloc(s, &p, nn * 8); if (rc) return rc; s->p[0] = (double*)p;
   rc = dalloc(s, &p, nn * 8); if (rc) return rc; s->p[1] = (double*)p;
   rc = dalloc(s, &p, nn * 8); if (rc) return rc; s->Ap = (double*)p;
+  for (double* a : {s->x, s->r, s->p[0], s->p[1], s->Ap}) SBP_CUDA(cudaMemset(a, 0, nn * 8));
+  make_operand(s->ox, s->x, n, s->ld, true);
+  make_operand(s->orr, s->r, n, s->ld, true);
+  make_operand(s->op[0], s->p[0], n, s->ld, true);
+  make_operand(s->op[1], s->p[1], n, s->ld, true);
   rc = dalloc(s, &p, sizeof(SolveState)); if (rc) return rc; s->st = (SolveState*)p;
   const size_t parts = (size_t)max_reduce_ctas(n) + 64;
   rc = dalloc(s, &p, parts * sizeof(double)); if (rc) return rc; s->rb.partials = (double*)p;
   rc = dalloc(s, &p, 64); if (rc) return rc; s->rb.ticket = (unsigned*)p;
   SBP_CUDA(cudaMemset(s->rb.ticket, 0, 64));
-  SBP_CUDA(cudaMemset(s->p[0], 0, nn * 8));
-  SBP_CUDA(cudaMemset(s->p[1], 0, nn * 8));
   SBP_CUDA(cudaMallocHost((void**)&s->st_host, 2 * sizeof(SolveState)));
   SBP_CUDA(cudaStreamCreateWithFlags(&s->cap, cudaStreamNonBlocking));
   SBP_CUDA(cudaEventCreateWithFlags(&s->ev[0], cudaEventDisableTiming));
@@ -588,24 +603,32 @@ int sbp_solver_create(sbp_solver** out, int n, const sbp_options* opts) {
   if (rc) return rc;
   if (s->mg) {
     const bool mixed = s->opts.precision == SBP_PREC_MIXED;
+    const bool f64 = !mixed;
     if (mixed) {
       rc = dalloc(s, &p, nn * sizeof(float)); if (rc) return rc; s->r_lo = (float*)p;
+      SBP_CUDA(cudaMemset(s->r_lo, 0, nn * sizeof(float)));
+      make_operand(s->orlo, s->r_lo, n, s->ld, false);
     }
     int m = n;
     while (true) {
       Level L;
       L.n = m;
-      const size_t bytes = (size_t)m * m * s->esize;
+      L.ld = padded_ld(m);
+      const size_t bytes = (size_t)L.ld * m * s->esize;
       if (s->levels.empty()) {
         L.b = mixed ? (void*)s->r_lo : (void*)s->r;
       } else {
         rc = dalloc(s, &L.b, bytes); if (rc) return rc;
+        SBP_CUDA(cudaMemset(L.b, 0, bytes));
         L.own_b = true;
       }
       rc = dalloc(s, &L.v[0], bytes); if (rc) return rc;
       rc = dalloc(s, &L.v[1], bytes); if (rc) return rc;
       SBP_CUDA(cudaMemset(L.v[0], 0, bytes));
       SBP_CUDA(cudaMemset(L.v[1], 0, bytes));
+      make_operand(L.ob, L.b, m, L.ld, f64);
+      make_operand(L.ov[0], L.v[0], m, L.ld, f64);
+      make_operand(L.ov[1], L.v[1], m, L.ld, f64);
       s->levels.push_back(L);
       if (m == s->opts.coarse_n) break;
       m = (m + 1) / 2;
@@ -669,16 +692,17 @@ int sbp_vcycle_apply(sbp_solver* s, const double* b, double* v, void* stream) {
   if (!s->mg) return SBP_ERR_UNSUPPORTED;
   cudaStream_t q = (cudaStream_t)stream;
   SBP_CUDA(cudaSetDevice(s->device));
-  const int n = s->n;
+  const int n = s->n, ld = s->ld;
   if (s->opts.precision == SBP_PREC_MIXED) {
-    SBP_CUDA((launch_copy<double, float>(cgrid<double>(b, n), grid<float>(s->r_lo, n), n, q)));
+    SBP_CUDA((launch_copy<double, float>(cgrid<double>(b, n), grid<float>(s->r_lo, ld), n, q)));
     SBP_CUDA(enqueue_vcycle<float>(s, 0, false, nullptr, q));
-    SBP_CUDA((launch_copy<float, double>(cgrid<float>(vcycle_out(s), n), grid<double>(v, n), n, q)));
+    SBP_CUDA((launch_copy<float, double>(cgrid<float>(vcycle_out(s), ld), grid<double>(v, n), n, q)));
   } else {
-    SBP_CUDA(cudaMemcpyAsync(s->r, b, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToDevice, q));
+    SBP_CUDA(cudaMemcpy2DAsync(s->r, (size_t)ld * 8, b, (size_t)n * 8, (size_t)n * 8, n,
+                               cudaMemcpyDeviceToDevice, q));
     SBP_CUDA(enqueue_vcycle<double>(s, 0, false, nullptr, q));
-    SBP_CUDA(cudaMemcpyAsync(v, vcycle_out(s), (size_t)n * n * sizeof(double),
-                             cudaMemcpyDeviceToDevice, q));
+    SBP_CUDA(cudaMemcpy2DAsync(v, (size_t)n * 8, vcycle_out(s), (size_t)ld * 8, (size_t)n * 8, n,
+                               cudaMemcpyDeviceToDevice, q));
   }
   return SBP_OK;
 }

@@ -7,38 +7,43 @@
 
 #include "sbp_kernels.cuh"
 #include "sbp_launch.h"
+#include "sbp_tma.h"
 
 namespace sbp {
 
-// Output tile of the stencil kernels: 64 points along the contiguous index
-// i (two 256-byte FP64 rows per warp pass) by 32 along j.  The staged tile
-// with halo is at most 67 x 37 points.
+// ---------------------------------------------------------------------------
+// Tiling.  Output tiles are 64 (i) x 32 (j) points; tile t of a dimension
+// covers [t*T + (t > 0), (t+1)*T + 1), so n = 2^k + 1 splits into whole tiles
+// (the extra point goes to the first tile).  Every tile stages fixed boxes:
+//   stencil box 72 x 37 at (64 ti - 4, j_lo - 2)   operand + halo (>= 2 in j)
+//   inner box   68 x 33 at (64 ti,     j_lo)       pointwise operands
+//   coarse box  40 x 20 at (32 ti - 4, (j_lo-2)>>1) prolongation source
+// The x origins are multiples of four elements (16 bytes for FP32), as TMA
+// requires; out-of-range elements read as zero.  The same boxes are staged
+// element-wise with cp.async when an operand is not TMA-addressable (the
+// caller's own arrays: n is odd, so their columns are not 16-byte aligned).
+// ---------------------------------------------------------------------------
 constexpr int TI = 64;
 constexpr int TJ = 32;
 using TileT = Tile<TI, TJ>;
-constexpr int kSmemPts = TileT::SI * TileT::SJ;
-constexpr int kIntPts = (TI + 1) * (TJ + 1);     // interior-staged operand
-// Coarse region under a fine tile (prolongation operand).
-constexpr int EP = TI / 2 + 4;
-constexpr int EJ = TJ / 2 + 6;
+constexpr int BI = kBoxI, BJ = kBoxJ;   // stencil box
+constexpr int QI = kInI, QJ = kInJ;     // inner box
+constexpr int CI = kCoI, CJ = kCoJ;     // coarse box
+static_assert(BI >= TI + 8 && BJ >= TJ + 5 && QI >= TI + 4 && QJ >= TJ + 1, "box sizes");
 
-// Coarse tile of the fused residual + restriction kernel.
+// Coarse tile of the fused residual + restriction kernel: its fine region
+// fits the same 72 x 37 stencil box at (64 ti - 4, 32 tj - 2).
 constexpr int RTI = 32;
 constexpr int RTJ = 16;
-constexpr int RVI = 2 * (RTI + 1) + 3;  // staged fine v region (max)
-constexpr int RVJ = 2 * (RTJ + 1) + 3;
-constexpr int RRI = RVI - 2;            // fine residual region (max)
-constexpr int RRJ = RVJ - 2;
 
 // Coarse dense solve: rows of Ainv per warp.
 constexpr int kGemvRowsPerWarp = 2;
-
 // Flat (pointwise) kernels: CTAs per launch cap.
 constexpr int kFlatCtas = 1216;
 // Upper bound on the CTAs of a persistent launch (SMs x resident CTAs).
 constexpr int kMaxPersistCtas = 4096;
 
-__host__ __device__ constexpr int align16(int b) { return (b + 15) & ~15; }
+__host__ __device__ constexpr int align128(int b) { return (b + 127) & ~127; }
 
 static inline dim3 tile_grid(int n) { return dim3(ntiles(n, TI), ntiles(n, TJ)); }
 
@@ -83,46 +88,204 @@ __device__ __forceinline__ Tile<A, B> tile_at(int id, int ntx, int n) {
 }
 
 // ---------------------------------------------------------------------------
+// Operand staging: a TMA map when the operand allows it, else element-wise
+// cp.async of the same box.
+// ---------------------------------------------------------------------------
+template <typename T>
+struct DevOperand {
+  const T* p;
+  int ld;
+  CUtensorMap box;
+  CUtensorMap inner;
+  CUtensorMap coarse;
+};
+
+template <typename T>
+static DevOperand<T> dev_operand(const Operand& o) {
+  DevOperand<T> d;
+  d.p = static_cast<const T*>(o.p);
+  d.ld = o.ld;
+  d.box = o.box;
+  d.inner = o.inner;
+  d.coarse = o.coarse;
+  return d;
+}
+
+// Stage a BW x BH box at (x0, y0) of an n x n operand into s (pitch BW).
+// TMA: thread 0 issues it (the caller has armed `bar` with the byte count).
+// cp.async: every thread copies its share; out-of-range elements are zeroed.
+template <bool TMA, int BW, int BH, typename T>
+__device__ __forceinline__ void stage_box(T* s, const DevOperand<T>& op, const CUtensorMap* map,
+                                          int x0, int y0, int n, unsigned long long* bar) {
+  if (TMA) {
+    if (threadIdx.x == 0) tma_load_2d(s, map, x0, y0, bar);
+  } else {
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    for (int c = w; c < BH; c += kWarps) {
+      const int j = y0 + c;
+      const bool jok = (j >= 0 && j < n);
+      for (int r = lane; r < BW; r += 32) {
+        const int i = x0 + r;
+        if (jok && i >= 0 && i < n)
+          cp_async_elem(&s[c * BW + r], op.p + (size_t)j * op.ld + i);
+        else
+          s[c * BW + r] = T(0);
+      }
+    }
+  }
+}
+
+template <typename T, int BW, int BH>
+__host__ __device__ constexpr unsigned box_bytes() {
+  return (unsigned)(sizeof(T) * BW * BH);
+}
+
+// Fine-tile box origins.
+struct TileBoxes {
+  int x0, y0;    // stencil box
+  int xi, yi;    // inner box
+  int xc, yc;    // coarse box
+  __device__ __forceinline__ TileBoxes(int ti, int j_lo) {
+    x0 = 64 * ti - 4;
+    y0 = j_lo - 2;
+    xi = 64 * ti;
+    yi = j_lo;
+    xc = 32 * ti - 4;
+    yc = (j_lo - 2) >> 1;
+  }
+};
+
+__device__ __forceinline__ bool tile_interior(const TileT& t, int n) {
+  return t.i_lo > 0 && t.i_hi < n && t.j_lo > 2 && t.j_hi < n - 3;
+}
+
+// Generic visitor (any tile): fn(i, j, SAcc centred on (i, j), inner index).
+template <typename T, typename Fn>
+__device__ __forceinline__ void visit_generic(const T* s, const TileT& t, const TileBoxes& bx,
+                                              Fn&& fn) {
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  const int mi = t.i_hi - t.i_lo;
+  const int mj = t.j_hi - t.j_lo;
+  for (int c = w; c < mj; c += kWarps) {
+    const int j = t.j_lo + c;
+    for (int r = lane; r < mi; r += 32) {
+      const int i = t.i_lo + r;
+      SAcc<T> a{s + (j - bx.y0) * BI + (i - bx.x0), BI};
+      fn(i, j, a, (j - bx.yi) * QI + (i - bx.xi));
+    }
+  }
+}
+
+// Interior tile (64 x 32, every point a plain 5-point stencil): thread
+// (r = tid & 63, g = tid >> 6) marches down columns 8g..8g+7 of row r,
+// keeping the j-1 / j / j+1 values in registers.  fn(i, j, um, u0, up, uw,
+// ue, inner index).
+template <typename T, typename Fn>
+__device__ __forceinline__ void visit_interior(const T* s, const TileT& t, Fn&& fn) {
+  const int r = threadIdx.x & 63;
+  const int g = threadIdx.x >> 6;
+  // stencil box: i - x0 = r + 5, j - y0 = c + 2; inner box: i - xi = r + 1, j - yi = c
+  const T* col = s + (8 * g + 2) * BI + r + 5;
+  T um = col[-BI];
+  T u0 = col[0];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const T up = col[(q + 1) * BI];
+    const T uw = col[q * BI - 1];
+    const T ue = col[q * BI + 1];
+    fn(t.i_lo + r, t.j_lo + 8 * g + q, um, u0, up, uw, ue, (8 * g + q) * QI + r + 1);
+    um = u0;
+    u0 = up;
+  }
+}
+
+// Apply fn(i, j, value&) to the staged box points a tile's stencil reads:
+// rows [i_lo-1, i_hi], columns [j_lo-hl, j_hi+hr-1], inside the domain.
+template <typename T, typename Fn>
+__device__ __forceinline__ void transform_box(T* s, const TileT& t, const TileBoxes& bx, int n,
+                                              Fn&& fn) {
+  const int i0 = max(t.i_lo - 1, 0), i1 = min(t.i_hi, n - 1);
+  const int j0 = max(t.j_lo - t.hl, 0), j1 = min(t.j_hi + t.hr - 1, n - 1);
+  const int ei = i1 - i0 + 1;
+  const int ej = j1 - j0 + 1;
+  const int cnt = ei * ej;
+  for (int k = threadIdx.x; k < cnt; k += kThreads) {
+    const int c = k / ei;
+    const int r = k - c * ei;
+    const int i = i0 + r, j = j0 + c;
+    fn(i, j, s[(j - bx.y0) * BI + (i - bx.x0)]);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Persistent, double-buffered tile pipeline.  A CTA walks tiles blockIdx.x,
-// blockIdx.x + gridDim.x, ...; while it computes tile k from one shared
-// buffer, cp.async is already fetching tile k+1 into the other, so HBM
-// latency overlaps compute instead of stalling every tile.  The grid is one
-// wave (SMs x resident CTAs), so neighbouring CTAs work on neighbouring tiles
-// and halo re-reads hit L2.
+// blockIdx.x + gridDim.x, ...; while it computes tile k from one buffer, the
+// copies of tile k+1 (TMA boxes completing on an mbarrier, or cp.async) are
+// already in flight into the other, so HBM latency overlaps compute.  The
+// grid is one wave (SMs x resident CTAs), so neighbouring CTAs work on
+// neighbouring tiles and halo re-reads hit L2.
 //
-// A Job provides: kStage (bytes of one buffer), kReduce, Acc (accumulator),
-// prepare() (reads device state; true = skip the launch), tiles(),
-// stage(buf, tile), compute(buf, tile, acc) and finish(total).
+// A Job provides: kStage (bytes of one buffer), kReduce, Acc, Ctx (per-launch
+// values read from device state), prepare(ctx) (true = skip the launch),
+// tiles(), tx_bytes(tile) (TMA bytes of one stage), issue(buf, bar, tile, ctx)
+// (called by all threads), compute(buf, tile, acc, ctx) and finish(total).
 // ---------------------------------------------------------------------------
 template <class Job>
-__global__ void __launch_bounds__(kThreads) k_persist(const Job job_in) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  Job job = job_in;
-  if (job.prepare()) return;
+__global__ void __launch_bounds__(kThreads) k_persist(const __grid_constant__ Job job) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) unsigned long long bar[2];
+  typename Job::Ctx ctx;
+  if (job.prepare(ctx)) return;
   const int total = job.tiles();
+  // TMA destinations must sit on 128-byte shared-memory boundaries; the
+  // launch reserves 128 extra bytes for this alignment.
+  unsigned char* const smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
   unsigned char* const buf0 = smem;
   unsigned char* const buf1 = smem + Job::kStage;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
   typename Job::Acc acc;
   int tile = blockIdx.x;
-  if (tile < total) job.stage(buf0, tile);
+  if (tile < total) {
+    if (threadIdx.x == 0) mbar_arrive_expect_tx(&bar[0], job.tx_bytes(tile));
+    job.issue(buf0, &bar[0], tile, ctx);
+  }
   cp_async_commit();
+  bool ok = true;
   for (int k = 0; tile < total; ++k, tile += gridDim.x) {
     const int next = tile + gridDim.x;
-    if (next < total) job.stage((k & 1) ? buf0 : buf1, next);
+    const int nb = (k + 1) & 1;
+    if (next < total) {
+      if (threadIdx.x == 0) {
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&bar[nb], job.tx_bytes(next));
+      }
+      job.issue(nb ? buf1 : buf0, &bar[nb], next, ctx);
+    }
     cp_async_commit();
     cp_async_wait<1>();
-    __syncthreads();
-    job.compute((k & 1) ? buf1 : buf0, tile, acc);
+    ok = mbar_wait_bounded(&bar[k & 1], (k >> 1) & 1);
+    if (!__syncthreads_and(ok)) break;
+    job.compute((k & 1) ? buf1 : buf0, tile, acc, ctx);
+    // this buffer is refilled by TMA (async proxy) after the barrier
+    fence_proxy_async_smem();
     __syncthreads();
   }
   cp_async_wait<0>();
+  if (!ok) return;  // a copy never arrived: the fault flag is set, results are void
   if (Job::kReduce) grid_reduce(acc.value(), job.rb, [&](double tot) { job.finish(tot); });
 }
 
 template <class Job>
 static int persist_ctas_per_sm() {
   static const int v = [] {
-    const int smem = 2 * Job::kStage;
+    const int smem = 2 * Job::kStage + 128;
     if (smem > 48 * 1024)
       cudaFuncSetAttribute(k_persist<Job>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     int b = 0;
@@ -139,50 +302,54 @@ template <class Job>
 static cudaError_t launch_persist(const Job& job, int total, cudaStream_t s) {
   const int cap = std::min(kMaxPersistCtas, sm_count() * persist_ctas_per_sm<Job>());
   const int grid = std::max(1, std::min(total, cap));
-  k_persist<Job><<<grid, kThreads, 2 * Job::kStage, s>>>(job);
+  k_persist<Job><<<grid, kThreads, 2 * Job::kStage + 128, s>>>(job);
   return cudaGetLastError();
 }
+
+struct NoCtx {};
 
 // ---------------------------------------------------------------------------
 // Operator apply: out = sign * A u, optional fused dot u.out.
 // ---------------------------------------------------------------------------
-template <typename T, bool DOT>
+template <typename T, bool DOT, bool TMA>
 struct ApplyJob {
-  static constexpr int kStage = align16(sizeof(T) * kSmemPts);
+  static constexpr int kStage = align128(box_bytes<T, BI, BJ>());
   static constexpr bool kReduce = DOT;
   using Acc = DotAcc<T>;
-  Grid<const T> u;
+  using Ctx = NoCtx;
+  DevOperand<T> u;
   Grid<T> out;
   int n, ntx, ntot, sign;
   ReduceBuf rb;
   double* dot_out;
-  __device__ bool prepare() { return false; }
+  __device__ bool prepare(Ctx&) const { return false; }
   __device__ int tiles() const { return ntot; }
-  __device__ void stage(unsigned char* buf, int id) const {
-    stage_tile_async(reinterpret_cast<T*>(buf), tile_at<TI, TJ>(id, ntx, n), u, n);
+  __device__ unsigned tx_bytes(int) const { return TMA ? box_bytes<T, BI, BJ>() : 0u; }
+  __device__ void issue(unsigned char* buf, unsigned long long* bar, int id, const Ctx&) const {
+    const TileBoxes bx(id % ntx, tile_at<TI, TJ>(id, ntx, n).j_lo);
+    stage_box<TMA, BI, BJ>(reinterpret_cast<T*>(buf), u, &u.box, bx.x0, bx.y0, n, bar);
   }
-  __device__ void compute(unsigned char* buf, int id, Acc& acc) const {
+  __device__ void compute(unsigned char* buf, int id, Acc& acc, const Ctx&) const {
     const TileT t = tile_at<TI, TJ>(id, ntx, n);
-    for_tile_points(reinterpret_cast<T*>(buf), t, [&](int i, int j, const SAcc<T>& a, int) {
-      const T v = signedA<T>(a, i, j, n, sign);
-      out.at(i, j) = v;
-      if (DOT) acc.add_prod(a(0, 0), v);
-    });
+    const TileBoxes bx(id % ntx, t.j_lo);
+    const T* s = reinterpret_cast<const T*>(buf);
+    if (tile_interior(t, n)) {
+      visit_interior(s, t, [&](int i, int j, T um, T u0, T up, T uw, T ue, int) {
+        const T sum = (uw + ue) + (um + up);
+        const T v = sign > 0 ? fma(T(4), u0, -sum) : fma(T(-4), u0, sum);
+        out.at(i, j) = v;
+        if (DOT) acc.add_prod(u0, v);
+      });
+    } else {
+      visit_generic(s, t, bx, [&](int i, int j, const SAcc<T>& a, int) {
+        const T v = signedA<T>(a, i, j, n, sign);
+        out.at(i, j) = v;
+        if (DOT) acc.add_prod(a(0, 0), v);
+      });
+    }
   }
   __device__ void finish(double tot) const { *dot_out = tot; }
 };
-
-template <typename T>
-cudaError_t launch_apply(Grid<const T> u, Grid<T> out, int n, int sign, ReduceBuf rb,
-                         double* dot_out, cudaStream_t s) {
-  const dim3 g = tile_grid(n);
-  const int total = (int)(g.x * g.y);
-  if (dot_out)
-    return launch_persist(ApplyJob<T, true>{u, out, n, (int)g.x, total, sign, rb, dot_out}, total,
-                          s);
-  return launch_persist(ApplyJob<T, false>{u, out, n, (int)g.x, total, sign, rb, nullptr}, total,
-                        s);
-}
 
 // ---------------------------------------------------------------------------
 // Initial residual r = b - opsign*A*x with ||r||^2 and Krylov-state setup.
@@ -196,35 +363,50 @@ struct ResFin {
   double* out2;
 };
 
-template <typename T>
+template <typename T, bool TMAX, bool TMAB>
 struct ResidualJob {
-  static constexpr int kStage = align16(sizeof(T) * (kSmemPts + kIntPts));
+  static constexpr int kOffB = align128(box_bytes<T, BI, BJ>());
+  static constexpr int kStage = kOffB + align128(box_bytes<T, QI, QJ>());
   static constexpr bool kReduce = true;
   using Acc = DotAcc<double>;
-  Grid<const T> x, b;
+  using Ctx = NoCtx;
+  DevOperand<T> x, b;
   Grid<T> r;
   Grid<float> rlo;
   int n, ntx, ntot, opsign;
   ResFin rf;
   ReduceBuf rb;
-  __device__ bool prepare() { return false; }
+  __device__ bool prepare(Ctx&) const { return false; }
   __device__ int tiles() const { return ntot; }
-  __device__ void stage(unsigned char* buf, int id) const {
-    const TileT t = tile_at<TI, TJ>(id, ntx, n);
-    T* s = reinterpret_cast<T*>(buf);
-    stage_tile_async(s, t, x, n);
-    stage_interior_async(s + kSmemPts, t, b, n);
+  __device__ unsigned tx_bytes(int) const {
+    return (TMAX ? box_bytes<T, BI, BJ>() : 0u) + (TMAB ? box_bytes<T, QI, QJ>() : 0u);
   }
-  __device__ void compute(unsigned char* buf, int id, Acc& acc) const {
+  __device__ void issue(unsigned char* buf, unsigned long long* bar, int id, const Ctx&) const {
+    const TileBoxes bx(id % ntx, tile_at<TI, TJ>(id, ntx, n).j_lo);
+    stage_box<TMAX, BI, BJ>(reinterpret_cast<T*>(buf), x, &x.box, bx.x0, bx.y0, n, bar);
+    stage_box<TMAB, QI, QJ>(reinterpret_cast<T*>(buf + kOffB), b, &b.inner, bx.xi, bx.yi, n, bar);
+  }
+  __device__ void compute(unsigned char* buf, int id, Acc& acc, const Ctx&) const {
     const TileT t = tile_at<TI, TJ>(id, ntx, n);
+    const TileBoxes bx(id % ntx, t.j_lo);
     const T* s = reinterpret_cast<const T*>(buf);
-    const T* sb = s + kSmemPts;
-    for_tile_points(s, t, [&](int i, int j, const SAcc<T>& a, int k) {
-      const T rv = sb[k] + signedA<T>(a, i, j, n, -opsign);
+    const T* sb = reinterpret_cast<const T*>(buf + kOffB);
+    auto emit = [&](int i, int j, T rv) {
       r.at(i, j) = rv;
       if (rlo.p) rlo.at(i, j) = convert<float>(rv);
       acc.add_prod((double)rv, (double)rv);
-    });
+    };
+    if (tile_interior(t, n)) {
+      visit_interior(s, t, [&](int i, int j, T um, T u0, T up, T uw, T ue, int k) {
+        const T sum = (uw + ue) + (um + up);
+        // r = b - opsign*A x, A x = 4 u0 - sum
+        emit(i, j, opsign > 0 ? sb[k] + (sum - T(4) * u0) : sb[k] - (sum - T(4) * u0));
+      });
+    } else {
+      visit_generic(s, t, bx, [&](int i, int j, const SAcc<T>& a, int k) {
+        emit(i, j, sb[k] + signedA<T>(a, i, j, n, -opsign));
+      });
+    }
   }
   __device__ void finish(double tot) const {
     if (rf.out2) *rf.out2 = tot;
@@ -247,74 +429,73 @@ struct ResidualJob {
   }
 };
 
-template <typename T>
-cudaError_t launch_residual(Grid<const T> x, Grid<const T> b, Grid<T> r, Grid<float> rlo, int n,
-                            int opsign, SolveState* st, double* norms, double abstol,
-                            double reltol, int plain, double* out2, ReduceBuf rb,
-                            cudaStream_t s) {
-  const dim3 g = tile_grid(n);
-  const int total = (int)(g.x * g.y);
-  ResFin rf{st, norms, abstol, reltol, plain, out2};
-  return launch_persist(ResidualJob<T>{x, b, r, rlo, n, (int)g.x, total, opsign, rf, rb}, total,
-                        s);
-}
-
 // ---------------------------------------------------------------------------
 // CG direction + operator + p.Ap  (one HBM pass: reads z, p_old; writes p, Ap)
 // ---------------------------------------------------------------------------
-template <typename T, typename Tz>
+struct DirCtx {
+  bool first;
+  double beta;
+};
+
+template <typename T, typename Tz, bool TMA>
 struct CgDirJob {
-  static constexpr int kOffZ = align16(sizeof(T) * kSmemPts);
-  static constexpr int kStage = kOffZ + align16(sizeof(Tz) * kSmemPts);
+  static constexpr int kOffZ = align128(box_bytes<T, BI, BJ>());
+  static constexpr int kStage = kOffZ + align128(box_bytes<Tz, BI, BJ>());
   static constexpr bool kReduce = true;
   using Acc = DotAcc<double>;
-  Grid<const Tz> z;
-  Grid<const T> pold;
+  using Ctx = DirCtx;
+  DevOperand<Tz> z;
+  DevOperand<T> pold;
   Grid<T> pnew, Ap;
   int n, ntx, ntot, opsign;
   SolveState* st;
   ReduceBuf rb;
-  bool first;
-  T beta;
-  __device__ bool prepare() {
+  __device__ bool prepare(Ctx& c) const {
     if (st->done) return true;
-    first = (st->iter == 0);
-    beta = T(st->beta);
+    c.first = (st->iter == 0);
+    c.beta = st->beta;
     return false;
   }
   __device__ int tiles() const { return ntot; }
-  __device__ void stage(unsigned char* buf, int id) const {
-    const TileT t = tile_at<TI, TJ>(id, ntx, n);
-    T* s = reinterpret_cast<T*>(buf);
-    Tz* sz = reinterpret_cast<Tz*>(buf + kOffZ);
-    stage_tile_async(sz, t, z, n);
-    if (!first) stage_tile_async(s, t, pold, n);
+  __device__ unsigned tx_bytes(int) const {
+    // on the first iteration p_old is not read; prepare() is per CTA, so the
+    // byte count is recomputed from the state here
+    return TMA ? box_bytes<Tz, BI, BJ>() + (st->iter == 0 ? 0u : box_bytes<T, BI, BJ>()) : 0u;
   }
-  __device__ void compute(unsigned char* buf, int id, Acc& acc) const {
+  __device__ void issue(unsigned char* buf, unsigned long long* bar, int id, const Ctx& c) const {
+    const TileBoxes bx(id % ntx, tile_at<TI, TJ>(id, ntx, n).j_lo);
+    stage_box<TMA, BI, BJ>(reinterpret_cast<Tz*>(buf + kOffZ), z, &z.box, bx.x0, bx.y0, n, bar);
+    if (!c.first)
+      stage_box<TMA, BI, BJ>(reinterpret_cast<T*>(buf), pold, &pold.box, bx.x0, bx.y0, n, bar);
+  }
+  __device__ void compute(unsigned char* buf, int id, Acc& acc, const Ctx& c) const {
     const TileT t = tile_at<TI, TJ>(id, ntx, n);
+    const TileBoxes bx(id % ntx, t.j_lo);
     T* s = reinterpret_cast<T*>(buf);
     const Tz* sz = reinterpret_cast<const Tz*>(buf + kOffZ);
-    {
-      constexpr int SI = TileT::SI;
-      const int lane = threadIdx.x & 31;
-      const int w = threadIdx.x >> 5;
-      const int ei = t.i_hi - t.i_lo + 2;
-      const int ej = t.j_hi - t.j_lo + t.hl + t.hr;
-      for (int c = w; c < ej; c += kWarps)
-        for (int r = lane; r < ei; r += 32) {
-          const int q = c * SI + r;
-          const T zz = convert<T>(sz[q]);
-          s[q] = first ? zz : fma(beta, s[q], zz);
-        }
-    }
+    const T beta = T(c.beta);
+    const bool first = c.first;
+    // p = z + beta p_old on every staged point the stencil reads
+    transform_box(s, t, bx, n, [&](int i, int j, T& v) {
+      const T zz = convert<T>(sz[&v - s]);
+      v = first ? zz : fma(beta, v, zz);
+    });
     __syncthreads();
-    for_tile_points(s, t, [&](int i, int j, const SAcc<T>& a, int) {
-      const T pv = a(0, 0);
-      const T ap = signedA<T>(a, i, j, n, opsign);
+    auto emit = [&](int i, int j, T pv, T ap) {
       pnew.at(i, j) = pv;
       Ap.at(i, j) = ap;
       acc.add_prod(pv, ap);
-    });
+    };
+    if (tile_interior(t, n)) {
+      visit_interior(s, t, [&](int i, int j, T um, T u0, T up, T uw, T ue, int) {
+        const T sum = (uw + ue) + (um + up);
+        emit(i, j, u0, opsign > 0 ? fma(T(4), u0, -sum) : fma(T(-4), u0, sum));
+      });
+    } else {
+      visit_generic(s, t, bx, [&](int i, int j, const SAcc<T>& a, int) {
+        emit(i, j, a(0, 0), signedA<T>(a, i, j, n, opsign));
+      });
+    }
   }
   __device__ void finish(double tot) const {
     st->pAp = tot;
@@ -325,19 +506,10 @@ struct CgDirJob {
   }
 };
 
-template <typename T, typename Tz>
-cudaError_t launch_cg_dir(Grid<const Tz> z, Grid<const T> pold, Grid<T> pnew, Grid<T> Ap, int n,
-                          int opsign, SolveState* st, ReduceBuf rb, cudaStream_t s) {
-  const dim3 g = tile_grid(n);
-  const int total = (int)(g.x * g.y);
-  return launch_persist(
-      CgDirJob<T, Tz>{z, pold, pnew, Ap, n, (int)g.x, total, opsign, st, rb, false, T(0)}, total,
-      s);
-}
-
 // ---------------------------------------------------------------------------
 // CG update (pointwise, flat, 16-byte vectors): x += alpha p; r -= alpha Ap;
-// ||r||^2; convergence test.  All solver arrays are contiguous n*n.
+// ||r||^2; convergence test.  The arrays share one layout; padding entries
+// are zero and stay zero.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void cg_update_pt(double& x, double& r, double p, double ap,
                                              double alpha, double& acc) {
@@ -404,86 +576,105 @@ __global__ void __launch_bounds__(kThreads)
 
 static inline bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
 
-template <typename T>
-cudaError_t launch_cg_update(Grid<T> x, Grid<T> r, Grid<const T> p, Grid<const T> Ap,
-                             Grid<float> rlo, int n, int plain, SolveState* st, double* norms,
-                             ReduceBuf rb, cudaStream_t s) {
-  static_assert(sizeof(T) == 8, "the Krylov vectors are FP64");
-  if (x.ld != n || r.ld != n || p.ld != n || Ap.ld != n) return cudaErrorInvalidValue;
-  const long long N = (long long)n * n;
-  const bool vec = aligned16(x.p) && aligned16(r.p) && aligned16(p.p) && aligned16(Ap.p) &&
-                   (!rlo.p || ((uintptr_t)rlo.p & 7u) == 0);
-  const int g = flat_grid(N, vec ? 4 : 2);
-  if (vec)
-    k_cg_update<true><<<g, kThreads, 0, s>>>(x.p, r.p, p.p, Ap.p, rlo.p, N, plain, st, norms, rb);
-  else
-    k_cg_update<false><<<g, kThreads, 0, s>>>(x.p, r.p, p.p, Ap.p, rlo.p, N, plain, st, norms, rb);
-  return cudaGetLastError();
-}
-
 // ---------------------------------------------------------------------------
 // Smoothing pass (Jacobi / Richardson) with the field variants.
 // ---------------------------------------------------------------------------
-template <typename T, int FIELD, int EPI, bool DOT>
+struct SmoothCtx {};
+
+template <typename T, int FIELD, int EPI, bool DOT, bool TMA>
 struct SmoothJob {
   static constexpr bool kNeedB = (EPI == kEpiSweep) || DOT;
-  static constexpr int kOffB = align16(sizeof(T) * kSmemPts);
-  static constexpr int kOffE = kOffB + (kNeedB ? align16(sizeof(T) * kIntPts) : 0);
-  static constexpr int kStage = kOffE + (FIELD == kFieldProlong ? align16(sizeof(T) * EP * EJ) : 0);
+  static constexpr int kOffB = align128(box_bytes<T, BI, BJ>());
+  static constexpr int kOffE = kOffB + (kNeedB ? align128(box_bytes<T, QI, QJ>()) : 0);
+  static constexpr int kStage =
+      kOffE + (FIELD == kFieldProlong ? align128(box_bytes<T, CI, CJ>()) : 0);
   static constexpr bool kReduce = DOT;
   using Acc = DotAcc<T>;
-  Grid<const T> vin, e, b;
+  using Ctx = NoCtx;
+  DevOperand<T> vin, e, b;
   Grid<T> vout;
   int n, ntx, ntot, smoother;
   T omega;
   SolveState* st;
   ReduceBuf rb;
-  __device__ bool prepare() { return st && st->done; }
+  __device__ bool prepare(Ctx&) const { return st && st->done; }
   __device__ int tiles() const { return ntot; }
-  __device__ void stage(unsigned char* buf, int id) const {
-    const TileT t = tile_at<TI, TJ>(id, ntx, n);
-    T* s = reinterpret_cast<T*>(buf);
-    stage_tile_async(s, t, FIELD == kFieldZero ? b : vin, n);
-    if (kNeedB) stage_interior_async(reinterpret_cast<T*>(buf + kOffB), t, b, n);
-    if (FIELD == kFieldProlong) {
-      const int nc = (n + 1) / 2;
-      const int I0 = (t.i_lo - 1) >> 1;
-      const int J0 = (t.j_lo - t.hl) >> 1;
-      const int ei = (t.i_hi >> 1) - I0 + 2;
-      const int ej = ((t.j_hi + t.hr - 1) >> 1) - J0 + 2;
-      stage_async<EP>(reinterpret_cast<T*>(buf + kOffE), e, I0, J0, ei, ej, nc);
-    }
+  __device__ unsigned tx_bytes(int) const {
+    if (!TMA) return 0u;
+    return box_bytes<T, BI, BJ>() + (kNeedB ? box_bytes<T, QI, QJ>() : 0u) +
+           (FIELD == kFieldProlong ? box_bytes<T, CI, CJ>() : 0u);
   }
-  __device__ void compute(unsigned char* buf, int id, Acc& acc) const {
+  __device__ void issue(unsigned char* buf, unsigned long long* bar, int id, const Ctx&) const {
+    const TileBoxes bx(id % ntx, tile_at<TI, TJ>(id, ntx, n).j_lo);
+    const DevOperand<T>& src = (FIELD == kFieldZero) ? b : vin;
+    stage_box<TMA, BI, BJ>(reinterpret_cast<T*>(buf), src, &src.box, bx.x0, bx.y0, n, bar);
+    if (kNeedB)
+      stage_box<TMA, QI, QJ>(reinterpret_cast<T*>(buf + kOffB), b, &b.inner, bx.xi, bx.yi, n,
+                             bar);
+    if (FIELD == kFieldProlong)
+      stage_box<TMA, CI, CJ>(reinterpret_cast<T*>(buf + kOffE), e, &e.coarse, bx.xc, bx.yc,
+                             (n + 1) / 2, bar);
+  }
+  __device__ void compute(unsigned char* buf, int id, Acc& acc, const Ctx&) const {
     const TileT t = tile_at<TI, TJ>(id, ntx, n);
+    const TileBoxes bx(id % ntx, t.j_lo);
     T* s = reinterpret_cast<T*>(buf);
     const T* sb = reinterpret_cast<const T*>(buf + kOffB);
     const bool jac = (smoother == kSmoothJacobi);
+    const bool interior = tile_interior(t, n);
     if (FIELD == kFieldProlong) {
       const T* se = reinterpret_cast<const T*>(buf + kOffE);
-      const int I0 = (t.i_lo - 1) >> 1;
-      const int J0 = (t.j_lo - t.hl) >> 1;
-      transform_staged(s, t, n,
-                       [&](int i, int j, T& v) { v += prolong_smem<EP>(se, I0, J0, i, j); });
+      transform_box(s, t, bx, n, [&](int i, int j, T& v) {
+        const int a = (i >> 1) - bx.xc, b2 = (j >> 1) - bx.yc;
+        const T* q = se + b2 * CI + a;
+        const bool oi = i & 1, oj = j & 1;
+        T pe = q[0];
+        if (oi) pe += q[1];
+        if (oj) {
+          pe += q[CI];
+          if (oi) pe += q[CI + 1];
+        }
+        v += pe * ((oi && oj) ? T(0.25) : ((oi || oj) ? T(0.5) : T(1)));
+      });
       __syncthreads();
-    } else if (FIELD == kFieldZero) {
+    } else if (FIELD == kFieldZero && !interior) {
       // first sweep from zero, once per staged point: v1 = omega D^-1 b
-      transform_staged(s, t, n, [&](int i, int j, T& v) {
+      transform_box(s, t, bx, n, [&](int i, int j, T& v) {
         v *= jac ? omega * inv_diagA<T>(i, j, n) : omega;
       });
       __syncthreads();
     }
-    for_tile_points(s, t, [&](int i, int j, const SAcc<T>& a, int k) {
-      const T f = a(0, 0);
-      const T bb = kNeedB ? sb[k] : T(0);
-      T vn = f;
-      if (EPI == kEpiSweep) {
-        const T m = jac ? omega * inv_diagA<T>(i, j, n) : omega;
-        vn = fma(m, bb + negA<T>(a, i, j, n), f);
-      }
+    auto emit = [&](int i, int j, T bb, T vn) {
       vout.at(i, j) = vn;
       if (DOT) acc.add_prod(bb, vn);
-    });
+    };
+    if (interior) {
+      const T m = jac ? omega * T(0.25) : omega;   // interior diag(A) = 4
+      visit_interior(s, t, [&](int i, int j, T um, T u0, T up, T uw, T ue, int k) {
+        const T sum = (uw + ue) + (um + up);
+        if (FIELD == kFieldZero) {
+          // staged raw b: F = m b, the stencil of F is m times the stencil of b
+          const T f = m * u0;
+          const T vn = (EPI == kEpiSweep) ? fma(m, fma(m, sum - T(4) * u0, u0), f) : f;
+          emit(i, j, u0, vn);
+        } else {
+          const T bb = kNeedB ? sb[k] : T(0);
+          const T vn = (EPI == kEpiSweep) ? fma(m, bb + (sum - T(4) * u0), u0) : u0;
+          emit(i, j, bb, vn);
+        }
+      });
+    } else {
+      visit_generic(s, t, bx, [&](int i, int j, const SAcc<T>& a, int k) {
+        const T f = a(0, 0);
+        const T bb = kNeedB ? sb[k] : T(0);
+        T vn = f;
+        if (EPI == kEpiSweep) {
+          const T m = jac ? omega * inv_diagA<T>(i, j, n) : omega;
+          vn = fma(m, bb + negA<T>(a, i, j, n), f);
+        }
+        emit(i, j, bb, vn);
+      });
+    }
   }
   __device__ void finish(double tot) const {
     if (!isfinite(tot)) {
@@ -496,29 +687,226 @@ struct SmoothJob {
   }
 };
 
-template <typename T, int FIELD, int EPI>
-static cudaError_t launch_smooth_fe(Grid<const T> vin, Grid<const T> e, Grid<const T> b,
-                                    Grid<T> vout, int n, int smoother, double omega, int dot,
-                                    SolveState* st, ReduceBuf rb, cudaStream_t s) {
+// ---------------------------------------------------------------------------
+// Fused residual + restriction: f = R (b - A v).  Tiles live on the coarse
+// grid (32 x 16 coarse points); the CTA stages b and v over the fine region
+// under its coarse tile (the same 72 x 37 box as the fine tiles), forms r in
+// place of b in shared memory, then applies the 3x3 restriction weights.
+// One HBM pass over v and b, a quarter-size write.
+// ---------------------------------------------------------------------------
+template <typename T, bool TMA>
+struct ResRestrictJob {
+  static constexpr int kOffV = align128(box_bytes<T, BI, BJ>());
+  static constexpr int kStage = kOffV + align128(box_bytes<T, BI, BJ>());
+  static constexpr bool kReduce = false;
+  using Acc = DotAcc<double>;
+  using Ctx = NoCtx;
+  DevOperand<T> v, b;
+  Grid<T> f;
+  int nf, nc, ntx, ntot, kind, has_v;
+  const SolveState* st;
+  ReduceBuf rb;
+  __device__ bool prepare(Ctx&) const { return st && st->done; }
+  __device__ int tiles() const { return ntot; }
+  __device__ unsigned tx_bytes(int) const {
+    return TMA ? box_bytes<T, BI, BJ>() * (has_v ? 2u : 1u) : 0u;
+  }
+  __device__ void issue(unsigned char* buf, unsigned long long* bar, int id, const Ctx&) const {
+    const int ti = id % ntx, tj = id / ntx;
+    const int x0 = 64 * ti - 4, y0 = 32 * tj - 2;
+    stage_box<TMA, BI, BJ>(reinterpret_cast<T*>(buf), b, &b.box, x0, y0, nf, bar);
+    if (has_v)
+      stage_box<TMA, BI, BJ>(reinterpret_cast<T*>(buf + kOffV), v, &v.box, x0, y0, nf, bar);
+  }
+  __device__ void compute(unsigned char* buf, int id, Acc&, const Ctx&) const {
+    const int ti = id % ntx, tj = id / ntx;
+    const Tile<RTI, RTJ> t = tile_at<RTI, RTJ>(id, ntx, nc);
+    const int x0 = 64 * ti - 4, y0 = 32 * tj - 2;
+    T* sr = reinterpret_cast<T*>(buf);
+    const T* sv = reinterpret_cast<const T*>(buf + kOffV);
+    const int m = t.i_hi - t.i_lo, mp = t.j_hi - t.j_lo;
+    const int ri0 = max(2 * t.i_lo - 1, 0), ri1 = min(2 * t.i_hi - 1, nf - 1);
+    const int rj0 = max(2 * t.j_lo - 1, 0), rj1 = min(2 * t.j_hi - 1, nf - 1);
+    if (has_v) {
+      const int ei = ri1 - ri0 + 1, ej = rj1 - rj0 + 1;
+      const int cnt = ei * ej;
+      const bool interior = ri0 > 0 && ri1 < nf - 1 && rj0 > 2 && rj1 < nf - 3;
+      for (int k = threadIdx.x; k < cnt; k += kThreads) {
+        const int c = k / ei;
+        const int r = k - c * ei;
+        const int i = ri0 + r, j = rj0 + c;
+        const int q = (j - y0) * BI + (i - x0);
+        T na;
+        if (interior) {
+          const T* a = sv + q;
+          na = ((a[-1] + a[1]) + (a[-BI] + a[BI])) - T(4) * a[0];
+        } else {
+          na = negA<T>(SAcc<T>{sv + q, BI}, i, j, nf);
+        }
+        sr[q] += na;
+      }
+      __syncthreads();
+    }
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    for (int c = w; c < mp; c += kWarps) {
+      const int J = t.j_lo + c;
+      for (int r = lane; r < m; r += 32) {
+        const int I = t.i_lo + r;
+        const T* q = sr + (2 * J - y0) * BI + (2 * I - x0);
+        T acc = T(0);
+#pragma unroll
+        for (int bj = -1; bj <= 1; ++bj) {
+          const T wj = restrict_w1<T>(kind, J, nc, bj);
+#pragma unroll
+          for (int ai = -1; ai <= 1; ++ai)
+            acc = fma(restrict_w1<T>(kind, I, nc, ai) * wj, q[bj * BI + ai], acc);
+        }
+        f.at(I, J) = acc;
+      }
+    }
+  }
+  __device__ void finish(double) const {}
+};
+
+// ---------------------------------------------------------------------------
+// Launchers.
+// ---------------------------------------------------------------------------
+static inline Operand raw_operand(const void* p, int n, int ld) {
+  Operand o;
+  o.p = p;
+  o.n = n;
+  o.ld = ld;
+  o.tma = false;
+  return o;
+}
+
+template <typename T>
+cudaError_t launch_apply_op(const Operand& u, Grid<T> out, int n, int sign, ReduceBuf rb,
+                            double* dot_out, cudaStream_t s) {
+  const dim3 g = tile_grid(n);
+  const int total = (int)(g.x * g.y);
+  const DevOperand<T> du = dev_operand<T>(u);
+#define SBP_APPLY(D, M)                                                                          \
+  return launch_persist(ApplyJob<T, D, M>{du, out, n, (int)g.x, total, sign, rb, dot_out}, total, s)
+  if (dot_out) {
+    if (u.tma) SBP_APPLY(true, true);
+    SBP_APPLY(true, false);
+  }
+  if (u.tma) SBP_APPLY(false, true);
+  SBP_APPLY(false, false);
+#undef SBP_APPLY
+}
+
+template <typename T>
+cudaError_t launch_apply(Grid<const T> u, Grid<T> out, int n, int sign, ReduceBuf rb,
+                         double* dot_out, cudaStream_t s) {
+  return launch_apply_op<T>(raw_operand(u.p, n, u.ld), out, n, sign, rb, dot_out, s);
+}
+
+template <typename T>
+cudaError_t launch_residual_op(const Operand& x, const Operand& b, Grid<T> r, Grid<float> rlo,
+                               int n, int opsign, SolveState* st, double* norms, double abstol,
+                               double reltol, int plain, double* out2, ReduceBuf rb,
+                               cudaStream_t s) {
+  const dim3 g = tile_grid(n);
+  const int total = (int)(g.x * g.y);
+  ResFin rf{st, norms, abstol, reltol, plain, out2};
+  const DevOperand<T> dx = dev_operand<T>(x), db = dev_operand<T>(b);
+#define SBP_RES(MX, MB)                                                                          \
+  return launch_persist(ResidualJob<T, MX, MB>{dx, db, r, rlo, n, (int)g.x, total, opsign, rf, rb}, \
+                        total, s)
+  if (x.tma && b.tma) SBP_RES(true, true);
+  if (x.tma) SBP_RES(true, false);
+  if (b.tma) SBP_RES(false, true);
+  SBP_RES(false, false);
+#undef SBP_RES
+}
+
+template <typename T>
+cudaError_t launch_residual(Grid<const T> x, Grid<const T> b, Grid<T> r, Grid<float> rlo, int n,
+                            int opsign, SolveState* st, double* norms, double abstol,
+                            double reltol, int plain, double* out2, ReduceBuf rb,
+                            cudaStream_t s) {
+  return launch_residual_op<T>(raw_operand(x.p, n, x.ld), raw_operand(b.p, n, b.ld), r, rlo, n,
+                               opsign, st, norms, abstol, reltol, plain, out2, rb, s);
+}
+
+template <typename T, typename Tz>
+cudaError_t launch_cg_dir_op(const Operand& z, const Operand& pold, Grid<T> pnew, Grid<T> Ap,
+                             int n, int opsign, SolveState* st, ReduceBuf rb, cudaStream_t s) {
+  const dim3 g = tile_grid(n);
+  const int total = (int)(g.x * g.y);
+  const DevOperand<Tz> dz = dev_operand<Tz>(z);
+  const DevOperand<T> dp = dev_operand<T>(pold);
+  if (z.tma && pold.tma)
+    return launch_persist(
+        CgDirJob<T, Tz, true>{dz, dp, pnew, Ap, n, (int)g.x, total, opsign, st, rb}, total, s);
+  return launch_persist(
+      CgDirJob<T, Tz, false>{dz, dp, pnew, Ap, n, (int)g.x, total, opsign, st, rb}, total, s);
+}
+
+template <typename T, typename Tz>
+cudaError_t launch_cg_dir(Grid<const Tz> z, Grid<const T> pold, Grid<T> pnew, Grid<T> Ap, int n,
+                          int opsign, SolveState* st, ReduceBuf rb, cudaStream_t s) {
+  return launch_cg_dir_op<T, Tz>(raw_operand(z.p, n, z.ld), raw_operand(pold.p, n, pold.ld), pnew,
+                                 Ap, n, opsign, st, rb, s);
+}
+
+template <typename T>
+cudaError_t launch_cg_update(Grid<T> x, Grid<T> r, Grid<const T> p, Grid<const T> Ap,
+                             Grid<float> rlo, int n, int plain, SolveState* st, double* norms,
+                             ReduceBuf rb, cudaStream_t s) {
+  static_assert(sizeof(T) == 8, "the Krylov vectors are FP64");
+  const int ld = x.ld;
+  if (r.ld != ld || p.ld != ld || Ap.ld != ld || (rlo.p && rlo.ld != ld) || ld < n)
+    return cudaErrorInvalidValue;
+  const long long N = (long long)ld * n;
+  const bool vec = aligned16(x.p) && aligned16(r.p) && aligned16(p.p) && aligned16(Ap.p) &&
+                   (!rlo.p || ((uintptr_t)rlo.p & 7u) == 0) && (ld % 2 == 0 || N % 2 == 0);
+  const int g = flat_grid(N, vec ? 4 : 2);
+  if (vec)
+    k_cg_update<true><<<g, kThreads, 0, s>>>(x.p, r.p, p.p, Ap.p, rlo.p, N, plain, st, norms, rb);
+  else
+    k_cg_update<false><<<g, kThreads, 0, s>>>(x.p, r.p, p.p, Ap.p, rlo.p, N, plain, st, norms, rb);
+  return cudaGetLastError();
+}
+
+template <typename T, int FIELD, int EPI, bool TMA>
+static cudaError_t launch_smooth_fem(const DevOperand<T>& vin, const DevOperand<T>& e,
+                                     const DevOperand<T>& b, Grid<T> vout, int n, int smoother,
+                                     double omega, int dot, SolveState* st, ReduceBuf rb,
+                                     cudaStream_t s) {
   const dim3 g = tile_grid(n);
   const int total = (int)(g.x * g.y);
   if (dot)
-    return launch_persist(SmoothJob<T, FIELD, EPI, true>{vin, e, b, vout, n, (int)g.x, total,
-                                                         smoother, T(omega), st, rb},
+    return launch_persist(SmoothJob<T, FIELD, EPI, true, TMA>{vin, e, b, vout, n, (int)g.x, total,
+                                                              smoother, T(omega), st, rb},
                           total, s);
-  return launch_persist(SmoothJob<T, FIELD, EPI, false>{vin, e, b, vout, n, (int)g.x, total,
-                                                        smoother, T(omega), st, rb},
+  return launch_persist(SmoothJob<T, FIELD, EPI, false, TMA>{vin, e, b, vout, n, (int)g.x, total,
+                                                             smoother, T(omega), st, rb},
                         total, s);
 }
 
 template <typename T>
-cudaError_t launch_smooth(int field, int epi, Grid<const T> vin, Grid<const T> e, Grid<const T> b,
-                          Grid<T> vout, int n, int smoother, double omega, int dot,
-                          SolveState* st, ReduceBuf rb, cudaStream_t s) {
+cudaError_t launch_smooth_op(int field, int epi, const Operand& vin, const Operand& e,
+                             const Operand& b, Grid<T> vout, int n, int smoother, double omega,
+                             int dot, SolveState* st, ReduceBuf rb, cudaStream_t s) {
   if (dot && !st) return cudaErrorInvalidValue;
-#define SBP_SMOOTH_CASE(F, E)                                                                  \
-  if (field == F && epi == E)                                                                  \
-    return launch_smooth_fe<T, F, E>(vin, e, b, vout, n, smoother, omega, dot, st, rb, s);
+  const DevOperand<T> dv = dev_operand<T>(vin), de = dev_operand<T>(e), db = dev_operand<T>(b);
+  // TMA only when every operand the variant stages is TMA-addressable
+  const bool need_b = (epi == kEpiSweep) || dot;
+  bool tma = (field == kFieldZero ? b.tma : vin.tma);
+  if (need_b) tma = tma && b.tma;
+  if (field == kFieldProlong) tma = tma && e.tma;
+#define SBP_SMOOTH_CASE(F, E)                                                                    \
+  if (field == F && epi == E) {                                                                  \
+    if (tma)                                                                                     \
+      return launch_smooth_fem<T, F, E, true>(dv, de, db, vout, n, smoother, omega, dot, st, rb, \
+                                              s);                                                \
+    return launch_smooth_fem<T, F, E, false>(dv, de, db, vout, n, smoother, omega, dot, st, rb,  \
+                                             s);                                                 \
+  }
   SBP_SMOOTH_CASE(kFieldPlain, kEpiSweep)
   SBP_SMOOTH_CASE(kFieldPlain, kEpiStore)
   SBP_SMOOTH_CASE(kFieldZero, kEpiSweep)
@@ -529,116 +917,83 @@ cudaError_t launch_smooth(int field, int epi, Grid<const T> vin, Grid<const T> e
   return cudaErrorInvalidValue;
 }
 
-// ---------------------------------------------------------------------------
-// Fused residual + restriction: f = R (b - A v).  Tiles live on the coarse
-// grid; the CTA stages b (as the residual buffer) and v for the fine region
-// under its coarse tile, forms r in shared memory, then applies the 3x3
-// restriction weights.  One HBM pass over v and b, a quarter-size write.
-// ---------------------------------------------------------------------------
 template <typename T>
-struct ResRestrictJob {
-  static constexpr int kOffV = align16(sizeof(T) * RRI * RRJ);
-  static constexpr int kStage = kOffV + align16(sizeof(T) * RVI * RVJ);
-  static constexpr bool kReduce = false;
-  using Acc = DotAcc<double>;
-  Grid<const T> v, b;
-  Grid<T> f;
-  int nf, nc, ntx, ntot, kind;
-  const SolveState* st;
-  ReduceBuf rb;
-  __device__ bool prepare() { return st && st->done; }
-  __device__ int tiles() const { return ntot; }
-  __device__ void stage(unsigned char* buf, int id) const {
-    const Tile<RTI, RTJ> t = tile_at<RTI, RTJ>(id, ntx, nc);
-    const int m = t.i_hi - t.i_lo, mp = t.j_hi - t.j_lo;
-    const int ri0 = 2 * t.i_lo - 1, rj0 = 2 * t.j_lo - 1;
-    stage_async<RRI>(reinterpret_cast<T*>(buf), b, ri0, rj0, 2 * m + 1, 2 * mp + 1, nf);
-    if (v.p)
-      stage_async<RVI>(reinterpret_cast<T*>(buf + kOffV), v, ri0 - 1, rj0 - 1, 2 * m + 3,
-                       2 * mp + 3, nf);
-  }
-  __device__ void compute(unsigned char* buf, int id, Acc&) const {
-    const Tile<RTI, RTJ> t = tile_at<RTI, RTJ>(id, ntx, nc);
-    T* sr = reinterpret_cast<T*>(buf);
-    const T* sv = reinterpret_cast<const T*>(buf + kOffV);
-    const int m = t.i_hi - t.i_lo, mp = t.j_hi - t.j_lo;
-    const int ri0 = 2 * t.i_lo - 1, rj0 = 2 * t.j_lo - 1;
-    const int rei = 2 * m + 1, rej = 2 * mp + 1;
-    const int lane = threadIdx.x & 31;
-    const int w = threadIdx.x >> 5;
-    if (v.p) {
-      for (int c = w; c < rej; c += kWarps) {
-        const int j = rj0 + c;
-        if (j < 0 || j >= nf) continue;
-        for (int r = lane; r < rei; r += 32) {
-          const int i = ri0 + r;
-          if (i < 0 || i >= nf) continue;
-          SAcc<T> a{sv + (c + 1) * RVI + (r + 1), RVI};
-          sr[c * RRI + r] += negA<T>(a, i, j, nf);
-        }
-      }
-      __syncthreads();
-    }
-    for (int c = w; c < mp; c += kWarps) {
-      const int J = t.j_lo + c;
-      for (int r = lane; r < m; r += 32) {
-        const int I = t.i_lo + r;
-        T acc = T(0);
-#pragma unroll
-        for (int bj = -1; bj <= 1; ++bj) {
-          const T wj = restrict_w1<T>(kind, J, nc, bj);
-#pragma unroll
-          for (int ai = -1; ai <= 1; ++ai) {
-            const T wi = restrict_w1<T>(kind, I, nc, ai);
-            acc = fma(wi * wj, sr[(2 * c + 1 + bj) * RRI + (2 * r + 1 + ai)], acc);
-          }
-        }
-        f.at(I, J) = acc;
-      }
-    }
-  }
-  __device__ void finish(double) const {}
-};
+cudaError_t launch_smooth(int field, int epi, Grid<const T> vin, Grid<const T> e, Grid<const T> b,
+                          Grid<T> vout, int n, int smoother, double omega, int dot,
+                          SolveState* st, ReduceBuf rb, cudaStream_t s) {
+  const int nc = (n + 1) / 2;
+  return launch_smooth_op<T>(field, epi, raw_operand(vin.p, n, vin.ld),
+                             raw_operand(e.p, nc, e.ld), raw_operand(b.p, n, b.ld), vout, n,
+                             smoother, omega, dot, st, rb, s);
+}
+
+template <typename T>
+cudaError_t launch_resrestrict_op(const Operand* v, const Operand& b, Grid<T> f, int nf, int kind,
+                                  const SolveState* st, cudaStream_t s) {
+  const int nc = (nf + 1) / 2;
+  const int ntx = ntiles(nc, RTI), nty = ntiles(nc, RTJ);
+  const int total = ntx * nty;
+  const Operand vv = v ? *v : Operand();
+  const DevOperand<T> dv = dev_operand<T>(vv), db = dev_operand<T>(b);
+  const int has_v = v ? 1 : 0;
+  if (b.tma && (!v || v->tma))
+    return launch_persist(
+        ResRestrictJob<T, true>{dv, db, f, nf, nc, ntx, total, kind, has_v, st, ReduceBuf{}},
+        total, s);
+  return launch_persist(
+      ResRestrictJob<T, false>{dv, db, f, nf, nc, ntx, total, kind, has_v, st, ReduceBuf{}},
+      total, s);
+}
 
 template <typename T>
 cudaError_t launch_resrestrict(Grid<const T> v, Grid<const T> b, Grid<T> f, int nf, int kind,
                                const SolveState* st, cudaStream_t s) {
-  const int nc = (nf + 1) / 2;
-  const int ntx = ntiles(nc, RTI), nty = ntiles(nc, RTJ);
-  const int total = ntx * nty;
-  return launch_persist(ResRestrictJob<T>{v, b, f, nf, nc, ntx, total, kind, st, ReduceBuf{}},
-                        total, s);
+  const Operand vo = raw_operand(v.p, nf, v.ld);
+  return launch_resrestrict_op<T>(v.p ? &vo : nullptr, raw_operand(b.p, nf, b.ld), f, nf, kind, st,
+                                  s);
 }
 
 // Resolve the launch configuration of every persistent kernel up front
 // (shared-memory attribute and occupancy), outside any stream capture.
-template <typename T>
+template <typename T, int F, int E, bool M>
+static void prep_smooth() {
+  persist_ctas_per_sm<SmoothJob<T, F, E, false, M>>();
+  persist_ctas_per_sm<SmoothJob<T, F, E, true, M>>();
+}
+template <typename T, bool M>
 static void prepare_precision() {
-  persist_ctas_per_sm<ApplyJob<T, false>>();
-  persist_ctas_per_sm<ApplyJob<T, true>>();
-  persist_ctas_per_sm<ResidualJob<T>>();
-  persist_ctas_per_sm<ResRestrictJob<T>>();
-  persist_ctas_per_sm<SmoothJob<T, kFieldPlain, kEpiSweep, false>>();
-  persist_ctas_per_sm<SmoothJob<T, kFieldPlain, kEpiSweep, true>>();
-  persist_ctas_per_sm<SmoothJob<T, kFieldPlain, kEpiStore, false>>();
-  persist_ctas_per_sm<SmoothJob<T, kFieldPlain, kEpiStore, true>>();
-  persist_ctas_per_sm<SmoothJob<T, kFieldZero, kEpiSweep, false>>();
-  persist_ctas_per_sm<SmoothJob<T, kFieldZero, kEpiSweep, true>>();
-  persist_ctas_per_sm<SmoothJob<T, kFieldZero, kEpiStore, false>>();
-  persist_ctas_per_sm<SmoothJob<T, kFieldZero, kEpiStore, true>>();
-  persist_ctas_per_sm<SmoothJob<T, kFieldProlong, kEpiSweep, false>>();
-  persist_ctas_per_sm<SmoothJob<T, kFieldProlong, kEpiSweep, true>>();
-  persist_ctas_per_sm<SmoothJob<T, kFieldProlong, kEpiStore, false>>();
-  persist_ctas_per_sm<SmoothJob<T, kFieldProlong, kEpiStore, true>>();
+  persist_ctas_per_sm<ApplyJob<T, false, M>>();
+  persist_ctas_per_sm<ApplyJob<T, true, M>>();
+  persist_ctas_per_sm<ResRestrictJob<T, M>>();
+  prep_smooth<T, kFieldPlain, kEpiSweep, M>();
+  prep_smooth<T, kFieldPlain, kEpiStore, M>();
+  prep_smooth<T, kFieldZero, kEpiSweep, M>();
+  prep_smooth<T, kFieldZero, kEpiStore, M>();
+  prep_smooth<T, kFieldProlong, kEpiSweep, M>();
+  prep_smooth<T, kFieldProlong, kEpiStore, M>();
 }
 
 cudaError_t prepare_kernels() {
   sm_count();
-  prepare_precision<double>();
-  prepare_precision<float>();
-  persist_ctas_per_sm<CgDirJob<double, double>>();
-  persist_ctas_per_sm<CgDirJob<double, float>>();
+  prepare_precision<double, false>();
+  prepare_precision<double, true>();
+  prepare_precision<float, false>();
+  prepare_precision<float, true>();
+  persist_ctas_per_sm<ResidualJob<double, false, false>>();
+  persist_ctas_per_sm<ResidualJob<double, true, false>>();
+  persist_ctas_per_sm<ResidualJob<double, true, true>>();
+  persist_ctas_per_sm<ResidualJob<double, false, true>>();
+  persist_ctas_per_sm<CgDirJob<double, double, false>>();
+  persist_ctas_per_sm<CgDirJob<double, double, true>>();
+  persist_ctas_per_sm<CgDirJob<double, float, false>>();
+  persist_ctas_per_sm<CgDirJob<double, float, true>>();
   return cudaGetLastError();
+}
+
+unsigned int read_device_fault() {
+  unsigned int v = 0;
+  cudaMemcpyFromSymbol(&v, g_sbp_fault, sizeof(v));
+  return v;
 }
 
 // ---------------------------------------------------------------------------
@@ -720,17 +1075,15 @@ cudaError_t launch_coarse_gemv(const double* Ainv, Grid<const T> f, Grid<T> e, i
 // ---------------------------------------------------------------------------
 template <typename Tin, typename Tout>
 __global__ void __launch_bounds__(kThreads)
-    k_copy(const Tin* __restrict__ in, Tout* __restrict__ out, long long N) {
-  const long long stride = (long long)gridDim.x * kThreads;
-  for (long long k = (long long)blockIdx.x * kThreads + threadIdx.x; k < N; k += stride)
-    out[k] = (Tout)__ldg(in + k);
+    k_copy(Grid<const Tin> in, Grid<Tout> out, int n) {
+  // grid-stride over columns, threads over rows
+  for (int j = blockIdx.x; j < n; j += gridDim.x)
+    for (int i = threadIdx.x; i < n; i += kThreads) out.at(i, j) = convert<Tout>(__ldg(&in.at(i, j)));
 }
 
 template <typename Tin, typename Tout>
 cudaError_t launch_copy(Grid<const Tin> in, Grid<Tout> out, int n, cudaStream_t s) {
-  if (in.ld != n || out.ld != n) return cudaErrorInvalidValue;
-  const long long N = (long long)n * n;
-  k_copy<Tin, Tout><<<flat_grid(N, 4), kThreads, 0, s>>>(in.p, out.p, N);
+  k_copy<Tin, Tout><<<std::min(n, 4096), kThreads, 0, s>>>(in, out, n);
   return cudaGetLastError();
 }
 
@@ -864,6 +1217,26 @@ SBP_INST_T(double)
 SBP_INST_T(float)
 #undef SBP_INST_T
 
+#define SBP_INST_OP(T)                                                                         \
+  template cudaError_t launch_apply_op<T>(const Operand&, Grid<T>, int, int, ReduceBuf, double*, \
+                                          cudaStream_t);                                         \
+  template cudaError_t launch_smooth_op<T>(int, int, const Operand&, const Operand&,             \
+                                           const Operand&, Grid<T>, int, int, double, int,       \
+                                           SolveState*, ReduceBuf, cudaStream_t);                \
+  template cudaError_t launch_resrestrict_op<T>(const Operand*, const Operand&, Grid<T>, int, int, \
+                                                const SolveState*, cudaStream_t);
+SBP_INST_OP(double)
+SBP_INST_OP(float)
+#undef SBP_INST_OP
+template cudaError_t launch_residual_op<double>(const Operand&, const Operand&, Grid<double>,
+                                                Grid<float>, int, int, SolveState*, double*, double,
+                                                double, int, double*, ReduceBuf, cudaStream_t);
+template cudaError_t launch_cg_dir_op<double, double>(const Operand&, const Operand&, Grid<double>,
+                                                      Grid<double>, int, int, SolveState*,
+                                                      ReduceBuf, cudaStream_t);
+template cudaError_t launch_cg_dir_op<double, float>(const Operand&, const Operand&, Grid<double>,
+                                                     Grid<double>, int, int, SolveState*,
+                                                     ReduceBuf, cudaStream_t);
 template cudaError_t launch_cg_dir<double, double>(Grid<const double>, Grid<const double>,
                                                    Grid<double>, Grid<double>, int, int,
                                                    SolveState*, ReduceBuf, cudaStream_t);

@@ -19,6 +19,8 @@
 //    needs no host round trip.
 #pragma once
 
+#include <cuda.h>
+
 #include "sbp_common.cuh"
 
 namespace sbp {
@@ -88,6 +90,66 @@ __device__ __forceinline__ void cp_async_commit() {
 template <int N>
 __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// ---------------------------------------------------------------------------
+// TMA (cp.async.bulk.tensor) and mbarrier helpers.  One thread issues a 2D
+// tensor copy of a whole staged box; the copy reports its bytes to an
+// mbarrier that the CTA waits on.  Out-of-range box elements are zero-filled
+// by the hardware, which replaces every bounds check of the staging.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+// Order this thread's earlier generic-proxy shared-memory accesses before
+// later async-proxy (TMA) writes to the same buffer.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
+                                            unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];\n" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned phase) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(phase)
+      : "memory");
+  return ok != 0u;
+}
+
+// Set (never cleared by the kernels) when a bounded wait gives up; read by
+// the host through read_device_fault().  This header is included by one
+// translation unit only (sbp_kernels.cu), which owns the definition.
+__device__ unsigned int g_sbp_fault = 0u;
+
+// Bounded wait on an mbarrier phase.  try_wait suspends for a bounded,
+// hardware-defined time per call, so the limit is seconds: far beyond any
+// legitimate TMA latency, short enough that a lost copy cannot hang the GPU.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned phase) {
+  for (unsigned it = 0; it < (1u << 22); ++it)
+    if (mbar_try_wait(bar, phase)) return true;
+  atomicOr(&g_sbp_fault, 1u);
+  return false;
 }
 
 // ---------------------------------------------------------------------------

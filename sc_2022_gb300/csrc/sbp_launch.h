@@ -5,8 +5,34 @@
 #include <cuda_runtime.h>
 
 #include "sbp_common.cuh"
+#include "sbp_tma.h"
 
 namespace sbp {
+
+// Operand-based launchers (TMA staging when the operands allow it).  The
+// Grid-based launchers below use element-wise cp.async staging and accept any
+// leading dimension.
+template <typename T>
+cudaError_t launch_apply_op(const Operand& u, Grid<T> out, int n, int sign, ReduceBuf rb,
+                            double* dot_out, cudaStream_t s);
+template <typename T>
+cudaError_t launch_residual_op(const Operand& x, const Operand& b, Grid<T> r, Grid<float> rlo,
+                               int n, int opsign, SolveState* st, double* norms, double abstol,
+                               double reltol, int plain, double* out2, ReduceBuf rb,
+                               cudaStream_t s);
+template <typename T, typename Tz>
+cudaError_t launch_cg_dir_op(const Operand& z, const Operand& pold, Grid<T> pnew, Grid<T> Ap,
+                             int n, int opsign, SolveState* st, ReduceBuf rb, cudaStream_t s);
+template <typename T>
+cudaError_t launch_smooth_op(int field, int epi, const Operand& vin, const Operand& e,
+                             const Operand& b, Grid<T> vout, int n, int smoother, double omega,
+                             int dot, SolveState* st, ReduceBuf rb, cudaStream_t s);
+template <typename T>
+cudaError_t launch_resrestrict_op(const Operand* v, const Operand& b, Grid<T> f, int nf, int kind,
+                                  const SolveState* st, cudaStream_t s);
+
+// Non-zero once a kernel's bounded wait on an asynchronous copy gave up.
+unsigned int read_device_fault();
 
 // Upper bound on the CTAs any reducing launch uses for an n x n grid; the
 // partials buffer of a ReduceBuf must hold this many doubles.
@@ -73,11 +99,11 @@ template <typename T>
 cudaError_t launch_coarse_gemv(const double* Ainv, Grid<const T> f, Grid<T> e, int nc,
                                const SolveState* st, cudaStream_t s);
 
-// out = convert(in) on an n x n grid.
+// out = convert(in) on an n x n grid (any leading dimensions).
 template <typename Tin, typename Tout>
 cudaError_t launch_copy(Grid<const Tin> in, Grid<Tout> out, int n, cudaStream_t s);
 
-// *out = sum(a .* b) on an n x n grid.
+// *out = sum(a .* b) on an n x n grid (contiguous, ld == n).
 template <typename T>
 cudaError_t launch_dot(Grid<const T> a, Grid<const T> b, int n, double* out, ReduceBuf rb,
                        cudaStream_t s);
