@@ -113,6 +113,26 @@ int sbp_apply_f32(const float* u, float* out, int n, int sign, void* stream);
 int sbp_apply_dot_f64(const double* u, double* out, int n, int sign, double* dot,
                       void* stream);
 
+/* Same result as sbp_apply_dot_f64, but the call allocates nothing.  It is
+ * for callers that cannot let a library allocate device memory on their
+ * behalf: hosts whose device memory is owned by their own allocator or pool
+ * (a language runtime's managed heap, a fixed memory budget) and
+ * latency-critical loops that must not enter the CUDA allocator.  No
+ * counterpart in the reference.
+ *
+ * The per-CTA partial sums of the dot product live in a static device
+ * array of the library: 1024 slots of 8 bytes plus a counter, about 8 KB,
+ * resident on every GPU that has used it until the process exits.  A launch
+ * needing more than 1024 CTAs is rejected with SBP_ERR_UNSUPPORTED (a
+ * 152-SM GB300 uses 760).  The first call on a device resolves the array's
+ * device address (cudaGetSymbolAddress) and caches it; make that first call
+ * before any stream capture.  Every call uses the same array: calls that
+ * may run concurrently on the GPU (different streams without ordering) race
+ * on it, so order them.  The counter is cleared at the start of each call;
+ * the partial slots are fully rewritten by every launch. */
+int sbp_apply_dot_f64_noalloc(const double* u, double* out, int n, int sign, double* dot,
+                              void* stream);
+
 /* *norm_host = ||b - sign*A*x||_2 (blocking).  The reference's residual
  * check norm(-Av - b) (matrix_free_mg_cg.jl:175). */
 int sbp_residual_norm_f64(const double* x, const double* b, int n, int sign, double* norm_host,

@@ -66,6 +66,7 @@ SIGNATURES = {
     "sbp_apply_f64": (_i, [_vp, _vp, _i, _i, _vp]),
     "sbp_apply_f32": (_i, [_vp, _vp, _i, _i, _vp]),
     "sbp_apply_dot_f64": (_i, [_vp, _vp, _i, _i, _vp, _vp]),
+    "sbp_apply_dot_f64_noalloc": (_i, [_vp, _vp, _i, _i, _vp, _vp]),
     "sbp_residual_norm_f64": (_i, [_vp, _vp, _i, _i, _dp, _vp]),
     "sbp_restrict_f64": (_i, [_vp, _vp, _i, _i, _vp]),
     "sbp_prolong_f64": (_i, [_vp, _vp, _i, _i, _vp]),

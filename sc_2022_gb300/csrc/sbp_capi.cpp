@@ -487,6 +487,16 @@ int sbp_apply_dot_f64(const double* u, double* out, int n, int sign, double* dot
   return SBP_OK;
 }
 
+int sbp_apply_dot_f64_noalloc(const double* u, double* out, int n, int sign, double* dot,
+                              void* stream) {
+  const int rc = apply_dot_f64_noalloc(u, out, n, sign, dot, (cudaStream_t)stream);
+  if (rc == SBP_ERR_CUDA) g_last_error = cudaGetErrorString(cudaGetLastError());
+  if (rc == SBP_ERR_UNSUPPORTED)
+    g_last_error = "sbp_apply_dot_f64_noalloc: the launch needs more than the 1024 partial-sum "
+                   "slots of the static scratch";
+  return rc;
+}
+
 int sbp_residual_norm_f64(const double* x, const double* b, int n, int sign, double* norm_host,
                           void* stream) {
   if (!x || !b || !norm_host || n < 3 || (sign != 1 && sign != -1)) return SBP_ERR_ARGS;

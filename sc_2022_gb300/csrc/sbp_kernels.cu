@@ -4,6 +4,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "sbp_kernels.cuh"
 #include "sbp_launch.h"
@@ -1254,5 +1255,73 @@ template cudaError_t launch_copy<float, double>(Grid<const float>, Grid<double>,
                                                 cudaStream_t);
 template cudaError_t launch_copy<float, float>(Grid<const float>, Grid<float>, int,
                                                cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// Allocation-free operator apply + dot (sbp_apply_dot_f64_noalloc).
+//
+// The regular sbp_apply_dot_f64 takes its per-CTA partial sums from
+// stream-ordered scratch (cudaMallocAsync).  This variant keeps that scratch
+// in the file-scope array below instead, so a call never reaches the CUDA
+// allocator.  The array is loaded with the library and stays resident on
+// every GPU that uses it until the process exits.
+// ---------------------------------------------------------------------------
+namespace {
+
+// Partial-sum slots: one per CTA of the launch.  A persistent launch uses
+// SMs x resident CTAs (760 for this kernel on a 152-SM GB300), so 1024 slots
+// cover it; a launch needing more is rejected.
+constexpr int kNoAllocSlots = 1024;
+constexpr size_t kNoAllocTicketOffset = kNoAllocSlots * sizeof(double);
+constexpr size_t kNoAllocBytes = kNoAllocTicketOffset + 256;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+// Device address of g_noalloc_scratch, resolved once per device.  Host code
+// must not pass the symbol itself to a kernel: on the host it names a
+// stand-in, not device memory.
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[64] = {nullptr};
+
+cudaError_t noalloc_scratch(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return cudaSuccess;
+}
+
+}  // namespace
+
+// Returns 0, or -1 (arguments), -2 (CUDA error), -6 (scratch too small).
+int apply_dot_f64_noalloc(const double* u, double* out, int n, int sign, double* dot,
+                          cudaStream_t s) {
+  if (!u || !out || !dot || n < 3 || (sign != 1 && sign != -1)) return -1;
+  void* scratch = nullptr;
+  if (noalloc_scratch(&scratch) != cudaSuccess) return -2;
+  using Job = ApplyJob<double, true, false>;
+  const dim3 g = tile_grid(n);
+  const int total = (int)(g.x * g.y);
+  const int cap = std::min(kMaxPersistCtas, sm_count() * persist_ctas_per_sm<Job>());
+  const int grid = std::max(1, std::min(total, cap));
+  if (grid > kNoAllocSlots) return -6;
+  unsigned char* base = static_cast<unsigned char*>(scratch);
+  ReduceBuf rb{reinterpret_cast<double*>(base),
+               reinterpret_cast<unsigned*>(base + kNoAllocTicketOffset)};
+  // the ticket must start at zero; the partial slots are overwritten by
+  // every launch before they are read
+  if (cudaMemsetAsync(rb.ticket, 0, sizeof(unsigned), s) != cudaSuccess) return -2;
+  const Operand uo = raw_operand(u, n, n);
+  const Job job{dev_operand<double>(uo), Grid<double>{out, n}, n, (int)g.x, total, sign, rb, dot};
+  k_persist<Job><<<grid, kThreads, 2 * Job::kStage + 128, s>>>(job);
+  return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
 
 }  // namespace sbp

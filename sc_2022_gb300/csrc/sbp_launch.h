@@ -31,6 +31,12 @@ template <typename T>
 cudaError_t launch_resrestrict_op(const Operand* v, const Operand& b, Grid<T> f, int nf, int kind,
                                   const SolveState* st, cudaStream_t s);
 
+// Allocation-free apply + dot with the reduction scratch in a static device
+// array (see sbp_apply_dot_f64_noalloc in sbpmg.h).  Returns 0 or a negative
+// sbp_status value.
+int apply_dot_f64_noalloc(const double* u, double* out, int n, int sign, double* dot,
+                          cudaStream_t s);
+
 // Non-zero once a kernel's bounded wait on an asynchronous copy gave up.
 unsigned int read_device_fault();
 
