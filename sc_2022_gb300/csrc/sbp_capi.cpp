@@ -223,8 +223,10 @@ cudaError_t enqueue_iteration(sbp_solver* s, int kind, int parity, int sign, cud
   const bool mixed = (kind == 0 && s->opts.precision == SBP_PREC_MIXED);
   if (kind == 0) {
     if (mixed)
-      e = launch_cg_dir_op<double, float>(vcycle_out_op(s), s->op[parity], grid<double>(pnew, ld),
-                                          grid<double>(s->Ap, ld), n, +1, s->st, s->rb, q);
+      // Ap is updated in place (each point reads its old value, then writes)
+      e = launch_cg_dir_mixed<double>(vcycle_out_op(s), cgrid<double>(s->p[parity], ld),
+                                      cgrid<double>(s->Ap, ld), grid<double>(pnew, ld),
+                                      grid<double>(s->Ap, ld), n, s->st, s->rb, q);
     else
       e = launch_cg_dir_op<double, double>(vcycle_out_op(s), s->op[parity], grid<double>(pnew, ld),
                                            grid<double>(s->Ap, ld), n, +1, s->st, s->rb, q);

@@ -508,6 +508,98 @@ struct CgDirJob {
 };
 
 // ---------------------------------------------------------------------------
+// Mixed-precision CG direction: z is the FP32 V-cycle output, p and Ap FP64.
+//   p  = z + beta p_old
+//   Ap = A z + beta Ap_old          (A p by linearity, Ap_old from last step)
+//   p.Ap -> alpha
+// A z is evaluated exactly on the FP32 pipe (float-float stencil) and the
+// FP64 pipe does only one add and three FMAs per point; p_old / Ap_old are
+// read pointwise, so only z is staged (with its halo).
+// ---------------------------------------------------------------------------
+template <bool TMA>
+struct CgDirMixedJob {
+  static constexpr int kStage = align128(box_bytes<float, BI, BJ>());
+  static constexpr bool kReduce = true;
+  using Acc = DotAcc<double>;
+  using Ctx = DirCtx;
+  DevOperand<float> z;
+  Grid<const double> pold, apold;
+  Grid<double> pnew, Ap;
+  int n, ntx, ntot;
+  SolveState* st;
+  ReduceBuf rb;
+  __device__ bool prepare(Ctx& c) const {
+    if (st->done) return true;
+    c.first = (st->iter == 0);
+    c.beta = st->beta;
+    return false;
+  }
+  __device__ int tiles() const { return ntot; }
+  __device__ unsigned tx_bytes(int) const { return TMA ? box_bytes<float, BI, BJ>() : 0u; }
+  __device__ void issue(unsigned char* buf, unsigned long long* bar, int id, const Ctx&) const {
+    const TileBoxes bx(id % ntx, tile_at<TI, TJ>(id, ntx, n).j_lo);
+    stage_box<TMA, BI, BJ>(reinterpret_cast<float*>(buf), z, &z.box, bx.x0, bx.y0, n, bar);
+  }
+  __device__ void compute(unsigned char* buf, int id, Acc& acc, const Ctx& c) const {
+    const TileT t = tile_at<TI, TJ>(id, ntx, n);
+    const TileBoxes bx(id % ntx, t.j_lo);
+    const float* s = reinterpret_cast<const float*>(buf);
+    const double beta = c.beta;
+    const bool first = c.first;
+    auto emit = [&](int i, int j, float zc, double az) {
+      const double zd = f32_to_f64(zc);
+      double pv = zd, ap = az;
+      if (!first) {
+        pv = fma(beta, __ldg(&pold.at(i, j)), zd);
+        ap = fma(beta, __ldg(&apold.at(i, j)), az);
+      }
+      pnew.at(i, j) = pv;
+      Ap.at(i, j) = ap;
+      acc.add_prod(pv, ap);
+    };
+    if (tile_interior(t, n)) {
+      visit_interior(s, t, [&](int i, int j, float um, float u0, float up, float uw, float ue,
+                               int) {
+        float hi, lo;
+        stencil_ff(uw, ue, um, up, u0, hi, lo);
+        // A z = -(stencil)
+        emit(i, j, u0, -(f32_to_f64(hi) + f32_to_f64(lo)));
+      });
+    } else {
+      visit_generic(s, t, bx, [&](int i, int j, const SAcc<float>& a, int) {
+        // boundary rows/columns: the SAT stencil in FP64 on the exact FP32 values
+        struct D {
+          const SAcc<float>* a;
+          __device__ double operator()(int di, int dj) const { return f32_to_f64((*a)(di, dj)); }
+        } d{&a};
+        emit(i, j, a(0, 0), -negA<double>(d, i, j, n));
+      });
+    }
+  }
+  __device__ void finish(double tot) const {
+    st->pAp = tot;
+    if (!isfinite(tot) || tot == 0.0)
+      st->done = kDoneBreakdown;
+    else
+      st->alpha = st->rz / tot;
+  }
+};
+
+template <typename T>
+cudaError_t launch_cg_dir_mixed(const Operand& z, Grid<const double> pold,
+                                Grid<const double> apold, Grid<double> pnew, Grid<double> Ap,
+                                int n, SolveState* st, ReduceBuf rb, cudaStream_t s) {
+  const dim3 g = tile_grid(n);
+  const int total = (int)(g.x * g.y);
+  const DevOperand<float> dz = dev_operand<float>(z);
+  if (z.tma)
+    return launch_persist(
+        CgDirMixedJob<true>{dz, pold, apold, pnew, Ap, n, (int)g.x, total, st, rb}, total, s);
+  return launch_persist(
+      CgDirMixedJob<false>{dz, pold, apold, pnew, Ap, n, (int)g.x, total, st, rb}, total, s);
+}
+
+// ---------------------------------------------------------------------------
 // CG update (pointwise, flat, 16-byte vectors): x += alpha p; r -= alpha Ap;
 // ||r||^2; convergence test.  The arrays share one layout; padding entries
 // are zero and stay zero.
@@ -988,6 +1080,8 @@ cudaError_t prepare_kernels() {
   persist_ctas_per_sm<CgDirJob<double, double, true>>();
   persist_ctas_per_sm<CgDirJob<double, float, false>>();
   persist_ctas_per_sm<CgDirJob<double, float, true>>();
+  persist_ctas_per_sm<CgDirMixedJob<false>>();
+  persist_ctas_per_sm<CgDirMixedJob<true>>();
   return cudaGetLastError();
 }
 
@@ -1238,6 +1332,9 @@ template cudaError_t launch_cg_dir_op<double, double>(const Operand&, const Oper
 template cudaError_t launch_cg_dir_op<double, float>(const Operand&, const Operand&, Grid<double>,
                                                      Grid<double>, int, int, SolveState*,
                                                      ReduceBuf, cudaStream_t);
+template cudaError_t launch_cg_dir_mixed<double>(const Operand&, Grid<const double>,
+                                                 Grid<const double>, Grid<double>, Grid<double>,
+                                                 int, SolveState*, ReduceBuf, cudaStream_t);
 template cudaError_t launch_cg_dir<double, double>(Grid<const double>, Grid<const double>,
                                                    Grid<double>, Grid<double>, int, int,
                                                    SolveState*, ReduceBuf, cudaStream_t);

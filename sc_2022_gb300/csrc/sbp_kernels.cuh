@@ -198,6 +198,29 @@ template <>
 __device__ __forceinline__ float convert<float, double>(double v) { return f64_to_f32(v); }
 
 // ---------------------------------------------------------------------------
+// Error-free FP32 arithmetic.  two_sum gives s + e == a + b exactly (Knuth).
+// stencil_ff returns the 5-point stencil (uw + ue) + (um + up) - 4 u0 of FP32
+// values as an unevaluated float pair hi + lo whose error is below 2^-45 of
+// the largest term: FP64-grade accuracy from the FP32 pipe, which GB300
+// issues 64x faster than FP64.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ void stencil_ff(float uw, float ue, float um, float up, float u0,
+                                           float& hi, float& lo) {
+  float a, ea, b, eb, c, ec, d, ed;
+  two_sum(uw, ue, a, ea);
+  two_sum(um, up, b, eb);
+  two_sum(a, b, c, ec);
+  two_sum(c, -4.0f * u0, d, ed);
+  hi = d;
+  lo = (ea + eb) + (ec + ed);
+}
+
+// ---------------------------------------------------------------------------
 // Dot-product accumulators.  FP64 data: an FP64 FMA per term.  FP32 data:
 // each product is split exactly into p + e (FMA) and summed with a
 // compensated (TwoSum) float-float accumulator, converted to FP64 once per
