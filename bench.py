@@ -44,7 +44,7 @@ def parse_args():
     p.add_argument("--n", type=int, default=4097)
     p.add_argument("--apply-iters", type=int, default=50)
     p.add_argument("--cpu-baseline", type=int, default=1, help="time the CPU baseline leg")
-    p.add_argument("--mode", choices=["full", "apply", "solve-fp64", "solve-mixed"],
+    p.add_argument("--mode", choices=["full", "apply", "solve-fp64", "solve-mixed", "vcycle"],
                    default="full", help="profiling modes run one part only and print a "
                    "short line (not the benchmark line)")
     return p.parse_args()
@@ -387,6 +387,29 @@ def run_part(args):
             assert rc == 0
         torch.cuda.synchronize()
         print(json.dumps({"mode": "apply", "n": n, "launches": args.warmup + args.steps}))
+        return
+    if args.mode == "vcycle":
+        # time one V-cycle (mixed and FP64) for the default hierarchy at --n
+        out = {"mode": "vcycle", "n": n}
+        gen = torch.Generator(device=dev).manual_seed(0)
+        b = torch.randn(n * n, generator=gen, device=dev, dtype=torch.float64)
+        v = torch.empty_like(b)
+        for name, prec in (("mixed", _lib.SBP_PREC_MIXED), ("fp64", _lib.SBP_PREC_FP64)):
+            s = sbp.Solver(n, sbp.default_options(prec))
+            for _ in range(args.warmup):
+                s.vcycle(b, v)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(args.steps):
+                s.vcycle(b, v)
+            e1.record()
+            torch.cuda.synchronize()
+            out[name + "_us"] = round(1e3 * e0.elapsed_time(e1) / args.steps, 2)
+            out["levels"] = s.levels
+            s.close()
+        print(json.dumps(out))
         return
     prec = _lib.SBP_PREC_MIXED if args.mode == "solve-mixed" else _lib.SBP_PREC_FP64
     f, g, _ = problems.manufactured(n, "baseline")
