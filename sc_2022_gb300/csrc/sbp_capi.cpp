@@ -130,6 +130,17 @@ void destroy_graphs(sbp_solver* s) {
 //         b.z into the Krylov state when `dot` is set.
 // Last level: v = Ainv b (dense FP64 GEMV).
 // ---------------------------------------------------------------------------
+// Temporal blocking (one fused pre-smoothing and one fused post-smoothing
+// kernel per level) for FP32 levels: their sweeps are memory-bound, so
+// recomputing halos in shared memory is cheap.  FP64 levels are bound by the
+// FP64 pipe and keep the one-sweep-per-pass schedule, which does no redundant
+// halo arithmetic.
+template <typename T>
+bool use_fused(const sbp_solver* s) {
+  const sbp_options& o = s->opts;
+  return sizeof(T) == 4 && o.nu_pre >= 1 && o.nu_pre <= 3 && o.nu_post >= 0 && o.nu_post <= 3;
+}
+
 template <typename T>
 cudaError_t enqueue_vcycle(sbp_solver* s, size_t l, bool dot, SolveState* st, cudaStream_t q) {
   Level& L = s->levels[l];
@@ -149,6 +160,18 @@ cudaError_t enqueue_vcycle(sbp_solver* s, size_t l, bool dot, SolveState* st, cu
                               n, sm, om, 1, st, s->rb, q);
       L.out = 1;
     }
+    return e;
+  }
+  if (use_fused<T>(s)) {
+    Level& C = s->levels[l + 1];
+    e = launch_pre_fused<T>(L.ob, grid<T>(L.v[0], L.ld), grid<T>(C.b, C.ld), n, o.nu_pre, sm, om,
+                            o.restriction, st, q);
+    if (e != cudaSuccess) return e;
+    e = enqueue_vcycle<T>(s, l + 1, false, st, q);
+    if (e != cudaSuccess) return e;
+    e = launch_post_fused<T>(L.ov[0], C.ov[C.out], L.ob, grid<T>(L.v[1], L.ld), n, o.nu_post, sm,
+                             om, dot ? 1 : 0, st, s->rb, q);
+    L.out = 1;
     return e;
   }
   int k;
@@ -188,7 +211,13 @@ long long vcycle_launches(const sbp_solver* s, bool dot) {
   const sbp_options& o = s->opts;
   long long c = 0;
   const size_t nl = s->levels.size();
+  const bool fused = (s->opts.precision == SBP_PREC_MIXED) ? use_fused<float>(s)
+                                                           : use_fused<double>(s);
   for (size_t l = 0; l + 1 < nl; ++l) {
+    if (fused) {
+      c += 2;                             // fused pre-smoothing, fused post-smoothing
+      continue;
+    }
     c += (o.nu_pre >= 2) ? 1 + (o.nu_pre - 2) : 1;
     c += 1;                               // residual + restriction
     c += std::max(1, o.nu_post);          // prolongation + post sweeps

@@ -34,6 +34,16 @@ template <typename T>
 cudaError_t launch_smooth_op(int field, int epi, const Operand& vin, const Operand& e,
                              const Operand& b, Grid<T> vout, int n, int smoother, double omega,
                              int dot, SolveState* st, ReduceBuf rb, cudaStream_t s);
+// Fused V-cycle passes (temporal blocking, sweeps <= 3): pre-smoothing from
+// zero + residual + restriction into f, and prolongation + post-smoothing.
+template <typename T>
+cudaError_t launch_pre_fused(const Operand& b, Grid<T> vout, Grid<T> f, int nf, int sweeps,
+                             int smoother, double omega, int kind, const SolveState* st,
+                             cudaStream_t s);
+template <typename T>
+cudaError_t launch_post_fused(const Operand& vin, const Operand& e, const Operand& b, Grid<T> vout,
+                              int n, int sweeps, int smoother, double omega, int dot,
+                              SolveState* st, ReduceBuf rb, cudaStream_t s);
 template <typename T>
 cudaError_t launch_resrestrict_op(const Operand* v, const Operand& b, Grid<T> f, int nf, int kind,
                                   const SolveState* st, cudaStream_t s);

@@ -39,6 +39,11 @@ bool encode(CUtensorMap* m, const void* p, int n, int ld, bool f64, int bi, int 
 
 }  // namespace
 
+bool make_box_map(CUtensorMap& m, const Operand& op, bool f64, int bi, int bj) {
+  if (!op.tma) return false;
+  return encode(&m, op.p, op.n, op.ld, f64, bi, bj);
+}
+
 bool make_operand(Operand& op, const void* p, int n, int ld, bool f64) {
   op.p = p;
   op.n = n;

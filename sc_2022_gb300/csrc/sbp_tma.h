@@ -31,6 +31,9 @@ struct Operand {
 // the layout is not TMA-addressable or the driver entry point is missing.
 bool make_operand(Operand& op, const void* p, int n, int ld, bool f64);
 
+// A tensor map of `op`'s array with an arbitrary box (bi x bj elements).
+bool make_box_map(CUtensorMap& m, const Operand& op, bool f64, int bi, int bj);
+
 // Leading dimension the solver uses for its own n x n arrays: a multiple of
 // four elements, so every column starts on a 16-byte boundary.
 inline int padded_ld(int n) { return (n + 3) & ~3; }
