@@ -135,10 +135,17 @@ void destroy_graphs(sbp_solver* s) {
 // recomputing halos in shared memory is cheap.  FP64 levels are bound by the
 // FP64 pipe and keep the one-sweep-per-pass schedule, which does no redundant
 // halo arithmetic.
+// Levels up to this size are fused: there the six-kernel schedule is bound
+// by launch latency, while on larger levels the one-sweep kernels already
+// run at memory speed and the fused kernels' halo arithmetic costs more than
+// the traffic it saves (measured at N = 4097 on GB300).
+constexpr int kFuseMaxN = 2049;
+
 template <typename T>
-bool use_fused(const sbp_solver* s) {
+bool use_fused(const sbp_solver* s, int n) {
   const sbp_options& o = s->opts;
-  return sizeof(T) == 4 && o.nu_pre >= 1 && o.nu_pre <= 3 && o.nu_post >= 0 && o.nu_post <= 3;
+  return sizeof(T) == 4 && n <= kFuseMaxN && o.nu_pre >= 1 && o.nu_pre <= 3 && o.nu_post >= 0 &&
+         o.nu_post <= 3;
 }
 
 template <typename T>
@@ -162,7 +169,7 @@ cudaError_t enqueue_vcycle(sbp_solver* s, size_t l, bool dot, SolveState* st, cu
     }
     return e;
   }
-  if (use_fused<T>(s)) {
+  if (use_fused<T>(s, n)) {
     Level& C = s->levels[l + 1];
     e = launch_pre_fused<T>(L.ob, grid<T>(L.v[0], L.ld), grid<T>(C.b, C.ld), n, o.nu_pre, sm, om,
                             o.restriction, st, q);
@@ -211,10 +218,10 @@ long long vcycle_launches(const sbp_solver* s, bool dot) {
   const sbp_options& o = s->opts;
   long long c = 0;
   const size_t nl = s->levels.size();
-  const bool fused = (s->opts.precision == SBP_PREC_MIXED) ? use_fused<float>(s)
-                                                           : use_fused<double>(s);
+  const bool mixed = (s->opts.precision == SBP_PREC_MIXED);
   for (size_t l = 0; l + 1 < nl; ++l) {
-    if (fused) {
+    const int n = s->levels[l].n;
+    if (mixed ? use_fused<float>(s, n) : use_fused<double>(s, n)) {
       c += 2;                             // fused pre-smoothing, fused post-smoothing
       continue;
     }

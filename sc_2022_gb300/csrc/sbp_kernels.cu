@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <mutex>
+#include <utility>
 
 #include "sbp_kernels.cuh"
 #include "sbp_launch.h"
@@ -56,6 +57,23 @@ static inline int flat_grid(long long N, int per) {
 int max_reduce_ctas(int n) {
   const dim3 g = tile_grid(n);
   return std::max((int)(g.x * g.y), kMaxPersistCtas);
+}
+
+// Launch with programmatic dependent launch enabled (see pdl_begin()).
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                              cudaStream_t s, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
 static int sm_count() {
@@ -237,6 +255,7 @@ template <class Job>
 __global__ void __launch_bounds__(kThreads) k_persist(const __grid_constant__ Job job) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) unsigned long long bar[2];
+  pdl_begin();
   typename Job::Ctx ctx;
   if (job.prepare(ctx)) return;
   const int total = job.tiles();
@@ -304,8 +323,8 @@ template <class Job>
 static cudaError_t launch_persist(const Job& job, int total, cudaStream_t s) {
   const int cap = std::min(kMaxPersistCtas, sm_count() * persist_ctas_per_sm<Job>());
   const int grid = std::max(1, std::min(total, cap));
-  k_persist<Job><<<grid, kThreads, 2 * Job::kStage + Job::kScratch + 128, s>>>(job);
-  return cudaGetLastError();
+  return launch_pdl(k_persist<Job>, dim3(grid), dim3(kThreads),
+                    (size_t)(2 * Job::kStage + Job::kScratch + 128), s, job);
 }
 
 struct NoCtx {};
@@ -645,6 +664,7 @@ __global__ void __launch_bounds__(kThreads)
     k_cg_update(double* __restrict__ x, double* __restrict__ r, const double* __restrict__ p,
                 const double* __restrict__ Ap, float* __restrict__ rlo, long long N, int plain,
                 SolveState* st, double* norms, ReduceBuf rb) {
+  pdl_begin();
   if (st->done) return;
   const double alpha = st->alpha;
   double acc = 0.0;
@@ -1255,10 +1275,10 @@ cudaError_t launch_cg_update(Grid<T> x, Grid<T> r, Grid<const T> p, Grid<const T
                    (!rlo.p || ((uintptr_t)rlo.p & 7u) == 0) && (ld % 2 == 0 || N % 2 == 0);
   const int g = flat_grid(N, vec ? 4 : 2);
   if (vec)
-    k_cg_update<true><<<g, kThreads, 0, s>>>(x.p, r.p, p.p, Ap.p, rlo.p, N, plain, st, norms, rb);
-  else
-    k_cg_update<false><<<g, kThreads, 0, s>>>(x.p, r.p, p.p, Ap.p, rlo.p, N, plain, st, norms, rb);
-  return cudaGetLastError();
+    return launch_pdl(k_cg_update<true>, dim3(g), dim3(kThreads), 0, s, x.p, r.p, p.p, Ap.p, rlo.p,
+                      N, plain, st, norms, rb);
+  return launch_pdl(k_cg_update<false>, dim3(g), dim3(kThreads), 0, s, x.p, r.p, p.p, Ap.p, rlo.p,
+                    N, plain, st, norms, rb);
 }
 
 template <typename T, int FIELD, int EPI, bool TMA>
@@ -1474,6 +1494,7 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads)
     k_coarse_gemv(const double* __restrict__ Ainv, Grid<const T> f, Grid<T> e, int nc,
                   const SolveState* st) {
+  pdl_begin();
   if (st && st->done) return;
   extern __shared__ double sf[];
   const int N = nc * nc;
@@ -1514,8 +1535,7 @@ cudaError_t launch_coarse_gemv(const double* Ainv, Grid<const T> f, Grid<T> e, i
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
   }
-  k_coarse_gemv<T><<<grid, kThreads, smem, s>>>(Ainv, f, e, nc, st);
-  return cudaGetLastError();
+  return launch_pdl(k_coarse_gemv<T>, dim3(grid), dim3(kThreads), smem, s, Ainv, f, e, nc, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -1556,14 +1576,14 @@ cudaError_t launch_dot(Grid<const T> a, Grid<const T> b, int n, double* out, Red
 }
 
 __global__ void k_state_init(SolveState* st, int maxiter) {
+  pdl_begin();
   SolveState z = {};
   z.maxiter = maxiter;
   *st = z;
 }
 
 cudaError_t launch_state_init(SolveState* st, int maxiter, cudaStream_t s) {
-  k_state_init<<<1, 1, 0, s>>>(st, maxiter);
-  return cudaGetLastError();
+  return launch_pdl(k_state_init, dim3(1), dim3(1), 0, s, st, maxiter);
 }
 
 // ---------------------------------------------------------------------------

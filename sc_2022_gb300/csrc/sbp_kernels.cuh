@@ -153,6 +153,19 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsig
 }
 
 // ---------------------------------------------------------------------------
+// Programmatic dependent launch.  Kernels of the solver are launched with the
+// programmatic-serialization attribute: the next kernel in the stream (or
+// graph) may be scheduled as soon as every CTA of this one has started, and
+// waits in pdl_begin() until this one has finished and its writes are
+// visible.  The launch latency of the dependent kernel thus overlaps this
+// kernel's execution.  pdl_begin() must precede every global-memory access.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void pdl_begin() {
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+
+// ---------------------------------------------------------------------------
 // float <-> double with integer instructions only.  On GB300 the FP64 pipe
 // issues about two lanes per clock per SM, and the hardware conversions run
 // there too; the solver's conversions (r -> FP32 for the V-cycle, z -> FP64
