@@ -68,7 +68,7 @@ typedef struct sbp_options {
   int nu_pre;       /* pre-smoothing sweeps */
   int nu_post;      /* post-smoothing sweeps */
   int restriction;  /* sbp_restriction */
-  int coarse_n;     /* grid size of the direct coarse solve (<= 65) */
+  int coarse_n;     /* grid size of the direct coarse solve (<= 257) */
   int precision;    /* sbp_precision */
   int reserved[5];
 } sbp_options;
@@ -95,7 +95,7 @@ void sbp_options_default(sbp_options* opts);
 /* The reference's own two-level GPU preconditioner
  * (matrix_free_Two_level_multigrid, matrix_free_mg_cg.jl:143-176):
  * Richardson omega = 0.15, nu = 3 + 3, NORMAL restriction, exact coarse
- * solve at (n+1)/2.  Requires (n+1)/2 <= 65. */
+ * solve at (n+1)/2.  Requires (n+1)/2 <= 257. */
 void sbp_options_reference_two_level(sbp_options* opts, int n);
 
 /* ---- single-grid operators (no handle) ------------------------------- */
@@ -180,8 +180,10 @@ int sbp_rhs_adjoint_f64(const double* lam, double* df, double* dgW, double* dgE,
 
 /* Create a solver for n x n grids on the current device.  opts == NULL
  * creates a plain-CG solver (no multigrid hierarchy); otherwise the MG
- * hierarchy, its buffers and the dense inverse of the coarse operator are
- * built (the reference's lu(A_2h), matrix_free_mg_cg.jl:460). */
+ * hierarchy, its buffers and the coarse direct solver are built (the
+ * reference's lu(A_2h), matrix_free_mg_cg.jl:460): the coarse operator is a
+ * Kronecker sum of two 1D operators, so it is inverted exactly by fast
+ * diagonalisation with two dense nc x nc FP64 eigenbases. */
 int sbp_solver_create(sbp_solver** out, int n, const sbp_options* opts);
 int sbp_solver_destroy(sbp_solver* s);
 /* Number of levels of the hierarchy (1 for a plain-CG solver). */
@@ -219,10 +221,10 @@ int sbp_vcycle_apply(sbp_solver* s, const double* b, double* v, void* stream);
 /* ---- host-only helpers ------------------------------------------------ */
 
 /* Dense inverse of the coarse operator A on an nc x nc grid (row-major,
- * nc^2 x nc^2), computed on the host by banded Cholesky; the solver uploads
- * it to replace the reference's per-V-cycle host LU solve
- * (matrix_free_mg_cg.jl:166).  `cap` is the capacity of `out` in doubles.
- * Needs no GPU. */
+ * nc^2 x nc^2, nc <= 129), computed on the host column by column from the
+ * same fast-diagonalisation factors the solver uploads to replace the
+ * reference's per-V-cycle host LU solve (matrix_free_mg_cg.jl:166).  `cap`
+ * is the capacity of `out` in doubles.  Needs no GPU. */
 int sbp_coarse_inverse_host(int nc, double* out, long long cap);
 
 /* Message of the last SBP_ERR_CUDA / SBP_ERR_NOMEM on this host thread. */

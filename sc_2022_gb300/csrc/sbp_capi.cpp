@@ -67,7 +67,7 @@ struct sbp_solver {
   sbp_options opts{};
   size_t esize = 8;                 // element size of the V-cycle levels
   std::vector<Level> levels;
-  double* Ainv = nullptr;
+  CoarseDev coarse{};               // fast-diagonalisation factors of the last level
   // Krylov vectors (FP64, padded leading dimension ld; padding stays zero)
   int ld = 0;
   double* x = nullptr;              // the iterate (the caller's x is copied in and out)
@@ -128,18 +128,15 @@ void destroy_graphs(sbp_solver* s) {
 //   post: first pass reads v + P e (prolongation folded into the sweep);
 //         remaining sweeps ping-pong.  On level 0 the last pass also reduces
 //         b.z into the Krylov state when `dot` is set.
-// Last level: v = Ainv b (dense FP64 GEMV).
+// Last level: v = A^{-1} b by fast diagonalisation (FP64, two launches).
 // ---------------------------------------------------------------------------
 // Temporal blocking (one fused pre-smoothing and one fused post-smoothing
 // kernel per level) for FP32 levels: their sweeps are memory-bound, so
 // recomputing halos in shared memory is cheap.  FP64 levels are bound by the
 // FP64 pipe and keep the one-sweep-per-pass schedule, which does no redundant
 // halo arithmetic.
-// Levels up to this size are fused: there the six-kernel schedule is bound
-// by launch latency, while on larger levels the one-sweep kernels already
-// run at memory speed and the fused kernels' halo arithmetic costs more than
-// the traffic it saves (measured at N = 4097 on GB300).
-constexpr int kFuseMaxN = 2049;
+// Levels up to this size use the fused passes (all FP32 levels at present).
+constexpr int kFuseMaxN = 1 << 30;
 
 template <typename T>
 bool use_fused(const sbp_solver* s, int n) {
@@ -159,7 +156,7 @@ cudaError_t enqueue_vcycle(sbp_solver* s, size_t l, bool dot, SolveState* st, cu
   cudaError_t e;
   if (l + 1 == s->levels.size()) {
     L.out = 0;
-    e = launch_coarse_gemv<T>(s->Ainv, cgrid<T>(L.b, L.ld), grid<T>(L.v[0], L.ld), n, st, q);
+    e = launch_coarse_solve<T>(s->coarse, cgrid<T>(L.b, L.ld), grid<T>(L.v[0], L.ld), st, q);
     if (e != cudaSuccess) return e;
     if (dot && l == 0) {
       // single-level hierarchy: still reduce b.z for the Krylov state
@@ -229,7 +226,7 @@ long long vcycle_launches(const sbp_solver* s, bool dot) {
     c += 1;                               // residual + restriction
     c += std::max(1, o.nu_post);          // prolongation + post sweeps
   }
-  c += 1;                                 // coarse GEMV
+  c += 2;                                 // coarse solve (two passes)
   if (dot && nl == 1) c += 1;
   return c;
 }
@@ -617,7 +614,7 @@ int sbp_solver_create(sbp_solver** out, int n, const sbp_options* opts) {
     sbp_options& o = s->opts;
     if (o.omega <= 0.0) o.omega = (o.smoother == SBP_SMOOTH_JACOBI) ? 2.0 / 3.0 : 0.15;
     if (!valid_mg_n(n) || !valid_mg_n(o.coarse_n) || o.coarse_n > n) return SBP_ERR_ARGS;
-    if (o.coarse_n > 65) return SBP_ERR_UNSUPPORTED;  // dense coarse inverse limit
+    if (o.coarse_n > 257) return SBP_ERR_UNSUPPORTED;  // limit of the coarse factors
     if (o.nu_pre < 1 || o.nu_post < 0 || o.nu_pre > 64 || o.nu_post > 64) return SBP_ERR_UNSUPPORTED;
     if (o.smoother != SBP_SMOOTH_JACOBI && o.smoother != SBP_SMOOTH_RICHARDSON) return SBP_ERR_ARGS;
     if (o.restriction < 0 || o.restriction > 2) return SBP_ERR_ARGS;
@@ -682,16 +679,22 @@ int sbp_solver_create(sbp_solver** out, int n, const sbp_options* opts) {
       m = (m + 1) / 2;
     }
     const int nc = s->opts.coarse_n;
-    std::shared_ptr<const std::vector<double>> X;
+    std::shared_ptr<const CoarseFactors> F;
     try {
-      X = coarse_inverse(nc);
+      F = coarse_factors(nc);
     } catch (const std::exception& ex) {
       g_last_error = ex.what();
       return SBP_ERR_CUDA;
     }
-    const size_t ab = X->size() * sizeof(double);
-    rc = dalloc(s, &p, ab); if (rc) return rc; s->Ainv = (double*)p;
-    SBP_CUDA(cudaMemcpy(s->Ainv, X->data(), ab, cudaMemcpyHostToDevice));
+    const size_t mb = (size_t)nc * nc * sizeof(double);
+    const std::vector<double>* src[5] = {&F->Vx, &F->VxT, &F->Vy, &F->VyT, &F->dinv};
+    double* dst[6];
+    for (int k = 0; k < 6; ++k) {
+      rc = dalloc(s, &p, mb); if (rc) return rc;
+      dst[k] = (double*)p;
+      if (k < 5) SBP_CUDA(cudaMemcpy(dst[k], src[k]->data(), mb, cudaMemcpyHostToDevice));
+    }
+    s->coarse = CoarseDev{dst[0], dst[1], dst[2], dst[3], dst[4], dst[5], nc};
   }
   SBP_CUDA(cudaDeviceSynchronize());
   guard.release();

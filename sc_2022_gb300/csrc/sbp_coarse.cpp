@@ -1,17 +1,18 @@
-// Host-side set-up of the coarse direct solve: assemble the re-discretised
-// coarse operator A_c (the reference builds it with Assembling_matrix(level-1)
-// and factors it with lu(), matrix_free_mg_cg.jl:455,460), factor it with a
-// banded Cholesky (A_c is SPD with half-bandwidth 2*nc in the flat ordering
-// because the Dirichlet SAT couples columns j and j+2), and form the dense
-// inverse so the per-V-cycle solve is one bandwidth-bound GEMV on the GPU
-// instead of a latency-bound triangular solve.  The inverse of each coarse
-// size is computed once per process and cached.
+// Host-side set-up of the coarse direct solve.  The reference assembles the
+// re-discretised coarse operator (Assembling_matrix(level-1)) and factors it
+// with lu() (matrix_free_mg_cg.jl:455,460).  Here the same operator is
+// inverted by fast diagonalisation: it is the Kronecker sum of two symmetric
+// 1D operators, so two dense nc x nc eigenbases replace the LU factors and the
+// GPU solve is four small matrix products instead of a sparse triangular
+// solve.  The 1D operators are checked, coefficient by coefficient, against
+// the stencil negA that every kernel applies.
 #include <algorithm>
 #include <cmath>
 #include <map>
 #include <memory>
 #include <mutex>
 #include <stdexcept>
+#include <string>
 #include <thread>
 #include <vector>
 
@@ -29,104 +30,245 @@ struct Indicator {
   double operator()(int a, int b) const { return (a == di && b == dj) ? 1.0 : 0.0; }
 };
 
-struct Band {
-  int N, w;                 // order, half-bandwidth
-  std::vector<double> a;    // a[k*(w+1) + d] = M(k, k-d), d = 0..w
-  double& at(int k, int d) { return a[(size_t)k * (w + 1) + d]; }
-  double get(int r, int c) const {  // r >= c
-    const int d = r - c;
-    return (d > w) ? 0.0 : a[(size_t)r * (w + 1) + d];
-  }
-};
+double weight(int k, int n) { return (k == 0 || k == n - 1) ? 0.5 : 1.0; }
 
-Band assemble_band(int nc) {
-  Band B;
-  B.N = nc * nc;
-  B.w = 2 * nc;
-  B.a.assign((size_t)B.N * (B.w + 1), 0.0);
-  static const int offs[7][2] = {{0, 0}, {-1, 0}, {1, 0}, {0, -1}, {0, 1}, {0, -2}, {0, 2}};
-  for (int j = 0; j < nc; ++j) {
+// 1D operators of negA (dense n x n, row-major): X along i (Neumann SAT),
+// Y along j (Dirichlet SAT).
+void one_d_operators(int n, std::vector<double>& X, std::vector<double>& Y) {
+  X.assign((size_t)n * n, 0.0);
+  Y.assign((size_t)n * n, 0.0);
+  auto x = [&](int r, int c) -> double& { return X[(size_t)r * n + c]; };
+  auto y = [&](int r, int c) -> double& { return Y[(size_t)r * n + c]; };
+  for (int r = 0; r < n; ++r) {
+    if (r == 0 || r == n - 1) {
+      const int in = (r == 0) ? 1 : n - 2;
+      x(r, r) += kN0;
+      x(r, in) += kN1;
+    } else {
+      x(r, r - 1) += 1.0;
+      x(r, r) += -2.0;
+      x(r, r + 1) += 1.0;
+    }
+    if (r == 0 || r == n - 1) {
+      const int s = (r == 0) ? 1 : -1;
+      y(r, r) += 0.5;
+      y(r, r + s) += -1.0;
+      y(r, r + 2 * s) += 0.5;
+    } else {
+      y(r, r - 1) += 1.0;
+      y(r, r) += -2.0;
+      y(r, r + 1) += 1.0;
+    }
+    if (r <= 2) y(r, 0) += (r == 0 ? kCD0 : (r == 1 ? kCD1 : kCD2));
+    if (r >= n - 3) {
+      const int d = n - 1 - r;
+      y(r, n - 1) += (d == 0 ? kCD0 : (d == 1 ? kCD1 : kCD2));
+    }
+  }
+}
+
+// negA(i, j) must equal w_j X(i, :) u(:, j) + w_i Y(j, :) u(i, :) for every
+// point and every neighbour offset the stencil can reach.
+void check_kronecker(int n, const std::vector<double>& X, const std::vector<double>& Y) {
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i)
+      for (int dj = -2; dj <= 2; ++dj)
+        for (int di = -2; di <= 2; ++di) {
+          const int ii = i + di, jj = j + dj;
+          if (ii < 0 || ii >= n || jj < 0 || jj >= n) continue;
+          const double got = negA<double>(Indicator{di, dj}, i, j, n);
+          double want = 0.0;
+          if (dj == 0) want += weight(j, n) * X[(size_t)i * n + ii];
+          if (di == 0) want += weight(i, n) * Y[(size_t)j * n + jj];
+          if (std::fabs(got - want) > 1e-14 * (1.0 + std::fabs(want)))
+            throw std::runtime_error("coarse operator is not a Kronecker sum at (" +
+                                     std::to_string(i) + "," + std::to_string(j) + ")");
+        }
+}
+
+// Cyclic Jacobi eigenvalue algorithm (Golub & Van Loan, Matrix Computations,
+// 4th ed., Alg. 8.5.3) on a dense symmetric n x n matrix S (row-major,
+// destroyed).  On return lam[k] are the eigenvalues and Q (row-major) holds
+// the orthonormal eigenvectors in its columns.
+void jacobi_eigen(int n, std::vector<double>& S, std::vector<double>& Q, std::vector<double>& lam) {
+  Q.assign((size_t)n * n, 0.0);
+  for (int k = 0; k < n; ++k) Q[(size_t)k * n + k] = 1.0;
+  auto s = [&](int r, int c) -> double& { return S[(size_t)r * n + c]; };
+  double total = 0.0;
+  for (double v : S) total += v * v;
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0.0;
+    for (int p = 0; p < n; ++p)
+      for (int q = p + 1; q < n; ++q) off += s(p, q) * s(p, q);
+    if (off <= 1e-32 * total) break;
+    for (int p = 0; p < n - 1; ++p) {
+      for (int q = p + 1; q < n; ++q) {
+        const double apq = s(p, q);
+        if (apq == 0.0) continue;
+        const double theta = (s(q, q) - s(p, p)) / (2.0 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0);
+        const double sn = t * c;
+        for (int k = 0; k < n; ++k) {  // columns p, q
+          const double akp = s(k, p), akq = s(k, q);
+          s(k, p) = c * akp - sn * akq;
+          s(k, q) = sn * akp + c * akq;
+        }
+        for (int k = 0; k < n; ++k) {  // rows p, q
+          const double apk = s(p, k), aqk = s(q, k);
+          s(p, k) = c * apk - sn * aqk;
+          s(q, k) = sn * apk + c * aqk;
+        }
+        for (int k = 0; k < n; ++k) {
+          double& vkp = Q[(size_t)k * n + p];
+          double& vkq = Q[(size_t)k * n + q];
+          const double a = vkp, b = vkq;
+          vkp = c * a - sn * b;
+          vkq = sn * a + c * b;
+        }
+      }
+    }
+  }
+  lam.resize(n);
+  for (int k = 0; k < n; ++k) lam[k] = s(k, k);
+}
+
+// Generalised eigenvectors of K v = l W v (K = -M, M row-major): V column-major
+// with V^T W V = I.
+void pencil_eigen(int n, const std::vector<double>& M, std::vector<double>& V,
+                  std::vector<double>& lam) {
+  std::vector<double> S((size_t)n * n);
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < n; ++c)
+      S[(size_t)r * n + c] = -M[(size_t)r * n + c] / std::sqrt(weight(r, n) * weight(c, n));
+  // symmetrise exactly (the 1D operators are symmetric; guard the rounding)
+  for (int r = 0; r < n; ++r)
+    for (int c = r + 1; c < n; ++c) {
+      const double a = S[(size_t)r * n + c], b = S[(size_t)c * n + r];
+      if (std::fabs(a - b) > 1e-13 * (1.0 + std::fabs(a)))
+        throw std::runtime_error("1D operator is not symmetric");
+      S[(size_t)r * n + c] = S[(size_t)c * n + r] = 0.5 * (a + b);
+    }
+  std::vector<double> Q;
+  jacobi_eigen(n, S, Q, lam);
+  V.resize((size_t)n * n);
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < n; ++c) V[(size_t)c * n + r] = Q[(size_t)r * n + c] / std::sqrt(weight(r, n));
+}
+
+std::shared_ptr<const CoarseFactors> build_factors(int nc) {
+  std::vector<double> X, Y;
+  one_d_operators(nc, X, Y);
+  check_kronecker(nc, X, Y);
+  auto f = std::make_shared<CoarseFactors>();
+  f->nc = nc;
+  std::vector<double> lx, ly;
+  pencil_eigen(nc, X, f->Vx, lx);
+  pencil_eigen(nc, Y, f->Vy, ly);
+  const size_t N = (size_t)nc * nc;
+  f->VxT.resize(N);
+  f->VyT.resize(N);
+  f->dinv.resize(N);
+  for (int r = 0; r < nc; ++r)
+    for (int c = 0; c < nc; ++c) {
+      f->VxT[(size_t)c * nc + r] = f->Vx[(size_t)r * nc + c];
+      f->VyT[(size_t)c * nc + r] = f->Vy[(size_t)r * nc + c];
+    }
+  for (int j = 0; j < nc; ++j)
     for (int i = 0; i < nc; ++i) {
-      const int row = j * nc + i;
-      for (const auto& o : offs) {
-        const int ii = i + o[0], jj = j + o[1];
-        if (ii < 0 || ii >= nc || jj < 0 || jj >= nc) continue;
-        const double c = -negA<double>(Indicator{o[0], o[1]}, i, j, nc);
-        if (c == 0.0) continue;
-        const int col = jj * nc + ii;
-        if (col <= row) B.at(row, row - col) += c;  // lower triangle (A is symmetric)
-      }
+      const double d = lx[i] + ly[j];
+      if (!(d > 0.0)) throw std::runtime_error("coarse operator is not positive definite");
+      f->dinv[(size_t)j * nc + i] = 1.0 / d;
     }
-  }
-  return B;
+  // Self-check: A (A^{-1} b) == b on a fixed vector.
+  std::vector<double> b(N), x(N);
+  for (size_t k = 0; k < N; ++k) b[k] = std::sin(0.37 * (double)k + 0.11) + 0.25;
+  coarse_solve_host(*f, b.data(), x.data());
+  double err = 0.0, nb = 0.0;
+  for (int j = 0; j < nc; ++j)
+    for (int i = 0; i < nc; ++i) {
+      struct G {
+        const double* x; int i, j, n;
+        double operator()(int di, int dj) const { return x[(size_t)(j + dj) * n + (i + di)]; }
+      } g{x.data(), i, j, nc};
+      const double ax = -negA<double>(g, i, j, nc);
+      err = std::max(err, std::fabs(ax - b[(size_t)j * nc + i]));
+      nb = std::max(nb, std::fabs(b[(size_t)j * nc + i]));
+    }
+  if (!(err <= 1e-9 * nb)) throw std::runtime_error("coarse fast-diagonalisation self-check failed");
+  return f;
 }
 
-// In-place banded Cholesky A = L L^T (lower band).
-void band_cholesky(Band& B) {
-  const int N = B.N, w = B.w;
-  for (int k = 0; k < N; ++k) {
-    const int j0 = std::max(0, k - w);
-    for (int j = j0; j <= k; ++j) {
-      double s = B.get(k, j);
-      const int m0 = std::max(j0, j - w);
-      for (int m = m0; m < j; ++m) s -= B.get(k, m) * B.get(j, m);
-      if (j == k) {
-        if (!(s > 0.0)) throw std::runtime_error("coarse operator is not positive definite");
-        B.at(k, 0) = std::sqrt(s);
-      } else {
-        B.at(k, k - j) = s / B.get(j, j);
-      }
+}  // namespace
+
+void coarse_solve_host(const CoarseFactors& f, const double* b, double* x) {
+  const int n = f.nc;
+  const size_t N = (size_t)n * n;
+  std::vector<double> t(N), y(N);
+  // t = B Vy ; y = Vx^T t ./ D ; t = y Vy^T ; x = Vx t
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) {
+      double a = 0.0;
+      for (int k = 0; k < n; ++k) a += b[(size_t)k * n + i] * f.Vy[(size_t)j * n + k];
+      t[(size_t)j * n + i] = a;
     }
-  }
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) {
+      double a = 0.0;
+      for (int k = 0; k < n; ++k) a += f.VxT[(size_t)k * n + i] * t[(size_t)j * n + k];
+      y[(size_t)j * n + i] = a * f.dinv[(size_t)j * n + i];
+    }
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) {
+      double a = 0.0;
+      for (int k = 0; k < n; ++k) a += y[(size_t)k * n + i] * f.VyT[(size_t)j * n + k];
+      t[(size_t)j * n + i] = a;
+    }
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) {
+      double a = 0.0;
+      for (int k = 0; k < n; ++k) a += f.Vx[(size_t)k * n + i] * t[(size_t)j * n + k];
+      x[(size_t)j * n + i] = a;
+    }
 }
 
-std::shared_ptr<const std::vector<double>> build_inverse(int nc) {
-  Band L = assemble_band(nc);
-  band_cholesky(L);
-  const int N = L.N, w = L.w;
+std::shared_ptr<const CoarseFactors> coarse_factors(int nc) {
+  if (nc < 3 || nc > 257) throw std::runtime_error("coarse size out of range");
+  static std::mutex mu;
+  static std::map<int, std::shared_ptr<const CoarseFactors>> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = cache.find(nc);
+  if (it != cache.end()) return it->second;
+  auto f = build_factors(nc);
+  cache[nc] = f;
+  return f;
+}
+
+std::shared_ptr<const std::vector<double>> coarse_inverse(int nc) {
+  auto f = coarse_factors(nc);
+  const int N = nc * nc;
   auto X = std::make_shared<std::vector<double>>((size_t)N * N, 0.0);
   unsigned nt = std::max(1u, std::thread::hardware_concurrency());
   nt = std::min(nt, 64u);
   auto worker = [&](unsigned t) {
-    std::vector<double> y(N), x(N);
+    std::vector<double> e(N, 0.0), x(N);
     for (int c = (int)t; c < N; c += (int)nt) {
-      // Forward: L y = e_c (y is zero above c).
-      for (int k = c; k < N; ++k) {
-        double s = (k == c) ? 1.0 : 0.0;
-        const int m0 = std::max(c, k - w);
-        for (int m = m0; m < k; ++m) s -= L.get(k, m) * y[m];
-        y[k] = s / L.get(k, k);
-      }
-      // Backward: L^T x = y, only rows >= c are needed (symmetry).
-      for (int k = N - 1; k >= c; --k) {
-        double s = y[k];
-        const int m1 = std::min(N - 1, k + w);
-        for (int m = k + 1; m <= m1; ++m) s -= L.get(m, k) * x[m];
-        x[k] = s / L.get(k, k);
-      }
-      for (int k = c; k < N; ++k) {
-        (*X)[(size_t)k * N + c] = x[k];
-        (*X)[(size_t)c * N + k] = x[k];
-      }
+      e[c] = 1.0;
+      coarse_solve_host(*f, e.data(), x.data());
+      e[c] = 0.0;
+      for (int k = 0; k < N; ++k) (*X)[(size_t)k * N + c] = x[k];
     }
   };
   std::vector<std::thread> th;
   for (unsigned t = 1; t < nt; ++t) th.emplace_back(worker, t);
   worker(0);
   for (auto& t : th) t.join();
-  return X;
-}
-
-}  // namespace
-
-std::shared_ptr<const std::vector<double>> coarse_inverse(int nc) {
-  static std::mutex mu;
-  static std::map<int, std::shared_ptr<const std::vector<double>>> cache;
-  std::lock_guard<std::mutex> lock(mu);
-  auto it = cache.find(nc);
-  if (it != cache.end()) return it->second;
-  auto X = build_inverse(nc);
-  cache[nc] = X;
+  // exact symmetry (A^{-1} is symmetric; the columns differ by rounding)
+  for (int r = 0; r < N; ++r)
+    for (int c = r + 1; c < N; ++c) {
+      const double v = 0.5 * ((*X)[(size_t)r * N + c] + (*X)[(size_t)c * N + r]);
+      (*X)[(size_t)r * N + c] = (*X)[(size_t)c * N + r] = v;
+    }
   return X;
 }
 

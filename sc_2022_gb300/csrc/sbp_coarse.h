@@ -1,4 +1,13 @@
-// Dense inverse of the re-discretised coarse operator (host, cached).
+// Coarse direct solve by fast diagonalisation (host set-up, cached).
+//
+// The operator is a Kronecker sum: (-A u)(i, j) = w_j (X u(:, j))_i +
+// w_i (Y u(i, :))_j with X the 1D Neumann operator along i, Y the 1D
+// Dirichlet operator along j and w the boundary weights (1/2 on the first and
+// last index, 1 elsewhere).  With Kx = -X, Ky = -Y and W = diag(w):
+//   A = W (x) Kx + Ky (x) W      (column-major vec, i fastest).
+// The generalised eigenproblems Kx Vx = W Vx Lx, Ky Vy = W Vy Ly with
+// Vx^T W Vx = Vy^T W Vy = I diagonalise A:
+//   A^{-1} B = Vx [ (Vx^T B Vy) ./ (lx_i + ly_j) ] Vy^T     (B an nc x nc grid).
 #pragma once
 
 #include <memory>
@@ -6,8 +15,23 @@
 
 namespace sbp {
 
-// Row-major (= column-major, it is symmetric) nc^2 x nc^2 inverse of A on an
-// nc x nc grid.  Throws std::runtime_error if the factorisation fails.
+struct CoarseFactors {
+  int nc = 0;
+  // All nc x nc, column-major (element (r, c) at r + c * nc).
+  std::vector<double> Vx, VxT, Vy, VyT;
+  std::vector<double> dinv;  // 1 / (lx_i + ly_j) at i + j * nc
+};
+
+// Factors of the coarse operator on an nc x nc grid (3 <= nc <= 257).  The
+// Kronecker structure is checked against the operator's own stencil
+// coefficients.  Throws std::runtime_error on failure.
+std::shared_ptr<const CoarseFactors> coarse_factors(int nc);
+
+// x = A^{-1} b on the host with the factors (column-major nc x nc grids).
+void coarse_solve_host(const CoarseFactors& f, const double* b, double* x);
+
+// Row-major (= column-major, it is symmetric) nc^2 x nc^2 inverse of A,
+// column by column from the factors.
 std::shared_ptr<const std::vector<double>> coarse_inverse(int nc);
 
 }  // namespace sbp

@@ -291,7 +291,9 @@ __global__ void __launch_bounds__(kThreads) k_persist(const __grid_constant__ Jo
     }
     cp_async_commit();
     cp_async_wait<1>();
-    ok = mbar_wait_bounded(&bar[k & 1], (k >> 1) & 1);
+    // TMA stages: one thread observes the transaction barrier, the block
+    // barrier then orders the staged data for every thread
+    if (threadIdx.x == 0) ok = mbar_wait_bounded(&bar[k & 1], (k >> 1) & 1);
     if (!__syncthreads_and(ok)) break;
     job.compute((k & 1) ? buf1 : buf0, tile, acc, ctx, scratch);
     // this buffer is refilled by TMA (async proxy) after the barrier
@@ -419,6 +421,17 @@ struct ResidualJob {
       if (rlo.p) rlo.at(i, j) = convert<float>(rv);
       acc.add_prod((double)rv, (double)rv);
     };
+    if constexpr (sizeof(T) == 8) {
+      // The iterate is zero on the whole stencil box (a zero initial guess):
+      // r = b exactly, without FP64 stencil arithmetic.
+      const unsigned long long* w = reinterpret_cast<const unsigned long long*>(s);
+      int nz = 0;
+      for (int k = threadIdx.x; k < BI * BJ; k += kThreads) nz |= (w[k] << 1) != 0ull;
+      if (!__syncthreads_or(nz)) {
+        visit_generic(s, t, bx, [&](int i, int j, const SAcc<T>&, int k) { emit(i, j, sb[k]); });
+        return;
+      }
+    }
     if (tile_interior(t, n)) {
       visit_interior(s, t, [&](int i, int j, T um, T u0, T up, T uw, T ue, int k) {
         const T sum = (uw + ue) + (um + up);
@@ -544,7 +557,11 @@ struct CgDirMixedJob {
   static constexpr int kStage = align128(box_bytes<float, BI, BJ>());
   static constexpr int kScratch = 0;
   static constexpr bool kReduce = true;
-  using Acc = DotAcc<double>;
+  // p.Ap from the FP32 roundings of p and Ap, accumulated with the
+  // compensated float pair: no FP64 instruction per point.  alpha and beta
+  // only need the scalars to ~1e-7 (r.z already comes from the FP32 r and z);
+  // the FP64 recurrences r -= alpha Ap, x += alpha p keep their accuracy.
+  using Acc = DotAcc<float>;
   using Ctx = DirCtx;
   DevOperand<float> z;
   Grid<const double> pold, apold;
@@ -579,7 +596,7 @@ struct CgDirMixedJob {
       }
       pnew.at(i, j) = pv;
       Ap.at(i, j) = ap;
-      acc.add_prod(pv, ap);
+      acc.add_prod(f64_to_f32(pv), f64_to_f32(ap));
     };
     if (tile_interior(t, n)) {
       // the old direction and operator values of this thread's 8 points are
@@ -609,7 +626,7 @@ struct CgDirMixedJob {
         const double ap = first ? az : fma(beta, ao[q], az);
         pnew.at(i, j0 + q) = pv;
         Ap.at(i, j0 + q) = ap;
-        acc.add_prod(pv, ap);
+        acc.add_prod(f64_to_f32(pv), f64_to_f32(ap));
         um = u0;
         u0 = up;
       }
@@ -923,31 +940,112 @@ struct ResRestrictJob {
 // ---------------------------------------------------------------------------
 constexpr int kMaxFusedSweeps = 3;
 
-// out = in + m (b + (-A in)) on the global-coordinate region [i0,i1]x[j0,j1]
-// of boxes with origin (X0, Y0) and pitch P.
+// Column march over a region [i0,i1] x [j0,j1] (global coordinates) of
+// shared-memory boxes with origin (X0, Y0) and pitch P: thread t takes row
+// i0 + t % w and a contiguous run of columns of group t / w, keeping the
+// j-1 / j / j+1 values in registers (three shared loads per point).
+// fn(i, j, k, um, u0, up, uw, ue) gets the box index k of (i, j) and the
+// five stencil values of `in`.  Threads beyond the last full group idle.
+template <typename T, int P, typename Fn>
+__device__ __forceinline__ void march_region(const T* in, int X0, int Y0, int i0, int i1, int j0,
+                                             int j1, Fn&& fn) {
+  static_assert(P <= kThreads, "a box row must fit in one thread block");
+  const int w = i1 - i0 + 1, h = j1 - j0 + 1;
+  if (w <= 0 || h <= 0) return;
+  const int G = kThreads / w;
+  const int g = threadIdx.x / w;
+  if (g >= G) return;
+  const int r = threadIdx.x - g * w;
+  const int per = (h + G - 1) / G;
+  const int cb = j0 + g * per;
+  const int ce = min(j1 + 1, cb + per);
+  if (cb >= ce) return;
+  const int i = i0 + r;
+  int k = (cb - Y0) * P + (i - X0);
+  T um = in[k - P], u0 = in[k];
+  for (int j = cb; j < ce; ++j, k += P) {
+    const T up = in[k + P];
+    fn(i, j, k, um, u0, up, in[k - 1], in[k + 1]);
+    um = u0;
+    u0 = up;
+  }
+}
+
+// The same march over a region of compile-time shape W x H whose (0, 0)
+// point sits at shared-memory index `base`, for the interior tiles of the
+// fused kernels: the column loop is unrolled, so every shared-memory access
+// is a base register plus an immediate offset, and runs in chunks of four
+// columns whose loads are all issued before the chunk's first store (the
+// shared-memory latency overlaps within a chunk).  For each point
+//   v = val(um, u0, up, uw, ue, a);  out[k] = v (if OUT);  epi(r, c, u0, v, a)
+// with r, c the region row and column and a = aux[k] (0 without AUX).
+template <typename T, int P, int W, int H, bool AUX, bool OUT, typename Val, typename Epi>
+__device__ __forceinline__ void sweep_fixed(const T* in, const T* aux, T* out, int base, Val&& val,
+                                            Epi&& epi) {
+  constexpr int G = kThreads / W;
+  static_assert(G >= 1 && W <= P, "a region row must fit in one thread block and one box row");
+  constexpr int C = (H + G - 1) / G;
+  const int g = threadIdx.x / W;
+  if (g >= G) return;
+  const int r = threadIdx.x - g * W;
+  const int c0 = g * C;
+  const int k0 = base + c0 * P + r;
+  const int cnt = min(C, H - c0);
+  const T* p = in + k0;
+  T um = p[-P], u0 = p[0];
+#pragma unroll
+  for (int q0 = 0; q0 < C; q0 += 4) {
+    T up[4], uw[4], ue[4], a[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int q = q0 + u;
+      if (q < C && q < cnt) {
+        up[u] = p[(q + 1) * P];
+        uw[u] = p[q * P - 1];
+        ue[u] = p[q * P + 1];
+        a[u] = AUX ? aux[k0 + q * P] : T(0);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int q = q0 + u;
+      if (q < C && q < cnt) {
+        const T v = val(um, u0, up[u], uw[u], ue[u], a[u]);
+        if (OUT) out[k0 + q * P] = v;
+        epi(r, c0 + q, u0, v, a[u]);
+        um = u0;
+        u0 = up[u];
+      }
+    }
+  }
+}
+
+// out = in + m (b + (-A in)) on the region [i0,i1] x [j0,j1].
 template <typename T, int P>
 __device__ __forceinline__ void box_sweep(T* out, const T* in, const T* bsm, int X0, int Y0, int i0,
                                           int i1, int j0, int j1, int n, bool jac, T omega) {
+  const bool interior = i0 > 0 && i1 < n - 1 && j0 > 2 && j1 < n - 3;
+  if (interior) {
+    const T m = jac ? omega * T(0.25) : omega;
+    march_region<T, P>(in, X0, Y0, i0, i1, j0, j1,
+                       [&](int, int, int k, T um, T u0, T up, T uw, T ue) {
+                         const T na = ((uw + ue) + (um + up)) - T(4) * u0;
+                         out[k] = fma(m, bsm[k] + na, u0);
+                       });
+    return;
+  }
   const int w = i1 - i0 + 1, h = j1 - j0 + 1;
   if (w <= 0 || h <= 0) return;
   const int cnt = w * h;
   const float inv_w = 1.0f / (float)w;
-  const bool interior = i0 > 0 && i1 < n - 1 && j0 > 2 && j1 < n - 3;
-  const T mi = jac ? omega * T(0.25) : omega;
   for (int q = threadIdx.x; q < cnt; q += kThreads) {
     const int c = (int)(((float)q + 0.5f) * inv_w);
     const int r = q - c * w;
     const int i = i0 + r, j = j0 + c;
     const int k = (j - Y0) * P + (i - X0);
     const T* a = in + k;
-    T na, m;
-    if (interior) {
-      na = ((a[-1] + a[1]) + (a[-P] + a[P])) - T(4) * a[0];
-      m = mi;
-    } else {
-      na = negA<T>(SAcc<T>{a, P}, i, j, n);
-      m = jac ? omega * inv_diagA<T>(i, j, n) : omega;
-    }
+    const T na = negA<T>(SAcc<T>{a, P}, i, j, n);
+    const T m = jac ? omega * inv_diagA<T>(i, j, n) : omega;
     out[k] = fma(m, bsm[k] + na, a[0]);
   }
 }
@@ -992,6 +1090,81 @@ struct PreFusedJob {
     const int ti = id % ntx, tj = id / ntx;
     stage_box<TMA, PBI, PBJ>(reinterpret_cast<T*>(buf), b, &bmap, 64 * ti - 4, 32 * tj - 4, nf, bar);
   }
+  // Interior tile (full 32 x 16 coarse tile; every swept fine point has the
+  // plain 5-point stencil and the constant smoother weight m).  Box offsets:
+  // the residual region Rr (65 x 33 fine points) starts at box (5, 5); the
+  // sweep k output lives on Rr grown by S - k + 1.  v1 = m b is never
+  // formed: v2 = v1 + m (b - A v1) = (2m - 4m^2) b + m^2 (sum of the four
+  // neighbours of b).
+  __device__ bool lean_ok(const Tile<RTI, RTJ>& t) const {
+    const int S = sweeps;
+    const int ri0 = 2 * t.i_lo - 1, ri1 = 2 * t.i_hi - 1;
+    const int rj0 = 2 * t.j_lo - 1, rj1 = 2 * t.j_hi - 1;
+    return t.i_lo > 0 && t.j_lo > 0 && t.i_hi - t.i_lo == RTI && t.j_hi - t.j_lo == RTJ &&
+           ri0 - S >= 1 && ri1 + S <= nf - 2 && rj0 - S >= 1 && rj1 + S <= nf - 2 &&
+           rj0 - (S - 1) >= 3 && rj1 + (S - 1) <= nf - 4;
+  }
+
+  template <int S>
+  __device__ void compute_lean(const Tile<RTI, RTJ>& t, int X0, int Y0, const T* B, T* V0,
+                               T* V1) const {
+    constexpr int R0 = 5;                      // box index of Rr's first row / column
+    const T m = (smoother == kSmoothJacobi) ? omega * T(0.25) : omega;
+    const T k1 = T(2) * m - T(4) * m * m, m2 = m * m;
+    const T* vs;                               // v_S on Rr + 1
+    auto none = [](int, int, T, T, T) {};
+    if constexpr (S >= 2) {
+      constexpr int h = S - 1;                 // v2 on Rr + (S - 1), straight from b
+      sweep_fixed<T, PBI, 65 + 2 * h, 33 + 2 * h, false, true>(
+          B, nullptr, V0, (R0 - h) * PBI + (R0 - h),
+          [&](T um, T u0, T up, T uw, T ue, T) { return fma(m2, (uw + ue) + (um + up), k1 * u0); },
+          none);
+      __syncthreads();
+      vs = V0;
+      if constexpr (S == 3) {                  // v3 on Rr + 1
+        sweep_fixed<T, PBI, 67, 35, true, true>(
+            V0, B, V1, (R0 - 1) * PBI + (R0 - 1),
+            [&](T um, T u0, T up, T uw, T ue, T bb) {
+              return fma(m, bb + (((uw + ue) + (um + up)) - T(4) * u0), u0);
+            },
+            none);
+        __syncthreads();
+        vs = V1;
+      }
+    } else {
+      vs = B;                                  // S = 1: v1 = m b, formed on the fly
+    }
+    // residual on Rr into the free buffer; own points of v_S (Rr minus its
+    // first row and column) to global
+    T* const R = (S == 3) ? V0 : V1;
+    const int gi0 = X0 + R0, gj0 = Y0 + R0;
+    sweep_fixed<T, PBI, 65, 33, true, true>(
+        vs, B, R, R0 * PBI + R0,
+        [&](T um, T u0, T up, T uw, T ue, T bb) {
+          const T nb = (uw + ue) + (um + up);
+          if constexpr (S == 1) return fma(m, nb - T(4) * u0, bb);
+          else return bb + (nb - T(4) * u0);
+        },
+        [&](int r, int c, T u0, T, T) {
+          if (r > 0 && c > 0) vout.at(gi0 + r, gj0 + c) = (S == 1) ? m * u0 : u0;
+        });
+    __syncthreads();
+    // restriction, constant interior weights: thread = (coarse row, pair of
+    // coarse columns); fine centres at box (6 + 2 a, 6 + 2 b)
+    const T sc = (kind == kRestrictGalerkin) ? T(1) : T(0.25);
+    const int a = threadIdx.x & 31, bp = threadIdx.x >> 5;
+    const T* q = R + (5 + 4 * bp) * PBI + (6 + 2 * a);
+    T cs[5];
+#pragma unroll
+    for (int u = 0; u < 5; ++u) {
+      const T* col = q + u * PBI;
+      cs[u] = fma(T(0.5), col[-1] + col[1], col[0]);
+    }
+    const int I = t.i_lo + a, J = t.j_lo + 2 * bp;
+    f.at(I, J) = sc * fma(T(0.5), cs[0] + cs[2], cs[1]);
+    f.at(I, J + 1) = sc * fma(T(0.5), cs[2] + cs[4], cs[3]);
+  }
+
   __device__ void compute(unsigned char* buf, int id, Acc&, const Ctx&, unsigned char* scr) const {
     const int ti = id % ntx, tj = id / ntx;
     const Tile<RTI, RTJ> t = tile_at<RTI, RTJ>(id, ntx, nc);
@@ -999,6 +1172,12 @@ struct PreFusedJob {
     const T* B = reinterpret_cast<const T*>(buf);
     T* const V0 = reinterpret_cast<T*>(scr);
     T* const V1 = reinterpret_cast<T*>(scr + kBox);
+    if (lean_ok(t)) {
+      if (sweeps == 3) compute_lean<3>(t, X0, Y0, B, V0, V1);
+      else if (sweeps == 2) compute_lean<2>(t, X0, Y0, B, V0, V1);
+      else compute_lean<1>(t, X0, Y0, B, V0, V1);
+      return;
+    }
     const bool jac = (smoother == kSmoothJacobi);
     // residual region and its expansions, clipped to the domain
     const int ri0 = 2 * t.i_lo - 1, ri1 = 2 * t.i_hi - 1;
@@ -1032,13 +1211,17 @@ struct PreFusedJob {
     {
       const int i0 = max(ri0, 0), i1 = min(ri1, nf - 1), j0 = max(rj0, 0), j1 = min(rj1, nf - 1);
       const bool interior = i0 > 0 && i1 < nf - 1 && j0 > 2 && j1 < nf - 3;
-      region_for(i0, i1, j0, j1, [&](int i, int j) {
-        const int k = (j - Y0) * PBI + (i - X0);
-        const T* a = VS + k;
-        const T na = interior ? ((a[-1] + a[1]) + (a[-PBI] + a[PBI])) - T(4) * a[0]
-                              : negA<T>(SAcc<T>{a, PBI}, i, j, nf);
-        R[k] = B[k] + na;
-      });
+      if (interior) {
+        march_region<T, PBI>(VS, X0, Y0, i0, i1, j0, j1,
+                             [&](int, int, int k, T um, T u0, T up, T uw, T ue) {
+                               R[k] = B[k] + (((uw + ue) + (um + up)) - T(4) * u0);
+                             });
+      } else {
+        region_for(i0, i1, j0, j1, [&](int i, int j) {
+          const int k = (j - Y0) * PBI + (i - X0);
+          R[k] = B[k] + negA<T>(SAcc<T>{VS + k, PBI}, i, j, nf);
+        });
+      }
     }
     __syncthreads();
     // restriction of r on the coarse tile (out-of-domain r entries carry
@@ -1106,6 +1289,90 @@ struct PostFusedJob {
     stage_box<TMA, QCI, QCJ>(reinterpret_cast<T*>(buf + kOffE), e, &emap, 32 * ti - 4,
                              (jl - 4) >> 1, (n + 1) / 2, bar);
   }
+  // Interior tile (full 64 x 32 fine tile, every swept point with the plain
+  // stencil and constant weight m).  Box offsets: the tile Rt starts at box
+  // (5, 4) of v and b; fine (i, j) of the F0 region has coarse box
+  // coordinates ((bi >> 1) + 2, (bj + 1) >> 1), i odd <=> bi odd and
+  // j odd <=> bj even.
+  __device__ bool lean_ok(const TileT& t) const {
+    const int S = sweeps;
+    return S >= 1 && t.i_lo > 0 && t.j_lo > 0 && t.i_hi - t.i_lo == TI &&
+           t.j_hi - t.j_lo == TJ && t.i_lo - S >= 1 && t.i_hi - 1 + S <= n - 2 &&
+           t.j_lo - S >= 1 && t.j_hi - 1 + S <= n - 2 && t.j_lo - (S - 1) >= 3 &&
+           t.j_hi - 1 + (S - 1) <= n - 4;
+  }
+
+  template <int S>
+  __device__ void compute_lean(const TileT& t, T* V0, T* V1, const T* B, const T* E,
+                               Acc& acc) const {
+    constexpr int RI = 5, RJ = 4;              // box index of Rt's first row / column
+    constexpr int W = TI + 2 * S, H = TJ + 2 * S;
+    const T m = (smoother == kSmoothJacobi) ? omega * T(0.25) : omega;
+    // F0 = v_in + P e on Rt + S.  Thread = (fine row, run of C columns, C
+    // even); the row-interpolated coarse values rv(J) are carried along.
+    {
+      constexpr int G = kThreads / W;
+      constexpr int C = (((H + G - 1) / G) + 1) & ~1;
+      const int g = threadIdx.x / W;
+      if (g < G) {
+        const int r = threadIdx.x - g * W;
+        const int bi = RI - S + r;
+        const int c0 = g * C;
+        const T w1 = (bi & 1) ? T(0.5) : T(0);
+        const T w0 = (bi & 1) ? T(0.5) : T(1);
+        const int bj0 = RJ - S + c0;                       // c0 even: parity of RJ - S
+        const T* erow = E + ((bi >> 1) + 2);
+        auto rv = [&](int cj) { return fma(w1, erow[cj * QCI + 1], w0 * erow[cj * QCI]); };
+        T* v = V0 + bj0 * QBI + bi;
+        // invariant before column bj: ra = rv(bj >> 1), rb = rv((bj >> 1) + 1)
+        int cj = bj0 >> 1;
+        T ra = rv(cj), rb = rv(cj + 1);
+#pragma unroll
+        for (int q = 0; q < C; ++q) {
+          if (c0 + q < H) {
+            // bj = bj0 + q; bj even -> j odd: average of rv(cj), rv(cj + 1)
+            if (((RJ - S + q) & 1) == 0) {
+              v[q * QBI] += T(0.5) * (ra + rb);
+            } else {
+              // bj odd -> j even: rv((bj + 1) >> 1) = rv(cj + 1); advance
+              v[q * QBI] += rb;
+              ra = rb;
+              ++cj;
+              rb = rv(cj + 1);
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();
+    T* cur = V0;
+    T* nxt = V1;
+    auto sweep = [&](T um, T u0, T up, T uw, T ue, T bb) {
+      return fma(m, bb + (((uw + ue) + (um + up)) - T(4) * u0), u0);
+    };
+    auto none = [](int, int, T, T, T) {};
+    if constexpr (S >= 2) {
+      constexpr int h = S - 1;                 // sweep 1 on Rt + (S - 1)
+      sweep_fixed<T, QBI, TI + 2 * h, TJ + 2 * h, true, true>(
+          cur, B, nxt, (RJ - h) * QBI + (RI - h), sweep, none);
+      __syncthreads();
+      T* tmp = cur; cur = nxt; nxt = tmp;
+    }
+    if constexpr (S == 3) {                    // sweep 2 on Rt + 1
+      sweep_fixed<T, QBI, TI + 2, TJ + 2, true, true>(cur, B, nxt, (RJ - 1) * QBI + (RI - 1),
+                                                      sweep, none);
+      __syncthreads();
+      T* tmp = cur; cur = nxt; nxt = tmp;
+    }
+    // last sweep on Rt, to global
+    const int gi0 = t.i_lo, gj0 = t.j_lo;
+    sweep_fixed<T, QBI, TI, TJ, true, false>(cur, B, nullptr, RJ * QBI + RI, sweep,
+                                             [&](int r, int c, T, T vn, T bb) {
+                                               vout.at(gi0 + r, gj0 + c) = vn;
+                                               if (DOT) acc.add_prod(bb, vn);
+                                             });
+  }
+
   __device__ void compute(unsigned char* buf, int id, Acc& acc, const Ctx&,
                           unsigned char* scr) const {
     const TileT t = tile_at<TI, TJ>(id, ntx, n);
@@ -1116,6 +1383,12 @@ struct PostFusedJob {
     T* const V1 = reinterpret_cast<T*>(scr);
     const T* B = reinterpret_cast<const T*>(buf + kOffB);
     const T* E = reinterpret_cast<const T*>(buf + kOffE);
+    if (lean_ok(t)) {
+      if (sweeps == 3) compute_lean<3>(t, V0, V1, B, E, acc);
+      else if (sweeps == 2) compute_lean<2>(t, V0, V1, B, E, acc);
+      else compute_lean<1>(t, V0, V1, B, E, acc);
+      return;
+    }
     const bool jac = (smoother == kSmoothJacobi);
     auto lo = [](int v, int h) { return max(v - h, 0); };
     auto hi = [&](int v, int h) { return min(v + h, n - 1); };
@@ -1146,26 +1419,30 @@ struct PostFusedJob {
     // last pass on the tile itself: to global (sweep, or F0 when S = 0)
     const T* in = cur1 ? V1 : V0;
     const bool interior = tile_interior(t, n);
-    const T mi = jac ? omega * T(0.25) : omega;
-    region_for(ti0, ti1, tj0, tj1, [&](int i, int j) {
-      const int k = (j - Y0) * QBI + (i - X0);
-      const T* a = in + k;
-      const T bb = B[k];
-      T vn = a[0];
-      if (sweeps > 0) {
-        T na, m;
-        if (interior) {
-          na = ((a[-1] + a[1]) + (a[-QBI] + a[QBI])) - T(4) * a[0];
-          m = mi;
-        } else {
-          na = negA<T>(SAcc<T>{a, QBI}, i, j, n);
-          m = jac ? omega * inv_diagA<T>(i, j, n) : omega;
+    if (interior && sweeps > 0) {
+      const T m = jac ? omega * T(0.25) : omega;
+      march_region<T, QBI>(in, X0, Y0, ti0, ti1, tj0, tj1,
+                           [&](int i, int j, int k, T um, T u0, T up, T uw, T ue) {
+                             const T bb = B[k];
+                             const T vn = fma(m, bb + (((uw + ue) + (um + up)) - T(4) * u0), u0);
+                             vout.at(i, j) = vn;
+                             if (DOT) acc.add_prod(bb, vn);
+                           });
+    } else {
+      region_for(ti0, ti1, tj0, tj1, [&](int i, int j) {
+        const int k = (j - Y0) * QBI + (i - X0);
+        const T* a = in + k;
+        const T bb = B[k];
+        T vn = a[0];
+        if (sweeps > 0) {
+          const T na = negA<T>(SAcc<T>{a, QBI}, i, j, n);
+          const T m = jac ? omega * inv_diagA<T>(i, j, n) : omega;
+          vn = fma(m, bb + na, a[0]);
         }
-        vn = fma(m, bb + na, a[0]);
-      }
-      vout.at(i, j) = vn;
-      if (DOT) acc.add_prod(bb, vn);
-    });
+        vout.at(i, j) = vn;
+        if (DOT) acc.add_prod(bb, vn);
+      });
+    }
   }
   __device__ void finish(double tot) const {
     if (!isfinite(tot)) {
@@ -1427,8 +1704,11 @@ static void prepare_precision() {
   prep_smooth<T, kFieldProlong, kEpiStore, M>();
 }
 
+cudaError_t prepare_coarse_kernels();
+
 cudaError_t prepare_kernels() {
   sm_count();
+  if (cudaError_t e = prepare_coarse_kernels(); e != cudaSuccess) return e;
   prepare_precision<double, false>();
   prepare_precision<double, true>();
   prepare_precision<float, false>();
@@ -1488,54 +1768,110 @@ cudaError_t launch_prolong(Grid<const T> e, Grid<T> out, int nc, int accumulate,
 }
 
 // ---------------------------------------------------------------------------
-// Coarse direct solve as a dense FP64 GEMV with the precomputed inverse.
+// Coarse direct solve by fast diagonalisation, in FP64:
+//   E = Vx [ (Vx^T B Vy) ./ D ] Vy^T
+// as two launches of one kernel, each computing out(:, j) = M (in c_j)
+// [.* dinv(:, j)] with one CTA per grid column j: pass 1 has in = B,
+// c_j = Vy(:, j), M = Vx^T and scales by dinv; pass 2 has in = Y,
+// c_j = Vy^T(:, j), M = Vx.  Every matrix is nc x nc column-major, so the
+// threads of a row slice read consecutive addresses.  Sums run in a fixed
+// order (four interleaved slices, then a fixed combine): deterministic.
 // ---------------------------------------------------------------------------
-template <typename T>
+constexpr int kFdSlices = kThreads / 64;
+// Coarse sizes up to this stage the input grid and M in shared memory (one
+// parallel load instead of a chain of dependent L2 reads per thread).
+constexpr int kFdStageMaxN = 65;
+
+__host__ __device__ constexpr size_t fd_smem_bytes(int nc, bool stage) {
+  return ((size_t)(2 + kFdSlices) * nc + (stage ? 2 * (size_t)nc * nc : 0)) * sizeof(double);
+}
+
+template <typename Tin, typename Tout, bool STAGE>
 __global__ void __launch_bounds__(kThreads)
-    k_coarse_gemv(const double* __restrict__ Ainv, Grid<const T> f, Grid<T> e, int nc,
-                  const SolveState* st) {
+    k_coarse_fd(Grid<const Tin> in, const double* __restrict__ C, const double* __restrict__ M,
+                const double* __restrict__ dinv, Grid<Tout> out, int nc, const SolveState* st) {
   pdl_begin();
   if (st && st->done) return;
-  extern __shared__ double sf[];
-  const int N = nc * nc;
-  for (int k = threadIdx.x; k < N; k += kThreads) {
-    const int j = k / nc;
-    const int i = k - j * nc;
-    sf[k] = convert<double>(f.at(i, j));
-  }
-  __syncthreads();
-  const int lane = threadIdx.x & 31;
-  const int w = threadIdx.x >> 5;
-#pragma unroll
-  for (int q = 0; q < kGemvRowsPerWarp; ++q) {
-    const int row = (blockIdx.x * kWarps + w) * kGemvRowsPerWarp + q;
-    if (row >= N) break;
-    const double* a = Ainv + (size_t)row * (size_t)N;
-    double acc = 0.0;
-#pragma unroll 8
-    for (int c = lane; c < N; c += 32) acc += __ldg(a + c) * sf[c];
-    acc = warp_sum(acc);
-    if (lane == 0) {
-      const int j = row / nc;
-      const int i = row - j * nc;
-      e.at(i, j) = convert<T>(acc);
+  extern __shared__ double fd_sm[];
+  double* c = fd_sm;                  // nc
+  double* sv = c + nc;                // nc
+  double* part = sv + nc;             // kFdSlices * nc
+  double* is = part + kFdSlices * nc; // STAGE: the input grid, nc * nc
+  double* ms = is + nc * nc;          // STAGE: M, nc * nc
+  const int j = blockIdx.x;
+  const int q = threadIdx.x >> 6, r = threadIdx.x & 63;
+  for (int k = threadIdx.x; k < nc; k += kThreads) c[k] = C[(size_t)j * nc + k];
+  if (STAGE) {
+    for (int k = threadIdx.x; k < nc * nc; k += kThreads) {
+      const int jj = k / nc;
+      is[k] = convert<double>(in.at(k - jj * nc, jj));
+      ms[k] = __ldg(M + k);
     }
   }
+  __syncthreads();
+  for (int i = r; i < nc; i += 64) {
+    double a = 0.0;
+#pragma unroll 4
+    for (int k = q; k < nc; k += kFdSlices)
+      a = fma(STAGE ? is[k * nc + i] : convert<double>(in.at(i, k)), c[k], a);
+    part[q * nc + i] = a;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nc; i += kThreads)
+    sv[i] = (part[i] + part[nc + i]) + (part[2 * nc + i] + part[3 * nc + i]);
+  __syncthreads();
+  for (int i = r; i < nc; i += 64) {
+    double a = 0.0;
+#pragma unroll 4
+    for (int k = q; k < nc; k += kFdSlices)
+      a = fma(STAGE ? ms[k * nc + i] : __ldg(M + (size_t)k * nc + i), sv[k], a);
+    part[q * nc + i] = a;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nc; i += kThreads) {
+    double t = (part[i] + part[nc + i]) + (part[2 * nc + i] + part[3 * nc + i]);
+    if (dinv) t *= __ldg(dinv + (size_t)j * nc + i);
+    out.at(i, j) = convert<Tout>(t);
+  }
+}
+static_assert(kFdSlices == 4, "the combine step sums four slices");
+
+template <typename Tin, typename Tout>
+cudaError_t launch_fd_pass(Grid<const Tin> in, const double* C, const double* M,
+                           const double* dinv, Grid<Tout> out, int nc, const SolveState* st,
+                           cudaStream_t s) {
+  if (nc <= kFdStageMaxN)
+    return launch_pdl(k_coarse_fd<Tin, Tout, true>, dim3(nc), dim3(kThreads),
+                      fd_smem_bytes(nc, true), s, in, C, M, dinv, out, nc, st);
+  return launch_pdl(k_coarse_fd<Tin, Tout, false>, dim3(nc), dim3(kThreads),
+                    fd_smem_bytes(nc, false), s, in, C, M, dinv, out, nc, st);
+}
+
+template <typename Tin, typename Tout>
+cudaError_t allow_fd_smem() {
+  return cudaFuncSetAttribute(k_coarse_fd<Tin, Tout, true>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)fd_smem_bytes(kFdStageMaxN, true));
+}
+
+// The staged coarse kernels need more than the default 48 KB of dynamic
+// shared memory; set once, outside any stream capture.
+cudaError_t prepare_coarse_kernels() {
+  cudaError_t e = allow_fd_smem<float, double>();
+  if (e == cudaSuccess) e = allow_fd_smem<double, float>();
+  if (e == cudaSuccess) e = allow_fd_smem<double, double>();
+  return e;
 }
 
 template <typename T>
-cudaError_t launch_coarse_gemv(const double* Ainv, Grid<const T> f, Grid<T> e, int nc,
-                               const SolveState* st, cudaStream_t s) {
-  const int N = nc * nc;
-  const int rows_per_cta = kWarps * kGemvRowsPerWarp;
-  const int grid = (N + rows_per_cta - 1) / rows_per_cta;
-  const size_t smem = (size_t)N * sizeof(double);
-  if (smem > 48 * 1024) {
-    cudaError_t err = cudaFuncSetAttribute(k_coarse_gemv<T>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (err != cudaSuccess) return err;
-  }
-  return launch_pdl(k_coarse_gemv<T>, dim3(grid), dim3(kThreads), smem, s, Ainv, f, e, nc, st);
+cudaError_t launch_coarse_solve(const CoarseDev& f, Grid<const T> b, Grid<T> e,
+                                const SolveState* st, cudaStream_t s) {
+  const int nc = f.nc;
+  cudaError_t err =
+      launch_fd_pass<T, double>(b, f.Vy, f.VxT, f.dinv, Grid<double>{f.y, nc}, nc, st, s);
+  if (err != cudaSuccess) return err;
+  return launch_fd_pass<double, T>(Grid<const double>{f.y, nc}, f.VyT, f.Vx, nullptr, e, nc, st,
+                                   s);
 }
 
 // ---------------------------------------------------------------------------
@@ -1676,8 +2012,8 @@ cudaError_t launch_rhs_adjoint(Grid<const double> lam, Grid<double> df, double* 
                                              const SolveState*, cudaStream_t);                  \
   template cudaError_t launch_prolong<T>(Grid<const T>, Grid<T>, int, int, const SolveState*,   \
                                          cudaStream_t);                                         \
-  template cudaError_t launch_coarse_gemv<T>(const double*, Grid<const T>, Grid<T>, int,        \
-                                             const SolveState*, cudaStream_t);                  \
+  template cudaError_t launch_coarse_solve<T>(const CoarseDev&, Grid<const T>, Grid<T>,         \
+                                              const SolveState*, cudaStream_t);                 \
   template cudaError_t launch_dot<T>(Grid<const T>, Grid<const T>, int, double*, ReduceBuf,     \
                                      cudaStream_t);
 

@@ -116,11 +116,23 @@ template <typename T>
 cudaError_t launch_prolong(Grid<const T> e, Grid<T> out, int nc, int accumulate,
                            const SolveState* st, cudaStream_t s);
 
-// e = Ainv f with Ainv the dense nc^2 x nc^2 inverse of the coarse operator
-// (FP64 regardless of T).
+// Device copy of the coarse fast-diagonalisation factors (all nc x nc,
+// column-major, FP64) plus an nc x nc FP64 scratch grid y.
+struct CoarseDev {
+  const double* Vx;
+  const double* VxT;
+  const double* Vy;
+  const double* VyT;
+  const double* dinv;
+  double* y;
+  int nc;
+};
+
+// e = A^{-1} f on the coarse grid (FP64 arithmetic regardless of T); two
+// launches.
 template <typename T>
-cudaError_t launch_coarse_gemv(const double* Ainv, Grid<const T> f, Grid<T> e, int nc,
-                               const SolveState* st, cudaStream_t s);
+cudaError_t launch_coarse_solve(const CoarseDev& f, Grid<const T> b, Grid<T> e,
+                                const SolveState* st, cudaStream_t s);
 
 // out = convert(in) on an n x n grid (any leading dimensions).
 template <typename Tin, typename Tout>

@@ -86,11 +86,11 @@ def CG_Matrix_Free_GPU_v2(x_GPU, Ap_GPU, b_reshaped_GPU, Nx, Ny, abstol: float =
 def _mg_options(n: int, nu: int, A_2h) -> Options:
     if isinstance(A_2h, Options):
         return A_2h
-    if (n + 1) // 2 <= 65:
+    if (n + 1) // 2 <= 257:
         o = reference_two_level_options(n)
     else:
         # The reference's exact coarse LU at (n+1)/2 is replaced by the
-        # multi-level V-cycle beyond a 65^2 coarse grid.
+        # multi-level V-cycle beyond a 257^2 coarse grid.
         o = default_options()
     o.nu_pre = o.nu_post = nu
     return o
@@ -106,7 +106,7 @@ def matrix_free_MGCG(b_GPU: torch.Tensor, x_GPU: torch.Tensor, A_2h=None,
     ``A_2h`` is the reference's coarse LU factor; here it may be a
     :class:`Solver` (reused), an :class:`Options`, or None: the reference's
     two-level Richardson preconditioner with an exact coarse solve when
-    (n+1)/2 <= 65, else the default V-cycle.  NUM_V_CYCLES, use_galerkin,
+    (n+1)/2 <= 257, else the default V-cycle.  NUM_V_CYCLES, use_galerkin,
     direct_sol and H_tilde are accepted for signature compatibility; the
     reference ignores them as well (SBPp must be 2).
     """

@@ -59,7 +59,7 @@ def test_cg_full_gpu_reference_semantics(sbp):
     assert relerr(host(x), xr) < 1e-8
 
 
-@pytest.mark.parametrize("n,expect", [(33, 18), (65, 19), (129, 18)])
+@pytest.mark.parametrize("n,expect", [(33, 18), (65, 19), (129, 18), (257, 17), (513, 17)])
 def test_mgcg_reference_two_level(sbp, n, expect):
     a, b, U = ref_problem(n)
     hier = o.Hierarchy(n, o.MGOptions.reference_two_level(n))
@@ -134,6 +134,36 @@ def test_mgcg_mixed_precision(sbp, n):
                                      C.byref(out), None) == 0
     assert out.value <= 2e-10 * np.linalg.norm(b)
     assert relerr(host(x32), host(x64)) < 1e-8
+
+
+@pytest.mark.parametrize("n,smoother,nu,restriction", [
+    (513, "jacobi", 3, "galerkin"),
+    (513, "jacobi", 2, "normal"),
+    (513, "richardson", 1, "sbp"),
+    (1025, "jacobi", 3, "galerkin"),
+    (257, "richardson", 3, "normal"),
+])
+def test_vcycle_mixed_matches_fp64_oracle(sbp, n, smoother, nu, restriction):
+    # The FP32 V-cycle (fused pre/post-smoothing kernels on every level, with
+    # the interior-tile and boundary-tile paths) against the oracle's FP64
+    # V-cycle: FP32 accuracy, relative 2e-5 in the 2-norm.
+    from sc_2022_gb300 import _lib
+    a, b, _ = ref_problem(n, "baseline")
+    om = 2.0 / 3.0 if smoother == "jacobi" else 0.15
+    hier = o.Hierarchy(n, o.MGOptions(smoother=smoother, omega=om, nu_pre=nu, nu_post=nu,
+                                      restriction=restriction, coarse_n=65))
+    z_ref = hier.vcycle(b)
+    kinds = {"normal": _lib.SBP_RESTRICT_NORMAL, "sbp": _lib.SBP_RESTRICT_SBP,
+             "galerkin": _lib.SBP_RESTRICT_GALERKIN}
+    opts = sbp.default_options(_lib.SBP_PREC_MIXED)
+    opts.smoother = _lib.SBP_SMOOTH_JACOBI if smoother == "jacobi" else _lib.SBP_SMOOTH_RICHARDSON
+    opts.omega = om
+    opts.nu_pre = opts.nu_post = nu
+    opts.restriction = kinds[restriction]
+    s = sbp.Solver(n, opts)
+    z = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    s.vcycle(dev(b), z)
+    assert relerr(host(z), z_ref) < 2e-5
 
 
 def test_mgcg_large_discretisation_error(sbp):
