@@ -30,6 +30,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "MGCG time to 1e-10 rel. residual at N=4097²: mixed vs FP64; apply GB/s vs HBM"
+# DRAM bytes (read + write) of one sbp_apply_f64 launch at N = 4097, measured
+# with ncu (dram__bytes_read.sum + dram__bytes_write.sum).
+APPLY_F64_TRAFFIC = 220.2e6
 WORKLOAD = ("plain/mixed matrix-free MGCG, N=4097 (16.8M unknowns), u=sin(pi x)cos(pi y), "
             "V-cycle to 65^2, weighted Jacobi 2/3 3+3, SBP-compatible restriction, "
             "bilinear prolongation, FP64 direct coarse solve, tol 1e-10")
@@ -44,6 +47,8 @@ def parse_args():
     p.add_argument("--n", type=int, default=4097)
     p.add_argument("--apply-iters", type=int, default=50)
     p.add_argument("--cpu-baseline", type=int, default=1, help="time the CPU baseline leg")
+    p.add_argument("--dtype", choices=["f64", "f32"], default="f64",
+                   help="operand type of --mode apply")
     p.add_argument("--mode", choices=["full", "apply", "solve-fp64", "solve-mixed", "vcycle"],
                    default="full", help="profiling modes run one part only and print a "
                    "short line (not the benchmark line)")
@@ -301,8 +306,22 @@ def run_ours(args, d: Dist):
     for _ in range(3):
         apply_pair()
     ms_apply2, _ = timed(apply_pair, args.apply_iters)
+    # the FP32 apply of the mixed V-cycle's operator (4 x 67 MB inputs/outputs)
+    us32 = [u.float() for u in us]
+    outs32 = [torch.empty_like(us32[0]) for _ in range(2)]
+
+    def apply_pair32():
+        for k in range(2):
+            rc = lib.sbp_apply_f32(C.c_void_p(us32[k].data_ptr()),
+                                   C.c_void_p(outs32[k].data_ptr()), n, -1, sp)
+            assert rc == 0
+
+    for _ in range(3):
+        apply_pair32()
+    ms_apply32_2, _ = timed(apply_pair32, args.apply_iters)
     clocks = sampler.stop()
     ms_apply = ms_apply2 / 2.0
+    ms_apply32 = d.max(ms_apply32_2 / 2.0)
 
     ms32 = d.max(ms32)
     ms64 = d.max(ms64)
@@ -340,8 +359,16 @@ def run_ours(args, d: Dist):
         "roofline": {"kernel": "k_apply<double> (operator apply, FP64)", "bound": "hbm",
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                     "algorithmic_bytes_per_launch": apply_bytes, "traffic": None,
+                     "algorithmic_bytes_per_launch": apply_bytes,
+                     # DRAM read + write of one launch at N = 4097 from a single ncu
+                     # capture (profiles/apply_f64_n4097.md); part of the output stays in L2
+                     "traffic": APPLY_F64_TRAFFIC if n == 4097 else None,
                      "ms_per_launch": round(ms_apply, 5)},
+        "apply_f32": {"kernel": "sbp_apply_f32 (operator apply, FP32)", "achieved_gbs":
+                      round(8.0 * n * n / (ms_apply32 * 1e-3) / 1e9, 1),
+                      "frac": round(8.0 * n * n / (ms_apply32 * 1e-3) / 1e9 / peak, 4),
+                      "algorithmic_bytes_per_launch": 8.0 * n * n,
+                      "ms_per_launch": round(ms_apply32, 5)},
         "clocks": clocks,
         "gpu_launches": int(launches32 * args.steps),
         "detail": {"iters_mixed": r32.iters, "iters_fp64": r64.iters,
@@ -379,14 +406,16 @@ def run_part(args):
     lib = sbp.load_library()
     if args.mode == "apply":
         gen = torch.Generator(device=dev).manual_seed(0)
-        us = [torch.randn(n * n, generator=gen, device=dev, dtype=torch.float64) for _ in range(2)]
+        dt = torch.float64 if args.dtype == "f64" else torch.float32
+        fn = lib.sbp_apply_f64 if args.dtype == "f64" else lib.sbp_apply_f32
+        us = [torch.randn(n * n, generator=gen, device=dev, dtype=dt) for _ in range(2)]
         outs = [torch.empty_like(us[0]) for _ in range(2)]
         for k in range(args.warmup + args.steps):
-            rc = lib.sbp_apply_f64(C.c_void_p(us[k % 2].data_ptr()),
-                                   C.c_void_p(outs[k % 2].data_ptr()), n, -1, sp)
+            rc = fn(C.c_void_p(us[k % 2].data_ptr()), C.c_void_p(outs[k % 2].data_ptr()), n, -1, sp)
             assert rc == 0
         torch.cuda.synchronize()
-        print(json.dumps({"mode": "apply", "n": n, "launches": args.warmup + args.steps}))
+        print(json.dumps({"mode": "apply", "dtype": args.dtype, "n": n,
+                          "launches": args.warmup + args.steps}))
         return
     if args.mode == "vcycle":
         # time one V-cycle (mixed and FP64) for the default hierarchy at --n

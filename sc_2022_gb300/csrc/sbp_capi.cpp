@@ -75,7 +75,7 @@ struct sbp_solver {
   double* p[2] = {nullptr, nullptr};
   double* Ap = nullptr;
   float* r_lo = nullptr;            // FP32 copy of r (mixed precision)
-  Operand ox, orr, op[2], orlo;
+  Operand ox, orr, op[2], oap, orlo;
   SolveState* st = nullptr;
   SolveState* st_host = nullptr;    // pinned, 2 slots
   double* norms = nullptr;
@@ -257,9 +257,9 @@ cudaError_t enqueue_iteration(sbp_solver* s, int kind, int parity, int sign, cud
   if (kind == 0) {
     if (mixed)
       // Ap is updated in place (each point reads its old value, then writes)
-      e = launch_cg_dir_mixed<double>(vcycle_out_op(s), cgrid<double>(s->p[parity], ld),
-                                      cgrid<double>(s->Ap, ld), grid<double>(pnew, ld),
-                                      grid<double>(s->Ap, ld), n, s->st, s->rb, q);
+      e = launch_cg_dir_mixed<double>(vcycle_out_op(s), s->op[parity], s->oap,
+                                      grid<double>(pnew, ld), grid<double>(s->Ap, ld), n, s->st,
+                                      s->rb, q);
     else
       e = launch_cg_dir_op<double, double>(vcycle_out_op(s), s->op[parity], grid<double>(pnew, ld),
                                            grid<double>(s->Ap, ld), n, +1, s->st, s->rb, q);
@@ -635,6 +635,7 @@ int sbp_solver_create(sbp_solver** out, int n, const sbp_options* opts) {
   make_operand(s->orr, s->r, n, s->ld, true);
   make_operand(s->op[0], s->p[0], n, s->ld, true);
   make_operand(s->op[1], s->p[1], n, s->ld, true);
+  make_operand(s->oap, s->Ap, n, s->ld, true);
   rc = dalloc(s, &p, sizeof(SolveState)); if (rc) return rc; s->st = (SolveState*)p;
   const size_t parts = (size_t)max_reduce_ctas(n) + 64;
   rc = dalloc(s, &p, parts * sizeof(double)); if (rc) return rc; s->rb.partials = (double*)p;

@@ -554,7 +554,11 @@ struct CgDirJob {
 // ---------------------------------------------------------------------------
 template <bool TMA>
 struct CgDirMixedJob {
-  static constexpr int kStage = align128(box_bytes<float, BI, BJ>());
+  // one stage: the z box (FP32, 72 x 37) and the p_old, Ap_old tiles (FP64,
+  // 68 x 33 at (64 ti, j_lo)), all three prefetched one tile ahead
+  static constexpr int kOffP = align128(box_bytes<float, BI, BJ>());
+  static constexpr int kOffA = kOffP + align128(box_bytes<double, QI, QJ>());
+  static constexpr int kStage = kOffA + align128(box_bytes<double, QI, QJ>());
   static constexpr int kScratch = 0;
   static constexpr bool kReduce = true;
   // p.Ap from the FP32 roundings of p and Ap, accumulated with the
@@ -564,7 +568,7 @@ struct CgDirMixedJob {
   using Acc = DotAcc<float>;
   using Ctx = DirCtx;
   DevOperand<float> z;
-  Grid<const double> pold, apold;
+  DevOperand<double> pold, apold;
   Grid<double> pnew, Ap;
   int n, ntx, ntot;
   SolveState* st;
@@ -576,68 +580,48 @@ struct CgDirMixedJob {
     return false;
   }
   __device__ int tiles() const { return ntot; }
-  __device__ unsigned tx_bytes(int) const { return TMA ? box_bytes<float, BI, BJ>() : 0u; }
+  __device__ unsigned tx_bytes(int) const {
+    return TMA ? box_bytes<float, BI, BJ>() + 2u * box_bytes<double, QI, QJ>() : 0u;
+  }
   __device__ void issue(unsigned char* buf, unsigned long long* bar, int id, const Ctx&) const {
     const TileBoxes bx(id % ntx, tile_at<TI, TJ>(id, ntx, n).j_lo);
     stage_box<TMA, BI, BJ>(reinterpret_cast<float*>(buf), z, &z.box, bx.x0, bx.y0, n, bar);
+    stage_box<TMA, QI, QJ>(reinterpret_cast<double*>(buf + kOffP), pold, &pold.inner, bx.xi,
+                           bx.yi, n, bar);
+    stage_box<TMA, QI, QJ>(reinterpret_cast<double*>(buf + kOffA), apold, &apold.inner, bx.xi,
+                           bx.yi, n, bar);
   }
   __device__ void compute(unsigned char* buf, int id, Acc& acc, const Ctx& c, unsigned char*) const {
     const TileT t = tile_at<TI, TJ>(id, ntx, n);
     const TileBoxes bx(id % ntx, t.j_lo);
     const float* s = reinterpret_cast<const float*>(buf);
+    const double* sp = reinterpret_cast<const double*>(buf + kOffP);
+    const double* sa = reinterpret_cast<const double*>(buf + kOffA);
     const double beta = c.beta;
     const bool first = c.first;
-    auto emit = [&](int i, int j, float zc, double az) {
+    auto emit = [&](int i, int j, int k, float zc, double az) {
       const double zd = f32_to_f64(zc);
-      double pv = zd, ap = az;
-      if (!first) {
-        pv = fma(beta, __ldg(&pold.at(i, j)), zd);
-        ap = fma(beta, __ldg(&apold.at(i, j)), az);
-      }
+      const double pv = first ? zd : fma(beta, sp[k], zd);
+      const double ap = first ? az : fma(beta, sa[k], az);
       pnew.at(i, j) = pv;
       Ap.at(i, j) = ap;
       acc.add_prod(f64_to_f32(pv), f64_to_f32(ap));
     };
     if (tile_interior(t, n)) {
-      // the old direction and operator values of this thread's 8 points are
-      // loaded up front: Ap is updated in place, so per-point loads after the
-      // previous point's store could not be reordered by the compiler
-      const int r = threadIdx.x & 63, g = threadIdx.x >> 6;
-      const int i = t.i_lo + r, j0 = t.j_lo + 8 * g;
-      double po[8], ao[8];
-      if (!first) {
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          po[q] = __ldg(&pold.at(i, j0 + q));
-          ao[q] = apold.at(i, j0 + q);
-        }
-      }
-      const float* col = s + (8 * g + 2) * BI + r + 5;
-      float um = col[-BI], u0 = col[0];
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const float up = col[(q + 1) * BI];
-        const float uw = col[q * BI - 1], ue = col[q * BI + 1];
+      visit_interior(s, t, [&](int i, int j, float um, float u0, float up, float uw, float ue,
+                               int k) {
         float hi, lo;
         stencil_ff(uw, ue, um, up, u0, hi, lo);
-        const double az = -(f32_to_f64(hi) + f32_to_f64(lo));   // A z = -(stencil)
-        const double zd = f32_to_f64(u0);
-        const double pv = first ? zd : fma(beta, po[q], zd);
-        const double ap = first ? az : fma(beta, ao[q], az);
-        pnew.at(i, j0 + q) = pv;
-        Ap.at(i, j0 + q) = ap;
-        acc.add_prod(f64_to_f32(pv), f64_to_f32(ap));
-        um = u0;
-        u0 = up;
-      }
+        emit(i, j, k, u0, -(f32_to_f64(hi) + f32_to_f64(lo)));   // A z = -(stencil)
+      });
     } else {
-      visit_generic(s, t, bx, [&](int i, int j, const SAcc<float>& a, int) {
+      visit_generic(s, t, bx, [&](int i, int j, const SAcc<float>& a, int k) {
         // boundary rows/columns: the SAT stencil in FP64 on the exact FP32 values
         struct D {
           const SAcc<float>* a;
           __device__ double operator()(int di, int dj) const { return f32_to_f64((*a)(di, dj)); }
         } d{&a};
-        emit(i, j, a(0, 0), -negA<double>(d, i, j, n));
+        emit(i, j, k, a(0, 0), -negA<double>(d, i, j, n));
       });
     }
   }
@@ -651,17 +635,18 @@ struct CgDirMixedJob {
 };
 
 template <typename T>
-cudaError_t launch_cg_dir_mixed(const Operand& z, Grid<const double> pold,
-                                Grid<const double> apold, Grid<double> pnew, Grid<double> Ap,
-                                int n, SolveState* st, ReduceBuf rb, cudaStream_t s) {
+cudaError_t launch_cg_dir_mixed(const Operand& z, const Operand& pold, const Operand& apold,
+                                Grid<double> pnew, Grid<double> Ap, int n, SolveState* st,
+                                ReduceBuf rb, cudaStream_t s) {
   const dim3 g = tile_grid(n);
   const int total = (int)(g.x * g.y);
   const DevOperand<float> dz = dev_operand<float>(z);
-  if (z.tma)
-    return launch_persist(
-        CgDirMixedJob<true>{dz, pold, apold, pnew, Ap, n, (int)g.x, total, st, rb}, total, s);
-  return launch_persist(
-      CgDirMixedJob<false>{dz, pold, apold, pnew, Ap, n, (int)g.x, total, st, rb}, total, s);
+  const DevOperand<double> dp = dev_operand<double>(pold), da = dev_operand<double>(apold);
+  if (z.tma && pold.tma && apold.tma)
+    return launch_persist(CgDirMixedJob<true>{dz, dp, da, pnew, Ap, n, (int)g.x, total, st, rb},
+                          total, s);
+  return launch_persist(CgDirMixedJob<false>{dz, dp, da, pnew, Ap, n, (int)g.x, total, st, rb},
+                        total, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -2046,9 +2031,9 @@ template cudaError_t launch_cg_dir_op<double, double>(const Operand&, const Oper
 template cudaError_t launch_cg_dir_op<double, float>(const Operand&, const Operand&, Grid<double>,
                                                      Grid<double>, int, int, SolveState*,
                                                      ReduceBuf, cudaStream_t);
-template cudaError_t launch_cg_dir_mixed<double>(const Operand&, Grid<const double>,
-                                                 Grid<const double>, Grid<double>, Grid<double>,
-                                                 int, SolveState*, ReduceBuf, cudaStream_t);
+template cudaError_t launch_cg_dir_mixed<double>(const Operand&, const Operand&, const Operand&,
+                                                 Grid<double>, Grid<double>, int, SolveState*,
+                                                 ReduceBuf, cudaStream_t);
 template cudaError_t launch_cg_dir<double, double>(Grid<const double>, Grid<const double>,
                                                    Grid<double>, Grid<double>, int, int,
                                                    SolveState*, ReduceBuf, cudaStream_t);

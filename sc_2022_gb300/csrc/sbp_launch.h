@@ -24,12 +24,13 @@ template <typename T, typename Tz>
 cudaError_t launch_cg_dir_op(const Operand& z, const Operand& pold, Grid<T> pnew, Grid<T> Ap,
                              int n, int opsign, SolveState* st, ReduceBuf rb, cudaStream_t s);
 // Mixed-precision CG direction: p = z + beta p_old, Ap = A z + beta Ap_old
-// (A z exact in float-float from the FP32 z), p.Ap -> alpha.  Reads p_old and
-// Ap_old pointwise; writes p_new and Ap (Ap_old and Ap must differ).
+// (A z exact in float-float from the FP32 z), p.Ap -> alpha.  p_old and
+// Ap_old are staged tile by tile (TMA when all three operands allow it);
+// Ap may be Ap_old's array (updated in place: tiles are disjoint).
 template <typename T>
-cudaError_t launch_cg_dir_mixed(const Operand& z, Grid<const double> pold,
-                                Grid<const double> apold, Grid<double> pnew, Grid<double> Ap,
-                                int n, SolveState* st, ReduceBuf rb, cudaStream_t s);
+cudaError_t launch_cg_dir_mixed(const Operand& z, const Operand& pold, const Operand& apold,
+                                Grid<double> pnew, Grid<double> Ap, int n, SolveState* st,
+                                ReduceBuf rb, cudaStream_t s);
 template <typename T>
 cudaError_t launch_smooth_op(int field, int epi, const Operand& vin, const Operand& e,
                              const Operand& b, Grid<T> vout, int n, int smoother, double omega,
