@@ -176,6 +176,15 @@ int sbp_rhs_f64(const double* f, const double* gW, const double* gE, const doubl
 int sbp_rhs_adjoint_f64(const double* lam, double* df, double* dgW, double* dgE, double* dgS,
                         double* dgN, int n, double fsign, void* stream);
 
+/* The H-norm misfit of the adjoint configuration: g = H~ (u - ut) and
+ * *loss = 1/2 (u - ut)' H~ (u - ut) with H~ = h^2 diag(w_i w_j), w = 1/2 on
+ * the first and last index (the H~ of Assembling_matrix,
+ * level_2_multigrid_new.jl:119).  g (n x n) and loss (one double in device
+ * memory) may each be NULL, not both.  Stream-ordered.  No reference
+ * counterpart: the adjoint path is new. */
+int sbp_h_misfit_f64(const double* u, const double* ut, double* g, int n, double* loss,
+                     void* stream);
+
 /* ---- solver handle ---------------------------------------------------- */
 
 /* Create a solver for n x n grids on the current device.  opts == NULL
@@ -217,6 +226,17 @@ int sbp_cg_solve(sbp_solver* s, const double* b, double* x, int sign, double abs
 /* One V-cycle from v = 0: v = M b.  matrix_free_Two_level_multigrid(b, A_2h;
  * nu) (matrix_free_mg_cg.jl:143-176) for the two-level options. */
 int sbp_vcycle_apply(sbp_solver* s, const double* b, double* v, void* stream);
+
+/* Adjoint MGCG: lam = A^-T gu = A^-1 gu (A is SPD) with the handle's MGCG
+ * from lam = 0 (tolerances as sbp_mgcg_solve), then the transpose of
+ * sbp_rhs_f64's map applied to lam.  For u = A^-1 sbp_rhs_f64(f, g, fsign)
+ * and a loss L(u) with dL/du = gu this gives dL/df (df, n x n) and dL/dg_side
+ * (dgW, dgE, dgS, dgN, length n); each of those may be NULL.  lam (n x n) is
+ * required.  Returns the solve's status (SBP_ERR_MAXITER still fills the
+ * gradients).  No reference counterpart: the reference has no adjoint. */
+int sbp_mgcg_adjoint_f64(sbp_solver* s, const double* gu, double* lam, double* df, double* dgW,
+                         double* dgE, double* dgS, double* dgN, double fsign, double abstol,
+                         double reltol, int maxiter, sbp_result* res, void* stream);
 
 /* ---- host-only helpers ------------------------------------------------ */
 

@@ -572,3 +572,23 @@ def cg(A, b, x=None, abstol=None, reltol=None, maxiter=None):
         p = r + (rsn / rs) * p
         rs = rsn
     return x, it, norms
+
+
+def misfit_loss_grad(asm: Assembled, f_ref, g: dict, ut):
+    """Adjoint-path oracle (the reference has no adjoint code; this restates
+    the calculus of its operator).  With b = asm.rhs(f_ref, g) and
+    u = A^-1 b by a sparse direct solve (``matrix_free_mg_cg.jl:460`` uses
+    ``lu`` the same way), L = 1/2 (u - ut)' H~ (u - ut),
+    lam = A^-1 H~ (u - ut) (A is symmetric), dL/df = -H~ lam and
+    dL/dg_side = -SAT_side' H~ lam (b = -H~ (f + sum SAT_side g_side)).
+    Returns (L, df, dg, u, lam), all flat float64 arrays (dg: side -> n)."""
+    lu = spla.splu(asm.A.tocsc())
+    u = lu.solve(asm.rhs(f_ref, g))
+    d = u - np.asarray(ut, dtype=np.float64).ravel()
+    hd = asm.H_tilde @ d
+    loss = 0.5 * float(d @ hd)
+    lam = lu.solve(hd)
+    hl = asm.H_tilde @ lam
+    df = -hl
+    dg = {s: -(asm.sat_r[s].T @ hl) for s in ("W", "E", "S", "N")}
+    return loss, df, dg, u, lam

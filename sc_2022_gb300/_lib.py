@@ -82,6 +82,9 @@ SIGNATURES = {
     "sbp_mgcg_solve": (_i, [_vp, _vp, _vp, _d, _d, _i, C.POINTER(sbp_result), _dp, _i, _vp]),
     "sbp_cg_solve": (_i, [_vp, _vp, _vp, _i, _d, _d, _i, C.POINTER(sbp_result), _dp, _i, _vp]),
     "sbp_vcycle_apply": (_i, [_vp, _vp, _vp, _vp]),
+    "sbp_h_misfit_f64": (_i, [_vp, _vp, _vp, _i, _vp, _vp]),
+    "sbp_mgcg_adjoint_f64": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _d, _d, _d, _i,
+                                  C.POINTER(sbp_result), _vp]),
     "sbp_coarse_inverse_host": (_i, [_i, _dp, C.c_longlong]),
 }
 

@@ -598,6 +598,18 @@ int sbp_rhs_adjoint_f64(const double* lam, double* df, double* dgW, double* dgE,
   return SBP_OK;
 }
 
+int sbp_h_misfit_f64(const double* u, const double* ut, double* g, int n, double* loss,
+                     void* stream) {
+  if (!u || !ut || n < 3 || (!g && !loss)) return SBP_ERR_ARGS;
+  cudaStream_t q = (cudaStream_t)stream;
+  TempReduce t;
+  int rc = t.alloc(n, q);
+  if (rc) return rc;
+  SBP_CUDA(launch_h_misfit(cgrid<double>(u, n), cgrid<double>(ut, n), grid<double>(g, n), n,
+                           loss, t.rb, q));
+  return SBP_OK;
+}
+
 int sbp_solver_create(sbp_solver** out, int n, const sbp_options* opts) {
   if (!out) return SBP_ERR_ARGS;
   *out = nullptr;
@@ -737,6 +749,23 @@ int sbp_cg_solve(sbp_solver* s, const double* b, double* x, int sign, double abs
   if (sign != 1 && sign != -1) return SBP_ERR_ARGS;
   return run_krylov(s, 1, b, x, sign, abstol, reltol, maxiter, res, norms, norms_cap,
                     (cudaStream_t)stream);
+}
+
+int sbp_mgcg_adjoint_f64(sbp_solver* s, const double* gu, double* lam, double* df, double* dgW,
+                         double* dgE, double* dgS, double* dgN, double fsign, double abstol,
+                         double reltol, int maxiter, sbp_result* res, void* stream) {
+  if (!s || !gu || !lam) return SBP_ERR_ARGS;
+  cudaStream_t q = (cudaStream_t)stream;
+  SBP_CUDA(cudaSetDevice(s->device));
+  const int n = s->n;
+  // A is symmetric: the adjoint solve is the forward MGCG on gu, from zero
+  SBP_CUDA(cudaMemsetAsync(lam, 0, (size_t)n * n * sizeof(double), q));
+  const int rc = run_krylov(s, 0, gu, lam, +1, abstol, reltol, maxiter, res, nullptr, 0, q);
+  if (rc != SBP_OK && rc != SBP_ERR_MAXITER) return rc;
+  if (df || dgW || dgE || dgS || dgN)
+    SBP_CUDA(launch_rhs_adjoint(cgrid<double>(lam, n), grid<double>(df, n), dgW, dgE, dgS, dgN,
+                                n, fsign, q));
+  return rc;
 }
 
 int sbp_vcycle_apply(sbp_solver* s, const double* b, double* v, void* stream) {

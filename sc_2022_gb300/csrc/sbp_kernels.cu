@@ -1896,6 +1896,35 @@ cudaError_t launch_dot(Grid<const T> a, Grid<const T> b, int n, double* out, Red
   return cudaGetLastError();
 }
 
+// g = H~ (u - ut) and *loss = 1/2 (u - ut)' H~ (u - ut), H~ = h^2 diag(w_i w_j)
+// (w = 1/2 on the first and last index): the H-norm misfit of the adjoint
+// configuration and its gradient.  Columns over CTAs, rows over threads;
+// deterministic reduction.
+__global__ void __launch_bounds__(kThreads)
+    k_h_misfit(Grid<const double> u, Grid<const double> ut, Grid<double> g, int n, double h2,
+               double* loss, ReduceBuf rb) {
+  double acc = 0.0;
+  for (int j = blockIdx.x; j < n; j += gridDim.x) {
+    const double cj = (j == 0 || j == n - 1) ? 0.5 * h2 : h2;
+    for (int i = threadIdx.x; i < n; i += kThreads) {
+      const double d = __ldg(&u.at(i, j)) - __ldg(&ut.at(i, j));
+      const double hd = ((i == 0 || i == n - 1) ? 0.5 * cj : cj) * d;
+      if (g.p) g.at(i, j) = hd;
+      acc = fma(hd, d, acc);
+    }
+  }
+  grid_reduce(acc, rb, [&](double tot) {
+    if (loss) *loss = 0.5 * tot;
+  });
+}
+
+cudaError_t launch_h_misfit(Grid<const double> u, Grid<const double> ut, Grid<double> g, int n,
+                            double* loss, ReduceBuf rb, cudaStream_t s) {
+  const double h = 1.0 / (double)(n - 1);
+  k_h_misfit<<<std::min(n, kFlatCtas), kThreads, 0, s>>>(u, ut, g, n, h * h, loss, rb);
+  return cudaGetLastError();
+}
+
 __global__ void k_state_init(SolveState* st, int maxiter) {
   pdl_begin();
   SolveState z = {};

@@ -163,4 +163,9 @@ cudaError_t launch_rhs(Grid<const double> f, const double* gW, const double* gE,
 cudaError_t launch_rhs_adjoint(Grid<const double> lam, Grid<double> df, double* dgW, double* dgE,
                                double* dgS, double* dgN, int n, double fsign, cudaStream_t s);
 
+// g = H~ (u - ut) (g.p may be null) and *loss = 1/2 (u - ut)' H~ (u - ut)
+// (loss may be null); H~ = h^2 diag(w_i w_j).
+cudaError_t launch_h_misfit(Grid<const double> u, Grid<const double> ut, Grid<double> g, int n,
+                            double* loss, ReduceBuf rb, cudaStream_t s);
+
 }  // namespace sbp

@@ -204,6 +204,31 @@ class Solver:
             self._h, ptr(b), ptr(x), sign, abstol, reltol, maxiter, res, buf, cap, sp),
             "sbp_cg_solve", maxiter, raise_on_fail)
 
+    def adjoint(self, gu: torch.Tensor, lam: torch.Tensor, df: torch.Tensor | None = None,
+                dg: dict | None = None, fsign: float = 1.0, abstol: float = 0.0,
+                reltol: float = 0.0, maxiter: int | None = None, stream=None,
+                raise_on_fail=True) -> SolveResult:
+        """Adjoint MGCG: lam = A^-1 gu (A is SPD), then the transposed
+        right-hand-side map: df = dL/df and dg[side] = dL/dg_side for
+        dL/du = gu (outputs written in place; df/dg may be None)."""
+        n = self._check_pair(gu, lam)
+        maxiter = n * n if maxiter is None else maxiter
+        sp = _stream_ptr(stream)
+        dg = dg or {}
+        for k, t in dg.items():
+            if t.dtype != torch.float64 or t.numel() != n or not t.is_contiguous():
+                raise ValueError(f"dg[{k!r}] must be a contiguous float64 vector of length {n}")
+        if df is not None:
+            check_grid(df, name="df")
+        outs = [ptr(df) if df is not None else None] + [
+            ptr(dg[k]) if dg.get(k) is not None else None for k in ("W", "E", "S", "N")]
+        res = L.sbp_result()
+        st = self._lib.sbp_mgcg_adjoint_f64(self._h, ptr(gu), ptr(lam), *outs, fsign, abstol,
+                                             reltol, maxiter, C.byref(res), sp)
+        if st < 0 and (raise_on_fail or st not in (L.SBP_ERR_MAXITER, L.SBP_ERR_BREAKDOWN)):
+            L.check(st, "sbp_mgcg_adjoint_f64")
+        return SolveResult(res.iters, st, [], res.initial_norm, res.final_norm, res.threshold)
+
     def vcycle(self, b: torch.Tensor, v: torch.Tensor, stream=None) -> torch.Tensor:
         """v = M b, one V-cycle from zero."""
         check_grid(b, name="b")

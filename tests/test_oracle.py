@@ -162,3 +162,25 @@ def test_vcycle_galerkin_h_independent():
         _, it, _ = o.mgcg(hier, a.rhs(F, g), reltol=1e-10)
         its.append(it)
     assert max(its) <= 8 and max(its) - min(its) <= 1
+
+
+def test_adjoint_oracle_matches_finite_differences():
+    # The oracle gradient of L = 1/2 |u - ut|_H^2 along seeded directions in
+    # (f, gW, gE, gS, gN): central differences are exact for a quadratic loss
+    # up to rounding.
+    n = 17
+    asm = o.assemble(n)
+    rng = np.random.default_rng(11)
+    f = rng.standard_normal(n * n)
+    g = {s: rng.standard_normal(n) for s in "WESN"}
+    ut = rng.standard_normal(n * n) * 0.01
+    loss, df, dg, u, lam = o.misfit_loss_grad(asm, f, g, ut)
+    eps = 1e-6
+    for _ in range(8):
+        d_f = rng.standard_normal(n * n)
+        d_g = {s: rng.standard_normal(n) for s in "WESN"}
+        lp = o.misfit_loss_grad(asm, f + eps * d_f, {s: g[s] + eps * d_g[s] for s in g}, ut)[0]
+        lm = o.misfit_loss_grad(asm, f - eps * d_f, {s: g[s] - eps * d_g[s] for s in g}, ut)[0]
+        fd = (lp - lm) / (2 * eps)
+        an = float(df @ d_f) + sum(float(dg[s] @ d_g[s]) for s in "WESN")
+        assert abs(fd - an) <= 1e-6 * abs(an) + 1e-12
