@@ -238,6 +238,34 @@ int sbp_mgcg_adjoint_f64(sbp_solver* s, const double* gu, double* lam, double* d
                          double* dgE, double* dgS, double* dgN, double fsign, double abstol,
                          double reltol, int maxiter, sbp_result* res, void* stream);
 
+/* ---- batched solves --------------------------------------------------- */
+
+/* A batch of independent MGCG problems of any grid sizes ns[0..count-1]
+ * (each 2^m+1 and >= opts->coarse_n; opts as sbp_solver_create, required).
+ * Every problem gets its own buffers, hierarchy and Krylov state; a solve
+ * runs all problems together: the problems of one grid size share every
+ * kernel launch (one pool of CTAs over all their tiles, per-problem
+ * reductions, finished problems skip their tiles), the grid sizes run as
+ * parallel branches, and one iteration of the whole batch is one CUDA graph.
+ * At most 512 problems per grid size.  No reference counterpart: the
+ * reference solves one problem per call (matrix_free_MGCG,
+ * matrix_free_mg_cg.jl:281-324). */
+typedef struct sbp_batch sbp_batch;
+int sbp_batch_create(sbp_batch** out, const int* ns, int count, const sbp_options* opts);
+int sbp_batch_destroy(sbp_batch* b);
+int sbp_batch_size(const sbp_batch* b);
+long long sbp_batch_device_bytes(const sbp_batch* b);
+/* Kernel launches of the last batched solve (batched launches, not per
+ * problem). */
+long long sbp_batch_last_launches(const sbp_batch* b);
+/* MGCG on A_k x_k = b_k for every problem k from the caller's x_k (device
+ * pointers in the caller's layout, ld = n_k; host arrays of count pointers),
+ * with the stopping rule of sbp_mgcg_solve applied per problem.  results
+ * (count entries, may be NULL) receives each problem's outcome.  Returns
+ * SBP_OK when every problem converged, else the first other status. */
+int sbp_batch_mgcg_solve(sbp_batch* b, const double* const* bs, double* const* xs, double abstol,
+                         double reltol, int maxiter, sbp_result* results, void* stream);
+
 /* ---- host-only helpers ------------------------------------------------ */
 
 /* Dense inverse of the coarse operator A on an nc x nc grid (row-major,

@@ -11,7 +11,8 @@ from .matrix_free import (CG_Matrix_Free_GPU_v2, CG_full_GPU, jacobi, matrix_fre
                           matrix_free_A_full_GPU_f32, matrix_free_MGCG,
                           matrix_free_prolongation_2d_GPU, matrix_free_restriction_2d_GPU,
                           matrix_free_richardson, matrix_free_Two_level_multigrid)
-from .solver import Options, SolveResult, Solver, default_options, reference_two_level_options
+from .solver import (BatchSolver, Options, SolveResult, Solver, default_options,
+                     reference_two_level_options)
 
 __all__ = [
     "CG_Matrix_Free_GPU_v2", "CG_full_GPU", "jacobi", "matrix_free_A_full_GPU",
@@ -19,7 +20,7 @@ __all__ = [
     "matrix_free_restriction_2d_GPU", "matrix_free_richardson",
     "matrix_free_Two_level_multigrid", "Options", "SolveResult", "Solver", "default_options",
     "reference_two_level_options", "SbpError", "load_library", "HMisfit", "PoissonSolve",
-    "mgcg_rrule",
+    "mgcg_rrule", "BatchSolver",
 ]
 
 

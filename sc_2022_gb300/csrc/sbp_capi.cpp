@@ -313,35 +313,65 @@ int capture_iteration(sbp_solver* s, int kind, int sign) {
   return SBP_OK;
 }
 
-// Shared driver of sbp_mgcg_solve (kind 0) and sbp_cg_solve (kind 1).
-int run_krylov(sbp_solver* s, int kind, const double* b, double* x, int sign, double abstol,
-               double reltol, int maxiter, sbp_result* res, double* norms_out, int norms_cap,
-               cudaStream_t q) {
+// Argument checks and per-solve buffers of a Krylov solve.
+int krylov_prepare(sbp_solver* s, int kind, const double* b, double* x, double abstol,
+                   double reltol, int maxiter) {
   if (!s || !b || !x) return SBP_ERR_ARGS;
   if (maxiter < 0) return SBP_ERR_ARGS;
   if (kind == 0 && !s->mg) return SBP_ERR_UNSUPPORTED;
   if (abstol <= 0.0 && reltol <= 0.0) return SBP_ERR_ARGS;
   SBP_CUDA(cudaSetDevice(s->device));
-  int rc = ensure_norms(s, maxiter);
-  if (rc) return rc;
-  const int n = s->n;
+  return ensure_norms(s, maxiter);
+}
+
+// Set-up of a solve: the caller's x into the padded iterate, state,
+// r0 = b - sign*A*x0, and (MGCG) z0 = M r0 with r.z.
+cudaError_t enqueue_setup(sbp_solver* s, int kind, const double* b, double* x, int sign,
+                          double abstol, double reltol, int maxiter, cudaStream_t q) {
+  const int n = s->n, ld = s->ld;
   const bool mixed = (kind == 0 && s->opts.precision == SBP_PREC_MIXED);
-  const int ld = s->ld;
-  // set-up: the caller's x into the padded iterate, state, r0 = b - sign*A*x0,
-  // z0 = M r0 and rz (MGCG)
-  SBP_CUDA(cudaMemcpy2DAsync(s->x, (size_t)ld * sizeof(double), x, (size_t)n * sizeof(double),
-                             (size_t)n * sizeof(double), n, cudaMemcpyDeviceToDevice, q));
-  SBP_CUDA(launch_state_init(s->st, maxiter, q));
+  cudaError_t e = copy_grid(s->x, ld, x, n, n, q);
+  if (e == cudaSuccess) e = launch_state_init(s->st, maxiter, q);
   Operand ob;
   ob.p = b;
   ob.n = n;
   ob.ld = n;
   ob.tma = false;
-  SBP_CUDA(launch_residual_op<double>(s->ox, ob, grid<double>(s->r, ld),
-                                      Grid<float>{mixed ? s->r_lo : nullptr, ld}, n, sign, s->st,
-                                      s->norms, abstol, reltol, kind == 1 ? 1 : 0, nullptr, s->rb,
-                                      q));
-  if (kind == 0) SBP_CUDA(enqueue_vcycle_any(s, true, s->st, q));
+  if (e == cudaSuccess)
+    e = launch_residual_op<double>(s->ox, ob, grid<double>(s->r, ld),
+                                   Grid<float>{mixed ? s->r_lo : nullptr, ld}, n, sign, s->st,
+                                   s->norms, abstol, reltol, kind == 1 ? 1 : 0, nullptr, s->rb, q);
+  if (e == cudaSuccess && kind == 0) e = enqueue_vcycle_any(s, true, s->st, q);
+  return e;
+}
+
+// Status and result fields from a final solver state.
+int finish_result(const SolveState& fs, sbp_result* res) {
+  int status;
+  if (fs.done == kDoneConverged)
+    status = SBP_OK;
+  else if (fs.done == kDoneBreakdown)
+    status = SBP_ERR_BREAKDOWN;
+  else
+    status = SBP_ERR_MAXITER;
+  if (res) {
+    res->iters = fs.iter;
+    res->status = status;
+    res->initial_norm = std::sqrt(fs.rr0);
+    res->final_norm = std::sqrt(fs.rr);
+    res->threshold = std::sqrt(fs.thresh2);
+  }
+  return status;
+}
+
+// Shared driver of sbp_mgcg_solve (kind 0) and sbp_cg_solve (kind 1).
+int run_krylov(sbp_solver* s, int kind, const double* b, double* x, int sign, double abstol,
+               double reltol, int maxiter, sbp_result* res, double* norms_out, int norms_cap,
+               cudaStream_t q) {
+  int rc = krylov_prepare(s, kind, b, x, abstol, reltol, maxiter);
+  if (rc) return rc;
+  const int n = s->n, ld = s->ld;
+  SBP_CUDA(enqueue_setup(s, kind, b, x, sign, abstol, reltol, maxiter, q));
   if (!s->iter_valid[kind] || s->iter_key_sign[kind] != sign || !s->iter_exec[kind][0]) {
     rc = capture_iteration(s, kind, sign);
     if (rc) return rc;
@@ -364,8 +394,7 @@ int run_krylov(sbp_solver* s, int kind, const double* b, double* x, int sign, do
     ++k;
     if (k > maxiter + 2) finished = true;  // safety net; kernels stop at maxiter
   }
-  SBP_CUDA(cudaMemcpy2DAsync(x, (size_t)n * sizeof(double), s->x, (size_t)ld * sizeof(double),
-                             (size_t)n * sizeof(double), n, cudaMemcpyDeviceToDevice, q));
+  SBP_CUDA(copy_grid(x, n, s->x, ld, n, q));
   SBP_CUDA(cudaMemcpyAsync(&s->st_host[0], s->st, sizeof(SolveState), cudaMemcpyDeviceToHost, q));
   SBP_CUDA(cudaStreamSynchronize(q));
   if (read_device_fault() != 0u) {
@@ -374,27 +403,12 @@ int run_krylov(sbp_solver* s, int kind, const double* b, double* x, int sign, do
   }
   const SolveState fs = s->st_host[0];
   s->last_launches = launches;
-  const int iters = fs.iter;
   if (norms_out && norms_cap > 0) {
-    const int cnt = std::min(norms_cap, iters + 1);
+    const int cnt = std::min(norms_cap, fs.iter + 1);
     SBP_CUDA(cudaMemcpy(norms_out, s->norms, (size_t)cnt * sizeof(double),
                         cudaMemcpyDeviceToHost));
   }
-  int status;
-  if (fs.done == kDoneConverged)
-    status = SBP_OK;
-  else if (fs.done == kDoneBreakdown)
-    status = SBP_ERR_BREAKDOWN;
-  else
-    status = SBP_ERR_MAXITER;
-  if (res) {
-    res->iters = iters;
-    res->status = status;
-    res->initial_norm = std::sqrt(fs.rr0);
-    res->final_norm = std::sqrt(fs.rr);
-    res->threshold = std::sqrt(fs.thresh2);
-  }
-  return status;
+  return finish_result(fs, res);
 }
 
 // Stream-ordered scratch for the single-grid reducing entry points.
@@ -786,6 +800,373 @@ int sbp_vcycle_apply(sbp_solver* s, const double* b, double* v, void* stream) {
                                cudaMemcpyDeviceToDevice, q));
   }
   return SBP_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Batched MGCG.  Every problem keeps its own solver (buffers, hierarchy,
+// Krylov state); the launches of one problem's set-up, iteration and finish
+// are recorded instead of launched, and the records at one position of all
+// problems of one grid size are launched as one batched kernel (one CTA pool
+// over all their tiles, per-problem reductions and early exit).  Grid sizes
+// are independent branches on their own streams, forked from and joined into
+// the caller's stream; one iteration of the whole batch is one CUDA graph per
+// p parity, and the host reads all problems' states once per iteration.
+// ===========================================================================
+namespace {
+
+struct BatchGroup {
+  BatchLaunchFn fn = nullptr;
+  int aux[4] = {0, 0, 0, 0};
+  int stride = 0;
+  size_t offset = 0;  // of the argument blobs in the arena
+};
+
+struct BatchArena {
+  unsigned char* dev = nullptr;
+  size_t cap = 0;
+  std::vector<BatchGroup> groups;
+};
+
+struct BatchClass {
+  int n = 0;
+  std::vector<int> members;  // problem indices, increasing
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  BatchScratch scr;
+  BatchArena iter[2], setup, finish;
+};
+
+}  // namespace
+
+struct sbp_batch {
+  int device = 0;
+  int count = 0;
+  sbp_options opts{};
+  std::vector<sbp_solver*> solvers;
+  std::vector<BatchClass> classes;  // decreasing n
+  SolveState* states = nullptr;       // device, one per problem
+  SolveState* states_host = nullptr;  // pinned, 2 x count
+  std::vector<void*> allocs;
+  cudaGraphExec_t iter_exec[2] = {nullptr, nullptr};
+  bool iter_valid = false;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  cudaStream_t cap = nullptr;
+  long long launches_per_iter = 0;
+  long long last_launches = 0;
+};
+
+namespace {
+
+void batch_free_arena(BatchArena& a) {
+  if (a.dev) cudaFree(a.dev);
+  a.dev = nullptr;
+  a.cap = 0;
+  a.groups.clear();
+}
+
+// Record `enqueue(solver)` for every member of class c and merge the records
+// position by position into the arena (one host-to-device copy).
+template <class F>
+int batch_record(sbp_batch* B, BatchClass& c, BatchArena& arena, F&& enqueue, cudaStream_t q) {
+  const size_t cnt = c.members.size();
+  std::vector<std::vector<LaunchRecord>> recs(cnt);
+  for (size_t m = 0; m < cnt; ++m) {
+    Recorder rec;
+    recorder_slot() = &rec;
+    const cudaError_t e = enqueue(B->solvers[c.members[m]]);
+    recorder_slot() = nullptr;
+    if (e != cudaSuccess) return fail_cuda(e, "batched schedule");
+    recs[m] = std::move(rec.recs);
+  }
+  const size_t len = recs[0].size();
+  std::vector<BatchGroup> groups(len);
+  size_t bytes = 0;
+  for (size_t k = 0; k < len; ++k) {
+    const LaunchRecord& r0 = recs[0][k];
+    BatchGroup& g = groups[k];
+    g.fn = r0.fn;
+    std::memcpy(g.aux, r0.aux, sizeof(g.aux));
+    const size_t al = (size_t)std::max(r0.align, 64);
+    g.stride = (int)((r0.blob.size() + al - 1) / al * al);
+    bytes = (bytes + 255) & ~(size_t)255;
+    g.offset = bytes;
+    bytes += (size_t)g.stride * cnt;
+  }
+  std::vector<unsigned char> host(std::max<size_t>(bytes, 1), 0);
+  for (size_t m = 0; m < cnt; ++m) {
+    if (recs[m].size() != len) {
+      g_last_error = "batched schedule: problems of one size recorded different launches";
+      return SBP_ERR_CUDA;
+    }
+    for (size_t k = 0; k < len; ++k) {
+      const LaunchRecord& r = recs[m][k];
+      const BatchGroup& g = groups[k];
+      if (r.fn != g.fn || std::memcmp(r.aux, g.aux, sizeof(g.aux)) != 0 ||
+          r.blob.size() != recs[0][k].blob.size()) {
+        g_last_error = "batched schedule: launch shapes differ within a grid size";
+        return SBP_ERR_CUDA;
+      }
+      std::memcpy(host.data() + g.offset + (size_t)g.stride * m, r.blob.data(), r.blob.size());
+    }
+  }
+  if (bytes > arena.cap) {
+    if (arena.dev) SBP_CUDA(cudaFree(arena.dev));
+    arena.dev = nullptr;
+    arena.cap = 0;
+    SBP_CUDA(cudaMalloc((void**)&arena.dev, bytes));
+    arena.cap = bytes;
+  }
+  if (bytes) SBP_CUDA(cudaMemcpyAsync(arena.dev, host.data(), bytes, cudaMemcpyHostToDevice, q));
+  arena.groups = std::move(groups);
+  return SBP_OK;
+}
+
+cudaError_t batch_launch(BatchClass& c, const BatchArena& a, cudaStream_t s) {
+  const int cnt = (int)c.members.size();
+  for (const BatchGroup& g : a.groups) {
+    const cudaError_t e = g.fn(a.dev + g.offset, g.stride, cnt, g.aux, c.scr, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// Run `pick(class)`'s arena on every class stream, forked from and joined
+// into q.
+template <class Pick>
+cudaError_t batch_run(sbp_batch* B, cudaStream_t q, Pick&& pick) {
+  for (BatchClass& c : B->classes) {
+    cudaError_t e = cudaEventRecord(c.fork, q);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c.stream, c.fork, 0);
+    if (e == cudaSuccess) e = batch_launch(c, pick(c), c.stream);
+    if (e == cudaSuccess) e = cudaEventRecord(c.join, c.stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(q, c.join, 0);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// Resolve every batched launch's configuration outside stream capture.
+cudaError_t batch_prepare(BatchClass& c, const BatchArena& a) {
+  for (const BatchGroup& g : a.groups) {
+    const cudaError_t e = g.fn(nullptr, g.stride, 0, g.aux, c.scr, nullptr);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+void batch_destroy_graphs(sbp_batch* B) {
+  for (auto& g : B->iter_exec)
+    if (g) cudaGraphExecDestroy(g);
+  B->iter_exec[0] = B->iter_exec[1] = nullptr;
+  B->iter_valid = false;
+}
+
+int batch_capture(sbp_batch* B, cudaStream_t q) {
+  long long per_iter = 0;
+  for (BatchClass& c : B->classes) {
+    for (int par = 0; par < 2; ++par) {
+      const int rc = batch_record(
+          B, c, c.iter[par],
+          [&](sbp_solver* s) { return enqueue_iteration(s, 0, par, +1, nullptr); }, q);
+      if (rc) return rc;
+      SBP_CUDA(batch_prepare(c, c.iter[par]));
+    }
+    per_iter += (long long)c.iter[0].groups.size();
+  }
+  SBP_CUDA(cudaStreamSynchronize(q));  // arenas uploaded before the graphs read them
+  batch_destroy_graphs(B);
+  for (int par = 0; par < 2; ++par) {
+    cudaGraph_t g = nullptr;
+    SBP_CUDA(cudaStreamBeginCapture(B->cap, cudaStreamCaptureModeThreadLocal));
+    const cudaError_t e = batch_run(B, B->cap, [&](BatchClass& c) -> const BatchArena& {
+      return c.iter[par];
+    });
+    const cudaError_t e2 = cudaStreamEndCapture(B->cap, &g);
+    if (e != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return fail_cuda(e, "batched iteration (capture)");
+    }
+    if (e2 != cudaSuccess) return fail_cuda(e2, "cudaStreamEndCapture");
+    const cudaError_t e3 = cudaGraphInstantiate(&B->iter_exec[par], g, 0);
+    cudaGraphDestroy(g);
+    if (e3 != cudaSuccess) return fail_cuda(e3, "cudaGraphInstantiate");
+  }
+  B->launches_per_iter = per_iter;
+  B->iter_valid = true;
+  return SBP_OK;
+}
+
+int batch_destroy(sbp_batch* B) {
+  if (!B) return SBP_OK;
+  cudaSetDevice(B->device);
+  batch_destroy_graphs(B);
+  for (BatchClass& c : B->classes) {
+    for (BatchArena* a : {&c.iter[0], &c.iter[1], &c.setup, &c.finish}) batch_free_arena(*a);
+    if (c.stream) cudaStreamDestroy(c.stream);
+    if (c.fork) cudaEventDestroy(c.fork);
+    if (c.join) cudaEventDestroy(c.join);
+  }
+  for (sbp_solver* s : B->solvers) sbp_solver_destroy(s);
+  for (void* p : B->allocs) cudaFree(p);
+  if (B->states_host) cudaFreeHost(B->states_host);
+  for (auto& e : B->ev)
+    if (e) cudaEventDestroy(e);
+  if (B->cap) cudaStreamDestroy(B->cap);
+  delete B;
+  return SBP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sbp_batch_create(sbp_batch** out, const int* ns, int count, const sbp_options* opts) {
+  if (!out || !ns || !opts || count < 1) return SBP_ERR_ARGS;
+  *out = nullptr;
+  for (int k = 0; k < count; ++k)
+    if (!valid_mg_n(ns[k]) || ns[k] < opts->coarse_n) return SBP_ERR_ARGS;
+  sbp_batch* B = new (std::nothrow) sbp_batch();
+  if (!B) return SBP_ERR_NOMEM;
+  std::unique_ptr<sbp_batch, int (*)(sbp_batch*)> guard(B, batch_destroy);
+  SBP_CUDA(cudaGetDevice(&B->device));
+  B->count = count;
+  B->opts = *opts;
+  void* p = nullptr;
+  SBP_CUDA(cudaMalloc(&p, (size_t)count * sizeof(SolveState)));
+  B->allocs.push_back(p);
+  B->states = static_cast<SolveState*>(p);
+  SBP_CUDA(cudaMallocHost((void**)&B->states_host, 2 * (size_t)count * sizeof(SolveState)));
+  B->solvers.assign(count, nullptr);
+  for (int k = 0; k < count; ++k) {
+    const int rc = sbp_solver_create(&B->solvers[k], ns[k], opts);
+    if (rc) return rc;
+    sbp_solver* s = B->solvers[k];
+    s->st = B->states + k;  // the batch reads every state in one copy
+    // resolve the V-cycle schedule (which buffer holds its output) before any
+    // iteration is recorded: record one V-cycle and discard it
+    Recorder scratch;
+    recorder_slot() = &scratch;
+    const cudaError_t e = enqueue_vcycle_any(s, true, s->st, nullptr);
+    recorder_slot() = nullptr;
+    if (e != cudaSuccess) return fail_cuda(e, "batched schedule");
+  }
+  std::vector<int> sizes(ns, ns + count);
+  std::sort(sizes.begin(), sizes.end(), std::greater<int>());
+  sizes.erase(std::unique(sizes.begin(), sizes.end()), sizes.end());
+  B->classes.resize(sizes.size());
+  for (size_t c = 0; c < sizes.size(); ++c) {
+    BatchClass& C = B->classes[c];
+    C.n = sizes[c];
+    for (int k = 0; k < count; ++k)
+      if (ns[k] == C.n) C.members.push_back(k);
+    if ((int)C.members.size() > kMaxBatchSlots) return SBP_ERR_UNSUPPORTED;
+    SBP_CUDA(cudaStreamCreateWithFlags(&C.stream, cudaStreamNonBlocking));
+    SBP_CUDA(cudaEventCreateWithFlags(&C.fork, cudaEventDisableTiming));
+    SBP_CUDA(cudaEventCreateWithFlags(&C.join, cudaEventDisableTiming));
+    const long long parts = (long long)kMaxPersistCtas * (long long)C.members.size();
+    SBP_CUDA(cudaMalloc(&p, (size_t)parts * sizeof(double) + 256));
+    B->allocs.push_back(p);
+    C.scr.partials = static_cast<double*>(p);
+    C.scr.ticket = reinterpret_cast<unsigned*>(static_cast<unsigned char*>(p) +
+                                               (size_t)parts * sizeof(double));
+    C.scr.cap = parts;
+    SBP_CUDA(cudaMemset(C.scr.ticket, 0, sizeof(unsigned)));
+  }
+  SBP_CUDA(cudaStreamCreateWithFlags(&B->cap, cudaStreamNonBlocking));
+  for (auto& e : B->ev) SBP_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  SBP_CUDA(cudaDeviceSynchronize());
+  guard.release();
+  *out = B;
+  return SBP_OK;
+}
+
+int sbp_batch_destroy(sbp_batch* B) { return batch_destroy(B); }
+
+int sbp_batch_size(const sbp_batch* B) { return B ? B->count : SBP_ERR_ARGS; }
+
+long long sbp_batch_device_bytes(const sbp_batch* B) {
+  if (!B) return SBP_ERR_ARGS;
+  long long t = (long long)B->count * (long long)sizeof(SolveState);
+  for (const sbp_solver* s : B->solvers) t += sbp_solver_device_bytes(s);
+  for (const BatchClass& c : B->classes) t += c.scr.cap * (long long)sizeof(double);
+  return t;
+}
+
+long long sbp_batch_last_launches(const sbp_batch* B) { return B ? B->last_launches : 0; }
+
+int sbp_batch_mgcg_solve(sbp_batch* B, const double* const* b, double* const* x, double abstol,
+                         double reltol, int maxiter, sbp_result* results, void* stream) {
+  if (!B || !b || !x) return SBP_ERR_ARGS;
+  cudaStream_t q = (cudaStream_t)stream;
+  SBP_CUDA(cudaSetDevice(B->device));
+  for (int k = 0; k < B->count; ++k) {
+    const int rc = krylov_prepare(B->solvers[k], 0, b[k], x[k], abstol, reltol, maxiter);
+    if (rc) return rc;
+  }
+  if (!B->iter_valid) {
+    const int rc = batch_capture(B, q);
+    if (rc) return rc;
+  }
+  // set-up and finish schedules carry this solve's pointers and tolerances
+  for (BatchClass& c : B->classes) {
+    int rc = batch_record(
+        B, c, c.setup,
+        [&](sbp_solver* s) {
+          const int k = (int)(s->st - B->states);
+          return enqueue_setup(s, 0, b[k], x[k], +1, abstol, reltol, maxiter, nullptr);
+        },
+        q);
+    if (rc) return rc;
+    rc = batch_record(
+        B, c, c.finish,
+        [&](sbp_solver* s) {
+          const int k = (int)(s->st - B->states);
+          return copy_grid(x[k], s->n, s->x, s->ld, s->n, nullptr);
+        },
+        q);
+    if (rc) return rc;
+    SBP_CUDA(batch_prepare(c, c.setup));
+    SBP_CUDA(batch_prepare(c, c.finish));
+  }
+  long long launches = 0;
+  for (BatchClass& c : B->classes) launches += (long long)c.setup.groups.size();
+  SBP_CUDA(batch_run(B, q, [](BatchClass& c) -> const BatchArena& { return c.setup; }));
+  const size_t sb = (size_t)B->count * sizeof(SolveState);
+  int k = 0;
+  bool finished = (maxiter == 0);
+  while (!finished) {
+    SBP_CUDA(cudaGraphLaunch(B->iter_exec[k & 1], q));
+    launches += B->launches_per_iter;
+    SBP_CUDA(cudaMemcpyAsync(B->states_host + (size_t)(k & 1) * B->count, B->states, sb,
+                             cudaMemcpyDeviceToHost, q));
+    SBP_CUDA(cudaEventRecord(B->ev[k & 1], q));
+    if (k >= 1) {
+      SBP_CUDA(cudaEventSynchronize(B->ev[(k - 1) & 1]));
+      const SolveState* h = B->states_host + (size_t)((k - 1) & 1) * B->count;
+      bool all = true;
+      for (int m = 0; m < B->count && all; ++m) all = h[m].done != 0;
+      if (all) finished = true;
+    }
+    ++k;
+    if (k > maxiter + 2) finished = true;  // safety net; kernels stop at maxiter
+  }
+  SBP_CUDA(batch_run(B, q, [](BatchClass& c) -> const BatchArena& { return c.finish; }));
+  for (BatchClass& c : B->classes) launches += (long long)c.finish.groups.size();
+  SBP_CUDA(cudaMemcpyAsync(B->states_host, B->states, sb, cudaMemcpyDeviceToHost, q));
+  SBP_CUDA(cudaStreamSynchronize(q));
+  if (read_device_fault() != 0u) {
+    g_last_error = "a kernel's bounded wait on an asynchronous copy gave up";
+    return SBP_ERR_CUDA;
+  }
+  B->last_launches = launches;
+  int status = SBP_OK;
+  for (int m = 0; m < B->count; ++m) {
+    const int st = finish_result(B->states_host[m], results ? results + m : nullptr);
+    if (st != SBP_OK && status == SBP_OK) status = st;
+  }
+  return status;
 }
 
 }  // extern "C"

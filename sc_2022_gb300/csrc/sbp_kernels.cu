@@ -4,6 +4,9 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <type_traits>
+#include <cstring>
+#include <climits>
 #include <mutex>
 #include <utility>
 
@@ -43,7 +46,6 @@ constexpr int kGemvRowsPerWarp = 2;
 // Flat (pointwise) kernels: CTAs per launch cap.
 constexpr int kFlatCtas = 1216;
 // Upper bound on the CTAs of a persistent launch (SMs x resident CTAs).
-constexpr int kMaxPersistCtas = 4096;
 
 __host__ __device__ constexpr int align128(int b) { return (b + 127) & ~127; }
 
@@ -305,6 +307,169 @@ __global__ void __launch_bounds__(kThreads) k_persist(const __grid_constant__ Jo
   if (Job::kReduce) grid_reduce(acc.value(), job.rb, [&](double tot) { job.finish(tot); });
 }
 
+// ---------------------------------------------------------------------------
+// Batched persistent kernel: `count` problems, each with its own Job (tensor
+// maps included) in device memory, `tpp` tiles each; work item id covers
+// problem id / tpp, tile id % tpp.  A CTA visits problems in increasing order,
+// keeps one accumulator per visited problem (block-summed into shared
+// memory when the problem changes), writes all `count` per-problem partials
+// at the end ([cta][problem], coalesced), and the last CTA finishes each
+// problem on its own thread (partials summed in CTA order: deterministic).
+// Problems whose prepare() says skip (done) stage nothing and compute
+// nothing.
+// ---------------------------------------------------------------------------
+template <class Job>
+constexpr size_t batch_smem_bytes() {
+  return (size_t)(2 * Job::kStage + Job::kScratch + 128) +
+         (Job::kReduce ? (size_t)kMaxBatchSlots * sizeof(double) : 0);
+}
+
+template <class Job>
+__global__ void __launch_bounds__(kThreads)
+    k_persist_batch(const unsigned char* __restrict__ blobs, int stride, int count, int tpp,
+                    double* partials, unsigned* ticket) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) unsigned long long bar[2];
+  __shared__ bool is_last;
+  pdl_begin();
+  const int total = count * tpp;
+  unsigned char* const smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
+  unsigned char* const buf0 = smem;
+  unsigned char* const buf1 = smem + Job::kStage;
+  unsigned char* const scratch = smem + 2 * Job::kStage;
+  double* const slot_part = reinterpret_cast<double*>(scratch + Job::kScratch);
+  auto job_at = [&](int slot) -> const Job& {
+    return *reinterpret_cast<const Job*>(blobs + (size_t)slot * (size_t)stride);
+  };
+  if (Job::kReduce)
+    for (int k = threadIdx.x; k < count; k += kThreads) slot_part[k] = 0.0;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  // stage tile `id` into buf on barrier b (problems that are done: an empty
+  // transaction, so the barrier phase still completes)
+  auto stage = [&](int id, unsigned char* buf, unsigned long long* b, bool fence) {
+    const int slot = id / tpp;
+    const Job& J = job_at(slot);
+    typename Job::Ctx c;
+    const bool act = !J.prepare(c);
+    if (threadIdx.x == 0) {
+      if (fence) fence_proxy_async_smem();
+      mbar_arrive_expect_tx(b, act ? J.tx_bytes(id - slot * tpp) : 0u);
+    }
+    if (act) J.issue(buf, b, id - slot * tpp, c);
+  };
+  typename Job::Acc acc;
+  int cur = -1;   // problem of acc
+  auto flush = [&]() {
+    const double v = block_sum(acc.value());
+    if (threadIdx.x == 0) slot_part[cur] = v;
+  };
+  int tile = blockIdx.x;
+  if (tile < total) stage(tile, buf0, &bar[0], false);
+  cp_async_commit();
+  bool ok = true;
+  for (int k = 0; tile < total; ++k, tile += gridDim.x) {
+    const int next = tile + gridDim.x;
+    const int nb = (k + 1) & 1;
+    if (next < total) stage(next, nb ? buf1 : buf0, &bar[nb], true);
+    cp_async_commit();
+    cp_async_wait<1>();
+    if (threadIdx.x == 0) ok = mbar_wait_bounded(&bar[k & 1], (k >> 1) & 1);
+    if (!__syncthreads_and(ok)) break;
+    const int slot = tile / tpp;
+    if (Job::kReduce && slot != cur) {
+      if (cur >= 0) flush();
+      cur = slot;
+      acc = typename Job::Acc{};
+    }
+    const Job& J = job_at(slot);
+    typename Job::Ctx c;
+    if (!J.prepare(c)) J.compute((k & 1) ? buf1 : buf0, tile - slot * tpp, acc, c, scratch);
+    fence_proxy_async_smem();
+    __syncthreads();
+  }
+  cp_async_wait<0>();
+  if (!ok) return;  // a copy never arrived: the fault flag is set, results are void
+  if (!Job::kReduce) return;
+  if (cur >= 0) flush();
+  __syncthreads();
+  for (int k = threadIdx.x; k < count; k += kThreads)
+    partials[(size_t)blockIdx.x * count + k] = slot_part[k];
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) is_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  for (int k = threadIdx.x; k < count; k += kThreads) {
+    double tot = 0.0;
+    for (unsigned c = 0; c < gridDim.x; ++c) tot += __ldcg(partials + (size_t)c * count + k);
+    const Job& J = job_at(k);
+    typename Job::Ctx c;
+    if (!J.prepare(c)) J.finish(tot);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *ticket = 0u;
+}
+
+template <class Job>
+static int batch_ctas_per_sm() {
+  static const int v = [] {
+    const int smem = (int)batch_smem_bytes<Job>();
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute(k_persist_batch<Job>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           smem);
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_persist_batch<Job>, kThreads, smem) !=
+            cudaSuccess ||
+        b < 1)
+      b = 1;
+    return b;
+  }();
+  return v;
+}
+
+// BatchLaunchFn of a persistent job: aux[0] = tiles per problem.
+template <class Job>
+cudaError_t launch_persist_batch(const unsigned char* blobs, int stride, int count, const int* aux,
+                                 const BatchScratch& scr, cudaStream_t s) {
+  const int cap = std::min(kMaxPersistCtas, sm_count() * batch_ctas_per_sm<Job>());
+  if (count == 0) return cudaGetLastError();
+  if (count > kMaxBatchSlots || stride % alignof(Job) != 0) return cudaErrorInvalidValue;
+  const long long total = (long long)count * aux[0];
+  if (total > INT_MAX) return cudaErrorInvalidValue;
+  const int grid = (int)std::max(1LL, std::min<long long>(total, cap));
+  if (Job::kReduce && (long long)grid * count > scr.cap) return cudaErrorInvalidValue;
+  return launch_pdl(k_persist_batch<Job>, dim3(grid), dim3(kThreads), batch_smem_bytes<Job>(), s,
+                    blobs, stride, count, aux[0], scr.partials, scr.ticket);
+}
+
+Recorder*& recorder_slot() {
+  static thread_local Recorder* r = nullptr;
+  return r;
+}
+
+template <class Args>
+static cudaError_t record_launch(BatchLaunchFn fn, const Args& a, int aux0, int aux1 = 0,
+                                 int aux2 = 0, int aux3 = 0) {
+  static_assert(std::is_trivially_copyable<Args>::value, "launch arguments are copied as bytes");
+  LaunchRecord r;
+  r.fn = fn;
+  r.aux[0] = aux0;
+  r.aux[1] = aux1;
+  r.aux[2] = aux2;
+  r.aux[3] = aux3;
+  r.align = (int)std::max<size_t>(16, alignof(Args));
+  r.blob.resize(sizeof(Args));
+  std::memcpy(r.blob.data(), &a, sizeof(Args));
+  recorder_slot()->recs.push_back(std::move(r));
+  return cudaSuccess;
+}
+
 template <class Job>
 static int persist_ctas_per_sm() {
   static const int v = [] {
@@ -323,6 +488,7 @@ static int persist_ctas_per_sm() {
 
 template <class Job>
 static cudaError_t launch_persist(const Job& job, int total, cudaStream_t s) {
+  if (recorder_slot()) return record_launch(&launch_persist_batch<Job>, job, total);
   const int cap = std::min(kMaxPersistCtas, sm_count() * persist_ctas_per_sm<Job>());
   const int grid = std::max(1, std::min(total, cap));
   return launch_pdl(k_persist<Job>, dim3(grid), dim3(kThreads),
@@ -661,18 +827,35 @@ __device__ __forceinline__ void cg_update_pt(double& x, double& r, double p, dou
   acc = fma(r, r, acc);
 }
 
+struct CgUpdateArgs {
+  double* x;
+  double* r;
+  const double* p;
+  const double* Ap;
+  float* rlo;
+  long long N;
+  int plain;
+  SolveState* st;
+  double* norms;
+  ReduceBuf rb;
+};
+
+// The update over CTAs cta = 0 .. ncta-1 of one problem.
 template <bool VEC>
-__global__ void __launch_bounds__(kThreads)
-    k_cg_update(double* __restrict__ x, double* __restrict__ r, const double* __restrict__ p,
-                const double* __restrict__ Ap, float* __restrict__ rlo, long long N, int plain,
-                SolveState* st, double* norms, ReduceBuf rb) {
-  pdl_begin();
+__device__ __forceinline__ void cg_update_run(const CgUpdateArgs& a, unsigned cta, unsigned ncta) {
+  SolveState* st = a.st;
   if (st->done) return;
   const double alpha = st->alpha;
   double acc = 0.0;
-  const long long tid = (long long)blockIdx.x * kThreads + threadIdx.x;
-  const long long stride = (long long)gridDim.x * kThreads;
+  const long long N = a.N;
+  const long long tid = (long long)cta * kThreads + threadIdx.x;
+  const long long stride = (long long)ncta * kThreads;
   long long done_to = 0;
+  double* __restrict__ x = a.x;
+  double* __restrict__ r = a.r;
+  const double* __restrict__ p = a.p;
+  const double* __restrict__ Ap = a.Ap;
+  float* __restrict__ rlo = a.rlo;
   if (VEC) {
     const long long nv = N / 2;
     double2* x2 = reinterpret_cast<double2*>(x);
@@ -700,7 +883,9 @@ __global__ void __launch_bounds__(kThreads)
     r[k] = rv;
     if (rlo) rlo[k] = f64_to_f32(rv);
   }
-  grid_reduce(acc, rb, [&](double tot) {
+  double* norms = a.norms;
+  const int plain = a.plain;
+  grid_reduce_n(acc, a.rb, [&](double tot) {
     const int it = st->iter + 1;
     st->iter = it;
     st->rr = tot;
@@ -715,7 +900,33 @@ __global__ void __launch_bounds__(kThreads)
       st->done = kDoneConverged;
     else if (it >= st->maxiter)
       st->done = kDoneMaxIter;
-  });
+  }, cta, ncta);
+}
+
+template <bool VEC>
+__global__ void __launch_bounds__(kThreads) k_cg_update(const CgUpdateArgs a) {
+  pdl_begin();
+  cg_update_run<VEC>(a, blockIdx.x, gridDim.x);
+}
+
+// one problem per blockIdx.y
+template <bool VEC>
+__global__ void __launch_bounds__(kThreads)
+    k_cg_update_batch(const unsigned char* __restrict__ blobs, int stride) {
+  pdl_begin();
+  const CgUpdateArgs a =
+      *reinterpret_cast<const CgUpdateArgs*>(blobs + (size_t)blockIdx.y * (size_t)stride);
+  cg_update_run<VEC>(a, blockIdx.x, gridDim.x);
+}
+
+// BatchLaunchFn: aux[0] = CTAs per problem.
+template <bool VEC>
+cudaError_t launch_cg_update_batch(const unsigned char* blobs, int stride, int count,
+                                   const int* aux, const BatchScratch&, cudaStream_t s) {
+  if (count == 0) return cudaSuccess;
+  if (count > 65535) return cudaErrorInvalidValue;
+  return launch_pdl(k_cg_update_batch<VEC>, dim3(aux[0], count), dim3(kThreads), 0, s, blobs,
+                    stride);
 }
 
 static inline bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
@@ -1536,11 +1747,12 @@ cudaError_t launch_cg_update(Grid<T> x, Grid<T> r, Grid<const T> p, Grid<const T
   const bool vec = aligned16(x.p) && aligned16(r.p) && aligned16(p.p) && aligned16(Ap.p) &&
                    (!rlo.p || ((uintptr_t)rlo.p & 7u) == 0) && (ld % 2 == 0 || N % 2 == 0);
   const int g = flat_grid(N, vec ? 4 : 2);
-  if (vec)
-    return launch_pdl(k_cg_update<true>, dim3(g), dim3(kThreads), 0, s, x.p, r.p, p.p, Ap.p, rlo.p,
-                      N, plain, st, norms, rb);
-  return launch_pdl(k_cg_update<false>, dim3(g), dim3(kThreads), 0, s, x.p, r.p, p.p, Ap.p, rlo.p,
-                    N, plain, st, norms, rb);
+  const CgUpdateArgs a{x.p, r.p, p.p, Ap.p, rlo.p, N, plain, st, norms, rb};
+  if (recorder_slot())
+    return vec ? record_launch(&launch_cg_update_batch<true>, a, g)
+               : record_launch(&launch_cg_update_batch<false>, a, g);
+  if (vec) return launch_pdl(k_cg_update<true>, dim3(g), dim3(kThreads), 0, s, a);
+  return launch_pdl(k_cg_update<false>, dim3(g), dim3(kThreads), 0, s, a);
 }
 
 template <typename T, int FIELD, int EPI, bool TMA>
@@ -1771,19 +1983,34 @@ __host__ __device__ constexpr size_t fd_smem_bytes(int nc, bool stage) {
   return ((size_t)(2 + kFdSlices) * nc + (stage ? 2 * (size_t)nc * nc : 0)) * sizeof(double);
 }
 
+struct FdArgs {
+  const void* in;
+  int in_ld;
+  const double* C;
+  const double* M;
+  const double* dinv;
+  void* out;
+  int out_ld;
+  int nc;
+  const SolveState* st;
+};
+
+// Column j of one pass (one CTA).
 template <typename Tin, typename Tout, bool STAGE>
-__global__ void __launch_bounds__(kThreads)
-    k_coarse_fd(Grid<const Tin> in, const double* __restrict__ C, const double* __restrict__ M,
-                const double* __restrict__ dinv, Grid<Tout> out, int nc, const SolveState* st) {
-  pdl_begin();
-  if (st && st->done) return;
+__device__ __forceinline__ void fd_run(const FdArgs& a, int j) {
+  if (a.st && a.st->done) return;
+  const Grid<const Tin> in{static_cast<const Tin*>(a.in), a.in_ld};
+  const Grid<Tout> out{static_cast<Tout*>(a.out), a.out_ld};
+  const double* __restrict__ C = a.C;
+  const double* __restrict__ M = a.M;
+  const double* __restrict__ dinv = a.dinv;
+  const int nc = a.nc;
   extern __shared__ double fd_sm[];
   double* c = fd_sm;                  // nc
   double* sv = c + nc;                // nc
   double* part = sv + nc;             // kFdSlices * nc
   double* is = part + kFdSlices * nc; // STAGE: the input grid, nc * nc
   double* ms = is + nc * nc;          // STAGE: M, nc * nc
-  const int j = blockIdx.x;
   const int q = threadIdx.x >> 6, r = threadIdx.x & 63;
   for (int k = threadIdx.x; k < nc; k += kThreads) c[k] = C[(size_t)j * nc + k];
   if (STAGE) {
@@ -1819,22 +2046,53 @@ __global__ void __launch_bounds__(kThreads)
     out.at(i, j) = convert<Tout>(t);
   }
 }
+template <typename Tin, typename Tout, bool STAGE>
+__global__ void __launch_bounds__(kThreads) k_coarse_fd(const FdArgs a) {
+  pdl_begin();
+  fd_run<Tin, Tout, STAGE>(a, blockIdx.x);
+}
+
+template <typename Tin, typename Tout, bool STAGE>
+__global__ void __launch_bounds__(kThreads)
+    k_coarse_fd_batch(const unsigned char* __restrict__ blobs, int stride) {
+  pdl_begin();
+  const FdArgs a = *reinterpret_cast<const FdArgs*>(blobs + (size_t)blockIdx.y * (size_t)stride);
+  fd_run<Tin, Tout, STAGE>(a, blockIdx.x);
+}
+
+// BatchLaunchFn: aux[0] = nc.
+template <typename Tin, typename Tout, bool STAGE>
+cudaError_t launch_fd_batch(const unsigned char* blobs, int stride, int count, const int* aux,
+                            const BatchScratch&, cudaStream_t s) {
+  if (count == 0) return cudaSuccess;
+  return launch_pdl(k_coarse_fd_batch<Tin, Tout, STAGE>, dim3(aux[0], count), dim3(kThreads),
+                    fd_smem_bytes(aux[0], STAGE), s, blobs, stride);
+}
 static_assert(kFdSlices == 4, "the combine step sums four slices");
 
 template <typename Tin, typename Tout>
 cudaError_t launch_fd_pass(Grid<const Tin> in, const double* C, const double* M,
                            const double* dinv, Grid<Tout> out, int nc, const SolveState* st,
                            cudaStream_t s) {
-  if (nc <= kFdStageMaxN)
+  const FdArgs a{in.p, in.ld, C, M, dinv, out.p, out.ld, nc, st};
+  const bool stage = nc <= kFdStageMaxN;
+  if (recorder_slot())
+    return stage ? record_launch(&launch_fd_batch<Tin, Tout, true>, a, nc)
+                 : record_launch(&launch_fd_batch<Tin, Tout, false>, a, nc);
+  if (stage)
     return launch_pdl(k_coarse_fd<Tin, Tout, true>, dim3(nc), dim3(kThreads),
-                      fd_smem_bytes(nc, true), s, in, C, M, dinv, out, nc, st);
+                      fd_smem_bytes(nc, true), s, a);
   return launch_pdl(k_coarse_fd<Tin, Tout, false>, dim3(nc), dim3(kThreads),
-                    fd_smem_bytes(nc, false), s, in, C, M, dinv, out, nc, st);
+                    fd_smem_bytes(nc, false), s, a);
 }
 
 template <typename Tin, typename Tout>
 cudaError_t allow_fd_smem() {
-  return cudaFuncSetAttribute(k_coarse_fd<Tin, Tout, true>,
+  cudaError_t e = cudaFuncSetAttribute(k_coarse_fd<Tin, Tout, true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)fd_smem_bytes(kFdStageMaxN, true));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_coarse_fd_batch<Tin, Tout, true>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)fd_smem_bytes(kFdStageMaxN, true));
 }
@@ -1932,8 +2190,63 @@ __global__ void k_state_init(SolveState* st, int maxiter) {
   *st = z;
 }
 
+struct StateInitArgs {
+  SolveState* st;
+  int maxiter;
+};
+
+__global__ void k_state_init_batch(const unsigned char* __restrict__ blobs, int stride) {
+  pdl_begin();
+  const StateInitArgs a =
+      *reinterpret_cast<const StateInitArgs*>(blobs + (size_t)blockIdx.x * (size_t)stride);
+  SolveState z = {};
+  z.maxiter = a.maxiter;
+  *a.st = z;
+}
+
+cudaError_t launch_state_init_batch(const unsigned char* blobs, int stride, int count, const int*,
+                                    const BatchScratch&, cudaStream_t s) {
+  if (count == 0) return cudaSuccess;
+  return launch_pdl(k_state_init_batch, dim3(count), dim3(1), 0, s, blobs, stride);
+}
+
 cudaError_t launch_state_init(SolveState* st, int maxiter, cudaStream_t s) {
+  if (recorder_slot()) return record_launch(&launch_state_init_batch, StateInitArgs{st, maxiter}, 0);
   return launch_pdl(k_state_init, dim3(1), dim3(1), 0, s, st, maxiter);
+}
+
+// Grid copies between leading dimensions (the caller's layout <-> the
+// padded one): plain copies when launched alone, one kernel per batch.
+struct Copy2DArgs {
+  double* dst;
+  int dld;
+  const double* src;
+  int sld;
+  int n;
+};
+
+__global__ void __launch_bounds__(kThreads)
+    k_copy_grid_batch(const unsigned char* __restrict__ blobs, int stride) {
+  pdl_begin();
+  const Copy2DArgs a =
+      *reinterpret_cast<const Copy2DArgs*>(blobs + (size_t)blockIdx.y * (size_t)stride);
+  for (int j = blockIdx.x; j < a.n; j += gridDim.x)
+    for (int i = threadIdx.x; i < a.n; i += kThreads)
+      a.dst[(size_t)j * a.dld + i] = __ldg(a.src + (size_t)j * a.sld + i);
+}
+
+cudaError_t launch_copy_grid_batch(const unsigned char* blobs, int stride, int count,
+                                   const int* aux, const BatchScratch&, cudaStream_t s) {
+  if (count == 0) return cudaSuccess;
+  return launch_pdl(k_copy_grid_batch, dim3(std::min(aux[0], 1024), count), dim3(kThreads), 0, s,
+                    blobs, stride);
+}
+
+cudaError_t copy_grid(double* dst, int dld, const double* src, int sld, int n, cudaStream_t s) {
+  if (recorder_slot())
+    return record_launch(&launch_copy_grid_batch, Copy2DArgs{dst, dld, src, sld, n}, n);
+  return cudaMemcpy2DAsync(dst, (size_t)dld * sizeof(double), src, (size_t)sld * sizeof(double),
+                           (size_t)n * sizeof(double), n, cudaMemcpyDeviceToDevice, s);
 }
 
 // ---------------------------------------------------------------------------

@@ -361,13 +361,15 @@ __device__ __forceinline__ double block_sum(double v) {
   return tot;
 }
 
+// The reduction over the CTAs cta = 0 .. nb-1 that share `red` (a batched
+// launch reduces each problem over blockIdx.x alone).
 template <typename Fin>
-__device__ __forceinline__ void grid_reduce(double v, const ReduceBuf& red, Fin&& fin) {
+__device__ __forceinline__ void grid_reduce_n(double v, const ReduceBuf& red, Fin&& fin,
+                                              unsigned cta, unsigned nb) {
   __shared__ bool is_last;
   const double bs = block_sum(v);
-  const unsigned nb = gridDim.x * gridDim.y;
   if (threadIdx.x == 0) {
-    red.partials[blockIdx.y * gridDim.x + blockIdx.x] = bs;
+    red.partials[cta] = bs;
     __threadfence();
     const unsigned t = atomicAdd(red.ticket, 1u);
     is_last = (t == nb - 1);
@@ -382,6 +384,11 @@ __device__ __forceinline__ void grid_reduce(double v, const ReduceBuf& red, Fin&
     fin(total);
     *red.ticket = 0u;
   }
+}
+
+template <typename Fin>
+__device__ __forceinline__ void grid_reduce(double v, const ReduceBuf& red, Fin&& fin) {
+  grid_reduce_n(v, red, fin, blockIdx.y * gridDim.x + blockIdx.x, gridDim.x * gridDim.y);
 }
 
 __device__ __forceinline__ bool finite_d(double x) { return isfinite(x); }

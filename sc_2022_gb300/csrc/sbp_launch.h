@@ -4,6 +4,8 @@
 
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "sbp_common.cuh"
 #include "sbp_tma.h"
 
@@ -162,6 +164,44 @@ cudaError_t launch_rhs(Grid<const double> f, const double* gW, const double* gE,
 // lambda.b with respect to f and the four boundary vectors.
 cudaError_t launch_rhs_adjoint(Grid<const double> lam, Grid<double> df, double* dgW, double* dgE,
                                double* dgS, double* dgN, int n, double fsign, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// Launch recording for batched solves.  While a Recorder is installed on the
+// calling host thread, the solver's launchers (persistent jobs, the CG
+// update, the coarse-solve passes, the state initialisation and grid copies)
+// append a LaunchRecord instead of launching.  Records of several problems
+// that agree in `fn` and `aux` are launched together as one batched kernel:
+// fn(blobs, stride, count, aux, scratch, stream) with `count` argument blobs
+// (one per problem, `stride` bytes apart) in device memory.  count == 0 only
+// resolves the launch configuration (occupancy, shared-memory attribute);
+// do that once outside stream capture.
+// ---------------------------------------------------------------------------
+struct BatchScratch {
+  double* partials = nullptr;   // per-CTA, per-problem partial sums
+  unsigned* ticket = nullptr;   // zero between launches
+  long long cap = 0;            // doubles in partials
+};
+using BatchLaunchFn = cudaError_t (*)(const unsigned char* blobs, int stride, int count,
+                                      const int* aux, const BatchScratch& scr, cudaStream_t s);
+struct LaunchRecord {
+  BatchLaunchFn fn = nullptr;
+  int aux[4] = {0, 0, 0, 0};     // launch shape; equal within a batched group
+  int align = 16;                // alignment of the argument blob in device memory
+  std::vector<unsigned char> blob;
+};
+struct Recorder {
+  std::vector<LaunchRecord> recs;
+};
+// The calling thread's recorder (nullptr: launch normally).
+Recorder*& recorder_slot();
+// Most problems one batched launch can carry (per-CTA partials live in
+// shared memory).
+constexpr int kMaxBatchSlots = 512;
+// Largest grid of a persistent kernel (one wave: SMs x resident CTAs).
+constexpr int kMaxPersistCtas = 4096;
+
+// dst (ld dld) = src (ld sld) on an n x n FP64 grid; recordable.
+cudaError_t copy_grid(double* dst, int dld, const double* src, int sld, int n, cudaStream_t s);
 
 // g = H~ (u - ut) (g.p may be null) and *loss = 1/2 (u - ut)' H~ (u - ut)
 // (loss may be null); H~ = h^2 diag(w_i w_j).

@@ -136,3 +136,24 @@ def rhs_adjoint(lam: torch.Tensor):
                                          ptr(dg["S"]), ptr(dg["N"]), n, 1.0, _stream_ptr()),
             "sbp_rhs_adjoint_f64")
     return df, dg
+
+
+def batch_sizes(count: int, seed: int, sizes=(65, 129, 257, 513, 1025)):
+    """Grid sizes drawn log-uniformly from `sizes` (uniform over the list of
+    powers of two plus one) by the project's counter-based stream."""
+    st = Stream(seed)
+    u = st.uniform(count)
+    return [int(sizes[min(int(v * len(sizes)), len(sizes) - 1)]) for v in u]
+
+
+def batch_problems(count: int, seed: int, device="cuda"):
+    """The batched-solve configuration: `count` problems with sizes from
+    :func:`batch_sizes` and bump/trig data of :func:`bump_problem` (seed
+    seed * 1000 + k for problem k).  Returns (ns, bs) with bs the assembled
+    right-hand sides on `device`."""
+    ns = batch_sizes(count, seed)
+    bs = []
+    for k, n in enumerate(ns):
+        f, g = bump_problem(n, seed * 1000 + k)
+        bs.append(assemble_rhs(f, g, device=device).reshape(-1))
+    return ns, bs

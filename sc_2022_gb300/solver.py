@@ -236,3 +236,64 @@ class Solver:
         L.check(self._lib.sbp_vcycle_apply(self._h, ptr(b), ptr(v), _stream_ptr(stream)),
                 "sbp_vcycle_apply")
         return v
+
+
+class BatchSolver:
+    """Batched MGCG over independent problems of any grid sizes (one solver
+    per problem; the problems of one size share every kernel launch, sizes
+    run as parallel graph branches).  ``options`` as for :class:`Solver`."""
+
+    def __init__(self, ns, options: Options):
+        self.ns = [int(n) for n in ns]
+        lib = L.load()
+        h = C.c_void_p()
+        arr = (C.c_int * len(self.ns))(*self.ns)
+        oc = options.to_c()
+        L.check(lib.sbp_batch_create(C.byref(h), arr, len(self.ns), C.byref(oc)),
+                "sbp_batch_create")
+        self._h = h
+        self._lib = lib
+        self.options = options
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.sbp_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __len__(self):
+        return len(self.ns)
+
+    @property
+    def device_bytes(self) -> int:
+        return int(self._lib.sbp_batch_device_bytes(self._h))
+
+    @property
+    def last_launches(self) -> int:
+        return int(self._lib.sbp_batch_last_launches(self._h))
+
+    def mgcg(self, bs, xs, abstol: float = 0.0, reltol: float = 0.0, maxiter: int | None = None,
+             stream=None, raise_on_fail=False):
+        """MGCG on every problem: xs[k] (initial guesses) are overwritten.
+        Returns one SolveResult per problem (norm histories not kept)."""
+        if len(bs) != len(self.ns) or len(xs) != len(self.ns):
+            raise ValueError("one b and one x per problem")
+        for k, (b, x, n) in enumerate(zip(bs, xs, self.ns)):
+            if check_grid(b, name=f"b[{k}]") != n or check_grid(x, name=f"x[{k}]") != n:
+                raise ValueError(f"problem {k}: grid size differs from n={n}")
+        cnt = len(self.ns)
+        maxiter = max(n * n for n in self.ns) if maxiter is None else maxiter
+        bp = (C.c_void_p * cnt)(*[b.data_ptr() for b in bs])
+        xp = (C.c_void_p * cnt)(*[x.data_ptr() for x in xs])
+        res = (L.sbp_result * cnt)()
+        st = self._lib.sbp_batch_mgcg_solve(self._h, bp, xp, abstol, reltol, maxiter, res,
+                                             _stream_ptr(stream))
+        if st < 0 and (raise_on_fail or st not in (L.SBP_ERR_MAXITER, L.SBP_ERR_BREAKDOWN)):
+            L.check(st, "sbp_batch_mgcg_solve")
+        return [SolveResult(r.iters, r.status, [], r.initial_norm, r.final_norm, r.threshold)
+                for r in res]

@@ -1,0 +1,110 @@
+"""Batched MGCG: problems of mixed grid sizes solved together, against the
+same problems solved one at a time (and the oracle for one of them)."""
+import time
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import sbp_oracle as o
+
+pytestmark = pytest.mark.gpu
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.detach().cpu().numpy().ravel()
+
+
+def relerr(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def _sequential(sbp, ns, bs, opts, reltol):
+    solvers = {n: sbp.Solver(n, opts) for n in sorted(set(ns))}
+    xs, res = [], []
+    for n, b in zip(ns, bs):
+        x = torch.zeros_like(b)
+        res.append(solvers[n].mgcg(b, x, reltol=reltol, maxiter=100))
+        xs.append(x)
+    return xs, res, solvers
+
+
+def test_batch_matches_sequential(sbp):
+    from sc_2022_gb300 import problems
+    ns = [129, 65, 257, 129, 65, 257, 129, 513]
+    bs = []
+    for k, n in enumerate(ns):
+        f, g = problems.bump_problem(n, 50 + k)
+        bs.append(problems.assemble_rhs(f, g).reshape(-1))
+    opts = sbp.default_options()
+    B = sbp.BatchSolver(ns, opts)
+    xs = [torch.zeros_like(b) for b in bs]
+    rb = B.mgcg(bs, xs, reltol=1e-10, maxiter=100)
+    xq, rq, _ = _sequential(sbp, ns, bs, opts, 1e-10)
+    for k in range(len(ns)):
+        assert rb[k].converged and rq[k].converged
+        assert abs(rb[k].iters - rq[k].iters) <= 1
+        assert relerr(host(xs[k]), host(xq[k])) < 1e-8
+    # one problem against the oracle (V-cycle to 65^2, same stopping rule)
+    n, b = ns[2], bs[2]
+    hier = o.Hierarchy(n, o.MGOptions(coarse_n=65))
+    xr, itr, nr = o.mgcg(hier, host(b), reltol=1e-10)
+    assert rb[2].iters == itr
+    assert relerr(host(xs[2]), xr) < 1e-9
+    # a second solve reuses the captured graphs and starts from the caller's x
+    xs2 = [torch.zeros_like(b) for b in bs]
+    rb2 = B.mgcg(bs, xs2, reltol=1e-10, maxiter=100)
+    for k in range(len(ns)):
+        assert rb2[k].iters == rb[k].iters
+        assert torch.equal(xs2[k], xs[k])
+
+
+def test_batch_mixed_precision(sbp):
+    from sc_2022_gb300 import _lib, problems
+    ns, bs = problems.batch_problems(12, seed=9)
+    opts = sbp.default_options(_lib.SBP_PREC_MIXED)
+    B = sbp.BatchSolver(ns, opts)
+    xs = [torch.zeros_like(b) for b in bs]
+    rb = B.mgcg(bs, xs, reltol=1e-10, maxiter=100)
+    xq, rq, _ = _sequential(sbp, ns, bs, sbp.default_options(), 1e-10)
+    for k in range(len(ns)):
+        assert rb[k].converged
+        assert rb[k].iters <= rq[k].iters + 1
+        assert relerr(host(xs[k]), host(xq[k])) < 1e-8
+
+
+def test_batch_config_256_problems(sbp):
+    # 256 problems, N log-uniform over {65, ..., 1025} by seed, bump/trig data,
+    # FP64 MGCG to 1e-10: batched solve against 256 sequential solves
+    from sc_2022_gb300 import problems
+    ns, bs = problems.batch_problems(256, seed=4)
+    assert len(set(ns)) == 5
+    opts = sbp.default_options()
+    B = sbp.BatchSolver(ns, opts)
+    xs = [torch.zeros_like(b) for b in bs]
+    B.mgcg(bs, xs, reltol=1e-10, maxiter=100)          # warm-up: capture
+    for x in xs:
+        x.zero_()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rb = B.mgcg(bs, xs, reltol=1e-10, maxiter=100)
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+    xq, rq, solvers = _sequential(sbp, ns, bs, opts, 1e-10)   # warm-up (captures)
+    for x in xq:
+        x.zero_()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for n, b, x in zip(ns, bs, xq):
+        solvers[n].mgcg(b, x, reltol=1e-10, maxiter=100)
+    torch.cuda.synchronize()
+    t_seq = time.perf_counter() - t0
+    worst = 0.0
+    for k in range(len(ns)):
+        assert rb[k].converged
+        assert abs(rb[k].iters - rq[k].iters) <= 1
+        worst = max(worst, relerr(host(xs[k]), host(xq[k])))
+    print(f"256 problems: batched {1e3 * t_batch:.1f} ms, sequential {1e3 * t_seq:.1f} ms "
+          f"({t_seq / t_batch:.2f}x), launches {B.last_launches}, worst rel. diff {worst:.2e}")
+    assert worst < 1e-8

@@ -219,3 +219,35 @@ def test_deterministic(sbp):
         runs.append((res.norms, host(x)))
     assert runs[0][0] == runs[1][0]
     assert np.array_equal(runs[0][1], runs[1][1])
+
+
+def test_mixed_n8193_bump_against_fp64(sbp):
+    # N = 8193 (67M unknowns), random Gaussian-bump source and trig boundary
+    # data: FP32 V-cycle inside FP64 PCG to 1e-10, against the FP64 MGCG solve
+    # of the same problem (the FP64 path is itself held to the oracle at
+    # smaller N).
+    from sc_2022_gb300 import _lib, problems
+    n = 8193
+    f, g = problems.bump_problem(n, seed=3)
+    b = problems.assemble_rhs(f, g).reshape(-1)
+    del f
+    xs, its = {}, {}
+    for prec in (_lib.SBP_PREC_FP64, _lib.SBP_PREC_MIXED):
+        s = sbp.Solver(n, sbp.default_options(prec))
+        x = torch.zeros_like(b)
+        res = s.mgcg(b, x, reltol=1e-10)
+        assert res.converged
+        xs[prec], its[prec] = x, res.iters
+        s.close()
+    assert its[_lib.SBP_PREC_MIXED] <= its[_lib.SBP_PREC_FP64] + 1
+    import ctypes as C
+    lib = sbp.load_library()
+    out = C.c_double()
+    x32 = xs[_lib.SBP_PREC_MIXED]
+    assert lib.sbp_residual_norm_f64(C.c_void_p(x32.data_ptr()), C.c_void_p(b.data_ptr()), n, 1,
+                                     C.byref(out), None) == 0
+    assert out.value <= 2e-10 * b.norm().item()
+    err = ((x32 - xs[_lib.SBP_PREC_FP64]).norm() / xs[_lib.SBP_PREC_FP64].norm()).item()
+    print(f"N=8193 mixed vs FP64: iterations {its}, relative solution difference {err:.3e}, "
+          f"true relative residual {out.value / b.norm().item():.3e}")
+    assert err < 1e-8
