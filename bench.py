@@ -49,7 +49,8 @@ def parse_args():
     p.add_argument("--cpu-baseline", type=int, default=1, help="time the CPU baseline leg")
     p.add_argument("--dtype", choices=["f64", "f32"], default="f64",
                    help="operand type of --mode apply")
-    p.add_argument("--mode", choices=["full", "apply", "solve-fp64", "solve-mixed", "vcycle"],
+    p.add_argument("--mode", choices=["full", "apply", "solve-fp64", "solve-mixed", "vcycle",
+                                      "batch"],
                    default="full", help="profiling modes run one part only and print a "
                    "short line (not the benchmark line)")
     return p.parse_args()
@@ -416,6 +417,46 @@ def run_part(args):
         torch.cuda.synchronize()
         print(json.dumps({"mode": "apply", "dtype": args.dtype, "n": n,
                           "launches": args.warmup + args.steps}))
+        return
+    if args.mode == "batch":
+        # 256 problems, N log-uniform over {65..1025}, bump/trig data, FP64
+        # MGCG to 1e-10: batched vs one solve at a time
+        import time
+        ns, bs = problems.batch_problems(256, seed=4, device=dev)
+        opts = sbp.default_options()
+        B = sbp.BatchSolver(ns, opts)
+        xs = [torch.zeros_like(b) for b in bs]
+        budgets = B.autotune(bs, xs)
+        solvers = {m: sbp.Solver(m, opts) for m in sorted(set(ns))}
+
+        def batched():
+            for x in xs:
+                x.zero_()
+            return B.mgcg(bs, xs, reltol=1e-10, maxiter=200)
+
+        def sequential():
+            out = []
+            for m, b, x in zip(ns, bs, xs):
+                x.zero_()
+                out.append(solvers[m].mgcg(b, x, reltol=1e-10, maxiter=200))
+            return out
+
+        res = {}
+        for name, fn in (("batched", batched), ("sequential", sequential)):
+            for _ in range(args.warmup):
+                fn()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                r = fn()
+            torch.cuda.synchronize()
+            res[name + "_ms"] = round(1e3 * (time.perf_counter() - t0) / args.steps, 3)
+            res[name + "_iters"] = sum(x.iters for x in r)
+        res.update({"mode": "batch", "problems": len(ns),
+                    "sizes": {str(m): ns.count(m) for m in sorted(set(ns))},
+                    "speedup": round(res["sequential_ms"] / res["batched_ms"], 3),
+                    "launches_batched": B.last_launches, "cta_budgets": budgets})
+        print(json.dumps(res))
         return
     if args.mode == "vcycle":
         # time one V-cycle (mixed and FP64) for the default hierarchy at --n

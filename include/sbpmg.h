@@ -258,6 +258,17 @@ long long sbp_batch_device_bytes(const sbp_batch* b);
 /* Kernel launches of the last batched solve (batched launches, not per
  * problem). */
 long long sbp_batch_last_launches(const sbp_batch* b);
+/* Number of grid sizes (classes) of the batch; their sizes, largest first,
+ * into ns (cap entries, may be NULL). */
+int sbp_batch_classes(const sbp_batch* b, int* ns, int cap);
+/* Launch-shape autotuner: for every grid size, time three batch iterations
+ * after a fresh set-up on the given problems (xs are overwritten) with each
+ * candidate CTA budget of the batched persistent kernels (one full wave,
+ * 2 x SMs, 1 x SMs, SMs / 2) and keep the fastest; the iteration graphs are
+ * recaptured with the choice.  budgets (one per class, may be NULL) receives
+ * the chosen budget, 0 meaning one full wave. */
+int sbp_batch_autotune(sbp_batch* b, const double* const* bs, double* const* xs, int* budgets,
+                       void* stream);
 /* MGCG on A_k x_k = b_k for every problem k from the caller's x_k (device
  * pointers in the caller's layout, ld = n_k; host arrays of count pointers),
  * with the stopping rule of sbp_mgcg_solve applied per problem.  results

@@ -93,6 +93,8 @@ SIGNATURES = {
     "sbp_batch_last_launches": (C.c_longlong, [_vp]),
     "sbp_batch_mgcg_solve": (_i, [_vp, C.POINTER(_vp), C.POINTER(_vp), _d, _d, _i,
                                   C.POINTER(sbp_result), _vp]),
+    "sbp_batch_classes": (_i, [_vp, C.POINTER(_i), _i]),
+    "sbp_batch_autotune": (_i, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_i), _vp]),
 }
 
 _lib = None

@@ -855,6 +855,7 @@ struct sbp_batch {
   cudaStream_t cap = nullptr;
   long long launches_per_iter = 0;
   long long last_launches = 0;
+  std::vector<double*> captured_norms;  // norm buffers the iteration graphs write
 };
 
 namespace {
@@ -994,8 +995,18 @@ int batch_capture(sbp_batch* B, cudaStream_t q) {
     if (e3 != cudaSuccess) return fail_cuda(e3, "cudaGraphInstantiate");
   }
   B->launches_per_iter = per_iter;
+  B->captured_norms.clear();
+  for (const sbp_solver* s : B->solvers) B->captured_norms.push_back(s->norms);
   B->iter_valid = true;
   return SBP_OK;
+}
+
+// The iteration graphs stay valid while no solver's norm buffer was regrown.
+bool batch_graphs_current(const sbp_batch* B) {
+  if (!B->iter_valid || B->captured_norms.size() != B->solvers.size()) return false;
+  for (size_t k = 0; k < B->solvers.size(); ++k)
+    if (B->solvers[k]->norms != B->captured_norms[k]) return false;
+  return true;
 }
 
 int batch_destroy(sbp_batch* B) {
@@ -1096,6 +1107,86 @@ long long sbp_batch_device_bytes(const sbp_batch* B) {
 
 long long sbp_batch_last_launches(const sbp_batch* B) { return B ? B->last_launches : 0; }
 
+int sbp_batch_autotune(sbp_batch* B, const double* const* b, double* const* x, int* budgets,
+                       void* stream) {
+  if (!B || !b || !x) return SBP_ERR_ARGS;
+  cudaStream_t q = (cudaStream_t)stream;
+  SBP_CUDA(cudaSetDevice(B->device));
+  const int kIters = 3;
+  for (int k = 0; k < B->count; ++k) {
+    const int rc = krylov_prepare(B->solvers[k], 0, b[k], x[k], 0.0, 1e-30, kIters + 4);
+    if (rc) return rc;
+  }
+  if (!batch_graphs_current(B)) {
+    const int rc = batch_capture(B, q);
+    if (rc) return rc;
+  }
+  const int sms = batch_sm_count();
+  const int cands[4] = {0, 2 * sms, sms, sms / 2};
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  SBP_CUDA(cudaEventCreate(&t0));
+  SBP_CUDA(cudaEventCreate(&t1));
+  int rc = SBP_OK;
+  for (size_t ci = 0; ci < B->classes.size() && rc == SBP_OK; ++ci) {
+    BatchClass& c = B->classes[ci];
+    rc = batch_record(
+        B, c, c.setup,
+        [&](sbp_solver* s) {
+          const int k = (int)(s->st - B->states);
+          return enqueue_setup(s, 0, b[k], x[k], +1, 0.0, 1e-30, kIters + 4, nullptr);
+        },
+        q);
+    if (rc) break;
+    if (cudaError_t e = batch_prepare(c, c.setup); e != cudaSuccess) {
+      rc = fail_cuda(e, "autotune");
+      break;
+    }
+    float best = 0.f;
+    int best_budget = 0;
+    for (int cand : cands) {
+      c.scr.cta_budget = cand;
+      cudaError_t e = cudaEventRecord(c.fork, q);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(c.stream, c.fork, 0);
+      if (e == cudaSuccess) e = batch_launch(c, c.setup, c.stream);
+      if (e == cudaSuccess) e = cudaEventRecord(t0, c.stream);
+      for (int it = 0; it < kIters && e == cudaSuccess; ++it)
+        e = batch_launch(c, c.iter[it & 1], c.stream);
+      if (e == cudaSuccess) e = cudaEventRecord(t1, c.stream);
+      if (e == cudaSuccess) e = cudaEventSynchronize(t1);
+      float ms = 0.f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, t0, t1);
+      if (e != cudaSuccess) {
+        rc = fail_cuda(e, "autotune");
+        break;
+      }
+      if (best_budget == 0 && cand == 0) best = ms;
+      if (ms < best) {
+        best = ms;
+        best_budget = cand;
+      }
+    }
+    c.scr.cta_budget = best_budget;
+    if (budgets) budgets[ci] = best_budget;
+  }
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  if (rc) return rc;
+  SBP_CUDA(cudaStreamSynchronize(q));
+  if (read_device_fault() != 0u) {
+    g_last_error = "a kernel's bounded wait on an asynchronous copy gave up";
+    return SBP_ERR_CUDA;
+  }
+  B->iter_valid = false;  // recapture with the chosen launch shapes
+  return batch_capture(B, q);
+}
+
+int sbp_batch_classes(const sbp_batch* B, int* ns, int cap) {
+  if (!B) return SBP_ERR_ARGS;
+  const int cnt = (int)B->classes.size();
+  for (int c = 0; c < cnt && ns && c < cap; ++c) ns[c] = B->classes[c].n;
+  return cnt;
+}
+
 int sbp_batch_mgcg_solve(sbp_batch* B, const double* const* b, double* const* x, double abstol,
                          double reltol, int maxiter, sbp_result* results, void* stream) {
   if (!B || !b || !x) return SBP_ERR_ARGS;
@@ -1105,7 +1196,7 @@ int sbp_batch_mgcg_solve(sbp_batch* B, const double* const* b, double* const* x,
     const int rc = krylov_prepare(B->solvers[k], 0, b[k], x[k], abstol, reltol, maxiter);
     if (rc) return rc;
   }
-  if (!B->iter_valid) {
+  if (!batch_graphs_current(B)) {
     const int rc = batch_capture(B, q);
     if (rc) return rc;
   }

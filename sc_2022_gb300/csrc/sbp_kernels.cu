@@ -437,7 +437,8 @@ static int batch_ctas_per_sm() {
 template <class Job>
 cudaError_t launch_persist_batch(const unsigned char* blobs, int stride, int count, const int* aux,
                                  const BatchScratch& scr, cudaStream_t s) {
-  const int cap = std::min(kMaxPersistCtas, sm_count() * batch_ctas_per_sm<Job>());
+  int cap = std::min(kMaxPersistCtas, sm_count() * batch_ctas_per_sm<Job>());
+  if (scr.cta_budget > 0) cap = std::min(cap, scr.cta_budget);
   if (count == 0) return cudaGetLastError();
   if (count > kMaxBatchSlots || stride % alignof(Job) != 0) return cudaErrorInvalidValue;
   const long long total = (long long)count * aux[0];
@@ -447,6 +448,8 @@ cudaError_t launch_persist_batch(const unsigned char* blobs, int stride, int cou
   return launch_pdl(k_persist_batch<Job>, dim3(grid), dim3(kThreads), batch_smem_bytes<Job>(), s,
                     blobs, stride, count, aux[0], scr.partials, scr.ticket);
 }
+
+int batch_sm_count() { return sm_count(); }
 
 Recorder*& recorder_slot() {
   static thread_local Recorder* r = nullptr;

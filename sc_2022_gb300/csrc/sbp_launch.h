@@ -180,6 +180,7 @@ struct BatchScratch {
   double* partials = nullptr;   // per-CTA, per-problem partial sums
   unsigned* ticket = nullptr;   // zero between launches
   long long cap = 0;            // doubles in partials
+  int cta_budget = 0;           // most CTAs of a batched persistent launch (0: one full wave)
 };
 using BatchLaunchFn = cudaError_t (*)(const unsigned char* blobs, int stride, int count,
                                       const int* aux, const BatchScratch& scr, cudaStream_t s);
@@ -199,6 +200,9 @@ Recorder*& recorder_slot();
 constexpr int kMaxBatchSlots = 512;
 // Largest grid of a persistent kernel (one wave: SMs x resident CTAs).
 constexpr int kMaxPersistCtas = 4096;
+
+// Streaming multiprocessors of the current device.
+int batch_sm_count();
 
 // dst (ld dld) = src (ld sld) on an n x n FP64 grid; recordable.
 cudaError_t copy_grid(double* dst, int dld, const double* src, int sld, int n, cudaStream_t s);

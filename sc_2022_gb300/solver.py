@@ -277,6 +277,26 @@ class BatchSolver:
     def last_launches(self) -> int:
         return int(self._lib.sbp_batch_last_launches(self._h))
 
+    @property
+    def classes(self) -> list:
+        cnt = self._lib.sbp_batch_classes(self._h, None, 0)
+        arr = (C.c_int * max(cnt, 1))()
+        self._lib.sbp_batch_classes(self._h, arr, cnt)
+        return list(arr[:cnt])
+
+    def autotune(self, bs, xs, stream=None) -> dict:
+        """Choose each grid size's CTA budget by timing a few iterations on
+        these problems (xs are overwritten).  Returns {n: budget} (0 = one
+        full wave)."""
+        cnt = len(self.ns)
+        bp = (C.c_void_p * cnt)(*[b.data_ptr() for b in bs])
+        xp = (C.c_void_p * cnt)(*[x.data_ptr() for x in xs])
+        cls = self.classes
+        out = (C.c_int * len(cls))()
+        L.check(self._lib.sbp_batch_autotune(self._h, bp, xp, out, _stream_ptr(stream)),
+                "sbp_batch_autotune")
+        return dict(zip(cls, list(out)))
+
     def mgcg(self, bs, xs, abstol: float = 0.0, reltol: float = 0.0, maxiter: int | None = None,
              stream=None, raise_on_fail=False):
         """MGCG on every problem: xs[k] (initial guesses) are overwritten.

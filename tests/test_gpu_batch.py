@@ -83,7 +83,9 @@ def test_batch_config_256_problems(sbp):
     opts = sbp.default_options()
     B = sbp.BatchSolver(ns, opts)
     xs = [torch.zeros_like(b) for b in bs]
-    B.mgcg(bs, xs, reltol=1e-10, maxiter=100)          # warm-up: capture
+    budgets = B.autotune(bs, xs)                     # per-size launch shapes
+    assert sorted(budgets) == sorted(set(ns))
+    B.mgcg(bs, xs, reltol=1e-10, maxiter=100)          # warm-up
     for x in xs:
         x.zero_()
     torch.cuda.synchronize()
@@ -106,5 +108,27 @@ def test_batch_config_256_problems(sbp):
         assert abs(rb[k].iters - rq[k].iters) <= 1
         worst = max(worst, relerr(host(xs[k]), host(xq[k])))
     print(f"256 problems: batched {1e3 * t_batch:.1f} ms, sequential {1e3 * t_seq:.1f} ms "
-          f"({t_seq / t_batch:.2f}x), launches {B.last_launches}, worst rel. diff {worst:.2e}")
+          f"({t_seq / t_batch:.2f}x), launches {B.last_launches}, worst rel. diff {worst:.2e}, "
+          f"CTA budgets {budgets}")
     assert worst < 1e-8
+
+
+def test_batch_maxiter_then_larger_maxiter(sbp):
+    # a first solve stopped by maxiter, then a solve with a larger maxiter
+    # (the per-problem norm buffers grow; the batch recaptures its graphs)
+    from sc_2022_gb300 import _lib, problems
+    ns, bs = problems.batch_problems(6, seed=21)
+    B = sbp.BatchSolver(ns, sbp.default_options())
+    xs = [torch.zeros_like(b) for b in bs]
+    r1 = B.mgcg(bs, xs, reltol=1e-10, maxiter=2)
+    for n, r in zip(ns, r1):
+        if n == 65:   # one level: the V-cycle is the exact coarse solve
+            assert r.converged and r.iters == 1
+        else:
+            assert r.status == _lib.SBP_ERR_MAXITER and r.iters == 2
+    xs = [torch.zeros_like(b) for b in bs]
+    r2 = B.mgcg(bs, xs, reltol=1e-10, maxiter=500)
+    xq, rq, _ = _sequential(sbp, ns, bs, sbp.default_options(), 1e-10)
+    for k in range(len(ns)):
+        assert r2[k].converged and abs(r2[k].iters - rq[k].iters) <= 1
+        assert relerr(host(xs[k]), host(xq[k])) < 1e-8
