@@ -143,6 +143,17 @@ __device__ __forceinline__ void stage_box(T* s, const DevOperand<T>& op, const C
   } else {
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
+    if (x0 >= 0 && y0 >= 0 && x0 + BW <= n && y0 + BH <= n) {
+      // the box lies inside the array: no bounds checks, pointer increments
+      for (int c = w; c < BH; c += kWarps) {
+        const T* src = op.p + (size_t)(y0 + c) * (size_t)op.ld + (x0 + lane);
+        T* dst = s + c * BW + lane;
+#pragma unroll
+        for (int r = 0; r < BW; r += 32)
+          if (r + lane < BW) cp_async_elem(dst + r, src + r);
+      }
+      return;
+    }
     for (int c = w; c < BH; c += kWarps) {
       const int j = y0 + c;
       const bool jok = (j >= 0 && j < n);
@@ -503,6 +514,10 @@ struct NoCtx {};
 // ---------------------------------------------------------------------------
 // Operator apply: out = sign * A u, optional fused dot u.out.
 // ---------------------------------------------------------------------------
+// Thread groups (64 threads each, 4 per CTA) of the FP64 apply that use FP64
+// instructions for the interior stencil; the rest use the integer pipe.
+constexpr int kFp64Groups = 2;
+
 template <typename T, bool DOT, bool TMA>
 struct ApplyJob {
   static constexpr int kStage = align128(box_bytes<T, BI, BJ>());
@@ -527,9 +542,20 @@ struct ApplyJob {
     const TileBoxes bx(id % ntx, t.j_lo);
     const T* s = reinterpret_cast<const T*>(buf);
     if (tile_interior(t, n)) {
+      // FP64: thread groups g >= kFp64Groups form the sum on the integer pipe
+      // (exact_stencil5), the others with FP64 instructions, so both pipes
+      // are busy; FP32: the FP32 pipe.
+      const bool exact = sizeof(T) == 8 && (threadIdx.x >> 6) >= kFp64Groups;
       visit_interior(s, t, [&](int i, int j, T um, T u0, T up, T uw, T ue, int) {
-        const T sum = (uw + ue) + (um + up);
-        const T v = sign > 0 ? fma(T(4), u0, -sum) : fma(T(-4), u0, sum);
+        T v;
+        double sx;
+        if (exact && exact_stencil5((double)u0, (double)uw, (double)ue, (double)um, (double)up,
+                                    sx)) {
+          v = (T)(sign > 0 ? -sx : sx);
+        } else {
+          const T sum = (uw + ue) + (um + up);
+          v = sign > 0 ? fma(T(4), u0, -sum) : fma(T(-4), u0, sum);
+        }
         out.at(i, j) = v;
         if (DOT) acc.add_prod(u0, v);
       });

@@ -211,6 +211,77 @@ template <>
 __device__ __forceinline__ float convert<float, double>(double v) { return f64_to_f32(v); }
 
 // ---------------------------------------------------------------------------
+// The 5-point sum S = (w + e + m + p) - 4c of FP64 values on the integer pipe.
+// Every operand's 53-bit significand is aligned to the largest exponent in a
+// signed 64-bit integer with 7 guard bits (|sum| < 5 * 2^60), the five terms
+// are added exactly, and the sum is rounded once to nearest-even.  Bits
+// shifted out during alignment are dropped (each term rounds toward -inf:
+// error below 5 units of 2^-7 ulp of the largest term; the FP64 evaluation
+// order errs by up to ~2 ulp of it).
+// GB300 issues about 2 FP64 lanes per clock per SM but 64x more integer
+// lanes, so this keeps FP64 stencils off the FP64 pipe.  Returns false (and
+// leaves s unset) for Inf/NaN operands or a result outside the normal range;
+// the caller then uses FP64 arithmetic.
+// ---------------------------------------------------------------------------
+struct ExactTerm {
+  long long v;   // signed significand, aligned later
+  int e;         // effective biased exponent (>= 1)
+};
+__device__ __forceinline__ bool exact_term(double x, int escale, ExactTerm& t) {
+  const unsigned hi = (unsigned)__double2hiint(x);
+  const unsigned lo = (unsigned)__double2loint(x);
+  const int ex = (int)((hi >> 20) & 0x7FFu);
+  const unsigned long long m =
+      ((unsigned long long)((hi & 0xFFFFFu) | (ex ? 0x100000u : 0u)) << 32) | lo;
+  t.v = (hi >> 31) ? -(long long)(m << 7) : (long long)(m << 7);
+  t.e = (ex ? ex : 1) + escale;
+  return ex != 0x7FF;
+}
+__device__ __forceinline__ long long exact_align(const ExactTerm& t, int E) {
+  const int d = E - t.e;
+  return d >= 63 ? 0LL : (t.v >> d);   // arithmetic shift: rounds toward -inf
+}
+__device__ __forceinline__ bool exact_stencil5(double c, double w, double e, double m, double p,
+                                               double& s) {
+  ExactTerm tc, tw, te, tm, tp;
+  bool ok = exact_term(c, 2, tc);   // 4 c: exponent + 2, exact
+  ok &= exact_term(w, 0, tw);
+  ok &= exact_term(e, 0, te);
+  ok &= exact_term(m, 0, tm);
+  ok &= exact_term(p, 0, tp);
+  const int E = max(max(max(tw.e, te.e), max(tm.e, tp.e)), tc.e);
+  const long long S = (exact_align(tw, E) + exact_align(te, E)) +
+                      (exact_align(tm, E) + exact_align(tp, E)) - exact_align(tc, E);
+  // value = S * 2^(E - 1082); round |S| to 53 bits
+  const unsigned long long a = S < 0 ? (unsigned long long)(-S) : (unsigned long long)S;
+  if (a == 0ULL) {
+    s = 0.0;
+    return ok;
+  }
+  const int msb = 63 - __clzll((long long)a);
+  int k = msb - 52;
+  unsigned long long mm;
+  if (k > 0) {
+    mm = a >> k;
+    const unsigned long long rem = a & ((1ULL << k) - 1ULL);
+    const unsigned long long half = 1ULL << (k - 1);
+    if (rem > half || (rem == half && (mm & 1ULL))) ++mm;
+    if (mm >> 53) {
+      mm >>= 1;
+      ++k;
+    }
+  } else {
+    mm = a << (-k);
+  }
+  const int be = k + E - 7;
+  if (be <= 0 || be >= 0x7FF) return false;
+  const unsigned hi = (S < 0 ? 0x80000000u : 0u) | ((unsigned)be << 20) |
+                      ((unsigned)(mm >> 32) & 0xFFFFFu);
+  s = __hiloint2double((int)hi, (int)(unsigned)mm);
+  return ok;
+}
+
+// ---------------------------------------------------------------------------
 // Error-free FP32 arithmetic.  two_sum gives s + e == a + b exactly (Knuth).
 // stencil_ff returns the 5-point stencil (uw + ue) + (um + up) - 4 u0 of FP32
 // values as an unevaluated float pair hi + lo whose error is below 2^-45 of

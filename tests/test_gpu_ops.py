@@ -194,3 +194,43 @@ def test_residual_norm(sbp):
                                      C.byref(out), None) == 0
     ref = np.linalg.norm(b - a.A @ x)
     assert abs(out.value - ref) <= 1e-12 * ref
+
+
+@pytest.mark.parametrize("field", ["wide", "smooth"])
+def test_apply_f64_exact_integer_path(sbp, field):
+    # Interior points of the FP64 apply are summed either on the integer pipe
+    # (thread groups 2..3 of a tile: tile columns j - j_lo >= 16) or with FP64
+    # instructions (groups 0..1).  Against the exact rational value of
+    # (w + e + m + p) - 4c: the integer path is within 1 ulp of the result
+    # plus 0.05 ulp of the largest term, the FP64 path within 3 ulp of it.
+    import math
+    from fractions import Fraction
+    n = 257
+    rng = np.random.default_rng(17)
+    if field == "wide":
+        u = rng.standard_normal(n * n) * 10.0 ** rng.uniform(-5, 5, n * n)
+    else:
+        x = np.linspace(0, 1, n)
+        u = (np.sin(3 * x)[None, :] * np.cos(2 * x)[:, None]).ravel() + 1e-3 * rng.random(n * n)
+    U = u.reshape(n, n)                      # U[j, i]
+    out = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    lib = sbp.load_library()
+    assert lib.sbp_apply_f64(C.c_void_p(dev(u).data_ptr()), C.c_void_p(out.data_ptr()), n, -1,
+                             None) == 0
+    got = host(out).reshape(n, n)
+    checked = {0: 0, 1: 0}
+    for _ in range(3000):
+        i = int(rng.integers(66, 192))       # interior tiles only (tile rows 65..192)
+        j = int(rng.integers(33, 224))       # tile columns 33..224
+        c, w, e, m, p = U[j, i], U[j, i - 1], U[j, i + 1], U[j - 1, i], U[j + 1, i]
+        exact = (Fraction(w) + Fraction(e) + Fraction(m) + Fraction(p)) - 4 * Fraction(c)
+        ref = float(exact)
+        big = max(abs(4 * c), abs(w), abs(e), abs(m), abs(p))
+        err = abs(float(Fraction(got[j, i]) - exact))
+        integer_path = ((j - 1) % 32) >= 16
+        if integer_path:
+            assert err <= math.ulp(ref) + 0.05 * math.ulp(big), (i, j, err)
+        else:
+            assert err <= 3 * math.ulp(big), (i, j, err)
+        checked[int(integer_path)] += 1
+    assert checked[0] > 100 and checked[1] > 100
