@@ -32,7 +32,7 @@ sys.path.insert(0, ROOT)
 METRIC = "MGCG time to 1e-10 rel. residual at N=4097²: mixed vs FP64; apply GB/s vs HBM"
 # DRAM bytes (read + write) of one sbp_apply_f64 launch at N = 4097, measured
 # with ncu (dram__bytes_read.sum + dram__bytes_write.sum).
-APPLY_F64_TRAFFIC = 220.2e6
+APPLY_F64_TRAFFIC = 222.6e6
 WORKLOAD = ("plain/mixed matrix-free MGCG, N=4097 (16.8M unknowns), u=sin(pi x)cos(pi y), "
             "V-cycle to 65^2, weighted Jacobi 2/3 3+3, SBP-compatible restriction, "
             "bilinear prolongation, FP64 direct coarse solve, tol 1e-10")

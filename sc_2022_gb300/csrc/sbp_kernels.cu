@@ -42,7 +42,6 @@ constexpr int RTI = 32;
 constexpr int RTJ = 16;
 
 // Coarse dense solve: rows of Ainv per warp.
-constexpr int kGemvRowsPerWarp = 2;
 // Flat (pointwise) kernels: CTAs per launch cap.
 constexpr int kFlatCtas = 1216;
 // Upper bound on the CTAs of a persistent launch (SMs x resident CTAs).
@@ -1709,10 +1708,104 @@ cudaError_t launch_apply_op(const Operand& u, Grid<T> out, int n, int sign, Redu
 #undef SBP_APPLY
 }
 
+// Operator apply on any layout (the caller's arrays, ld = n) without
+// shared-memory staging: a CTA takes a block of 256 rows and a run of
+// kApplyCols columns, each thread one row, marching down the columns with
+// the j-1 / j / j+1 values in registers; the i-1 / i+1 neighbours are the
+// neighbouring threads' values and come from L1.  DRAM traffic is one read
+// and one write per point (plus the run's two halo columns).  FP64: odd warps
+// form interior sums on the integer pipe (exact_stencil5), even warps with
+// FP64 instructions.
+constexpr int kApplyCols = 32;
+// columns whose loads are issued together (FP64 keeps fewer in registers)
+template <typename T>
+__host__ __device__ constexpr int apply_chunk() { return sizeof(T) == 8 ? 4 : 8; }
+static_assert(kApplyCols % 8 == 0 && kApplyCols % 4 == 0, "column runs are whole chunks");
+
+template <typename T, bool DOT>
+__global__ void __launch_bounds__(kThreads)
+    k_apply_direct(Grid<const T> u, Grid<T> out, int n, int sign, ReduceBuf rb, double* dot_out) {
+  pdl_begin();
+  constexpr int kApplyChunk = apply_chunk<T>();
+  const int nrb = (n + kThreads - 1) / kThreads;
+  const int items = nrb * ((n + kApplyCols - 1) / kApplyCols);
+  const bool exact = sizeof(T) == 8 && ((threadIdx.x >> 5) & 1);
+  const size_t ld = (size_t)u.ld;
+  DotAcc<T> acc;
+  for (int w = blockIdx.x; w < items; w += gridDim.x) {
+    const int i = (w % nrb) * kThreads + threadIdx.x;
+    if (i >= n) continue;
+    const int j0 = (w / nrb) * kApplyCols;
+    const int j1 = min(n, j0 + kApplyCols);
+    const T* col = u.p + (size_t)j0 * ld + i;
+    const bool irow = (i > 0 && i < n - 1);
+    T um = j0 > 0 ? __ldg(col - ld) : T(0);
+    T u0 = __ldg(col);
+    // chunks of kApplyChunk columns: all their loads are issued first, so a
+    // warp keeps several DRAM lines in flight
+    for (int jc = j0; jc < j1; jc += kApplyChunk, col += kApplyChunk * ld) {
+      T cu[kApplyChunk + 2], cw[kApplyChunk], ce[kApplyChunk];
+      cu[0] = um;
+      cu[1] = u0;
+#pragma unroll
+      for (int q = 0; q < kApplyChunk; ++q) {
+        const int j = jc + q;
+        cu[q + 2] = (j + 1 < n) ? __ldg(col + (size_t)(q + 1) * ld) : T(0);
+        if (j < j1 && irow) {
+          cw[q] = __ldg(col + (size_t)q * ld - 1);
+          ce[q] = __ldg(col + (size_t)q * ld + 1);
+        } else {
+          cw[q] = ce[q] = T(0);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < kApplyChunk; ++q) {
+        const int j = jc + q;
+        if (j >= j1) break;
+        const T cm = cu[q], c0 = cu[q + 1], cp = cu[q + 2];
+        T v;
+        if (irow && j > 2 && j < n - 3) {
+          double sx;
+          if (exact && exact_stencil5((double)c0, (double)cw[q], (double)ce[q], (double)cm,
+                                      (double)cp, sx)) {
+            v = (T)(sign > 0 ? -sx : sx);
+          } else {
+            const T sum = (cw[q] + ce[q]) + (cm + cp);
+            v = sign > 0 ? fma(T(4), c0, -sum) : fma(T(-4), c0, sum);
+          }
+        } else {
+          // SAT rows and columns: negA reads only in-domain neighbours
+          struct G {
+            const T* p;
+            size_t ld;
+            __device__ T operator()(int di, int dj) const {
+              return __ldg(p + (ptrdiff_t)dj * (ptrdiff_t)ld + di);
+            }
+          } g{col + (size_t)q * ld, ld};
+          const T na = negA<T>(g, i, j, n);
+          v = sign > 0 ? -na : na;
+        }
+        out.at(i, j) = v;
+        if (DOT) acc.add_prod(c0, v);
+      }
+      um = cu[kApplyChunk];
+      u0 = cu[kApplyChunk + 1];
+    }
+  }
+  if (DOT) grid_reduce(acc.value(), rb, [&](double tot) { *dot_out = tot; });
+}
+
 template <typename T>
 cudaError_t launch_apply(Grid<const T> u, Grid<T> out, int n, int sign, ReduceBuf rb,
                          double* dot_out, cudaStream_t s) {
-  return launch_apply_op<T>(raw_operand(u.p, n, u.ld), out, n, sign, rb, dot_out, s);
+  const long long items = (long long)((n + kThreads - 1) / kThreads) *
+                          ((n + kApplyCols - 1) / kApplyCols);
+  const int grid = (int)std::min<long long>(items, kMaxPersistCtas);
+  if (dot_out)
+    return launch_pdl(k_apply_direct<T, true>, dim3(grid), dim3(kThreads), 0, s, u, out, n, sign,
+                      rb, dot_out);
+  return launch_pdl(k_apply_direct<T, false>, dim3(grid), dim3(kThreads), 0, s, u, out, n, sign,
+                    rb, dot_out);
 }
 
 template <typename T>

@@ -198,9 +198,9 @@ def test_residual_norm(sbp):
 
 @pytest.mark.parametrize("field", ["wide", "smooth"])
 def test_apply_f64_exact_integer_path(sbp, field):
-    # Interior points of the FP64 apply are summed either on the integer pipe
-    # (thread groups 2..3 of a tile: tile columns j - j_lo >= 16) or with FP64
-    # instructions (groups 0..1).  Against the exact rational value of
+    # Interior points of the FP64 apply on the caller's layout are summed
+    # either on the integer pipe (odd warps: rows with (i mod 256) // 32 odd)
+    # or with FP64 instructions (even warps).  Against the exact rational value of
     # (w + e + m + p) - 4c: the integer path is within 1 ulp of the result
     # plus 0.05 ulp of the largest term, the FP64 path within 3 ulp of it.
     import math
@@ -220,14 +220,14 @@ def test_apply_f64_exact_integer_path(sbp, field):
     got = host(out).reshape(n, n)
     checked = {0: 0, 1: 0}
     for _ in range(3000):
-        i = int(rng.integers(66, 192))       # interior tiles only (tile rows 65..192)
-        j = int(rng.integers(33, 224))       # tile columns 33..224
+        i = int(rng.integers(1, n - 1))
+        j = int(rng.integers(3, n - 3))
         c, w, e, m, p = U[j, i], U[j, i - 1], U[j, i + 1], U[j - 1, i], U[j + 1, i]
         exact = (Fraction(w) + Fraction(e) + Fraction(m) + Fraction(p)) - 4 * Fraction(c)
         ref = float(exact)
         big = max(abs(4 * c), abs(w), abs(e), abs(m), abs(p))
         err = abs(float(Fraction(got[j, i]) - exact))
-        integer_path = ((j - 1) % 32) >= 16
+        integer_path = ((i % 256) // 32) % 2 == 1
         if integer_path:
             assert err <= math.ulp(ref) + 0.05 * math.ulp(big), (i, j, err)
         else:
