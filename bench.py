@@ -50,7 +50,7 @@ def parse_args():
     p.add_argument("--dtype", choices=["f64", "f32"], default="f64",
                    help="operand type of --mode apply")
     p.add_argument("--mode", choices=["full", "apply", "solve-fp64", "solve-mixed", "vcycle",
-                                      "batch"],
+                                      "batch", "spmv"],
                    default="full", help="profiling modes run one part only and print a "
                    "short line (not the benchmark line)")
     return p.parse_args()
@@ -417,6 +417,41 @@ def run_part(args):
         torch.cuda.synchronize()
         print(json.dumps({"mode": "apply", "dtype": args.dtype, "n": n,
                           "launches": args.warmup + args.steps}))
+        return
+    if args.mode == "spmv":
+        # the reference's matrix-free vs assembled-SpMV comparison at --n:
+        # FP64 y = A x with this project's CSR SpMV and with the matrix-free apply
+        from sc_2022_gb300 import csr
+        A = csr.CsrOperator(n, device=dev)
+        gen = torch.Generator(device=dev).manual_seed(0)
+        xs = [torch.randn(n * n, generator=gen, device=dev, dtype=torch.float64) for _ in range(2)]
+        ys = [torch.empty_like(xs[0]) for _ in range(2)]
+        out = {"mode": "spmv", "n": n, "nnz": A.nnz}
+
+        def run_spmv(k):
+            A.matvec(xs[k % 2], ys[k % 2])
+
+        def run_mf(k):
+            assert lib.sbp_apply_f64(C.c_void_p(xs[k % 2].data_ptr()),
+                                     C.c_void_p(ys[k % 2].data_ptr()), n, 1, sp) == 0
+
+        for name, fn, nbytes in (("spmv", run_spmv, A.device_bytes + 16 * n * n),
+                                 ("matrix_free", run_mf, 16 * n * n)):
+            for k in range(args.warmup):
+                fn(k)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for k in range(args.steps):
+                fn(k)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / args.steps
+            out[name + "_us"] = round(1e3 * ms, 2)
+            out[name + "_gbs"] = round(nbytes / (ms * 1e-3) / 1e9, 1)
+        out["matrix_free_speedup"] = round(out["spmv_us"] / out["matrix_free_us"], 3)
+        print(json.dumps(out))
         return
     if args.mode == "batch":
         # 256 problems, N log-uniform over {65..1025}, bump/trig data, FP64

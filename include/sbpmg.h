@@ -185,6 +185,20 @@ int sbp_rhs_adjoint_f64(const double* lam, double* df, double* dgW, double* dgE,
 int sbp_h_misfit_f64(const double* u, const double* ut, double* g, int n, double* loss,
                      void* stream);
 
+/* ---- assembled-operator comparator ------------------------------------ */
+
+/* The reference compares its matrix-free apply with SpMV on the assembled
+ * matrix (Poisson_CG.jl:217, 244-271; kernel_comparisons/SPMV_test.jl).
+ * sbp_csr_assemble_host writes A (SPD, = -H~(D2 + SAT) of Assembling_matrix)
+ * on n x n points as CSR into host arrays: row_ptr (n^2 + 1 entries), col
+ * and val (cap entries, increasing columns per row; rows and columns are
+ * j * n + i).  With NULL arrays it only reports *nnz.  Needs no GPU. */
+int sbp_csr_assemble_host(int n, long long* row_ptr, int* col, double* val, long long cap,
+                          long long* nnz);
+/* y = A x for a CSR matrix in device memory (row pointers as 64-bit ints). */
+int sbp_csr_spmv_f64(long long nrows, const long long* row_ptr, const int* col,
+                     const double* val, const double* x, double* y, void* stream);
+
 /* ---- solver handle ---------------------------------------------------- */
 
 /* Create a solver for n x n grids on the current device.  opts == NULL

@@ -592,3 +592,38 @@ def misfit_loss_grad(asm: Assembled, f_ref, g: dict, ut):
     df = -hl
     dg = {s: -(asm.sat_r[s].T @ hl) for s in ("W", "E", "S", "N")}
     return loss, df, dg, u, lam
+
+
+def cg_tolerance(A, b, x0, abstol):
+    """IterativeSolvers.jl ``cg!`` stopping threshold used by the reference's
+    nested iteration: max(reltol * |b - A x0|, abstol), reltol = sqrt(eps)."""
+    r0 = float(np.linalg.norm(np.asarray(b) - A @ np.asarray(x0)))
+    return max(math.sqrt(np.finfo(float).eps) * r0, abstol)
+
+
+def nested_cg(n: int, b, b_2h, abstol: float):
+    """``initial_guess_interpolation_CG`` (``matrix_free_mg_cg.jl:372-377``):
+    exact solve of the coarse problem A_2h x_2h = b_2h (its own right-hand
+    side), bilinear prolongation of x_2h as the initial guess, CG on A x = b.
+    Returns (x, iters, norms)."""
+    nc = (n + 1) // 2
+    A = assemble(n).A
+    x2h = spla.splu(assemble(nc).A.tocsc()).solve(np.asarray(b_2h, dtype=np.float64))
+    x0 = prolongation_2d(nc) @ x2h
+    return cg(A, b, x0, abstol=cg_tolerance(A, b, x0, abstol))
+
+
+def nested_cg_three_level(n: int, b, b_2h, b_4h, abstol: float):
+    """``initial_guess_interpolation_three_level_CG_GPU``
+    (``matrix_free_mg_cg.jl:386-396``): exact solve on 4h, prolong, CG on 2h,
+    prolong, CG on h.  Returns (x, iters_2h, iters_h, norms_2h, norms_h)."""
+    n2 = (n + 1) // 2
+    n4 = (n2 + 1) // 2
+    A2 = assemble(n2).A
+    A = assemble(n).A
+    x4 = spla.splu(assemble(n4).A.tocsc()).solve(np.asarray(b_4h, dtype=np.float64))
+    x2_0 = prolongation_2d(n4) @ x4
+    x2, it2, nr2 = cg(A2, b_2h, x2_0, abstol=cg_tolerance(A2, b_2h, x2_0, abstol))
+    x0 = prolongation_2d(n2) @ x2
+    x, it, nr = cg(A, b, x0, abstol=cg_tolerance(A, b, x0, abstol))
+    return x, it2, it, nr2, nr

@@ -7,7 +7,9 @@ matrix_free_prolongation_2d_GPU.
 from . import _lib
 from ._lib import SbpError
 from .adjoint import HMisfit, PoissonSolve, mgcg_rrule
-from .matrix_free import (CG_Matrix_Free_GPU_v2, CG_full_GPU, jacobi, matrix_free_A_full_GPU,
+from .matrix_free import (CG_Matrix_Free_GPU_v2, CG_full_GPU, initial_guess_interpolation_CG_GPU,
+                          initial_guess_interpolation_three_level_CG_GPU, jacobi,
+                          matrix_free_A_full_GPU,
                           matrix_free_A_full_GPU_f32, matrix_free_MGCG,
                           matrix_free_prolongation_2d_GPU, matrix_free_restriction_2d_GPU,
                           matrix_free_richardson, matrix_free_Two_level_multigrid)
@@ -20,7 +22,8 @@ __all__ = [
     "matrix_free_restriction_2d_GPU", "matrix_free_richardson",
     "matrix_free_Two_level_multigrid", "Options", "SolveResult", "Solver", "default_options",
     "reference_two_level_options", "SbpError", "load_library", "HMisfit", "PoissonSolve",
-    "mgcg_rrule", "BatchSolver",
+    "mgcg_rrule", "BatchSolver", "initial_guess_interpolation_CG_GPU",
+    "initial_guess_interpolation_three_level_CG_GPU",
 ]
 
 

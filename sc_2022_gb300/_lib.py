@@ -86,6 +86,9 @@ SIGNATURES = {
     "sbp_mgcg_adjoint_f64": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _d, _d, _d, _i,
                                   C.POINTER(sbp_result), _vp]),
     "sbp_coarse_inverse_host": (_i, [_i, _dp, C.c_longlong]),
+    "sbp_csr_assemble_host": (_i, [_i, C.POINTER(C.c_longlong), C.POINTER(_i), _dp,
+                                   C.c_longlong, C.POINTER(C.c_longlong)]),
+    "sbp_csr_spmv_f64": (_i, [C.c_longlong, _vp, _vp, _vp, _vp, _vp, _vp]),
     "sbp_batch_create": (_i, [C.POINTER(_vp), C.POINTER(_i), _i, C.POINTER(sbp_options)]),
     "sbp_batch_destroy": (_i, [_vp]),
     "sbp_batch_size": (_i, [_vp]),

@@ -612,6 +612,13 @@ int sbp_rhs_adjoint_f64(const double* lam, double* df, double* dgW, double* dgE,
   return SBP_OK;
 }
 
+int sbp_csr_spmv_f64(long long nrows, const long long* row_ptr, const int* col,
+                     const double* val, const double* x, double* y, void* stream) {
+  if (nrows < 1 || !row_ptr || !col || !val || !x || !y) return SBP_ERR_ARGS;
+  SBP_CUDA(launch_csr_spmv(nrows, row_ptr, col, val, x, y, (cudaStream_t)stream));
+  return SBP_OK;
+}
+
 int sbp_h_misfit_f64(const double* u, const double* ut, double* g, int n, double* loss,
                      void* stream) {
   if (!u || !ut || n < 3 || (!g && !loss)) return SBP_ERR_ARGS;

@@ -2276,6 +2276,56 @@ cudaError_t launch_dot(Grid<const T> a, Grid<const T> b, int n, double* out, Red
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// CSR SpMV y = A x (the assembled-operator comparator).  A CTA takes 256
+// consecutive rows; their nonzeros are one contiguous segment, staged into
+// shared memory with coalesced loads (at most kSpmvSeg entries, else each
+// thread reads its row from global memory), then each thread sums its row,
+// gathering x (the stencil's neighbours: L1/L2 hits).
+// ---------------------------------------------------------------------------
+constexpr int kSpmvSeg = 256 * 9;
+
+__global__ void __launch_bounds__(kThreads)
+    k_csr_spmv(long long nrows, const long long* __restrict__ row_ptr,
+               const int* __restrict__ col, const double* __restrict__ val,
+               const double* __restrict__ x, double* __restrict__ y) {
+  __shared__ int scol[kSpmvSeg];
+  __shared__ double sval[kSpmvSeg];
+  for (long long r0 = (long long)blockIdx.x * kThreads; r0 < nrows;
+       r0 += (long long)gridDim.x * kThreads) {
+    const long long r1 = min(nrows, r0 + kThreads);
+    const long long s0 = __ldg(row_ptr + r0), s1 = __ldg(row_ptr + r1);
+    const int seg = (int)(s1 - s0);
+    const bool staged = seg <= kSpmvSeg;
+    if (staged)
+      for (int k = threadIdx.x; k < seg; k += kThreads) {
+        scol[k] = __ldg(col + s0 + k);
+        sval[k] = __ldg(val + s0 + k);
+      }
+    __syncthreads();
+    const long long r = r0 + threadIdx.x;
+    if (r < r1) {
+      const long long a = __ldg(row_ptr + r), b = __ldg(row_ptr + r + 1);
+      double acc = 0.0;
+      if (staged) {
+        for (long long k = a - s0; k < b - s0; ++k) acc = fma(sval[k], __ldg(x + scol[k]), acc);
+      } else {
+        for (long long k = a; k < b; ++k) acc = fma(__ldg(val + k), __ldg(x + __ldg(col + k)), acc);
+      }
+      y[r] = acc;
+    }
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_csr_spmv(long long nrows, const long long* row_ptr, const int* col,
+                            const double* val, const double* x, double* y, cudaStream_t s) {
+  const long long blocks = (nrows + kThreads - 1) / kThreads;
+  const int grid = (int)std::min<long long>(blocks, (long long)sm_count() * 8);
+  k_csr_spmv<<<std::max(grid, 1), kThreads, 0, s>>>(nrows, row_ptr, col, val, x, y);
+  return cudaGetLastError();
+}
+
 // g = H~ (u - ut) and *loss = 1/2 (u - ut)' H~ (u - ut), H~ = h^2 diag(w_i w_j)
 // (w = 1/2 on the first and last index): the H-norm misfit of the adjoint
 // configuration and its gradient.  Columns over CTAs, rows over threads;

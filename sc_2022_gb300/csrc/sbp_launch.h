@@ -207,6 +207,10 @@ int batch_sm_count();
 // dst (ld dld) = src (ld sld) on an n x n FP64 grid; recordable.
 cudaError_t copy_grid(double* dst, int dld, const double* src, int sld, int n, cudaStream_t s);
 
+// y = A x for a CSR matrix with nrows rows (64-bit row pointers).
+cudaError_t launch_csr_spmv(long long nrows, const long long* row_ptr, const int* col,
+                            const double* val, const double* x, double* y, cudaStream_t s);
+
 // g = H~ (u - ut) (g.p may be null) and *loss = 1/2 (u - ut)' H~ (u - ut)
 // (loss may be null); H~ = h^2 diag(w_i w_j).
 cudaError_t launch_h_misfit(Grid<const double> u, Grid<const double> ut, Grid<double> g, int n,

@@ -176,3 +176,71 @@ def matrix_free_prolongation_2d_GPU(idata: torch.Tensor, odata: torch.Tensor,
         raise ValueError("odata must be (2n-1)^2")
     L.check(L.load().sbp_prolong_f64(ptr(idata), ptr(odata), nc, int(accumulate),
                                      _stream_ptr()), "sbp_prolong_f64")
+
+
+# ---------------------------------------------------------------------------
+# Nested iteration (initial guess from the coarse problem)
+# ---------------------------------------------------------------------------
+def _coarse_exact(b_2h: torch.Tensor) -> torch.Tensor:
+    """x = A^-1 b on the grid of b: the fast-diagonalisation direct solve of a
+    one-level handle (coarse grids up to 257^2), else MGCG to 1e-14."""
+    n = check_grid(b_2h, name="b_2h")
+    x = torch.zeros_like(b_2h)
+    if n <= 257:
+        o = default_options()
+        o.coarse_n = n
+        _cached_solver(n, o).vcycle(b_2h, x)
+    else:
+        _cached_solver(n, default_options()).mgcg(b_2h, x, reltol=1e-14, raise_on_fail=True)
+    return x
+
+
+def _prolong(xc: torch.Tensor, n: int) -> torch.Tensor:
+    nc = check_grid(xc, name="coarse")
+    if 2 * nc - 1 != n:
+        raise ValueError(f"coarse grid {nc} does not prolong to {n}")
+    out = torch.empty(n * n, dtype=torch.float64, device=xc.device)
+    L.check(L.load().sbp_prolong_f64(ptr(xc), ptr(out), nc, 0, _stream_ptr()), "sbp_prolong_f64")
+    return out
+
+
+def _cg_from(b: torch.Tensor, x: torch.Tensor, abstol: float, maxiter: int | None):
+    """IterativeSolvers-style cg!: stop at max(sqrt(eps) |b - A x0|, abstol)."""
+    n = check_grid(b, name="b")
+    r0 = C.c_double()
+    L.check(L.load().sbp_residual_norm_f64(ptr(x), ptr(b), n, 1, C.byref(r0), _stream_ptr()),
+            "sbp_residual_norm_f64")
+    tol = max(SQRT_EPS * r0.value, abstol)
+    res = _cached_solver(n, None).cg(b, x, sign=1, abstol=tol,
+                                      maxiter=n * n if maxiter is None else maxiter)
+    return res
+
+
+def initial_guess_interpolation_CG_GPU(b_GPU: torch.Tensor, b_2h: torch.Tensor, x=None,
+                                       Nx_2h=None, abstol: float = SQRT_EPS,
+                                       maxiter: int | None = None):
+    """``matrix_free_mg_cg.jl:379-384``: exact solve of the coarse problem
+    A_2h x_2h = b_2h (its own right-hand side), bilinear prolongation of x_2h
+    as the initial guess, CG on A x = b.  Returns (x, iters, resnorms).  ``x``
+    and ``Nx_2h`` are accepted for signature compatibility (the reference
+    ignores x as well; the coarse size is b_2h's)."""
+    n = check_grid(b_GPU, name="b")
+    xs = _prolong(_coarse_exact(b_2h.reshape(-1)), n)
+    res = _cg_from(b_GPU.reshape(-1), xs, abstol, maxiter)
+    return xs, res.iters, list(res.norms)
+
+
+def initial_guess_interpolation_three_level_CG_GPU(b_GPU: torch.Tensor, b_2h_GPU: torch.Tensor,
+                                                   b_4h: torch.Tensor, x=None, Nx_2h=None,
+                                                   Nx_4h=None, abstol: float = SQRT_EPS,
+                                                   maxiter: int | None = None):
+    """``matrix_free_mg_cg.jl:386-396``: exact solve on 4h, prolong, CG on 2h
+    with b_2h, prolong, CG on h.  Returns (x, iters_2h, iters_h, resnorm_2h,
+    resnorm_h)."""
+    n = check_grid(b_GPU, name="b")
+    n2 = check_grid(b_2h_GPU, name="b_2h")
+    x2 = _prolong(_coarse_exact(b_4h.reshape(-1)), n2)
+    r2 = _cg_from(b_2h_GPU.reshape(-1), x2, abstol, maxiter)
+    xs = _prolong(x2, n)
+    r1 = _cg_from(b_GPU.reshape(-1), xs, abstol, maxiter)
+    return xs, r2.iters, r1.iters, list(r2.norms), list(r1.norms)

@@ -81,3 +81,16 @@ def test_coarse_inverse_rejects_bad_size(lib):
     X = np.zeros(10)
     assert lib.sbp_coarse_inverse_host(6, X.ctypes.data_as(C.POINTER(C.c_double)), 10) < 0
     assert lib.sbp_coarse_inverse_host(5, X.ctypes.data_as(C.POINTER(C.c_double)), 10) < 0
+
+
+@pytest.mark.parametrize("n", [5, 17, 33])
+def test_csr_assembly_equals_oracle_matrix(lib, n):
+    # the comparator's CSR matrix is Assembling_matrix's A, bit for bit
+    from sc_2022_gb300 import csr
+    rp, col, val = csr.assemble_csr_host(n)
+    A = o.assemble(n).A.tocsr()
+    A.sort_indices()
+    A.eliminate_zeros()
+    assert np.array_equal(A.indptr, rp)
+    assert np.array_equal(A.indices, col)
+    assert np.array_equal(A.data, val)

@@ -234,3 +234,22 @@ def test_apply_f64_exact_integer_path(sbp, field):
             assert err <= 3 * math.ulp(big), (i, j, err)
         checked[int(integer_path)] += 1
     assert checked[0] > 100 and checked[1] > 100
+
+
+@pytest.mark.parametrize("n", [257, 1025])
+def test_csr_spmv_matches_matrix_free(sbp, n):
+    from sc_2022_gb300 import csr
+    A = csr.CsrOperator(n)
+    rng = np.random.default_rng(23)
+    x = rng.standard_normal(n * n)
+    xd = dev(x)
+    y = A.matvec(xd)
+    mf = torch.empty_like(xd)
+    lib = sbp.load_library()
+    assert lib.sbp_apply_f64(C.c_void_p(xd.data_ptr()), C.c_void_p(mf.data_ptr()), n, 1,
+                             None) == 0
+    rel = np.linalg.norm(host(y) - host(mf)) / np.linalg.norm(host(mf))
+    assert rel < 1e-14
+    if n == 257:
+        ref = o.assemble(n).A @ x
+        assert np.linalg.norm(host(y) - ref) / np.linalg.norm(ref) < 1e-14

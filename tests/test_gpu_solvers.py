@@ -251,3 +251,26 @@ def test_mixed_n8193_bump_against_fp64(sbp):
     print(f"N=8193 mixed vs FP64: iterations {its}, relative solution difference {err:.3e}, "
           f"true relative residual {out.value / b.norm().item():.3e}")
     assert err < 1e-8
+
+
+@pytest.mark.parametrize("n", [65, 257])
+def test_nested_iteration_matches_oracle(sbp, n):
+    rhs = {}
+    for m in (n, (n + 1) // 2, (n + 3) // 4):
+        a = o.assemble(m)
+        F, g, U = o.manufactured(m, "reference")
+        rhs[m] = a.rhs(F, g)
+    b = rhs[n]
+    abstol = float(np.linalg.norm(b)) * SQRT_EPS
+    xr, itr, nr = o.nested_cg(n, b, rhs[(n + 1) // 2], abstol)
+    x, it, norms = sbp.initial_guess_interpolation_CG_GPU(dev(b), dev(rhs[(n + 1) // 2]),
+                                                         abstol=abstol)
+    assert abs(it - itr) <= 1
+    assert relerr(host(x), xr) < 1e-8
+    assert norms[0] == pytest.approx(nr[0], rel=1e-10)
+    x3r, it2r, it1r, _, _ = o.nested_cg_three_level(n, b, rhs[(n + 1) // 2], rhs[(n + 3) // 4],
+                                                    abstol)
+    x3, it2, it1, n2, n1 = sbp.initial_guess_interpolation_three_level_CG_GPU(
+        dev(b), dev(rhs[(n + 1) // 2]), dev(rhs[(n + 3) // 4]), abstol=abstol)
+    assert abs(it2 - it2r) <= 1 and abs(it1 - it1r) <= 1
+    assert relerr(host(x3), x3r) < 1e-8

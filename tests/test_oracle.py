@@ -184,3 +184,21 @@ def test_adjoint_oracle_matches_finite_differences():
         fd = (lp - lm) / (2 * eps)
         an = float(df @ d_f) + sum(float(dg[s] @ d_g[s]) for s in "WESN")
         assert abs(fd - an) <= 1e-6 * abs(an) + 1e-12
+
+
+def test_nested_iteration_oracle_saves_iterations():
+    # matrix_free_mg_cg.jl:372-396: the coarse problem's solution, prolonged,
+    # is a better CG start than zero (reference problem, its own coarse b)
+    n = 65
+    rhs = {}
+    for m in (n, (n + 1) // 2, (n + 3) // 4):
+        a = o.assemble(m)
+        F, g, U = o.manufactured(m, "reference")
+        rhs[m] = a.rhs(F, g)
+    b = rhs[n]
+    abstol = float(np.linalg.norm(b)) * math.sqrt(np.finfo(float).eps)
+    _, it0, _ = o.cg(o.assemble(n).A, b, abstol=abstol)
+    x, it, nr = o.nested_cg(n, b, rhs[33], abstol)
+    assert it < it0 and nr[-1] < abstol
+    x3, it2, it1, nr2, nr1 = o.nested_cg_three_level(n, b, rhs[33], rhs[17], abstol)
+    assert it1 < it0 and nr1[-1] < abstol
