@@ -44,7 +44,8 @@ def parse_args():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--n", type=int, default=4097)
+    p.add_argument("--grid", "--n", dest="n", type=int, default=4097,
+                   help="points per side (use --grid under torch.distributed.run)")
     p.add_argument("--apply-iters", type=int, default=50)
     p.add_argument("--cpu-baseline", type=int, default=1, help="time the CPU baseline leg")
     p.add_argument("--dtype", choices=["f64", "f32"], default="f64",
@@ -157,10 +158,10 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # CPU baseline: the reference's sparse CPU path restated in C (OpenMP)
 # ---------------------------------------------------------------------------
-def cpu_mgcg_timing(n: int, b_host, steps: int, warmup: int):
+def cpu_mgcg_timing(n: int, b_host, steps: int, warmup: int, threads: int | None = None):
     from oracle import cpu_path
     import numpy as np
-    threads = os.cpu_count() or 1
+    threads = threads or os.cpu_count() or 1
     cpu_path.set_threads(threads)
     t0 = time.perf_counter()
     m = cpu_path.CpuMG(n, smoother="jacobi", restriction="galerkin", coarse_n=65)
@@ -381,11 +382,13 @@ def run_ours(args, d: Dist):
     if d.rank == 0 and args.cpu_baseline:
         bh = b.detach().cpu().numpy()
         r = cpu_mgcg_timing(n, bh, steps=1, warmup=0)
+        r1 = cpu_mgcg_timing(n, bh, steps=1, warmup=0, threads=1)
         line["cpu_baseline"] = {
             "value": round(r["ms_per_solve"], 2), "unit": "ms", "cores": r["threads"],
             "kind": "port", "sample": f"1 full FP64 MGCG solve at N={n} ({r['iters']} iterations) "
                                       "with the C restatement of the reference's sparse CPU path "
-                                      "(CSR SpMV, same V-cycle), setup excluded"}
+                                      "(CSR SpMV, same V-cycle), setup excluded",
+            "value_1_core": round(r1["ms_per_solve"], 2)}
     if d.rank == 0:
         print(json.dumps(line), flush=True)
     s32.close()
