@@ -516,6 +516,27 @@ struct NoCtx {};
 // Thread groups (64 threads each, 4 per CTA) of the FP64 apply that use FP64
 // instructions for the interior stencil; the rest use the integer pipe.
 constexpr int kFp64Groups = 2;
+// The same split for FP64 kernels that also spend FP64 instructions outside
+// the stencil (sweeps, residuals, CG direction): one group on the FP64 pipe.
+constexpr int kFp64GroupsFused = 1;
+
+// S = (uw + ue) + (um + up) - 4 u0, i.e. (-A u) at an interior point.  FP64
+// with `exact`: the integer-pipe sum of exact_stencil5 (FP64 instructions
+// when it declines); otherwise one FP add chain + FMA in T.
+template <typename T>
+__device__ __forceinline__ T neg_stencil(T um, T u0, T up, T uw, T ue, bool exact) {
+  if constexpr (sizeof(T) == 8) {
+    double sx;
+    if (exact && exact_stencil5((double)u0, (double)uw, (double)ue, (double)um, (double)up, sx))
+      return (T)sx;
+  }
+  return fma(T(-4), u0, (uw + ue) + (um + up));
+}
+// This thread's group uses the integer path (FP64 kernels only).
+template <typename T, int FP64_GROUPS>
+__device__ __forceinline__ bool exact_group() {
+  return sizeof(T) == 8 && (int)(threadIdx.x >> 6) >= FP64_GROUPS;
+}
 
 template <typename T, bool DOT, bool TMA>
 struct ApplyJob {
@@ -627,10 +648,11 @@ struct ResidualJob {
       }
     }
     if (tile_interior(t, n)) {
+      const bool exact = exact_group<T, kFp64GroupsFused>();
       visit_interior(s, t, [&](int i, int j, T um, T u0, T up, T uw, T ue, int k) {
-        const T sum = (uw + ue) + (um + up);
-        // r = b - opsign*A x, A x = 4 u0 - sum
-        emit(i, j, opsign > 0 ? sb[k] + (sum - T(4) * u0) : sb[k] - (sum - T(4) * u0));
+        // r = b - opsign*A x, A x = 4 u0 - sum = -S
+        const T S = neg_stencil<T>(um, u0, up, uw, ue, exact);
+        emit(i, j, opsign > 0 ? sb[k] + S : sb[k] - S);
       });
     } else {
       visit_generic(s, t, bx, [&](int i, int j, const SAcc<T>& a, int k) {
@@ -718,9 +740,10 @@ struct CgDirJob {
       acc.add_prod(pv, ap);
     };
     if (tile_interior(t, n)) {
+      const bool exact = exact_group<T, kFp64GroupsFused>();
       visit_interior(s, t, [&](int i, int j, T um, T u0, T up, T uw, T ue, int) {
-        const T sum = (uw + ue) + (um + up);
-        emit(i, j, u0, opsign > 0 ? fma(T(4), u0, -sum) : fma(T(-4), u0, sum));
+        const T S = neg_stencil<T>(um, u0, up, uw, ue, exact);   // -A p
+        emit(i, j, u0, opsign > 0 ? -S : S);
       });
     } else {
       visit_generic(s, t, bx, [&](int i, int j, const SAcc<T>& a, int) {
@@ -1034,16 +1057,18 @@ struct SmoothJob {
     };
     if (interior) {
       const T m = jac ? omega * T(0.25) : omega;   // interior diag(A) = 4
+      const bool exact = exact_group<T, kFp64GroupsFused>();
       visit_interior(s, t, [&](int i, int j, T um, T u0, T up, T uw, T ue, int k) {
-        const T sum = (uw + ue) + (um + up);
         if (FIELD == kFieldZero) {
           // staged raw b: F = m b, the stencil of F is m times the stencil of b
           const T f = m * u0;
-          const T vn = (EPI == kEpiSweep) ? fma(m, fma(m, sum - T(4) * u0, u0), f) : f;
+          T vn = f;
+          if (EPI == kEpiSweep) vn = fma(m, fma(m, neg_stencil<T>(um, u0, up, uw, ue, exact), u0), f);
           emit(i, j, u0, vn);
         } else {
           const T bb = kNeedB ? sb[k] : T(0);
-          const T vn = (EPI == kEpiSweep) ? fma(m, bb + (sum - T(4) * u0), u0) : u0;
+          T vn = u0;
+          if (EPI == kEpiSweep) vn = fma(m, bb + neg_stencil<T>(um, u0, up, uw, ue, exact), u0);
           emit(i, j, bb, vn);
         }
       });
@@ -1116,6 +1141,7 @@ struct ResRestrictJob {
       const int ei = ri1 - ri0 + 1, ej = rj1 - rj0 + 1;
       const int cnt = ei * ej;
       const bool interior = ri0 > 0 && ri1 < nf - 1 && rj0 > 2 && rj1 < nf - 3;
+      const bool exact = exact_group<T, kFp64GroupsFused>();
       for (int k = threadIdx.x; k < cnt; k += kThreads) {
         const int c = k / ei;
         const int r = k - c * ei;
@@ -1124,7 +1150,7 @@ struct ResRestrictJob {
         T na;
         if (interior) {
           const T* a = sv + q;
-          na = ((a[-1] + a[1]) + (a[-BI] + a[BI])) - T(4) * a[0];
+          na = neg_stencil<T>(a[-BI], a[0], a[BI], a[-1], a[1], exact);
         } else {
           na = negA<T>(SAcc<T>{sv + q, BI}, i, j, nf);
         }
@@ -1140,12 +1166,25 @@ struct ResRestrictJob {
         const int I = t.i_lo + r;
         const T* q = sr + (2 * J - y0) * BI + (2 * I - x0);
         T acc = T(0);
+        if (I > 0 && I < nc - 1 && J > 0 && J < nc - 1) {
+          // interior coarse point: weights (1/2, 1, 1/2) x (1/2, 1, 1/2)
+          // (galerkin), times 1/4 for the full-weighting kinds
+          T cs[3];
 #pragma unroll
-        for (int bj = -1; bj <= 1; ++bj) {
-          const T wj = restrict_w1<T>(kind, J, nc, bj);
+          for (int bj = -1; bj <= 1; ++bj) {
+            const T* col = q + bj * BI;
+            cs[bj + 1] = fma(T(0.5), col[-1] + col[1], col[0]);
+          }
+          acc = fma(T(0.5), cs[0] + cs[2], cs[1]);
+          if (kind != kRestrictGalerkin) acc *= T(0.25);
+        } else {
 #pragma unroll
-          for (int ai = -1; ai <= 1; ++ai)
-            acc = fma(restrict_w1<T>(kind, I, nc, ai) * wj, q[bj * BI + ai], acc);
+          for (int bj = -1; bj <= 1; ++bj) {
+            const T wj = restrict_w1<T>(kind, J, nc, bj);
+#pragma unroll
+            for (int ai = -1; ai <= 1; ++ai)
+              acc = fma(restrict_w1<T>(kind, I, nc, ai) * wj, q[bj * BI + ai], acc);
+          }
         }
         f.at(I, J) = acc;
       }
