@@ -185,6 +185,22 @@ int sbp_rhs_adjoint_f64(const double* lam, double* df, double* dgW, double* dgE,
 int sbp_h_misfit_f64(const double* u, const double* ut, double* g, int n, double* loss,
                      void* stream);
 
+/* ---- fourth-order operator (p = 4) ------------------------------------ */
+
+/* The p = 4 diagonal-norm SBP-SAT operator of Operators_2d(...; p = 4) /
+ * Assembling_matrix(level; p = 4) (level_2_multigrid_new.jl:48-188 with the
+ * p == 4 branches of diagonal_sbp.jl): interior D2 stencil
+ * (-1/12, 4/3, -5/2, 4/3, -1/12) along both directions, 4 x 6 boundary
+ * closures, the same SAT penalties as p = 2.  out = sign * A u, FP64, the
+ * caller's layout (ld = n), n >= 9.  The reference's GPU path has p = 2 only;
+ * its CPU path assembles any p. */
+int sbp_apply_p4_f64(const double* u, double* out, int n, int sign, void* stream);
+/* Plain CG on (sign * A_p4) x = b from the caller's x (device arrays,
+ * ld = n), stopping rule and results as sbp_cg_solve.  Allocates its
+ * temporaries stream-ordered. */
+int sbp_cg_p4_solve(const double* b, double* x, int n, int sign, double abstol, double reltol,
+                    int maxiter, sbp_result* res, double* norms, int norms_cap, void* stream);
+
 /* ---- assembled-operator comparator ------------------------------------ */
 
 /* The reference compares its matrix-free apply with SpMV on the assembled

@@ -95,6 +95,56 @@ def sbp_1d(n: int):
     return D2, H, HI, BS
 
 
+# --------------------------------------------------------------------------
+# 1D SBP operators, p = 4
+# --------------------------------------------------------------------------
+# diagonal_sbp.jl, p == 4 branches of diagonal_sbp_D2 (:198-210) and
+# diagonal_sbp_D1 (:62-67): norm weights H = h / bhinv on the first and last
+# four points, the interior D2 stencil d, the 4 x 6 boundary closure bd
+# (mirrored at the far end with the same values), and the boundary
+# derivative BS.
+P4_BHINV = (48 / 17, 48 / 59, 48 / 43, 48 / 49)
+P4_D = (-1 / 12, 4 / 3, -5 / 2, 4 / 3, -1 / 12)
+P4_BD = ((2.0, -5.0, 4.0, -1.0, 0.0, 0.0),
+         (1.0, -2.0, 1.0, 0.0, 0.0, 0.0),
+         (-4 / 43, 59 / 43, -110 / 43, 59 / 43, -4 / 43, 0.0),
+         (-1 / 49, 0.0, 59 / 49, -118 / 49, 64 / 49, -4 / 49))
+P4_BS = (11 / 6, -3.0, 3 / 2, -1 / 3)
+
+
+def sbp_1d_p4(n: int):
+    """1D fourth-order diagonal-norm SBP pieces on n points of [0, 1]
+    (``diagonal_sbp.jl:198-210, 414-452`` for D2/S0/SN; ``:62-67, 112-146``
+    for the norm H).  Returns (D2, H, HI, BS) as scipy CSR matrices."""
+    bm, bn = 4, 6
+    if n - 1 < max(bn, 2 * bm):
+        raise ValueError("SBP p=4 operator needs n >= 9")
+    h = 1.0 / (n - 1)
+    rows, cols, vals = [], [], []
+    for r in range(bm, n - bm):
+        for k, c in enumerate(P4_D):
+            rows.append(r)
+            cols.append(r - 2 + k)
+            vals.append(c / h**2)
+    for r in range(bm):
+        for c in range(bn):
+            if P4_BD[r][c] != 0.0:
+                rows += [r, n - 1 - r]
+                cols += [c, n - 1 - c]
+                vals += [P4_BD[r][c] / h**2] * 2
+    D2 = sp.csr_matrix((vals, (rows, cols)), shape=(n, n))
+    hv = np.ones(n)
+    for k in range(bm):
+        hv[k] = hv[n - 1 - k] = 1.0 / P4_BHINV[k]
+    H = sp.diags(h * hv).tocsr()
+    HI = sp.diags(1.0 / (h * hv)).tocsr()
+    bs = np.array(P4_BS) / h
+    S0 = sp.csr_matrix((-bs, ([0] * 4, [0, 1, 2, 3])), shape=(n, n))
+    SN = sp.csr_matrix((bs, ([n - 1] * 4, [n - 1, n - 2, n - 3, n - 4])), shape=(n, n))
+    BS = (SN - S0).tocsr()
+    return D2, H, HI, BS
+
+
 def _e(k: int, n: int):
     return sp.csr_matrix(([1.0], ([k], [0])), shape=(n, 1))
 
@@ -123,13 +173,20 @@ class Assembled:
         return -(self.H_tilde @ acc)
 
 
-def assemble(n: int) -> Assembled:
+def assemble(n: int, p: int = 2) -> Assembled:
     """Restates ``Operators_2d`` + ``Assembling_matrix``
-    (``level_2_multigrid_new.jl:48-188``) for N_x = N_y = n - 1 intervals.
+    (``level_2_multigrid_new.jl:48-188``) for N_x = N_y = n - 1 intervals and
+    SBP order p (2 or 4; the penalty parameters are the same for both, as in
+    the reference).
 
     kron(X, I) acts on the slow index j, kron(I, X) on the fast index i.
     """
-    D2x, H1x, HIx, BSx = sbp_1d(n)
+    if p == 2:
+        D2x, H1x, HIx, BSx = sbp_1d(n)
+    elif p == 4:
+        D2x, H1x, HIx, BSx = sbp_1d_p4(n)
+    else:
+        raise ValueError("only p = 2 and p = 4 are restated")
     D2y, H1y, HIy, BSy = D2x, H1x, HIx, BSx
     I = sp.identity(n, format="csr")
     e1 = _e(0, n)

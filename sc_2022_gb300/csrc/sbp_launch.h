@@ -207,6 +207,22 @@ int batch_sm_count();
 // dst (ld dld) = src (ld sld) on an n x n FP64 grid; recordable.
 cudaError_t copy_grid(double* dst, int dld, const double* src, int sld, int n, cudaStream_t s);
 
+// Fourth-order operator: out = sign * A u (+ *dot_out = u . out), FP64, any
+// leading dimension; n >= 9.  prepare_p4_tables() uploads the closure
+// coefficients once (outside stream capture).
+cudaError_t prepare_p4_tables();
+// With st (CG), the reduction sets p.Ap and alpha; the kernel exits at once
+// when the state is done.
+cudaError_t launch_apply_p4(Grid<const double> u, Grid<double> out, int n, int sign, ReduceBuf rb,
+                            double* dot_out, SolveState* st, cudaStream_t s);
+// Plain-CG pieces on flat arrays of N entries: set-up (r = b - r, p = r, state)
+// and the direction p = r + beta p.
+cudaError_t launch_cg_init_flat(const double* b, double* r, double* p, long long N,
+                                SolveState* st, double* norms, double abstol, double reltol,
+                                ReduceBuf rb, cudaStream_t s);
+cudaError_t launch_cg_dir_flat(const double* r, double* p, long long N, const SolveState* st,
+                               cudaStream_t s);
+
 // y = A x for a CSR matrix with nrows rows (64-bit row pointers).
 cudaError_t launch_csr_spmv(long long nrows, const long long* row_ptr, const int* col,
                             const double* val, const double* x, double* y, cudaStream_t s);

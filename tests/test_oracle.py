@@ -202,3 +202,30 @@ def test_nested_iteration_oracle_saves_iterations():
     assert it < it0 and nr[-1] < abstol
     x3, it2, it1, nr2, nr1 = o.nested_cg_three_level(n, b, rhs[33], rhs[17], abstol)
     assert it1 < it0 and nr1[-1] < abstol
+
+
+@pytest.mark.parametrize("n", [9, 17, 33])
+def test_p4_sbp_pieces(n):
+    # diagonal_sbp.jl p = 4: D2 exact on cubics (boundary closure order 2),
+    # H D2 - BS symmetric negative semidefinite (summation by parts)
+    D2, H, HI, BS = o.sbp_1d_p4(n)
+    x = np.linspace(0.0, 1.0, n)
+    for k, d2 in ((0, 0 * x), (1, 0 * x), (2, 2 + 0 * x), (3, 6 * x)):
+        np.testing.assert_allclose(D2 @ x**k, d2, atol=1e-9 * (n - 1) ** 2)
+    M = (H @ D2 - BS).toarray()
+    assert np.abs(M - M.T).max() < 1e-10 * np.abs(M).max()
+    assert np.linalg.eigvalsh(0.5 * (M + M.T)).max() < 1e-9 * np.abs(M).max()
+    np.testing.assert_allclose((H @ np.ones(n)).sum(), 1.0, rtol=1e-14)
+
+
+def test_p4_operator_spd_and_fourth_order():
+    for n in (9, 17):
+        A = o.assemble(n, 4).A
+        assert abs(A - A.T).max() < 1e-12 * abs(A).max()
+        assert np.linalg.eigvalsh(A.toarray()).min() > 0
+    errs = []
+    for n in (17, 33, 65):
+        a = o.assemble(n, 4)
+        F, g, U = o.manufactured(n, "reference")
+        errs.append(o.h_error(a, spla.spsolve(a.A.tocsc(), a.rhs(F, g)), U))
+    assert errs[0] / errs[1] > 12.0 and errs[1] / errs[2] > 12.0
