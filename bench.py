@@ -51,6 +51,7 @@ def parse_args():
     p.add_argument("--dtype", choices=["f64", "f32"], default="f64",
                    help="operand type of --mode apply")
     p.add_argument("--mode", choices=["full", "apply", "solve-fp64", "solve-mixed", "vcycle",
+                                      "high-order",
                                       "batch", "spmv"],
                    default="full", help="profiling modes run one part only and print a "
                    "short line (not the benchmark line)")
@@ -495,6 +496,50 @@ def run_part(args):
                     "speedup": round(res["sequential_ms"] / res["batched_ms"], 3),
                     "launches_batched": B.last_launches, "cta_budgets": budgets})
         print(json.dumps(res))
+        return
+    if args.mode == "high-order":
+        # p = 4 and p = 6 operators at --n: the FP64 apply (16 B per point
+        # moved) and MGCG to 1e-10 from zero on a seeded random right-hand side
+        out = {"mode": "high-order", "n": n}
+        gen = torch.Generator(device=dev).manual_seed(0)
+        us = [torch.randn(n * n, generator=gen, device=dev, dtype=torch.float64) for _ in range(2)]
+        outs = [torch.empty_like(us[0]) for _ in range(2)]
+        hbm, hbm_src = measured_peaks()
+        out["hbm_peak_gbs"] = hbm
+        out["hbm_peak_source"] = hbm_src
+        for p in (4, 6):
+            for k in range(args.warmup):
+                sbp.matrix_free_A_high_order_GPU(us[k % 2], outs[k % 2], p=p)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for k in range(args.steps):
+                sbp.matrix_free_A_high_order_GPU(us[k % 2], outs[k % 2], p=p)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / args.steps
+            gbs = 16.0 * n * n / (ms * 1e-3) / 1e9
+            out[f"p{p}_apply_us"] = round(1e3 * ms, 2)
+            out[f"p{p}_apply_gbs"] = round(gbs, 1)
+            out[f"p{p}_apply_frac_of_hbm"] = round(gbs / hbm, 3)
+            s = sbp.HighOrderSolver(n, p)
+            x = torch.zeros_like(us[0])
+            for _ in range(args.warmup):
+                x.zero_()
+                s.mgcg(us[0], x, reltol=1e-10, maxiter=200)
+            torch.cuda.synchronize()
+            e0.record()
+            for _ in range(args.steps):
+                x.zero_()
+                r = s.mgcg(us[0], x, reltol=1e-10, maxiter=200)
+            e1.record()
+            torch.cuda.synchronize()
+            out[f"p{p}_mgcg_ms"] = round(e0.elapsed_time(e1) / args.steps, 3)
+            out[f"p{p}_mgcg_iters"] = r.iters
+            out[f"p{p}_mgcg_converged"] = r.converged
+            s.close()
+        print(json.dumps(out))
         return
     if args.mode == "vcycle":
         # time one V-cycle (mixed and FP64) for the default hierarchy at --n

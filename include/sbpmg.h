@@ -185,21 +185,45 @@ int sbp_rhs_adjoint_f64(const double* lam, double* df, double* dgW, double* dgE,
 int sbp_h_misfit_f64(const double* u, const double* ut, double* g, int n, double* loss,
                      void* stream);
 
-/* ---- fourth-order operator (p = 4) ------------------------------------ */
+/* ---- higher-order operators (p = 4, 6) ------------------------------- */
 
-/* The p = 4 diagonal-norm SBP-SAT operator of Operators_2d(...; p = 4) /
- * Assembling_matrix(level; p = 4) (level_2_multigrid_new.jl:48-188 with the
- * p == 4 branches of diagonal_sbp.jl): interior D2 stencil
- * (-1/12, 4/3, -5/2, 4/3, -1/12) along both directions, 4 x 6 boundary
- * closures, the same SAT penalties as p = 2.  out = sign * A u, FP64, the
- * caller's layout (ld = n), n >= 9.  The reference's GPU path has p = 2 only;
- * its CPU path assembles any p. */
-int sbp_apply_p4_f64(const double* u, double* out, int n, int sign, void* stream);
-/* Plain CG on (sign * A_p4) x = b from the caller's x (device arrays,
- * ld = n), stopping rule and results as sbp_cg_solve.  Allocates its
- * temporaries stream-ordered. */
-int sbp_cg_p4_solve(const double* b, double* x, int n, int sign, double abstol, double reltol,
-                    int maxiter, sbp_result* res, double* norms, int norms_cap, void* stream);
+/* The order-p diagonal-norm SBP-SAT operator of Operators_2d(...; p) /
+ * Assembling_matrix(level; p) (level_2_multigrid_new.jl:48-188 with the
+ * p == 4 and p == 6 branches of diagonal_sbp.jl:62-79, 198-222):
+ * - interior D2 stencils (-1/12, 4/3, -5/2, 4/3, -1/12) for p = 4 and
+ *   (1/90, -3/20, 3/2, -49/18, ...) for p = 6;
+ * - 4 x 6 and 6 x 9 boundary closures;
+ * - the same SAT penalties as p = 2.
+ * The reference assembles these on the CPU only; its GPU kernels are
+ * second order.  Arrays are contiguous FP64 n x n device grids (ld = n),
+ * n >= 8 (p = 4) or 12 (p = 6). */
+int sbp_apply_ho_f64(const double* u, double* out, int n, int p, int sign, void* stream);
+
+/* Order-p solver handle.  opts (NULL = sbp_options_default) must be FP64;
+ * the V-cycle re-discretises the order-p operator on every level.  It
+ * smooths with the chosen Jacobi or Richardson sweeps, uses the chosen
+ * restriction and bilinear prolongation, and solves the coarse level
+ * exactly by fast diagonalisation.  This is precond_matrix(A, b; SBPp)
+ * (initial_guess_cg.jl:458-510) over any number of levels.
+ * Multigrid needs n = 2^k + 1 coarsening to coarse_n (2^m + 1, at least
+ * the minimum n of p, at most 257), or n <= min(coarse_n, 257): a single
+ * direct level.  Any n >= the minimum gets plain CG. */
+typedef struct sbp_ho_solver sbp_ho_solver;
+int sbp_ho_solver_create(sbp_ho_solver** out, int n, int p, const sbp_options* opts);
+int sbp_ho_solver_destroy(sbp_ho_solver* s);
+/* Multigrid levels (0 when the handle supports CG only). */
+int sbp_ho_solver_levels(const sbp_ho_solver* s);
+long long sbp_ho_solver_device_bytes(const sbp_ho_solver* s);
+/* MGCG on A_p x = b; stopping rule, norms and results as sbp_mgcg_solve. */
+int sbp_ho_mgcg_solve(sbp_ho_solver* s, const double* b, double* x, double abstol, double reltol,
+                      int maxiter, sbp_result* res, double* norms, int norms_cap, void* stream);
+/* Plain CG on (sign * A_p) x = b (CG_CPU, level_2_multigrid_new.jl:258-291,
+ * on the order-p matrix), as sbp_cg_solve. */
+int sbp_ho_cg_solve(sbp_ho_solver* s, const double* b, double* x, int sign, double abstol,
+                    double reltol, int maxiter, sbp_result* res, double* norms, int norms_cap,
+                    void* stream);
+/* v = one V-cycle from zero for the right-hand side b. */
+int sbp_ho_vcycle_apply(sbp_ho_solver* s, const double* b, double* v, void* stream);
 
 /* ---- assembled-operator comparator ------------------------------------ */
 

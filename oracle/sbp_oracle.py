@@ -96,13 +96,13 @@ def sbp_1d(n: int):
 
 
 # --------------------------------------------------------------------------
-# 1D SBP operators, p = 4
+# 1D SBP operators, p = 4 and p = 6
 # --------------------------------------------------------------------------
-# diagonal_sbp.jl, p == 4 branches of diagonal_sbp_D2 (:198-210) and
-# diagonal_sbp_D1 (:62-67): norm weights H = h / bhinv on the first and last
-# four points, the interior D2 stencil d, the 4 x 6 boundary closure bd
-# (mirrored at the far end with the same values), and the boundary
-# derivative BS.
+# diagonal_sbp.jl, the p == 4 and p == 6 branches of diagonal_sbp_D2
+# (:198-222) and diagonal_sbp_D1 (:62-79): norm weights H = h / bhinv on the
+# first and last bm points, the interior D2 stencil d, the bm x bn boundary
+# closure bd (mirrored at the far end with the same values), and the boundary
+# derivative BS.  Fractions are written as the reference writes them.
 P4_BHINV = (48 / 17, 48 / 59, 48 / 43, 48 / 49)
 P4_D = (-1 / 12, 4 / 3, -5 / 2, 4 / 3, -1 / 12)
 P4_BD = ((2.0, -5.0, 4.0, -1.0, 0.0, 0.0),
@@ -111,38 +111,70 @@ P4_BD = ((2.0, -5.0, 4.0, -1.0, 0.0, 0.0),
          (-1 / 49, 0.0, 59 / 49, -118 / 49, 64 / 49, -4 / 49))
 P4_BS = (11 / 6, -3.0, 3 / 2, -1 / 3)
 
+P6_BHINV = (43200 / 13649, 8640 / 12013, 4320 / 2711, 4320 / 5359, 8640 / 7877, 43200 / 43801)
+P6_D = (1 / 90, -3 / 20, 3 / 2, -49 / 18, 3 / 2, -3 / 20, 1 / 90)
+P6_BD = (
+    (114170 / 40947, -438107 / 54596, 336409 / 40947, -276997 / 81894, 3747 / 13649,
+     21035 / 163788, 0.0, 0.0, 0.0),
+    (6173 / 5860, -2066 / 879, 3283 / 1758, -303 / 293, 2111 / 3516, -601 / 4395, 0.0, 0.0, 0.0),
+    (-52391 / 81330, 134603 / 32532, -21982 / 2711, 112915 / 16266, -46969 / 16266,
+     30409 / 54220, 0.0, 0.0, 0.0),
+    (68603 / 321540, -12423 / 10718, 112915 / 32154, -75934 / 16077, 53369 / 21436,
+     -54899 / 160770, 48 / 5359, 0.0, 0.0),
+    (-7053 / 39385, 86551 / 94524, -46969 / 23631, 53369 / 15754, -87904 / 23631,
+     820271 / 472620, -1296 / 7877, 96 / 7877, 0.0),
+    (21035 / 525612, -24641 / 131403, 30409 / 87602, -54899 / 131403, 820271 / 525612,
+     -117600 / 43801, 64800 / 43801, -6480 / 43801, 480 / 43801))
+P6_BS = (25 / 12, -4.0, 3.0, -4 / 3, 1 / 4)
 
-def sbp_1d_p4(n: int):
-    """1D fourth-order diagonal-norm SBP pieces on n points of [0, 1]
-    (``diagonal_sbp.jl:198-210, 414-452`` for D2/S0/SN; ``:62-67, 112-146``
-    for the norm H).  Returns (D2, H, HI, BS) as scipy CSR matrices."""
-    bm, bn = 4, 6
-    if n - 1 < max(bn, 2 * bm):
-        raise ValueError("SBP p=4 operator needs n >= 9")
+HIGH_ORDER = {4: (P4_BHINV, P4_D, P4_BD, P4_BS), 6: (P6_BHINV, P6_D, P6_BD, P6_BS)}
+
+
+def high_order_min_n(p: int) -> int:
+    """Smallest grid the reference accepts (diagonal_sbp.jl:417-420:
+    N + 1 >= max(bn, 2 bm))."""
+    bhinv, _, bd, _ = HIGH_ORDER[p]
+    return max(len(bd[0]), 2 * len(bhinv))
+
+
+def sbp_1d_high(n: int, p: int):
+    """1D diagonal-norm SBP pieces of order p in {4, 6} on n points of
+    [0, 1] (``diagonal_sbp.jl:198-222, 414-452`` for D2/S0/SN; ``:62-79,
+    112-146`` for the norm H).  Returns (D2, H, HI, BS) as scipy CSR."""
+    bhinv, d, bd, bsv = HIGH_ORDER[p]
+    bm, bn, half = len(bhinv), len(bd[0]), len(d) // 2
+    if n < high_order_min_n(p):
+        raise ValueError(f"SBP p={p} operator needs n >= {high_order_min_n(p)}")
     h = 1.0 / (n - 1)
     rows, cols, vals = [], [], []
     for r in range(bm, n - bm):
-        for k, c in enumerate(P4_D):
+        for k, c in enumerate(d):
             rows.append(r)
-            cols.append(r - 2 + k)
+            cols.append(r - half + k)
             vals.append(c / h**2)
     for r in range(bm):
         for c in range(bn):
-            if P4_BD[r][c] != 0.0:
+            if bd[r][c] != 0.0:
                 rows += [r, n - 1 - r]
                 cols += [c, n - 1 - c]
-                vals += [P4_BD[r][c] / h**2] * 2
+                vals += [bd[r][c] / h**2] * 2
     D2 = sp.csr_matrix((vals, (rows, cols)), shape=(n, n))
     hv = np.ones(n)
     for k in range(bm):
-        hv[k] = hv[n - 1 - k] = 1.0 / P4_BHINV[k]
+        hv[k] = hv[n - 1 - k] = 1.0 / bhinv[k]
     H = sp.diags(h * hv).tocsr()
     HI = sp.diags(1.0 / (h * hv)).tocsr()
-    bs = np.array(P4_BS) / h
-    S0 = sp.csr_matrix((-bs, ([0] * 4, [0, 1, 2, 3])), shape=(n, n))
-    SN = sp.csr_matrix((bs, ([n - 1] * 4, [n - 1, n - 2, n - 3, n - 4])), shape=(n, n))
+    bs = np.array(bsv) / h
+    nb = len(bsv)
+    S0 = sp.csr_matrix((-bs, ([0] * nb, list(range(nb)))), shape=(n, n))
+    SN = sp.csr_matrix((bs, ([n - 1] * nb, [n - 1 - k for k in range(nb)])), shape=(n, n))
     BS = (SN - S0).tocsr()
     return D2, H, HI, BS
+
+
+def sbp_1d_p4(n: int):
+    """The p = 4 pieces (:func:`sbp_1d_high` with p = 4)."""
+    return sbp_1d_high(n, 4)
 
 
 def _e(k: int, n: int):
@@ -176,17 +208,17 @@ class Assembled:
 def assemble(n: int, p: int = 2) -> Assembled:
     """Restates ``Operators_2d`` + ``Assembling_matrix``
     (``level_2_multigrid_new.jl:48-188``) for N_x = N_y = n - 1 intervals and
-    SBP order p (2 or 4; the penalty parameters are the same for both, as in
-    the reference).
+    SBP order p (2, 4 or 6; the penalty parameters are the same for all, as
+    in the reference).
 
     kron(X, I) acts on the slow index j, kron(I, X) on the fast index i.
     """
     if p == 2:
         D2x, H1x, HIx, BSx = sbp_1d(n)
-    elif p == 4:
-        D2x, H1x, HIx, BSx = sbp_1d_p4(n)
+    elif p in HIGH_ORDER:
+        D2x, H1x, HIx, BSx = sbp_1d_high(n, p)
     else:
-        raise ValueError("only p = 2 and p = 4 are restated")
+        raise ValueError("only p = 2, 4 and 6 are restated")
     D2y, H1y, HIy, BSy = D2x, H1x, HIx, BSx
     I = sp.identity(n, format="csr")
     e1 = _e(0, n)
@@ -528,8 +560,9 @@ class Hierarchy:
     (``matrix_free_mg_cg.jl:455``), coarse level solved by a sparse LU
     (``:460``, ``A_2h \\ f`` at :166)."""
 
-    def __init__(self, n: int, opts: MGOptions):
+    def __init__(self, n: int, opts: MGOptions, p: int = 2):
         self.opts = opts
+        self.p = p
         self.ns = [n]
         while self.ns[-1] > opts.coarse_n:
             nn = (self.ns[-1] + 1) // 2
@@ -538,7 +571,7 @@ class Hierarchy:
             self.ns.append(nn)
         if self.ns[-1] != opts.coarse_n and len(self.ns) > 1:
             raise ValueError(f"n={n} does not coarsen to coarse_n={opts.coarse_n}")
-        self.asm = [assemble(m) for m in self.ns]
+        self.asm = [assemble(m, p) for m in self.ns]
         self.A = [a.A for a in self.asm]
         self.diag = [A.diagonal() for A in self.A]
         self.R = [restriction_2d(m, opts.restriction) for m in self.ns[:-1]]

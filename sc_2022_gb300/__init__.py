@@ -7,7 +7,8 @@ matrix_free_prolongation_2d_GPU.
 from . import _lib
 from ._lib import SbpError
 from .adjoint import HMisfit, PoissonSolve, mgcg_rrule
-from .high_order import CG_p4_GPU, matrix_free_A_p4_GPU
+from .high_order import (CG_high_order_GPU, CG_p4_GPU, HighOrderSolver, MGCG_high_order_GPU,
+                         matrix_free_A_high_order_GPU, matrix_free_A_p4_GPU)
 from .matrix_free import (CG_Matrix_Free_GPU_v2, CG_full_GPU, initial_guess_interpolation_CG_GPU,
                           initial_guess_interpolation_three_level_CG_GPU, jacobi,
                           matrix_free_A_full_GPU,
@@ -25,6 +26,7 @@ __all__ = [
     "reference_two_level_options", "SbpError", "load_library", "HMisfit", "PoissonSolve",
     "mgcg_rrule", "BatchSolver", "initial_guess_interpolation_CG_GPU",
     "initial_guess_interpolation_three_level_CG_GPU", "CG_p4_GPU", "matrix_free_A_p4_GPU",
+    "CG_high_order_GPU", "HighOrderSolver", "MGCG_high_order_GPU", "matrix_free_A_high_order_GPU",
 ]
 
 

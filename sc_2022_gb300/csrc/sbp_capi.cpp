@@ -14,24 +14,45 @@
 
 #include "../../include/sbpmg.h"
 #include "sbp_coarse.h"
+#include "sbp_host.h"
 #include "sbp_launch.h"
 
 using namespace sbp;
 
 namespace {
-
 thread_local std::string g_last_error;
+}  // namespace
+
+namespace sbp {
+
+void set_last_error(const std::string& msg) { g_last_error = msg; }
 
 int fail_cuda(cudaError_t e, const char* what) {
   g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
   return SBP_ERR_CUDA;
 }
 
-#define SBP_CUDA(call)                                     \
-  do {                                                     \
-    cudaError_t _e = (call);                               \
-    if (_e != cudaSuccess) return fail_cuda(_e, #call);    \
-  } while (0)
+int finish_result(const SolveState& fs, sbp_result* res) {
+  int status;
+  if (fs.done == kDoneConverged)
+    status = SBP_OK;
+  else if (fs.done == kDoneBreakdown)
+    status = SBP_ERR_BREAKDOWN;
+  else
+    status = SBP_ERR_MAXITER;
+  if (res) {
+    res->iters = fs.iter;
+    res->status = status;
+    res->initial_norm = std::sqrt(fs.rr0);
+    res->final_norm = std::sqrt(fs.rr);
+    res->threshold = std::sqrt(fs.thresh2);
+  }
+  return status;
+}
+
+}  // namespace sbp
+
+namespace {
 
 bool valid_mg_n(int n) {
   if (n < 3) return false;
@@ -346,24 +367,6 @@ cudaError_t enqueue_setup(sbp_solver* s, int kind, const double* b, double* x, i
 }
 
 // Status and result fields from a final solver state.
-int finish_result(const SolveState& fs, sbp_result* res) {
-  int status;
-  if (fs.done == kDoneConverged)
-    status = SBP_OK;
-  else if (fs.done == kDoneBreakdown)
-    status = SBP_ERR_BREAKDOWN;
-  else
-    status = SBP_ERR_MAXITER;
-  if (res) {
-    res->iters = fs.iter;
-    res->status = status;
-    res->initial_norm = std::sqrt(fs.rr0);
-    res->final_norm = std::sqrt(fs.rr);
-    res->threshold = std::sqrt(fs.thresh2);
-  }
-  return status;
-}
-
 // Shared driver of sbp_mgcg_solve (kind 0) and sbp_cg_solve (kind 1).
 int run_krylov(sbp_solver* s, int kind, const double* b, double* x, int sign, double abstol,
                double reltol, int maxiter, sbp_result* res, double* norms_out, int norms_cap,
@@ -610,78 +613,6 @@ int sbp_rhs_adjoint_f64(const double* lam, double* df, double* dgW, double* dgE,
   SBP_CUDA(launch_rhs_adjoint(cgrid<double>(lam, n), grid<double>(df, n), dgW, dgE, dgS, dgN, n,
                               fsign, (cudaStream_t)stream));
   return SBP_OK;
-}
-
-int sbp_apply_p4_f64(const double* u, double* out, int n, int sign, void* stream) {
-  if (!u || !out || n < 9 || (sign != 1 && sign != -1)) return SBP_ERR_ARGS;
-  SBP_CUDA(prepare_p4_tables());
-  ReduceBuf none{nullptr, nullptr};
-  SBP_CUDA(launch_apply_p4(cgrid<double>(u, n), grid<double>(out, n), n, sign, none, nullptr,
-                           nullptr, (cudaStream_t)stream));
-  return SBP_OK;
-}
-
-int sbp_cg_p4_solve(const double* b, double* x, int n, int sign, double abstol, double reltol,
-                    int maxiter, sbp_result* res, double* norms_out, int norms_cap,
-                    void* stream) {
-  if (!b || !x || n < 9 || (sign != 1 && sign != -1) || maxiter < 0) return SBP_ERR_ARGS;
-  if (abstol <= 0.0 && reltol <= 0.0) return SBP_ERR_ARGS;
-  cudaStream_t q = (cudaStream_t)stream;
-  SBP_CUDA(prepare_p4_tables());
-  const long long N = (long long)n * n;
-  const size_t vb = (size_t)N * sizeof(double);
-  const long long parts = max_reduce_ctas(n);
-  // r, p, Ap | norms | state | two reduction buffers (partials + ticket)
-  const size_t bytes = 3 * vb + (size_t)(maxiter + 1) * sizeof(double) + 256 +
-                       2 * ((size_t)parts * sizeof(double) + 256);
-  unsigned char* base = nullptr;
-  SBP_CUDA(cudaMallocAsync((void**)&base, bytes, q));
-  double* r = reinterpret_cast<double*>(base);
-  double* p = r + N;
-  double* Ap = p + N;
-  unsigned char* cur = reinterpret_cast<unsigned char*>(Ap + N);
-  double* norms = reinterpret_cast<double*>(cur);
-  cur += (size_t)(maxiter + 1) * sizeof(double);
-  cur = reinterpret_cast<unsigned char*>(((uintptr_t)cur + 255) & ~(uintptr_t)255);
-  SolveState* st = reinterpret_cast<SolveState*>(cur);
-  cur += 256;
-  ReduceBuf rbs[2];
-  for (auto& rb : rbs) {
-    rb.partials = reinterpret_cast<double*>(cur);
-    cur += (size_t)parts * sizeof(double);
-    rb.ticket = reinterpret_cast<unsigned*>(cur);
-    cur += 256;
-  }
-  struct Free {
-    void* p;
-    cudaStream_t q;
-    ~Free() { cudaFreeAsync(p, q); }
-  } guard{base, q};
-  for (auto& rb : rbs) SBP_CUDA(cudaMemsetAsync(rb.ticket, 0, sizeof(unsigned), q));
-  SBP_CUDA(launch_state_init(st, maxiter, q));
-  // r = sign A x, then r = b - r, p = r, state
-  SBP_CUDA(launch_apply_p4(cgrid<double>(x, n), grid<double>(r, n), n, sign, ReduceBuf{}, nullptr,
-                           nullptr, q));
-  SBP_CUDA(launch_cg_init_flat(b, r, p, N, st, norms, abstol, reltol, rbs[0], q));
-  SolveState hs{};
-  for (int k = 0; k <= maxiter + 1; ++k) {
-    SBP_CUDA(cudaMemcpyAsync(&hs, st, sizeof(SolveState), cudaMemcpyDeviceToHost, q));
-    SBP_CUDA(cudaStreamSynchronize(q));
-    if (hs.done) break;
-    SBP_CUDA(launch_apply_p4(cgrid<double>(p, n), grid<double>(Ap, n), n, sign, rbs[0], nullptr,
-                             st, q));
-    SBP_CUDA(launch_cg_update<double>(grid<double>(x, n), grid<double>(r, n), cgrid<double>(p, n),
-                                      cgrid<double>(Ap, n), Grid<float>{nullptr, n}, n, 1, st,
-                                      norms, rbs[1], q));
-    SBP_CUDA(launch_cg_dir_flat(r, p, N, st, q));
-  }
-  SBP_CUDA(cudaMemcpyAsync(&hs, st, sizeof(SolveState), cudaMemcpyDeviceToHost, q));
-  SBP_CUDA(cudaStreamSynchronize(q));
-  if (norms_out && norms_cap > 0) {
-    const int cnt = std::min(norms_cap, hs.iter + 1);
-    SBP_CUDA(cudaMemcpy(norms_out, norms, (size_t)cnt * sizeof(double), cudaMemcpyDeviceToHost));
-  }
-  return finish_result(hs, res);
 }
 
 int sbp_csr_spmv_f64(long long nrows, const long long* row_ptr, const int* col,

@@ -16,8 +16,9 @@
 #include <thread>
 #include <vector>
 
-#include "sbp_common.cuh"
 #include "sbp_coarse.h"
+#include "sbp_common.cuh"
+#include "sbp_high_order.cuh"
 
 namespace sbp {
 
@@ -133,14 +134,14 @@ void jacobi_eigen(int n, std::vector<double>& S, std::vector<double>& Q, std::ve
   for (int k = 0; k < n; ++k) lam[k] = s(k, k);
 }
 
-// Generalised eigenvectors of K v = l W v (K = -M, M row-major): V column-major
-// with V^T W V = I.
-void pencil_eigen(int n, const std::vector<double>& M, std::vector<double>& V,
-                  std::vector<double>& lam) {
+// Generalised eigenvectors of K v = l W v (K = -M, M row-major, W = diag(w)):
+// V column-major with V^T W V = I.
+void pencil_eigen(int n, const std::vector<double>& M, const std::vector<double>& w,
+                  std::vector<double>& V, std::vector<double>& lam) {
   std::vector<double> S((size_t)n * n);
   for (int r = 0; r < n; ++r)
     for (int c = 0; c < n; ++c)
-      S[(size_t)r * n + c] = -M[(size_t)r * n + c] / std::sqrt(weight(r, n) * weight(c, n));
+      S[(size_t)r * n + c] = -M[(size_t)r * n + c] / std::sqrt(w[r] * w[c]);
   // symmetrise exactly (the 1D operators are symmetric; guard the rounding)
   for (int r = 0; r < n; ++r)
     for (int c = r + 1; c < n; ++c) {
@@ -153,18 +154,53 @@ void pencil_eigen(int n, const std::vector<double>& M, std::vector<double>& V,
   jacobi_eigen(n, S, Q, lam);
   V.resize((size_t)n * n);
   for (int r = 0; r < n; ++r)
-    for (int c = 0; c < n; ++c) V[(size_t)c * n + r] = Q[(size_t)r * n + c] / std::sqrt(weight(r, n));
+    for (int c = 0; c < n; ++c) V[(size_t)c * n + r] = Q[(size_t)r * n + c] / std::sqrt(w[r]);
 }
 
-std::shared_ptr<const CoarseFactors> build_factors(int nc) {
-  std::vector<double> X, Y;
-  one_d_operators(nc, X, Y);
-  check_kronecker(nc, X, Y);
+// 1D operators and norm weights of order p (p = 4, 6: the closure tables of
+// sbp_high_order.cuh).
+template <int P>
+void one_d_high(int n, std::vector<double>& X, std::vector<double>& Y, std::vector<double>& w) {
+  X.assign((size_t)n * n, 0.0);
+  Y.assign((size_t)n * n, 0.0);
+  ho::one_d<P>(n, X.data(), Y.data());
+  w.resize(n);
+  for (int k = 0; k < n; ++k) w[k] = ho::weight<P>(k, n);
+}
+
+// (-A u) from the Kronecker form: w_j (X u(:, j))_i + w_i (Y u(i, :))_j.
+void kron_apply(int n, const std::vector<double>& X, const std::vector<double>& Y,
+                const std::vector<double>& w, const double* u, double* out) {
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) {
+      double xi = 0.0, yj = 0.0;
+      for (int k = 0; k < n; ++k) {
+        xi += X[(size_t)i * n + k] * u[(size_t)j * n + k];
+        yj += Y[(size_t)j * n + k] * u[(size_t)k * n + i];
+      }
+      out[(size_t)j * n + i] = w[j] * xi + w[i] * yj;
+    }
+}
+
+std::shared_ptr<const CoarseFactors> build_factors(int nc, int p) {
+  std::vector<double> X, Y, w;
+  if (p == 2) {
+    one_d_operators(nc, X, Y);
+    check_kronecker(nc, X, Y);
+    w.resize(nc);
+    for (int k = 0; k < nc; ++k) w[k] = weight(k, nc);
+  } else if (p == 4) {
+    one_d_high<4>(nc, X, Y, w);
+  } else if (p == 6) {
+    one_d_high<6>(nc, X, Y, w);
+  } else {
+    throw std::runtime_error("SBP order must be 2, 4 or 6");
+  }
   auto f = std::make_shared<CoarseFactors>();
   f->nc = nc;
   std::vector<double> lx, ly;
-  pencil_eigen(nc, X, f->Vx, lx);
-  pencil_eigen(nc, Y, f->Vy, ly);
+  pencil_eigen(nc, X, w, f->Vx, lx);
+  pencil_eigen(nc, Y, w, f->Vy, ly);
   const size_t N = (size_t)nc * nc;
   f->VxT.resize(N);
   f->VyT.resize(N);
@@ -185,13 +221,18 @@ std::shared_ptr<const CoarseFactors> build_factors(int nc) {
   for (size_t k = 0; k < N; ++k) b[k] = std::sin(0.37 * (double)k + 0.11) + 0.25;
   coarse_solve_host(*f, b.data(), x.data());
   double err = 0.0, nb = 0.0;
+  std::vector<double> kx;
+  if (p != 2) {   // the order-p stencil's own Kronecker form (p = 2: the kernels' negA)
+    kx.resize(N);
+    kron_apply(nc, X, Y, w, x.data(), kx.data());
+  }
   for (int j = 0; j < nc; ++j)
     for (int i = 0; i < nc; ++i) {
       struct G {
         const double* x; int i, j, n;
         double operator()(int di, int dj) const { return x[(size_t)(j + dj) * n + (i + di)]; }
       } g{x.data(), i, j, nc};
-      const double ax = -negA<double>(g, i, j, nc);
+      const double ax = p == 2 ? -negA<double>(g, i, j, nc) : -kx[(size_t)j * nc + i];
       err = std::max(err, std::fabs(ax - b[(size_t)j * nc + i]));
       nb = std::max(nb, std::fabs(b[(size_t)j * nc + i]));
     }
@@ -232,16 +273,21 @@ void coarse_solve_host(const CoarseFactors& f, const double* b, double* x) {
     }
 }
 
-std::shared_ptr<const CoarseFactors> coarse_factors(int nc) {
-  if (nc < 3 || nc > 257) throw std::runtime_error("coarse size out of range");
+std::shared_ptr<const CoarseFactors> coarse_factors(int nc, int p) {
+  const int lo = p == 2 ? 3 : ho_min_points(p);
+  if (lo == 0 || nc < lo || nc > 257) throw std::runtime_error("coarse size out of range");
   static std::mutex mu;
-  static std::map<int, std::shared_ptr<const CoarseFactors>> cache;
+  static std::map<std::pair<int, int>, std::shared_ptr<const CoarseFactors>> cache;
   std::lock_guard<std::mutex> lock(mu);
-  auto it = cache.find(nc);
+  auto it = cache.find({nc, p});
   if (it != cache.end()) return it->second;
-  auto f = build_factors(nc);
-  cache[nc] = f;
+  auto f = build_factors(nc, p);
+  cache[{nc, p}] = f;
   return f;
+}
+
+int ho_min_points(int p) {
+  return p == 4 ? ho::Order<4>::kMinN : (p == 6 ? ho::Order<6>::kMinN : 0);
 }
 
 std::shared_ptr<const std::vector<double>> coarse_inverse(int nc) {

@@ -22,10 +22,14 @@ struct CoarseFactors {
   std::vector<double> dinv;  // 1 / (lx_i + ly_j) at i + j * nc
 };
 
-// Factors of the coarse operator on an nc x nc grid (3 <= nc <= 257).  The
-// Kronecker structure is checked against the operator's own stencil
+// Factors of the coarse operator of SBP order p (2, 4 or 6) on an nc x nc
+// grid (nc <= 257 and at least 3 for p = 2, ho_min_points(p) otherwise).  For
+// p = 2 the Kronecker structure is checked against the kernels' own stencil
 // coefficients.  Throws std::runtime_error on failure.
-std::shared_ptr<const CoarseFactors> coarse_factors(int nc);
+std::shared_ptr<const CoarseFactors> coarse_factors(int nc, int p = 2);
+
+// Smallest grid of the order-p operator (p = 4, 6; 0 otherwise).
+int ho_min_points(int p);
 
 // x = A^{-1} b on the host with the factors (column-major nc x nc grids).
 void coarse_solve_host(const CoarseFactors& f, const double* b, double* x);

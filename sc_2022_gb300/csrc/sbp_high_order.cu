@@ -1,0 +1,270 @@
+// Higher-order (p = 4, 6) SBP-SAT kernels, FP64, on contiguous n x n grids.
+//
+// One kernel template covers the operator's three uses:
+// - the apply (out = sign * A u, optionally u . out into the Krylov state);
+// - the residual (out = b - A u, optionally ||out||^2);
+// - a weighted-Jacobi sweep (out = u + omega D^-1 (b - A u)).
+// The reference builds these operators only as assembled CPU matrices
+// (Operators_2d / Assembling_matrix with p = 4, 6,
+// level_2_multigrid_new.jl:48-188) and smooths with weighted Jacobi in its
+// CPU multigrid preconditioner (precond_matrix, initial_guess_cg.jl:458-510).
+//
+// Access pattern: each thread owns a row i and marches along j over a run of
+// columns, keeping the 2R+1 columns of its own row that the j-direction
+// stencil needs in registers.  The i-neighbours come from the cache: a warp
+// covers 32 consecutive rows of a column, so those loads are coalesced.
+// Boundary rows and columns (the first and last bm) apply the bm x bn closure
+// tables from constant memory.
+#include <algorithm>
+#include <mutex>
+
+#include "sbp_high_order.cuh"
+#include "sbp_kernels.cuh"
+#include "sbp_launch.h"
+
+namespace sbp {
+
+namespace {
+
+__constant__ double c_ho4[2][4 * 6];   // [X | Y][r * bn + c]
+__constant__ double c_ho6[2][6 * 9];
+
+template <int P>
+__device__ __forceinline__ const double* tab(int which);
+template <>
+__device__ __forceinline__ const double* tab<4>(int which) {
+  return c_ho4[which];
+}
+template <>
+__device__ __forceinline__ const double* tab<6>(int which) {
+  return c_ho6[which];
+}
+
+template <int P, int MODE, bool DOT>
+__global__ void __launch_bounds__(kThreads) k_ho(const HoArgs a) {
+  using O = ho::Order<P>;
+  constexpr int R = O::kHalf, W = 2 * R + 1, BM = O::kBm, BN = O::kBn;
+  // interior A diagonal is -2 d(0); its reciprocal needs no division
+  constexpr double kInvDiagIn = -0.5 / O::d(0);
+  pdl_begin();
+  if (a.st && a.st->done) return;
+  const int n = a.n;
+  const int cols = a.cols;
+  const int nrb = (n + kThreads - 1) / kThreads;
+  const int items = nrb * ((n + cols - 1) / cols);
+  const double* __restrict__ u = a.u;
+  const double* __restrict__ b = a.b;
+  double* __restrict__ out = a.out;
+  const double* tx = tab<P>(0);
+  const double* ty = tab<P>(1);
+  DotAcc<double> acc;
+  for (int w = blockIdx.x; w < items; w += gridDim.x) {
+    const int i = (w % nrb) * kThreads + threadIdx.x;
+    if (i >= n) continue;
+    const int j0 = (w / nrb) * cols;
+    const int j1 = min(n, j0 + cols);
+    const double wi = ho::weight<P>(i, n);
+    const bool xin = i >= BM && i <= n - 1 - BM;
+    const bool xlo = i < BM;
+    const int xr = xlo ? i : n - 1 - i;   // closure row when !xin
+    const double dxx = xin ? O::d(0) : tx[xr * BN + xr];
+    if (MODE == kHoJacobi && a.zero_in) {
+      // first sweep from v = 0: out = omega D^-1 b
+      for (int j = j0; j < j1; ++j) {
+        const bool yin = j >= BM && j <= n - 1 - BM;
+        const int yr = j < BM ? j : n - 1 - j;
+        const double dyy = yin ? O::d(0) : ty[yr * BN + yr];
+        const double inv = a.richardson ? 1.0
+                           : (xin && yin) ? kInvDiagIn
+                                          : -1.0 / (ho::weight<P>(j, n) * dxx + wi * dyy);
+        out[(size_t)j * n + i] = a.omega * __ldg(b + (size_t)j * n + i) * inv;
+      }
+      continue;
+    }
+    const double* row = u + i;
+    auto at = [&](int ii, int jj) { return __ldg(u + (size_t)jj * n + ii); };
+    auto col = [&](int jj) { return (jj >= 0 && jj < n) ? __ldg(row + (size_t)jj * n) : 0.0; };
+    double c[W];
+#pragma unroll
+    for (int k = 0; k < W - 1; ++k) c[k] = col(j0 - R + k);
+    for (int j = j0; j < j1; ++j) {
+      c[W - 1] = col(j + R);
+      double xi;
+      if (xin) {
+        xi = O::d(0) * c[R];
+#pragma unroll
+        for (int k = 1; k <= R; ++k) xi = fma(O::d(k), at(i - k, j) + at(i + k, j), xi);
+      } else {
+        xi = 0.0;
+#pragma unroll
+        for (int q = 0; q < BN; ++q) xi = fma(tx[xr * BN + q], at(xlo ? q : n - 1 - q, j), xi);
+      }
+      const bool yin = j >= BM && j <= n - 1 - BM;
+      const bool ylo = j < BM;
+      const int yr = ylo ? j : n - 1 - j;
+      double yj;
+      if (yin) {
+        yj = O::d(0) * c[R];
+#pragma unroll
+        for (int k = 1; k <= R; ++k) yj = fma(O::d(k), c[R - k] + c[R + k], yj);
+      } else {
+        yj = 0.0;
+#pragma unroll
+        for (int q = 0; q < BN; ++q) yj = fma(ty[yr * BN + q], col(ylo ? q : n - 1 - q), yj);
+      }
+      const double wj = ho::weight<P>(j, n);
+      const double na = fma(wj, xi, wi * yj);   // (-A u)(i, j)
+      double v;
+      if (MODE == kHoApply) {
+        v = a.sign > 0 ? -na : na;
+      } else if (MODE == kHoResid) {
+        v = __ldg(b + (size_t)j * n + i) + (a.sign > 0 ? na : -na);
+      } else {
+        double inv = 1.0;
+        if (!a.richardson) {
+          const double dyy = yin ? O::d(0) : ty[yr * BN + yr];
+          inv = (xin && yin) ? kInvDiagIn : -1.0 / (wj * dxx + wi * dyy);
+        }
+        v = fma(a.omega * inv, __ldg(b + (size_t)j * n + i) + na, c[R]);
+      }
+      out[(size_t)j * n + i] = v;
+      if (DOT) acc.add_prod(MODE == kHoApply ? c[R] : v, v);
+#pragma unroll
+      for (int k = 0; k < W - 1; ++k) c[k] = c[k + 1];
+    }
+  }
+  if (DOT)
+    grid_reduce(acc.value(), a.rb, [&](double tot) {
+      if (a.dot_out) *a.dot_out = tot;
+      SolveState* st = a.st;
+      if (!st) return;
+      if (MODE == kHoApply) {   // CG: p.Ap -> alpha
+        st->pAp = tot;
+        if (!isfinite(tot) || tot == 0.0)
+          st->done = kDoneBreakdown;
+        else
+          st->alpha = st->rz / tot;
+      } else if (MODE == kHoResid && a.init) {   // Krylov set-up from ||r0||^2
+        st->rr0 = st->rr = tot;
+        st->rz = tot;
+        st->thresh2 = a.abstol > 0.0 ? a.abstol * a.abstol : a.reltol * a.reltol * tot;
+        st->iter = 0;
+        if (a.norms) a.norms[0] = sqrt(tot);
+        if (!isfinite(tot))
+          st->done = kDoneBreakdown;
+        else if (tot < st->thresh2 || tot == 0.0)
+          st->done = kDoneConverged;
+        else if (st->maxiter <= 0)
+          st->done = kDoneMaxIter;
+      }
+    });
+}
+
+// r.z into the Krylov state: beta = rz_new / rz (0 on the first direction).
+__global__ void __launch_bounds__(kThreads)
+    k_ho_rz(const double* __restrict__ r, const double* __restrict__ z, long long N,
+            SolveState* st, ReduceBuf rb, int first) {
+  pdl_begin();
+  if (st->done) return;
+  double acc = 0.0;
+  for (long long k = (long long)blockIdx.x * kThreads + threadIdx.x; k < N;
+       k += (long long)gridDim.x * kThreads)
+    acc = fma(__ldg(r + k), __ldg(z + k), acc);
+  grid_reduce(acc, rb, [&](double tot) {
+    st->beta = first ? 0.0 : tot / st->rz;
+    st->rz = tot;
+    if (!isfinite(tot) || tot <= 0.0) st->done = kDoneBreakdown;
+  });
+}
+
+// p = z + beta p (p = z on the first direction).
+__global__ void __launch_bounds__(kThreads)
+    k_ho_dir(const double* __restrict__ z, double* __restrict__ p, long long N,
+             const SolveState* st, int first) {
+  pdl_begin();
+  if (st->done) return;
+  const double beta = st->beta;
+  for (long long k = (long long)blockIdx.x * kThreads + threadIdx.x; k < N;
+       k += (long long)gridDim.x * kThreads)
+    p[k] = first ? __ldg(z + k) : fma(beta, p[k], __ldg(z + k));
+}
+
+int flat_ctas(long long N) {
+  const long long want = (N + (long long)kThreads * 4 - 1) / ((long long)kThreads * 4);
+  return (int)std::max(1LL, std::min<long long>(want, kMaxPersistCtas));
+}
+
+template <int P>
+void fill_tables(double* x, double* y) {
+  using O = ho::Order<P>;
+  for (int r = 0; r < O::kBm; ++r)
+    for (int c = 0; c < O::kBn; ++c) {
+      x[r * O::kBn + c] = ho::x_coef<P>(r, c);
+      y[r * O::kBn + c] = ho::y_coef<P>(r, c);
+    }
+}
+
+template <int P, int MODE>
+cudaError_t launch_mode(const HoArgs& a, dim3 grid, cudaStream_t s) {
+  if (a.rb.partials)
+    return launch_pdl(k_ho<P, MODE, true>, grid, dim3(kThreads), 0, s, a);
+  return launch_pdl(k_ho<P, MODE, false>, grid, dim3(kThreads), 0, s, a);
+}
+
+template <int P>
+cudaError_t launch_order(int mode, const HoArgs& a, dim3 grid, cudaStream_t s) {
+  switch (mode) {
+    case kHoApply: return launch_mode<P, kHoApply>(a, grid, s);
+    case kHoResid: return launch_mode<P, kHoResid>(a, grid, s);
+    case kHoJacobi: return launch_mode<P, kHoJacobi>(a, grid, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace
+
+int ho_min_n(int p) {
+  return p == 4 ? ho::Order<4>::kMinN : (p == 6 ? ho::Order<6>::kMinN : 0);
+}
+
+cudaError_t prepare_ho_tables() {
+  static std::once_flag once;
+  static cudaError_t err = cudaSuccess;
+  std::call_once(once, [] {
+    double t4[2][4 * 6], t6[2][6 * 9];
+    fill_tables<4>(t4[0], t4[1]);
+    fill_tables<6>(t6[0], t6[1]);
+    err = cudaMemcpyToSymbol(c_ho4, t4, sizeof(t4));
+    if (err == cudaSuccess) err = cudaMemcpyToSymbol(c_ho6, t6, sizeof(t6));
+  });
+  return err;
+}
+
+int ho_cols(int n) {
+  // columns per work item: enough items to fill the GPU on small grids,
+  // long column runs (fewer window refills) on large ones
+  const long long nrb = (n + kThreads - 1) / kThreads;
+  const long long c = (long long)n * nrb / (2LL * 152);
+  return (int)std::max(1LL, std::min(32LL, c));
+}
+
+cudaError_t launch_ho(int p, int mode, HoArgs a, cudaStream_t s) {
+  if (ho_min_n(p) == 0 || a.n < ho_min_n(p) || !a.out) return cudaErrorInvalidValue;
+  if (a.cols <= 0) a.cols = ho_cols(a.n);
+  const long long nrb = (a.n + kThreads - 1) / kThreads;
+  const long long items = nrb * ((a.n + a.cols - 1) / a.cols);
+  const dim3 grid((unsigned)std::min<long long>(items, kMaxPersistCtas));
+  return p == 4 ? launch_order<4>(mode, a, grid, s) : launch_order<6>(mode, a, grid, s);
+}
+
+cudaError_t launch_ho_rz(const double* r, const double* z, long long N, SolveState* st,
+                         ReduceBuf rb, int first, cudaStream_t s) {
+  return launch_pdl(k_ho_rz, dim3(flat_ctas(N)), dim3(kThreads), 0, s, r, z, N, st, rb, first);
+}
+
+cudaError_t launch_ho_dir(const double* z, double* p, long long N, const SolveState* st,
+                          int first, cudaStream_t s) {
+  return launch_pdl(k_ho_dir, dim3(flat_ctas(N)), dim3(kThreads), 0, s, z, p, N, st, first);
+}
+
+}  // namespace sbp

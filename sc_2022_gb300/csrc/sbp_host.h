@@ -1,0 +1,26 @@
+// Host-side helpers shared by the C-ABI translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "../../include/sbpmg.h"
+#include "sbp_common.cuh"
+
+namespace sbp {
+
+// The message sbp_last_error() returns on this thread.
+void set_last_error(const std::string& msg);
+// Record "what: <CUDA error string>" and return SBP_ERR_CUDA.
+int fail_cuda(cudaError_t e, const char* what);
+// sbp_result and status code from a finished Krylov state.
+int finish_result(const SolveState& fs, sbp_result* res);
+
+}  // namespace sbp
+
+#define SBP_CUDA(call)                                          \
+  do {                                                          \
+    cudaError_t _e = (call);                                    \
+    if (_e != cudaSuccess) return ::sbp::fail_cuda(_e, #call);  \
+  } while (0)

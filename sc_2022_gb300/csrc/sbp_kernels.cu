@@ -11,7 +11,6 @@
 #include <utility>
 
 #include "sbp_kernels.cuh"
-#include "sbp_p4.cuh"
 #include "sbp_launch.h"
 #include "sbp_tma.h"
 
@@ -59,23 +58,6 @@ static inline int flat_grid(long long N, int per) {
 int max_reduce_ctas(int n) {
   const dim3 g = tile_grid(n);
   return std::max((int)(g.x * g.y), kMaxPersistCtas);
-}
-
-// Launch with programmatic dependent launch enabled (see pdl_begin()).
-template <typename... KArgs, typename... Args>
-static cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
-                              cudaStream_t s, Args&&... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
 static int sm_count() {
@@ -2364,170 +2346,6 @@ cudaError_t launch_csr_spmv(long long nrows, const long long* row_ptr, const int
   const int grid = (int)std::min<long long>(blocks, (long long)sm_count() * 8);
   k_csr_spmv<<<std::max(grid, 1), kThreads, 0, s>>>(nrows, row_ptr, col, val, x, y);
   return cudaGetLastError();
-}
-
-// ---------------------------------------------------------------------------
-// Fourth-order (p = 4) operator, FP64, on any layout (the caller's arrays):
-// out = sign * A u (+ u . out), the same row-per-thread column march as
-// k_apply_direct with a five-column register window; the boundary closures
-// (first and last four rows / columns) read their six taps from the tables
-// of sbp_p4.cuh.
-// ---------------------------------------------------------------------------
-__constant__ double c_p4_x[4][6];
-__constant__ double c_p4_y[4][6];
-
-__device__ __forceinline__ double p4_w(int k, int n) {
-  return k < 4 ? p4::w_end(k) : (k > n - 5 ? p4::w_end(n - 1 - k) : 1.0);
-}
-
-template <bool DOT>
-__global__ void __launch_bounds__(kThreads)
-    k_apply_p4(Grid<const double> u, Grid<double> out, int n, int sign, ReduceBuf rb,
-               double* dot_out, SolveState* st) {
-  pdl_begin();
-  if (st && st->done) return;
-  const int nrb = (n + kThreads - 1) / kThreads;
-  const int items = nrb * ((n + kApplyCols - 1) / kApplyCols);
-  const size_t ld = (size_t)u.ld;
-  DotAcc<double> acc;
-  for (int w = blockIdx.x; w < items; w += gridDim.x) {
-    const int i = (w % nrb) * kThreads + threadIdx.x;
-    if (i >= n) continue;
-    const int j0 = (w / nrb) * kApplyCols;
-    const int j1 = min(n, j0 + kApplyCols);
-    const double* row = u.p + i;                       // u(i, j) = row[j * ld]
-    auto at = [&](int ii, int jj) { return __ldg(u.p + (size_t)jj * ld + ii); };
-    auto col = [&](int jj) { return (jj >= 0 && jj < n) ? __ldg(row + (size_t)jj * ld) : 0.0; };
-    double c0 = col(j0 - 2), c1 = col(j0 - 1), c2 = col(j0), c3 = col(j0 + 1);
-    const double wi = p4_w(i, n);
-    for (int j = j0; j < j1; ++j) {
-      const double c4 = col(j + 2);
-      // along i (X): interior d, closures from the table
-      double xi;
-      if (i >= 4 && i <= n - 5) {
-        xi = fma(p4::kD0, at(i - 2, j) + at(i + 2, j),
-                 fma(p4::kD1, at(i - 1, j) + at(i + 1, j), p4::kD2 * c2));
-      } else {
-        const bool lo = i < 4;
-        const int r = lo ? i : n - 1 - i;
-        xi = 0.0;
-#pragma unroll
-        for (int c = 0; c < 6; ++c) xi = fma(c_p4_x[r][c], at(lo ? c : n - 1 - c, j), xi);
-      }
-      // along j (Y): interior d on the register window, closures from the table
-      double yj;
-      if (j >= 4 && j <= n - 5) {
-        yj = fma(p4::kD0, c0 + c4, fma(p4::kD1, c1 + c3, p4::kD2 * c2));
-      } else {
-        const bool lo = j < 4;
-        const int r = lo ? j : n - 1 - j;
-        yj = 0.0;
-#pragma unroll
-        for (int c = 0; c < 6; ++c) yj = fma(c_p4_y[r][c], col(lo ? c : n - 1 - c), yj);
-      }
-      const double na = fma(p4_w(j, n), xi, wi * yj);   // (-A u)(i, j)
-      const double v = sign > 0 ? -na : na;
-      out.at(i, j) = v;
-      if (DOT) acc.add_prod(c2, v);
-      c0 = c1;
-      c1 = c2;
-      c2 = c3;
-      c3 = c4;
-    }
-  }
-  if (DOT)
-    grid_reduce(acc.value(), rb, [&](double tot) {
-      if (dot_out) *dot_out = tot;
-      if (st) {   // CG: p.Ap -> alpha
-        st->pAp = tot;
-        if (!isfinite(tot) || tot == 0.0)
-          st->done = kDoneBreakdown;
-        else
-          st->alpha = st->rz / tot;
-      }
-    });
-}
-
-// CG set-up on flat arrays: r = b - Ax (Ax = sign A x already in r), p = r,
-// ||r||^2 and the Krylov state (plain CG: r.z = r.r).
-__global__ void __launch_bounds__(kThreads)
-    k_cg_init_flat(const double* __restrict__ b, double* __restrict__ r, double* __restrict__ p,
-                   long long N, SolveState* st, double* norms, double abstol, double reltol,
-                   ReduceBuf rb) {
-  pdl_begin();
-  double acc = 0.0;
-  for (long long k = (long long)blockIdx.x * kThreads + threadIdx.x; k < N;
-       k += (long long)gridDim.x * kThreads) {
-    const double rv = __ldg(b + k) - r[k];
-    r[k] = rv;
-    p[k] = rv;
-    acc = fma(rv, rv, acc);
-  }
-  grid_reduce(acc, rb, [&](double tot) {
-    st->rr0 = st->rr = st->rz = tot;
-    st->thresh2 = abstol > 0.0 ? abstol * abstol : reltol * reltol * tot;
-    st->iter = 0;
-    if (norms) norms[0] = sqrt(tot);
-    if (!isfinite(tot))
-      st->done = kDoneBreakdown;
-    else if (tot < st->thresh2 || tot == 0.0)
-      st->done = kDoneConverged;
-    else if (st->maxiter <= 0)
-      st->done = kDoneMaxIter;
-  });
-}
-
-// p = r + beta p on flat arrays (beta from the state)
-__global__ void __launch_bounds__(kThreads)
-    k_cg_dir_flat(const double* __restrict__ r, double* __restrict__ p, long long N,
-                  const SolveState* st) {
-  pdl_begin();
-  if (st->done) return;
-  const double beta = st->beta;
-  for (long long k = (long long)blockIdx.x * kThreads + threadIdx.x; k < N;
-       k += (long long)gridDim.x * kThreads)
-    p[k] = fma(beta, p[k], __ldg(r + k));
-}
-
-cudaError_t launch_cg_init_flat(const double* b, double* r, double* p, long long N,
-                                SolveState* st, double* norms, double abstol, double reltol,
-                                ReduceBuf rb, cudaStream_t s) {
-  return launch_pdl(k_cg_init_flat, dim3(flat_grid(N, 2)), dim3(kThreads), 0, s, b, r, p, N, st,
-                    norms, abstol, reltol, rb);
-}
-
-cudaError_t launch_cg_dir_flat(const double* r, double* p, long long N, const SolveState* st,
-                               cudaStream_t s) {
-  return launch_pdl(k_cg_dir_flat, dim3(flat_grid(N, 4)), dim3(kThreads), 0, s, r, p, N, st);
-}
-
-cudaError_t prepare_p4_tables() {
-  static std::once_flag once;
-  static cudaError_t err = cudaSuccess;
-  std::call_once(once, [] {
-    double x[4][6], y[4][6];
-    for (int r = 0; r < 4; ++r)
-      for (int c = 0; c < 6; ++c) {
-        x[r][c] = p4::x_coef(r, c);
-        y[r][c] = p4::y_coef(r, c);
-      }
-    err = cudaMemcpyToSymbol(c_p4_x, x, sizeof(x));
-    if (err == cudaSuccess) err = cudaMemcpyToSymbol(c_p4_y, y, sizeof(y));
-  });
-  return err;
-}
-
-cudaError_t launch_apply_p4(Grid<const double> u, Grid<double> out, int n, int sign, ReduceBuf rb,
-                            double* dot_out, SolveState* st, cudaStream_t s) {
-  if (n < p4::kMinN) return cudaErrorInvalidValue;
-  const long long items = (long long)((n + kThreads - 1) / kThreads) *
-                          ((n + kApplyCols - 1) / kApplyCols);
-  const int grid = (int)std::min<long long>(items, kMaxPersistCtas);
-  if (dot_out || st)
-    return launch_pdl(k_apply_p4<true>, dim3(grid), dim3(kThreads), 0, s, u, out, n, sign, rb,
-                      dot_out, st);
-  return launch_pdl(k_apply_p4<false>, dim3(grid), dim3(kThreads), 0, s, u, out, n, sign, rb,
-                    dot_out, st);
 }
 
 // g = H~ (u - ut) and *loss = 1/2 (u - ut)' H~ (u - ut), H~ = h^2 diag(w_i w_j)

@@ -1,5 +1,6 @@
-// Kernel templates for the SBP-SAT Poisson path.  Included by sbp_kernels.cu
-// only; the launch wrappers declared in sbp_launch.h are the interface.
+// Kernel templates for the SBP-SAT Poisson path.  Included by the kernel
+// translation units (sbp_kernels.cu, sbp_high_order.cu); the launch wrappers
+// declared in sbp_launch.h are the interface.
 //
 // Design (GB300, HBM-bound stencil, no tensor cores):
 //  * Every stencil kernel works on 2D tiles of the column-major grid.  A CTA
@@ -20,6 +21,8 @@
 #pragma once
 
 #include <cuda.h>
+
+#include <utility>
 
 #include "sbp_common.cuh"
 
@@ -138,9 +141,10 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned 
 }
 
 // Set (never cleared by the kernels) when a bounded wait gives up; read by
-// the host through read_device_fault().  This header is included by one
-// translation unit only (sbp_kernels.cu), which owns the definition.
-__device__ unsigned int g_sbp_fault = 0u;
+// the host through read_device_fault().  Internal linkage: each translation
+// unit that includes this header has its own copy; the kernels with bounded
+// waits all live in sbp_kernels.cu, whose copy read_device_fault() reads.
+static __device__ unsigned int g_sbp_fault = 0u;
 
 // Bounded wait on an mbarrier phase.  try_wait suspends for a bounded,
 // hardware-defined time per call, so the limit is seconds: far beyond any
@@ -163,6 +167,23 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsig
 __device__ __forceinline__ void pdl_begin() {
   asm volatile("griddepcontrol.wait;\n" ::: "memory");
   asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+
+// Launch with programmatic dependent launch enabled (see pdl_begin()).
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                              cudaStream_t s, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
 // ---------------------------------------------------------------------------

@@ -207,21 +207,36 @@ int batch_sm_count();
 // dst (ld dld) = src (ld sld) on an n x n FP64 grid; recordable.
 cudaError_t copy_grid(double* dst, int dld, const double* src, int sld, int n, cudaStream_t s);
 
-// Fourth-order operator: out = sign * A u (+ *dot_out = u . out), FP64, any
-// leading dimension; n >= 9.  prepare_p4_tables() uploads the closure
-// coefficients once (outside stream capture).
-cudaError_t prepare_p4_tables();
-// With st (CG), the reduction sets p.Ap and alpha; the kernel exits at once
-// when the state is done.
-cudaError_t launch_apply_p4(Grid<const double> u, Grid<double> out, int n, int sign, ReduceBuf rb,
-                            double* dot_out, SolveState* st, cudaStream_t s);
-// Plain-CG pieces on flat arrays of N entries: set-up (r = b - r, p = r, state)
-// and the direction p = r + beta p.
-cudaError_t launch_cg_init_flat(const double* b, double* r, double* p, long long N,
-                                SolveState* st, double* norms, double abstol, double reltol,
-                                ReduceBuf rb, cudaStream_t s);
-cudaError_t launch_cg_dir_flat(const double* r, double* p, long long N, const SolveState* st,
-                               cudaStream_t s);
+
+// ---- higher-order (p = 4, 6) operators, FP64, contiguous n x n grids ----
+enum { kHoApply = 0, kHoResid = 1, kHoJacobi = 2 };
+struct HoArgs {
+  const double* u;     // operator input (unused by a Jacobi sweep with zero_in)
+  const double* b;     // right-hand side (residual, Jacobi)
+  double* out;
+  int n;
+  int sign;            // apply: out = sign * A u; residual: out = b - sign * A u
+  double omega;        // smoother weight
+  int richardson;      // smoother: out = u + omega (b - A u) instead of Jacobi
+  int zero_in;         // smoother from u = 0: out = omega D^-1 b
+  int cols;            // columns per work item (0: chosen by the launcher)
+  ReduceBuf rb;        // non-null partials: reduce (apply: u . out, residual: ||out||^2)
+  double* dot_out;     // the reduction, if non-null
+  SolveState* st;      // kernels exit at once when st->done; apply: p.Ap -> alpha
+  int init;            // residual with st: set up the Krylov state from ||r0||^2
+  double abstol, reltol;
+  double* norms;       // init: norms[0] = ||r0||
+};
+// Smallest grid of order p (0 if p is not 4 or 6).
+int ho_min_n(int p);
+// Upload the closure tables once (outside stream capture).
+cudaError_t prepare_ho_tables();
+cudaError_t launch_ho(int p, int mode, HoArgs a, cudaStream_t s);
+// r.z -> beta (0 when first) and rz in the state; p = z + beta p (p = z when first).
+cudaError_t launch_ho_rz(const double* r, const double* z, long long N, SolveState* st,
+                         ReduceBuf rb, int first, cudaStream_t s);
+cudaError_t launch_ho_dir(const double* z, double* p, long long N, const SolveState* st,
+                          int first, cudaStream_t s);
 
 // y = A x for a CSR matrix with nrows rows (64-bit row pointers).
 cudaError_t launch_csr_spmv(long long nrows, const long long* row_ptr, const int* col,
