@@ -523,22 +523,23 @@ def run_part(args):
             out[f"p{p}_apply_us"] = round(1e3 * ms, 2)
             out[f"p{p}_apply_gbs"] = round(gbs, 1)
             out[f"p{p}_apply_frac_of_hbm"] = round(gbs / hbm, 3)
-            s = sbp.HighOrderSolver(n, p)
-            x = torch.zeros_like(us[0])
-            for _ in range(args.warmup):
-                x.zero_()
-                s.mgcg(us[0], x, reltol=1e-10, maxiter=200)
-            torch.cuda.synchronize()
-            e0.record()
-            for _ in range(args.steps):
-                x.zero_()
-                r = s.mgcg(us[0], x, reltol=1e-10, maxiter=200)
-            e1.record()
-            torch.cuda.synchronize()
-            out[f"p{p}_mgcg_ms"] = round(e0.elapsed_time(e1) / args.steps, 3)
-            out[f"p{p}_mgcg_iters"] = r.iters
-            out[f"p{p}_mgcg_converged"] = r.converged
-            s.close()
+            for tag, prec in (("fp64", _lib.SBP_PREC_FP64), ("mixed", _lib.SBP_PREC_MIXED)):
+                s = sbp.HighOrderSolver(n, p, sbp.default_options(prec))
+                x = torch.zeros_like(us[0])
+                for _ in range(args.warmup):
+                    x.zero_()
+                    s.mgcg(us[0], x, reltol=1e-10, maxiter=200)
+                torch.cuda.synchronize()
+                e0.record()
+                for _ in range(args.steps):
+                    x.zero_()
+                    r = s.mgcg(us[0], x, reltol=1e-10, maxiter=200)
+                e1.record()
+                torch.cuda.synchronize()
+                out[f"p{p}_mgcg_{tag}_ms"] = round(e0.elapsed_time(e1) / args.steps, 3)
+                out[f"p{p}_mgcg_{tag}_iters"] = r.iters
+                out[f"p{p}_mgcg_{tag}_converged"] = r.converged
+                s.close()
         print(json.dumps(out))
         return
     if args.mode == "vcycle":

@@ -28,104 +28,120 @@ namespace {
 
 __constant__ double c_ho4[2][4 * 6];   // [X | Y][r * bn + c]
 __constant__ double c_ho6[2][6 * 9];
+__constant__ float c_ho4f[2][4 * 6];   // the same, rounded to FP32
+__constant__ float c_ho6f[2][6 * 9];
 
-template <int P>
-__device__ __forceinline__ const double* tab(int which);
+template <int P, typename T>
+__device__ __forceinline__ const T* tab(int which);
 template <>
-__device__ __forceinline__ const double* tab<4>(int which) {
+__device__ __forceinline__ const double* tab<4, double>(int which) {
   return c_ho4[which];
 }
 template <>
-__device__ __forceinline__ const double* tab<6>(int which) {
+__device__ __forceinline__ const double* tab<6, double>(int which) {
   return c_ho6[which];
 }
+template <>
+__device__ __forceinline__ const float* tab<4, float>(int which) {
+  return c_ho4f[which];
+}
+template <>
+__device__ __forceinline__ const float* tab<6, float>(int which) {
+  return c_ho6f[which];
+}
 
-template <int P, int MODE, bool DOT>
-__global__ void __launch_bounds__(kThreads) k_ho(const HoArgs a) {
+__device__ __forceinline__ double fmaT(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fmaT(float a, float b, float c) { return fmaf(a, b, c); }
+
+template <int P, int MODE, bool DOT, typename T>
+__global__ void __launch_bounds__(kThreads) k_ho(const HoArgsT<T> a) {
   using O = ho::Order<P>;
   constexpr int R = O::kHalf, W = 2 * R + 1, BM = O::kBm, BN = O::kBn;
   // interior A diagonal is -2 d(0); its reciprocal needs no division
-  constexpr double kInvDiagIn = -0.5 / O::d(0);
+  constexpr T kInvDiagIn = T(-0.5 / O::d(0));
+  constexpr T kD0 = T(O::d(0)), kD1 = T(O::d(1)), kD2 = T(O::d(2)), kD3 = T(O::d(3 % (R + 1)));
+  auto dk = [](int k) { return k == 1 ? kD1 : (k == 2 ? kD2 : kD3); };
   pdl_begin();
   if (a.st && a.st->done) return;
   const int n = a.n;
   const int cols = a.cols;
   const int nrb = (n + kThreads - 1) / kThreads;
   const int items = nrb * ((n + cols - 1) / cols);
-  const double* __restrict__ u = a.u;
-  const double* __restrict__ b = a.b;
-  double* __restrict__ out = a.out;
-  const double* tx = tab<P>(0);
-  const double* ty = tab<P>(1);
-  DotAcc<double> acc;
+  const T* __restrict__ u = a.u;
+  const T* __restrict__ b = a.b;
+  T* __restrict__ out = a.out;
+  const T* tx = tab<P, T>(0);
+  const T* ty = tab<P, T>(1);
+  const T omega = T(a.omega);
+  DotAcc<T> acc;
   for (int w = blockIdx.x; w < items; w += gridDim.x) {
     const int i = (w % nrb) * kThreads + threadIdx.x;
     if (i >= n) continue;
     const int j0 = (w / nrb) * cols;
     const int j1 = min(n, j0 + cols);
-    const double wi = ho::weight<P>(i, n);
+    const T wi = T(ho::weight<P>(i, n));
     const bool xin = i >= BM && i <= n - 1 - BM;
     const bool xlo = i < BM;
     const int xr = xlo ? i : n - 1 - i;   // closure row when !xin
-    const double dxx = xin ? O::d(0) : tx[xr * BN + xr];
+    const T dxx = xin ? kD0 : tx[xr * BN + xr];
     if (MODE == kHoJacobi && a.zero_in) {
       // first sweep from v = 0: out = omega D^-1 b
       for (int j = j0; j < j1; ++j) {
         const bool yin = j >= BM && j <= n - 1 - BM;
         const int yr = j < BM ? j : n - 1 - j;
-        const double dyy = yin ? O::d(0) : ty[yr * BN + yr];
-        const double inv = a.richardson ? 1.0
-                           : (xin && yin) ? kInvDiagIn
-                                          : -1.0 / (ho::weight<P>(j, n) * dxx + wi * dyy);
-        out[(size_t)j * n + i] = a.omega * __ldg(b + (size_t)j * n + i) * inv;
+        const T dyy = yin ? kD0 : ty[yr * BN + yr];
+        const T inv = a.richardson ? T(1)
+                      : (xin && yin) ? kInvDiagIn
+                                     : T(-1) / (T(ho::weight<P>(j, n)) * dxx + wi * dyy);
+        out[(size_t)j * n + i] = omega * __ldg(b + (size_t)j * n + i) * inv;
       }
       continue;
     }
-    const double* row = u + i;
+    const T* row = u + i;
     auto at = [&](int ii, int jj) { return __ldg(u + (size_t)jj * n + ii); };
-    auto col = [&](int jj) { return (jj >= 0 && jj < n) ? __ldg(row + (size_t)jj * n) : 0.0; };
-    double c[W];
+    auto col = [&](int jj) { return (jj >= 0 && jj < n) ? __ldg(row + (size_t)jj * n) : T(0); };
+    T c[W];
 #pragma unroll
     for (int k = 0; k < W - 1; ++k) c[k] = col(j0 - R + k);
     for (int j = j0; j < j1; ++j) {
       c[W - 1] = col(j + R);
-      double xi;
+      T xi;
       if (xin) {
-        xi = O::d(0) * c[R];
+        xi = kD0 * c[R];
 #pragma unroll
-        for (int k = 1; k <= R; ++k) xi = fma(O::d(k), at(i - k, j) + at(i + k, j), xi);
+        for (int k = 1; k <= R; ++k) xi = fmaT(dk(k), at(i - k, j) + at(i + k, j), xi);
       } else {
-        xi = 0.0;
+        xi = T(0);
 #pragma unroll
-        for (int q = 0; q < BN; ++q) xi = fma(tx[xr * BN + q], at(xlo ? q : n - 1 - q, j), xi);
+        for (int q = 0; q < BN; ++q) xi = fmaT(tx[xr * BN + q], at(xlo ? q : n - 1 - q, j), xi);
       }
       const bool yin = j >= BM && j <= n - 1 - BM;
       const bool ylo = j < BM;
       const int yr = ylo ? j : n - 1 - j;
-      double yj;
+      T yj;
       if (yin) {
-        yj = O::d(0) * c[R];
+        yj = kD0 * c[R];
 #pragma unroll
-        for (int k = 1; k <= R; ++k) yj = fma(O::d(k), c[R - k] + c[R + k], yj);
+        for (int k = 1; k <= R; ++k) yj = fmaT(dk(k), c[R - k] + c[R + k], yj);
       } else {
-        yj = 0.0;
+        yj = T(0);
 #pragma unroll
-        for (int q = 0; q < BN; ++q) yj = fma(ty[yr * BN + q], col(ylo ? q : n - 1 - q), yj);
+        for (int q = 0; q < BN; ++q) yj = fmaT(ty[yr * BN + q], col(ylo ? q : n - 1 - q), yj);
       }
-      const double wj = ho::weight<P>(j, n);
-      const double na = fma(wj, xi, wi * yj);   // (-A u)(i, j)
-      double v;
+      const T wj = T(ho::weight<P>(j, n));
+      const T na = fmaT(wj, xi, wi * yj);   // (-A u)(i, j)
+      T v;
       if (MODE == kHoApply) {
         v = a.sign > 0 ? -na : na;
       } else if (MODE == kHoResid) {
         v = __ldg(b + (size_t)j * n + i) + (a.sign > 0 ? na : -na);
       } else {
-        double inv = 1.0;
+        T inv = T(1);
         if (!a.richardson) {
-          const double dyy = yin ? O::d(0) : ty[yr * BN + yr];
-          inv = (xin && yin) ? kInvDiagIn : -1.0 / (wj * dxx + wi * dyy);
+          const T dyy = yin ? kD0 : ty[yr * BN + yr];
+          inv = (xin && yin) ? kInvDiagIn : T(-1) / (wj * dxx + wi * dyy);
         }
-        v = fma(a.omega * inv, __ldg(b + (size_t)j * n + i) + na, c[R]);
+        v = fmaT(omega * inv, __ldg(b + (size_t)j * n + i) + na, c[R]);
       }
       out[(size_t)j * n + i] = v;
       if (DOT) acc.add_prod(MODE == kHoApply ? c[R] : v, v);
@@ -161,15 +177,16 @@ __global__ void __launch_bounds__(kThreads) k_ho(const HoArgs a) {
 }
 
 // r.z into the Krylov state: beta = rz_new / rz (0 on the first direction).
+template <typename Tz>
 __global__ void __launch_bounds__(kThreads)
-    k_ho_rz(const double* __restrict__ r, const double* __restrict__ z, long long N,
+    k_ho_rz(const double* __restrict__ r, const Tz* __restrict__ z, long long N,
             SolveState* st, ReduceBuf rb, int first) {
   pdl_begin();
   if (st->done) return;
   double acc = 0.0;
   for (long long k = (long long)blockIdx.x * kThreads + threadIdx.x; k < N;
        k += (long long)gridDim.x * kThreads)
-    acc = fma(__ldg(r + k), __ldg(z + k), acc);
+    acc = fma(__ldg(r + k), convert<double>(__ldg(z + k)), acc);
   grid_reduce(acc, rb, [&](double tot) {
     st->beta = first ? 0.0 : tot / st->rz;
     st->rz = tot;
@@ -178,15 +195,18 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // p = z + beta p (p = z on the first direction).
+template <typename Tz>
 __global__ void __launch_bounds__(kThreads)
-    k_ho_dir(const double* __restrict__ z, double* __restrict__ p, long long N,
+    k_ho_dir(const Tz* __restrict__ z, double* __restrict__ p, long long N,
              const SolveState* st, int first) {
   pdl_begin();
   if (st->done) return;
   const double beta = st->beta;
   for (long long k = (long long)blockIdx.x * kThreads + threadIdx.x; k < N;
-       k += (long long)gridDim.x * kThreads)
-    p[k] = first ? __ldg(z + k) : fma(beta, p[k], __ldg(z + k));
+       k += (long long)gridDim.x * kThreads) {
+    const double zk = convert<double>(__ldg(z + k));
+    p[k] = first ? zk : fma(beta, p[k], zk);
+  }
 }
 
 int flat_ctas(long long N) {
@@ -204,15 +224,15 @@ void fill_tables(double* x, double* y) {
     }
 }
 
-template <int P, int MODE>
-cudaError_t launch_mode(const HoArgs& a, dim3 grid, cudaStream_t s) {
+template <int P, int MODE, typename T>
+cudaError_t launch_mode(const HoArgsT<T>& a, dim3 grid, cudaStream_t s) {
   if (a.rb.partials)
-    return launch_pdl(k_ho<P, MODE, true>, grid, dim3(kThreads), 0, s, a);
-  return launch_pdl(k_ho<P, MODE, false>, grid, dim3(kThreads), 0, s, a);
+    return launch_pdl(k_ho<P, MODE, true, T>, grid, dim3(kThreads), 0, s, a);
+  return launch_pdl(k_ho<P, MODE, false, T>, grid, dim3(kThreads), 0, s, a);
 }
 
-template <int P>
-cudaError_t launch_order(int mode, const HoArgs& a, dim3 grid, cudaStream_t s) {
+template <int P, typename T>
+cudaError_t launch_order(int mode, const HoArgsT<T>& a, dim3 grid, cudaStream_t s) {
   switch (mode) {
     case kHoApply: return launch_mode<P, kHoApply>(a, grid, s);
     case kHoResid: return launch_mode<P, kHoResid>(a, grid, s);
@@ -232,10 +252,17 @@ cudaError_t prepare_ho_tables() {
   static cudaError_t err = cudaSuccess;
   std::call_once(once, [] {
     double t4[2][4 * 6], t6[2][6 * 9];
+    float f4[2][4 * 6], f6[2][6 * 9];
     fill_tables<4>(t4[0], t4[1]);
     fill_tables<6>(t6[0], t6[1]);
+    for (int w = 0; w < 2; ++w) {
+      for (int k = 0; k < 4 * 6; ++k) f4[w][k] = (float)t4[w][k];
+      for (int k = 0; k < 6 * 9; ++k) f6[w][k] = (float)t6[w][k];
+    }
     err = cudaMemcpyToSymbol(c_ho4, t4, sizeof(t4));
     if (err == cudaSuccess) err = cudaMemcpyToSymbol(c_ho6, t6, sizeof(t6));
+    if (err == cudaSuccess) err = cudaMemcpyToSymbol(c_ho4f, f4, sizeof(f4));
+    if (err == cudaSuccess) err = cudaMemcpyToSymbol(c_ho6f, f6, sizeof(f6));
   });
   return err;
 }
@@ -248,7 +275,8 @@ int ho_cols(int n) {
   return (int)std::max(1LL, std::min(32LL, c));
 }
 
-cudaError_t launch_ho(int p, int mode, HoArgs a, cudaStream_t s) {
+template <typename T>
+cudaError_t launch_ho(int p, int mode, HoArgsT<T> a, cudaStream_t s) {
   if (ho_min_n(p) == 0 || a.n < ho_min_n(p) || !a.out) return cudaErrorInvalidValue;
   if (a.cols <= 0) a.cols = ho_cols(a.n);
   const long long nrb = (a.n + kThreads - 1) / kThreads;
@@ -257,14 +285,28 @@ cudaError_t launch_ho(int p, int mode, HoArgs a, cudaStream_t s) {
   return p == 4 ? launch_order<4>(mode, a, grid, s) : launch_order<6>(mode, a, grid, s);
 }
 
-cudaError_t launch_ho_rz(const double* r, const double* z, long long N, SolveState* st,
+template <typename Tz>
+cudaError_t launch_ho_rz(const double* r, const Tz* z, long long N, SolveState* st,
                          ReduceBuf rb, int first, cudaStream_t s) {
-  return launch_pdl(k_ho_rz, dim3(flat_ctas(N)), dim3(kThreads), 0, s, r, z, N, st, rb, first);
+  return launch_pdl(k_ho_rz<Tz>, dim3(flat_ctas(N)), dim3(kThreads), 0, s, r, z, N, st, rb,
+                    first);
 }
 
-cudaError_t launch_ho_dir(const double* z, double* p, long long N, const SolveState* st,
+template <typename Tz>
+cudaError_t launch_ho_dir(const Tz* z, double* p, long long N, const SolveState* st,
                           int first, cudaStream_t s) {
-  return launch_pdl(k_ho_dir, dim3(flat_ctas(N)), dim3(kThreads), 0, s, z, p, N, st, first);
+  return launch_pdl(k_ho_dir<Tz>, dim3(flat_ctas(N)), dim3(kThreads), 0, s, z, p, N, st, first);
 }
+
+template cudaError_t launch_ho<double>(int, int, HoArgsT<double>, cudaStream_t);
+template cudaError_t launch_ho<float>(int, int, HoArgsT<float>, cudaStream_t);
+template cudaError_t launch_ho_rz<double>(const double*, const double*, long long, SolveState*,
+                                          ReduceBuf, int, cudaStream_t);
+template cudaError_t launch_ho_rz<float>(const double*, const float*, long long, SolveState*,
+                                         ReduceBuf, int, cudaStream_t);
+template cudaError_t launch_ho_dir<double>(const double*, double*, long long, const SolveState*,
+                                           int, cudaStream_t);
+template cudaError_t launch_ho_dir<float>(const float*, double*, long long, const SolveState*,
+                                          int, cudaStream_t);
 
 }  // namespace sbp

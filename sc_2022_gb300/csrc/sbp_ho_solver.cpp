@@ -33,19 +33,21 @@
 using namespace sbp;
 
 struct sbp_ho_solver {
+  // Level buffers hold doubles, or floats for the mixed-precision V-cycle.
   struct Lvl {
     int n = 0;
-    double* b = nullptr;   // level 0: the solver's r
-    double* v[2] = {nullptr, nullptr};
-    double* t = nullptr;   // residual scratch
+    void* b = nullptr;   // level 0: the solver's r (FP64) or r_lo (mixed)
+    void* v[2] = {nullptr, nullptr};
+    void* t = nullptr;   // residual scratch
   };
   int n = 0, p = 0, device = 0;
   bool mg = false;
+  bool mixed = false;
+  float* r_lo = nullptr;   // mixed: FP32 copy of r, written by the update
   sbp_options opts{};
   std::vector<Lvl> lv;
   CoarseDev coarse{};
   double *x = nullptr, *r = nullptr, *pd = nullptr, *ap = nullptr;
-  double* z = nullptr;   // where the V-cycle leaves its result (set by enqueue)
   double* norms = nullptr;
   int norms_cap = 0;
   SolveState* st = nullptr;
@@ -66,9 +68,10 @@ bool pow2_plus1(int n) {
   return n >= 3 && (m & (m - 1)) == 0;
 }
 
-int dalloc(sbp_ho_solver* s, double** out, size_t count) {
+template <typename T>
+int dalloc(sbp_ho_solver* s, T** out, size_t count) {
   void* p = nullptr;
-  const size_t bytes = std::max<size_t>(count * sizeof(double), 256);
+  const size_t bytes = std::max<size_t>(count * sizeof(T), 256);
   const cudaError_t e = cudaMalloc(&p, bytes);
   if (e != cudaSuccess) {
     set_last_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
@@ -76,28 +79,35 @@ int dalloc(sbp_ho_solver* s, double** out, size_t count) {
   }
   s->allocs.push_back(p);
   s->dev_bytes += (long long)bytes;
-  *out = static_cast<double*>(p);
+  *out = static_cast<T*>(p);
   return SBP_OK;
 }
 
-HoArgs ho_args(int n) {
-  HoArgs a{};
+template <typename T = double>
+HoArgsT<T> ho_args(int n) {
+  HoArgsT<T> a{};
   a.n = n;
   a.sign = 1;
   return a;
 }
 
+template <typename T>
+T* as(void* p) {
+  return static_cast<T*>(p);
+}
+
 // Smoothing sweeps on level L from v[cur]; returns the buffer index holding
 // the result.  zero: start from v = 0.
+template <typename T>
 int smooth(sbp_ho_solver* s, const sbp_ho_solver::Lvl& L, int cur, int sweeps, bool zero,
            cudaStream_t q, cudaError_t& err) {
   const bool rich = s->opts.smoother == SBP_SMOOTH_RICHARDSON;
   const double omega = s->opts.omega > 0.0 ? s->opts.omega : (rich ? 0.15 : 2.0 / 3.0);
   for (int k = 0; k < sweeps && err == cudaSuccess; ++k) {
-    HoArgs a = ho_args(L.n);
-    a.u = L.v[cur];
-    a.b = L.b;
-    a.out = L.v[1 - cur];
+    HoArgsT<T> a = ho_args<T>(L.n);
+    a.u = as<T>(L.v[cur]);
+    a.b = as<T>(L.b);
+    a.out = as<T>(L.v[1 - cur]);
     a.omega = omega;
     a.richardson = rich ? 1 : 0;
     a.zero_in = (zero && k == 0) ? 1 : 0;
@@ -109,40 +119,53 @@ int smooth(sbp_ho_solver* s, const sbp_ho_solver::Lvl& L, int cur, int sweeps, b
 }
 
 // One V-cycle from v = 0 on level l for the right-hand side lv[l].b; returns
-// the buffer holding the result.
-double* vcycle(sbp_ho_solver* s, size_t l, cudaStream_t q, cudaError_t& err) {
+// the buffer holding the result.  T: the V-cycle's arithmetic (the coarse
+// solve computes in FP64 either way).
+template <typename T>
+T* vcycle(sbp_ho_solver* s, size_t l, cudaStream_t q, cudaError_t& err) {
   auto& L = s->lv[l];
   const int n = L.n;
   if (l + 1 == s->lv.size()) {
-    err = launch_coarse_solve<double>(s->coarse, Grid<const double>{L.b, n},
-                                      Grid<double>{L.v[0], n}, s->st, q);
-    return L.v[0];
+    err = launch_coarse_solve<T>(s->coarse, Grid<const T>{as<T>(L.b), n},
+                                 Grid<T>{as<T>(L.v[0]), n}, s->st, q);
+    return as<T>(L.v[0]);
   }
   int cur = 0;
   if (s->opts.nu_pre > 0) {
-    cur = smooth(s, L, 1, s->opts.nu_pre, true, q, err);
+    cur = smooth<T>(s, L, 1, s->opts.nu_pre, true, q, err);
   } else {
-    err = cudaMemsetAsync(L.v[0], 0, (size_t)n * n * sizeof(double), q);
+    err = cudaMemsetAsync(L.v[0], 0, (size_t)n * n * sizeof(T), q);
   }
   if (err != cudaSuccess) return nullptr;
-  HoArgs a = ho_args(n);
-  a.u = L.v[cur];
-  a.b = L.b;
-  a.out = L.t;
+  HoArgsT<T> a = ho_args<T>(n);
+  a.u = as<T>(L.v[cur]);
+  a.b = as<T>(L.b);
+  a.out = as<T>(L.t);
   a.st = s->st;
   err = launch_ho(s->p, kHoResid, a, q);
   if (err != cudaSuccess) return nullptr;
   auto& C = s->lv[l + 1];
-  err = launch_resrestrict<double>(Grid<const double>{nullptr, 0}, Grid<const double>{L.t, n},
-                                   Grid<double>{C.b, C.n}, n, s->opts.restriction, s->st, q);
+  err = launch_resrestrict<T>(Grid<const T>{nullptr, 0}, Grid<const T>{as<T>(L.t), n},
+                              Grid<T>{as<T>(C.b), C.n}, n, s->opts.restriction, s->st, q);
   if (err != cudaSuccess) return nullptr;
-  double* e = vcycle(s, l + 1, q, err);
+  T* e = vcycle<T>(s, l + 1, q, err);
   if (err != cudaSuccess) return nullptr;
-  err = launch_prolong<double>(Grid<const double>{e, C.n}, Grid<double>{L.v[cur], n}, C.n, 1,
-                               s->st, q);
+  err = launch_prolong<T>(Grid<const T>{e, C.n}, Grid<T>{as<T>(L.v[cur]), n}, C.n, 1, s->st, q);
   if (err != cudaSuccess) return nullptr;
-  cur = smooth(s, L, cur, s->opts.nu_post, false, q, err);
-  return L.v[cur];
+  cur = smooth<T>(s, L, cur, s->opts.nu_post, false, q, err);
+  return as<T>(L.v[cur]);
+}
+
+// z = V(r), then beta = r.z / r.z_old and p = z + beta p (first: p = z).
+template <typename T>
+cudaError_t precondition(sbp_ho_solver* s, int first, cudaStream_t q) {
+  cudaError_t err = cudaSuccess;
+  const long long N = (long long)s->n * s->n;
+  T* z = vcycle<T>(s, 0, q, err);
+  if (err != cudaSuccess) return err;
+  err = launch_ho_rz<T>(s->r, z, N, s->st, s->rb[2], first, q);
+  if (err != cudaSuccess) return err;
+  return launch_ho_dir<T>(z, s->pd, N, s->st, first, q);
 }
 
 // The iteration body: Ap and alpha, x/r update and ||r||^2, then the new
@@ -158,18 +181,15 @@ cudaError_t enqueue_iteration(sbp_ho_solver* s, int kind, int sign, cudaStream_t
   a.st = s->st;
   cudaError_t err = launch_ho(s->p, kHoApply, a, q);
   if (err != cudaSuccess) return err;
+  // the update also refreshes the FP32 copy of r for a mixed V-cycle
+  const bool lo = kind == 0 && s->mixed;
   err = launch_cg_update<double>(Grid<double>{s->x, n}, Grid<double>{s->r, n},
                                  Grid<const double>{s->pd, n}, Grid<const double>{s->ap, n},
-                                 Grid<float>{nullptr, n}, n, kind == 1 ? 1 : 0, s->st, s->norms,
-                                 s->rb[1], q);
+                                 Grid<float>{lo ? s->r_lo : nullptr, n}, n, kind == 1 ? 1 : 0,
+                                 s->st, s->norms, s->rb[1], q);
   if (err != cudaSuccess) return err;
-  if (kind == 1) return launch_ho_dir(s->r, s->pd, N, s->st, 0, q);
-  double* z = vcycle(s, 0, q, err);
-  if (err != cudaSuccess) return err;
-  s->z = z;
-  err = launch_ho_rz(s->r, z, N, s->st, s->rb[2], 0, q);
-  if (err != cudaSuccess) return err;
-  return launch_ho_dir(z, s->pd, N, s->st, 0, q);
+  if (kind == 1) return launch_ho_dir<double>(s->r, s->pd, N, s->st, 0, q);
+  return s->mixed ? precondition<float>(s, 0, q) : precondition<double>(s, 0, q);
 }
 
 void destroy_graphs(sbp_ho_solver* s) {
@@ -240,13 +260,13 @@ int solve(sbp_ho_solver* s, int kind, const double* b, double* x, int sign, doub
   a.norms = s->norms;
   SBP_CUDA(launch_ho(s->p, kHoResid, a, q));
   if (kind == 1) {
-    SBP_CUDA(launch_ho_dir(s->r, s->pd, N, s->st, 1, q));
+    SBP_CUDA(launch_ho_dir<double>(s->r, s->pd, N, s->st, 1, q));
+  } else if (s->mixed) {
+    SBP_CUDA(launch_copy<double, float>(Grid<const double>{s->r, n}, Grid<float>{s->r_lo, n}, n,
+                                        q));
+    SBP_CUDA(precondition<float>(s, 1, q));
   } else {
-    cudaError_t err = cudaSuccess;
-    double* z = vcycle(s, 0, q, err);
-    SBP_CUDA(err);
-    SBP_CUDA(launch_ho_rz(s->r, z, N, s->st, s->rb[2], 1, q));
-    SBP_CUDA(launch_ho_dir(z, s->pd, N, s->st, 1, q));
+    SBP_CUDA(precondition<double>(s, 1, q));
   }
   if (!s->exec[kind] || s->exec_sign[kind] != sign) {
     rc = capture(s, kind, sign);
@@ -301,10 +321,7 @@ int sbp_ho_solver_create(sbp_ho_solver** out, int n, int p, const sbp_options* o
   sbp_options o;
   sbp_options_default(&o);
   if (opts) o = *opts;
-  if (o.precision != SBP_PREC_FP64) {
-    set_last_error("the order-p solver computes in FP64 only");
-    return SBP_ERR_UNSUPPORTED;
-  }
+  if (o.precision != SBP_PREC_FP64 && o.precision != SBP_PREC_MIXED) return SBP_ERR_ARGS;
   if (o.nu_pre < 0 || o.nu_post < 0 || o.restriction < 0 || o.restriction > 2 ||
       (o.smoother != SBP_SMOOTH_JACOBI && o.smoother != SBP_SMOOTH_RICHARDSON))
     return SBP_ERR_ARGS;
@@ -322,6 +339,8 @@ int sbp_ho_solver_create(sbp_ho_solver** out, int n, int p, const sbp_options* o
   s->n = n;
   s->p = p;
   s->opts = o;
+  s->mixed = o.precision == SBP_PREC_MIXED;
+  const size_t esize = s->mixed ? sizeof(float) : sizeof(double);
   const size_t N = (size_t)n * n;
   int rc = 0;
   for (double** v : {&s->x, &s->r, &s->pd, &s->ap}) {
@@ -353,23 +372,28 @@ int sbp_ho_solver_create(sbp_ho_solver** out, int n, int p, const sbp_options* o
   const bool direct = n <= std::min(cn, 257);
   s->mg = direct || (pow2_plus1(n) && pow2_plus1(cn) && cn >= ho_min_n(p) && cn <= 257);
   if (s->mg) {
+    if (s->mixed) {
+      rc = dalloc(s.get(), &s->r_lo, N);
+      if (rc) return rc;
+    }
     int m = n;
     while (true) {
       sbp_ho_solver::Lvl L;
       L.n = m;
-      const size_t M = (size_t)m * m;
+      const size_t M = (size_t)m * m * esize / sizeof(float);   // in floats
+      float* buf = nullptr;
       if (s->lv.empty()) {
-        L.b = s->r;
+        L.b = s->mixed ? (void*)s->r_lo : (void*)s->r;
       } else {
-        rc = dalloc(s.get(), &L.b, M);
+        rc = dalloc(s.get(), &buf, M);
         if (rc) return rc;
+        L.b = buf;
       }
-      rc = dalloc(s.get(), &L.v[0], M);
-      if (rc) return rc;
-      rc = dalloc(s.get(), &L.v[1], M);
-      if (rc) return rc;
-      rc = dalloc(s.get(), &L.t, M);
-      if (rc) return rc;
+      for (void** dst : {&L.v[0], &L.v[1], &L.t}) {
+        rc = dalloc(s.get(), &buf, M);
+        if (rc) return rc;
+        *dst = buf;
+      }
       s->lv.push_back(L);
       if (direct || m == cn) break;
       m = (m + 1) / 2;
@@ -441,9 +465,18 @@ int sbp_ho_vcycle_apply(sbp_ho_solver* s, const double* b, double* v, void* stre
   SBP_CUDA(launch_state_init(s->st, 1, q));
   SBP_CUDA(cudaMemcpyAsync(s->r, b, bytes, cudaMemcpyDeviceToDevice, q));
   cudaError_t err = cudaSuccess;
-  double* z = vcycle(s, 0, q, err);
-  SBP_CUDA(err);
-  SBP_CUDA(cudaMemcpyAsync(v, z, bytes, cudaMemcpyDeviceToDevice, q));
+  const int n = s->n;
+  if (s->mixed) {
+    SBP_CUDA(launch_copy<double, float>(Grid<const double>{s->r, n}, Grid<float>{s->r_lo, n}, n,
+                                        q));
+    float* z = vcycle<float>(s, 0, q, err);
+    SBP_CUDA(err);
+    SBP_CUDA(launch_copy<float, double>(Grid<const float>{z, n}, Grid<double>{v, n}, n, q));
+  } else {
+    double* z = vcycle<double>(s, 0, q, err);
+    SBP_CUDA(err);
+    SBP_CUDA(cudaMemcpyAsync(v, z, bytes, cudaMemcpyDeviceToDevice, q));
+  }
   SBP_CUDA(cudaStreamSynchronize(q));
   return SBP_OK;
 }

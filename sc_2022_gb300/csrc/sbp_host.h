@@ -19,8 +19,8 @@ int finish_result(const SolveState& fs, sbp_result* res);
 
 }  // namespace sbp
 
-#define SBP_CUDA(call)                                          \
-  do {                                                          \
-    cudaError_t _e = (call);                                    \
-    if (_e != cudaSuccess) return ::sbp::fail_cuda(_e, #call);  \
+#define SBP_CUDA(...)                                                 \
+  do {                                                                \
+    cudaError_t _e = (__VA_ARGS__);                                   \
+    if (_e != cudaSuccess) return ::sbp::fail_cuda(_e, #__VA_ARGS__); \
   } while (0)

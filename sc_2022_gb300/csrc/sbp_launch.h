@@ -210,10 +210,11 @@ cudaError_t copy_grid(double* dst, int dld, const double* src, int sld, int n, c
 
 // ---- higher-order (p = 4, 6) operators, FP64, contiguous n x n grids ----
 enum { kHoApply = 0, kHoResid = 1, kHoJacobi = 2 };
-struct HoArgs {
-  const double* u;     // operator input (unused by a Jacobi sweep with zero_in)
-  const double* b;     // right-hand side (residual, Jacobi)
-  double* out;
+template <typename T>
+struct HoArgsT {
+  const T* u;          // operator input (unused by a Jacobi sweep with zero_in)
+  const T* b;          // right-hand side (residual, Jacobi)
+  T* out;
   int n;
   int sign;            // apply: out = sign * A u; residual: out = b - sign * A u
   double omega;        // smoother weight
@@ -227,15 +228,21 @@ struct HoArgs {
   double abstol, reltol;
   double* norms;       // init: norms[0] = ||r0||
 };
+using HoArgs = HoArgsT<double>;
 // Smallest grid of order p (0 if p is not 4 or 6).
 int ho_min_n(int p);
 // Upload the closure tables once (outside stream capture).
 cudaError_t prepare_ho_tables();
-cudaError_t launch_ho(int p, int mode, HoArgs a, cudaStream_t s);
-// r.z -> beta (0 when first) and rz in the state; p = z + beta p (p = z when first).
-cudaError_t launch_ho_rz(const double* r, const double* z, long long N, SolveState* st,
+// T = double (FP64 arithmetic) or float (FP32 arithmetic, the mixed V-cycle).
+template <typename T>
+cudaError_t launch_ho(int p, int mode, HoArgsT<T> a, cudaStream_t s);
+// r.z -> beta (0 when first) and rz in the state; p = z + beta p (p = z
+// when first).  Tz = double or float (the mixed V-cycle's z).
+template <typename Tz>
+cudaError_t launch_ho_rz(const double* r, const Tz* z, long long N, SolveState* st,
                          ReduceBuf rb, int first, cudaStream_t s);
-cudaError_t launch_ho_dir(const double* z, double* p, long long N, const SolveState* st,
+template <typename Tz>
+cudaError_t launch_ho_dir(const Tz* z, double* p, long long N, const SolveState* st,
                           int first, cudaStream_t s);
 
 // y = A x for a CSR matrix with nrows rows (64-bit row pointers).

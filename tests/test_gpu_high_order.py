@@ -181,3 +181,56 @@ def test_mgcg_n4097_residual(sbp, p):
     ax = torch.empty_like(x)
     sbp.matrix_free_A_high_order_GPU(x, ax, p=p, sign=1)
     assert float((b - ax).norm() / b.norm()) < 2e-10
+
+
+MIXED_VCYCLE_RTOL = 2e-5   # FP32 V-cycle vs the FP64 oracle's, relative 2-norm
+
+
+@pytest.mark.parametrize("p,n", [(4, 129), (6, 257)])
+def test_mixed_vcycle_close_to_fp64_oracle(sbp, p, n):
+    opts = mg_options(sbp, 33)
+    opts.precision = 1   # SBP_PREC_MIXED
+    hier = o.Hierarchy(n, o.MGOptions(restriction="galerkin", coarse_n=33), p)
+    b = np.random.default_rng(17 + p).standard_normal(n * n)
+    want = hier.vcycle(b)
+    s = sbp.HighOrderSolver(n, p, opts)
+    v = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    s.vcycle(dev(b), v)
+    assert relerr(host(v), want) < MIXED_VCYCLE_RTOL
+
+
+@pytest.mark.parametrize("p,n", [(4, 257), (6, 257)])
+def test_mixed_mgcg_matches_fp64(sbp, p, n):
+    # the FP32 V-cycle inside FP64 PCG: the FP64 iteration count (+-1) and a
+    # solution at the FP64 tolerance
+    a = o.assemble(n, p)
+    F, g, U = o.manufactured(n, "baseline")
+    b = a.rhs(F, g)
+    xs = spla.spsolve(a.A.tocsc(), b)
+    its = {}
+    for prec in (0, 1):
+        opts = mg_options(sbp, 33)
+        opts.precision = prec
+        s = sbp.HighOrderSolver(n, p, opts)
+        x = torch.zeros(n * n, dtype=torch.float64, device="cuda")
+        res = s.mgcg(dev(b), x, reltol=1e-10)
+        assert res.converged
+        its[prec] = res.iters
+        assert relerr(host(x), xs) < SOL_RTOL * 10
+    assert abs(its[1] - its[0]) <= 1
+
+
+@pytest.mark.parametrize("p", [4, 6])
+def test_mixed_mgcg_n4097_residual(sbp, p):
+    n = 4097
+    g = torch.Generator(device="cuda").manual_seed(12)
+    b = torch.randn(n * n, generator=g, device="cuda", dtype=torch.float64)
+    x = torch.zeros_like(b)
+    opts = sbp.default_options(1)
+    s = sbp.HighOrderSolver(n, p, opts)
+    res = s.mgcg(b, x, reltol=1e-10, maxiter=100)
+    assert res.converged
+    assert res.iters <= (12 if p == 4 else 16)
+    ax = torch.empty_like(x)
+    sbp.matrix_free_A_high_order_GPU(x, ax, p=p, sign=1)
+    assert float((b - ax).norm() / b.norm()) < 2e-10
