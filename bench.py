@@ -51,7 +51,7 @@ def parse_args():
     p.add_argument("--dtype", choices=["f64", "f32"], default="f64",
                    help="operand type of --mode apply")
     p.add_argument("--mode", choices=["full", "apply", "solve-fp64", "solve-mixed", "vcycle",
-                                      "high-order",
+                                      "high-order", "variable",
                                       "batch", "spmv"],
                    default="full", help="profiling modes run one part only and print a "
                    "short line (not the benchmark line)")
@@ -540,6 +540,52 @@ def run_part(args):
                 out[f"p{p}_mgcg_{tag}_iters"] = r.iters
                 out[f"p{p}_mgcg_{tag}_converged"] = r.converged
                 s.close()
+        print(json.dumps(out))
+        return
+    if args.mode == "variable":
+        # div(c grad u) at --n with the seeded layered coefficient (c from 1
+        # to 10 across y = 1/2): the FP64 apply from nodal c (u, c read, out
+        # written: 24 B per point) and MGCG to 1e-10 from zero
+        out = {"mode": "variable", "n": n, "coefficient": "layered 1..10"}
+        x1 = torch.linspace(0.0, 1.0, n, device=dev, dtype=torch.float64)
+        coef = (1.0 + 4.5 * (1.0 + torch.tanh((x1 - 0.5) * (n - 1) / 2.0)))[:, None].expand(
+            n, n).contiguous().reshape(-1)
+        gen = torch.Generator(device=dev).manual_seed(0)
+        us = [torch.randn(n * n, generator=gen, device=dev, dtype=torch.float64) for _ in range(2)]
+        outs = [torch.empty_like(us[0]) for _ in range(2)]
+        hbm, hbm_src = measured_peaks()
+        for k in range(args.warmup):
+            sbp.matrix_free_A_variable_GPU(us[k % 2], coef, outs[k % 2])
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for k in range(args.steps):
+            sbp.matrix_free_A_variable_GPU(us[k % 2], coef, outs[k % 2])
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        gbs = 24.0 * n * n / (ms * 1e-3) / 1e9
+        out.update({"apply_us": round(1e3 * ms, 2), "apply_gbs": round(gbs, 1),
+                    "apply_frac_of_hbm": round(gbs / hbm, 3), "hbm_peak_source": hbm_src})
+        for tag, prec in (("fp64", _lib.SBP_PREC_FP64), ("mixed", _lib.SBP_PREC_MIXED)):
+            s = sbp.VariableCoefficientSolver(n, coef, sbp.default_options(prec))
+            x = torch.zeros_like(us[0])
+            for _ in range(args.warmup):
+                x.zero_()
+                s.mgcg(us[0], x, reltol=1e-10, maxiter=200)
+            torch.cuda.synchronize()
+            e0.record()
+            for _ in range(args.steps):
+                x.zero_()
+                r = s.mgcg(us[0], x, reltol=1e-10, maxiter=200)
+            e1.record()
+            torch.cuda.synchronize()
+            out[f"mgcg_{tag}_ms"] = round(e0.elapsed_time(e1) / args.steps, 3)
+            out[f"mgcg_{tag}_iters"] = r.iters
+            out[f"mgcg_{tag}_converged"] = r.converged
+            out["levels"] = s.levels
+            s.close()
         print(json.dumps(out))
         return
     if args.mode == "vcycle":

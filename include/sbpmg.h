@@ -225,6 +225,44 @@ int sbp_ho_cg_solve(sbp_ho_solver* s, const double* b, double* x, int sign, doub
 /* v = one V-cycle from zero for the right-hand side b. */
 int sbp_ho_vcycle_apply(sbp_ho_solver* s, const double* b, double* v, void* stream);
 
+/* ---- variable coefficients (p = 2) ------------------------------------ */
+
+/* The second-order SBP-SAT operator for div(c grad u) = f with nodal
+ * coefficients c > 0.  Every grid line carries variable_diagonal_sbp_D2(2, N,
+ * B) (diagonal_sbp.jl:470-495, 709-740) of its own coefficients; the 2D
+ * assembly is get_operators' (legacy_functions.jl:100-174) with the SATs of
+ * Assembling_matrix (level_2_multigrid_new.jl:145-150).  The boundary flux
+ * and the Dirichlet penalty tau_D are scaled by c at the boundary point.
+ * c = 1 gives the constant-coefficient operator.  Arrays are contiguous FP64
+ * n x n device grids (ld = n), n >= 3.  Computed straight from c: u, c and
+ * out are the only traffic. */
+int sbp_apply_vc_f64(const double* u, const double* c, double* out, int n, int sign,
+                     void* stream);
+
+/* Variable-coefficient solver handle for the coefficient field c (copied
+ * at creation).  opts (NULL = sbp_options_default) as for sbp_ho_solver_create.
+ * - V-cycle levels re-discretise the operator with the coefficients
+ *   injected to each coarse grid.
+ * - The coarse level is solved exactly with a dense inverse; coarse_n is
+ *   capped at 33.
+ * - Any n >= 3 gets plain CG; multigrid needs n = 2^k + 1 or n <= 33. */
+typedef struct sbp_vc_solver sbp_vc_solver;
+int sbp_vc_solver_create(sbp_vc_solver** out, int n, const double* c, const sbp_options* opts);
+int sbp_vc_solver_destroy(sbp_vc_solver* s);
+int sbp_vc_solver_levels(const sbp_vc_solver* s);
+long long sbp_vc_solver_device_bytes(const sbp_vc_solver* s);
+int sbp_vc_mgcg_solve(sbp_vc_solver* s, const double* b, double* x, double abstol, double reltol,
+                      int maxiter, sbp_result* res, double* norms, int norms_cap, void* stream);
+int sbp_vc_cg_solve(sbp_vc_solver* s, const double* b, double* x, int sign, double abstol,
+                    double reltol, int maxiter, sbp_result* res, double* norms, int norms_cap,
+                    void* stream);
+int sbp_vc_vcycle_apply(sbp_vc_solver* s, const double* b, double* v, void* stream);
+/* The variable-coefficient A as CSR on the host (rows in column order),
+ * from the same per-point stencil the GPU solver uses; c is a host array.
+ * Needs no GPU.  Returns SBP_ERR_ARGS with *nnz set when cap is too small. */
+int sbp_vc_assemble_host(int n, const double* c, long long* row_ptr, int* col, double* val,
+                         long long cap, long long* nnz);
+
 /* ---- assembled-operator comparator ------------------------------------ */
 
 /* The reference compares its matrix-free apply with SpMV on the assembled

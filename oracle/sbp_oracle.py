@@ -18,6 +18,10 @@ Reference files restated here (paths inside AlexandreChern/SC_2022):
 * ``preconditioned_CG/level_2_multigrid_new.jl:358-382`` ``Two_level_multigrid``
 * ``preconditioned_CG/level_2_multigrid_new.jl:480-524`` ``mg_preconditioned_CG``
 * ``split_matrix_free.jl:32-49, 324-486`` ``matrix_free_A_full_GPU`` (the -A apply)
+* ``diagonal_sbp.jl:198-222`` p = 4 and p = 6 branches of ``diagonal_sbp_D2``
+* ``diagonal_sbp.jl:462-495, 709-740`` ``variable_diagonal_sbp_D2`` (p = 2)
+* ``preconditioned_CG/legacy_functions.jl:100-174`` ``get_operators`` (2D
+  assembly from the variable-coefficient D2)
 * ``preconditioned_CG/matrix_free_mg_cg.jl:17-38, 80-94`` matrix-free transfers
 
 Parity pin: the reference is Julia and no Julia toolchain exists here, and
@@ -263,6 +267,167 @@ def assemble(n: int, p: int = 2) -> Assembled:
     A.eliminate_zeros()
     A.sort_indices()
     return Assembled(n=n, A=A, H_tilde=H_tilde, sat_r=sat_r)
+
+
+# --------------------------------------------------------------------------
+# Variable-coefficient operator, p = 2
+# --------------------------------------------------------------------------
+def variable_sbp_1d(n: int, c) -> tuple:
+    """``variable_diagonal_sbp_D2(2, N, B)`` (``diagonal_sbp.jl:470-495,
+    709-740``) on n points of [0, 1] with nodal coefficients c (length n):
+    M symmetric with face values (c_k + c_k+1)/2, S0 = -c_0 BS/h on the first
+    row, SN = c_n-1 BS/h on the last (BS = (3/2, -2, 1/2)), and
+    D = HI (-M + SN - S0).  Returns (D, S0, SN, HI, H, M), scipy CSR."""
+    c = np.asarray(c, dtype=np.float64).ravel()
+    assert c.size == n and n >= 3
+    h = 1.0 / (n - 1)
+    face = 0.5 * (c[:-1] + c[1:])                 # c_{k+1/2}
+    diag = np.zeros(n)
+    diag[:-1] += face
+    diag[1:] += face
+    M = sp.diags([-face, diag, -face], [-1, 0, 1], shape=(n, n)).tocsr() / h
+    bs = np.array([1.5, -2.0, 0.5])
+    S0 = sp.csr_matrix((-c[0] * bs / h, ([0, 0, 0], [0, 1, 2])), shape=(n, n))
+    SN = sp.csr_matrix((c[-1] * bs / h, ([n - 1] * 3, [n - 1, n - 2, n - 3])), shape=(n, n))
+    hv = np.ones(n)
+    hv[0] = hv[-1] = 0.5
+    H = sp.diags(h * hv).tocsr()
+    HI = sp.diags(1.0 / (h * hv)).tocsr()
+    D = (HI @ (-M + SN - S0)).tocsr()
+    return D, S0, SN, HI, H, M
+
+
+def assemble_variable(n: int, c) -> Assembled:
+    """Second-order SBP-SAT operator for div(c grad u) = f_ref on the n x n
+    grid, nodal coefficients c (flat, i fast), with the SATs of
+    ``Assembling_matrix`` (``level_2_multigrid_new.jl:125-188``): Dirichlet
+    on the slow-index sides W/E, Neumann on the fast-index sides S/N.  Each
+    grid line carries the 1D operator of :func:`variable_sbp_1d` built from
+    that line's coefficients (the 2D assembly of ``get_operators``,
+    ``legacy_functions.jl:100-174``, which the reference runs with c = 1).
+    The coefficient enters the SATs through the boundary derivative
+    (SN - S0 carry c) and the Dirichlet penalty tau_D * c at the boundary
+    point; with c = 1 the matrix is :func:`assemble`'s.  A = -H~ (D2 + SAT)
+    is symmetric positive definite for c > 0."""
+    c = np.asarray(c, dtype=np.float64).reshape(n, n)   # [j, i]
+    h = 1.0 / (n - 1)
+    tau_d = TAU_D_TIMES_H / h
+    N = n * n
+    # fast direction i (Neumann, tau_N = -1 on the boundary flux), per j
+    rows_fast = []
+    for j in range(n):
+        D, S0, SN, HI, H, M = variable_sbp_1d(n, c[j, :])
+        E = sp.diags(np.r_[1.0, np.zeros(n - 2), 1.0]).tocsr()
+        rows_fast.append(D + TAU_N * HI @ E @ (SN - S0))
+    L_fast = sp.block_diag(rows_fast).tocsr()
+    # slow direction j (Dirichlet), per i, assembled on the transposed
+    # ordering and permuted back
+    rows_slow = []
+    sat_w, sat_e = [], []
+    for i in range(n):
+        D, S0, SN, HI, H, M = variable_sbp_1d(n, c[:, i])
+        BS = (SN - S0).tocsr()
+        e1 = np.zeros(n)
+        e1[0] = 1.0
+        en = np.zeros(n)
+        en[-1] = 1.0
+        E1, En = sp.diags(e1).tocsr(), sp.diags(en).tocsr()
+        pen = tau_d * (c[0, i] * HI @ E1 + c[-1, i] * HI @ En) + BETA * HI @ BS.T @ (E1 + En)
+        rows_slow.append(D + pen)
+        sat_w.append(tau_d * c[0, i] * HI @ e1 + BETA * HI @ BS.T @ e1)
+        sat_e.append(tau_d * c[-1, i] * HI @ en + BETA * HI @ BS.T @ en)
+    perm = np.arange(N).reshape(n, n).T.ravel()   # (i fast) <- (j fast)
+    P = sp.csr_matrix((np.ones(N), (np.arange(N), perm)), shape=(N, N))
+    L_slow = (P.T @ sp.block_diag(rows_slow) @ P).tocsr()
+    _, _, _, HI1, H1, _ = variable_sbp_1d(n, np.ones(n))
+    H_tilde = sp.kron(H1, H1).tocsr()
+    A = (-(H_tilde @ (L_fast + L_slow))).tocsr()
+    A.eliminate_zeros()
+    A.sort_indices()
+    # boundary-data maps (the data are u on W/E and the flux c du/dn on S/N)
+    def side_map(vals_per_line, index_of):
+        rr, cc, vv = [], [], []
+        for line, vec in enumerate(vals_per_line):
+            vec = np.asarray(vec).ravel()
+            for k in np.nonzero(vec)[0]:
+                rr.append(index_of(line, k))
+                cc.append(line)
+                vv.append(vec[k])
+        return sp.csr_matrix((vv, (rr, cc)), shape=(N, n))
+    hi0 = 1.0 / (h * 0.5)
+    sat_r = {
+        "W": side_map(sat_w, lambda i, k: k * n + i),
+        "E": side_map(sat_e, lambda i, k: k * n + i),
+        "S": sp.csr_matrix((np.full(n, TAU_N * hi0), (np.arange(n) * n, np.arange(n))),
+                           shape=(N, n)),
+        "N": sp.csr_matrix((np.full(n, TAU_N * hi0), (np.arange(n) * n + n - 1, np.arange(n))),
+                           shape=(N, n)),
+    }
+    return Assembled(n=n, A=A, H_tilde=H_tilde, sat_r=sat_r)
+
+
+def coefficient_field(n: int, kind: str = "smooth") -> np.ndarray:
+    """Seeded coefficient fields (flat, i fast), all >= 0.5.
+    'smooth': c = 1 + 0.5 sin(2 pi x + 1) cos(3 pi y);
+    'layered': c jumps between 1 and 10 across y = 0.5 (smoothed over 2h)."""
+    x = grid(n)
+    X = x[None, :]
+    Y = x[:, None]
+    if kind == "smooth":
+        C = 1.0 + 0.5 * np.sin(2 * math.pi * X + 1.0) * np.cos(3 * math.pi * Y)
+    elif kind == "layered":
+        C = 1.0 + 9.0 * 0.5 * (1.0 + np.tanh((Y - 0.5) * (n - 1) / 2.0)) + 0 * X
+    else:
+        raise ValueError(kind)
+    return C.ravel()
+
+
+def manufactured_variable(n: int):
+    """u = sin(pi x) cos(pi y) with div(c grad u) = f_ref for the 'smooth'
+    field; boundary data: u on W/E (y = 0, 1) and the outward flux
+    c du/dn on S/N (x = 0, 1).  Returns (c, f_ref, g, u_exact), flat."""
+    x = grid(n)
+    X = x[None, :]
+    Y = x[:, None]
+    pi = math.pi
+    U = np.sin(pi * X) * np.cos(pi * Y)
+    Ux = pi * np.cos(pi * X) * np.cos(pi * Y)
+    Uy = -pi * np.sin(pi * X) * np.sin(pi * Y)
+    C = 1.0 + 0.5 * np.sin(2 * pi * X + 1.0) * np.cos(3 * pi * Y)
+    Cx = 0.5 * 2 * pi * np.cos(2 * pi * X + 1.0) * np.cos(3 * pi * Y)
+    Cy = -0.5 * 3 * pi * np.sin(2 * pi * X + 1.0) * np.sin(3 * pi * Y)
+    F = C * (-2 * pi**2 * U) + Cx * Ux + Cy * Uy
+    g = {"W": np.sin(pi * x), "E": -np.sin(pi * x),
+         "S": -(C[:, 0] * Ux[:, 0]), "N": C[:, -1] * Ux[:, -1]}
+    return C.ravel(), F.ravel(), g, U.ravel()
+
+
+def neg_A_variable_matrix_free(u, c, n: int) -> np.ndarray:
+    """(-A u) of :func:`assemble_variable` point by point: face-averaged
+    coefficients in a 5-point stencil, the Dirichlet closure of the
+    second-order operator scaled by the boundary coefficient."""
+    U = np.asarray(u, dtype=np.float64).reshape(n, n)   # [j, i]
+    C = np.asarray(c, dtype=np.float64).reshape(n, n)
+    w = np.ones(n)
+    w[0] = w[-1] = 0.5
+    out = np.zeros_like(U)
+    fx = 0.5 * (C[:, :-1] + C[:, 1:])     # faces along i
+    fy = 0.5 * (C[:-1, :] + C[1:, :])     # faces along j
+    X = np.zeros_like(U)
+    X[:, :-1] += fx * (U[:, 1:] - U[:, :-1])
+    X[:, 1:] += fx * (U[:, :-1] - U[:, 1:])
+    Y = np.zeros_like(U)
+    Y[:-1, :] += fy * (U[1:, :] - U[:-1, :])
+    Y[1:, :] += fy * (U[:-1, :] - U[1:, :])
+    bs = (1.5, -2.0, 0.5)
+    for jb, s in ((0, 1), (n - 1, -1)):
+        cb = C[jb, :]
+        Y[jb, :] += cb * (bs[0] * U[jb, :] + bs[1] * U[jb + s, :] + bs[2] * U[jb + 2 * s, :])
+        Y[jb, :] += TAU_D_TIMES_H * cb * U[jb, :]
+        for k in range(3):
+            Y[jb + k * s, :] += BETA * bs[k] * cb * U[jb, :]
+    out = w[:, None] * X + w[None, :] * Y
+    return out.ravel()
 
 
 # --------------------------------------------------------------------------
@@ -560,7 +725,10 @@ class Hierarchy:
     (``matrix_free_mg_cg.jl:455``), coarse level solved by a sparse LU
     (``:460``, ``A_2h \\ f`` at :166)."""
 
-    def __init__(self, n: int, opts: MGOptions, p: int = 2):
+    def __init__(self, n: int, opts: MGOptions, p: int = 2, coef=None):
+        """p: SBP order of every level.  coef (flat n x n, i fast): nodal
+        coefficients of the variable-coefficient operator, injected to each
+        coarse grid (c_2h(I, J) = c_h(2I, 2J))."""
         self.opts = opts
         self.p = p
         self.ns = [n]
@@ -571,7 +739,14 @@ class Hierarchy:
             self.ns.append(nn)
         if self.ns[-1] != opts.coarse_n and len(self.ns) > 1:
             raise ValueError(f"n={n} does not coarsen to coarse_n={opts.coarse_n}")
-        self.asm = [assemble(m, p) for m in self.ns]
+        if coef is None:
+            self.asm = [assemble(m, p) for m in self.ns]
+        else:
+            cs = [np.asarray(coef, dtype=np.float64).reshape(n, n)]
+            for m in self.ns[1:]:
+                cs.append(cs[-1][::2, ::2].copy())
+            self.coefs = [c.ravel() for c in cs]
+            self.asm = [assemble_variable(m, c) for m, c in zip(self.ns, self.coefs)]
         self.A = [a.A for a in self.asm]
         self.diag = [A.diagonal() for A in self.A]
         self.R = [restriction_2d(m, opts.restriction) for m in self.ns[:-1]]

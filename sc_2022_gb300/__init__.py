@@ -15,6 +15,8 @@ from .matrix_free import (CG_Matrix_Free_GPU_v2, CG_full_GPU, initial_guess_inte
                           matrix_free_A_full_GPU_f32, matrix_free_MGCG,
                           matrix_free_prolongation_2d_GPU, matrix_free_restriction_2d_GPU,
                           matrix_free_richardson, matrix_free_Two_level_multigrid)
+from .variable import (MGCG_variable_GPU, VariableCoefficientSolver, assemble_variable_host,
+                       matrix_free_A_variable_GPU)
 from .solver import (BatchSolver, Options, SolveResult, Solver, default_options,
                      reference_two_level_options)
 
@@ -27,6 +29,8 @@ __all__ = [
     "mgcg_rrule", "BatchSolver", "initial_guess_interpolation_CG_GPU",
     "initial_guess_interpolation_three_level_CG_GPU", "CG_p4_GPU", "matrix_free_A_p4_GPU",
     "CG_high_order_GPU", "HighOrderSolver", "MGCG_high_order_GPU", "matrix_free_A_high_order_GPU",
+    "MGCG_variable_GPU", "VariableCoefficientSolver", "assemble_variable_host",
+    "matrix_free_A_variable_GPU",
 ]
 
 

@@ -95,6 +95,17 @@ SIGNATURES = {
     "sbp_ho_cg_solve": (_i, [_vp, _vp, _vp, _i, _d, _d, _i, C.POINTER(sbp_result), _dp, _i,
                              _vp]),
     "sbp_ho_vcycle_apply": (_i, [_vp, _vp, _vp, _vp]),
+    "sbp_apply_vc_f64": (_i, [_vp, _vp, _vp, _i, _i, _vp]),
+    "sbp_vc_solver_create": (_i, [C.POINTER(_vp), _i, _vp, C.POINTER(sbp_options)]),
+    "sbp_vc_solver_destroy": (_i, [_vp]),
+    "sbp_vc_solver_levels": (_i, [_vp]),
+    "sbp_vc_solver_device_bytes": (C.c_longlong, [_vp]),
+    "sbp_vc_mgcg_solve": (_i, [_vp, _vp, _vp, _d, _d, _i, C.POINTER(sbp_result), _dp, _i, _vp]),
+    "sbp_vc_cg_solve": (_i, [_vp, _vp, _vp, _i, _d, _d, _i, C.POINTER(sbp_result), _dp, _i,
+                             _vp]),
+    "sbp_vc_vcycle_apply": (_i, [_vp, _vp, _vp, _vp]),
+    "sbp_vc_assemble_host": (_i, [_i, _dp, C.POINTER(C.c_longlong), C.POINTER(_i), _dp,
+                                  C.c_longlong, C.POINTER(C.c_longlong)]),
     "sbp_csr_assemble_host": (_i, [_i, C.POINTER(C.c_longlong), C.POINTER(_i), _dp,
                                    C.c_longlong, C.POINTER(C.c_longlong)]),
     "sbp_csr_spmv_f64": (_i, [C.c_longlong, _vp, _vp, _vp, _vp, _vp, _vp]),

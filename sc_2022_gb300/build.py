@@ -19,8 +19,8 @@ INCLUDE = PKG.parent / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libsbpmg.so"
 
-SOURCES = ["sbp_kernels.cu", "sbp_high_order.cu", "sbp_capi.cpp", "sbp_ho_solver.cpp",
-           "sbp_coarse.cpp", "sbp_tma.cpp", "sbp_csr.cpp"]
+SOURCES = ["sbp_kernels.cu", "sbp_high_order.cu", "sbp_varcoef.cu", "sbp_capi.cpp",
+           "sbp_op_solver.cpp", "sbp_coarse.cpp", "sbp_tma.cpp", "sbp_csr.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

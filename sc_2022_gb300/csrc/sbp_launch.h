@@ -229,6 +229,16 @@ struct HoArgsT {
   double* norms;       // init: norms[0] = ||r0||
 };
 using HoArgs = HoArgsT<double>;
+// The variable-coefficient kernels take the same arguments plus the level's
+// stencil arrays (sbp_varcoef.cuh).
+template <typename T>
+struct VcArgsT : HoArgsT<T> {
+  const T* E;
+  const T* N;
+  const T* D;
+  const T* flo;
+  const T* fhi;
+};
 // Smallest grid of order p (0 if p is not 4 or 6).
 int ho_min_n(int p);
 // Upload the closure tables once (outside stream capture).
@@ -244,6 +254,24 @@ cudaError_t launch_ho_rz(const double* r, const Tz* z, long long N, SolveState* 
 template <typename Tz>
 cudaError_t launch_ho_dir(const Tz* z, double* p, long long N, const SolveState* st,
                           int first, cudaStream_t s);
+
+// ---- variable-coefficient operator (sbp_varcoef.cuh), contiguous grids ----
+// out = sign * A u straight from the nodal coefficients c (FP64; dot_out: u . out).
+cudaError_t launch_vc_apply_c(const double* u, const double* c, double* out, int n, int sign,
+                              ReduceBuf rb, double* dot_out, cudaStream_t s);
+// The level's stencil arrays from its nodal coefficients.
+template <typename T>
+cudaError_t launch_vc_stencil(const double* c, T* E, T* N, T* D, T* flo, T* fhi, int n,
+                              cudaStream_t s);
+// Coarse nodal coefficients by injection: cc(I, J) = cf(2I, 2J).
+cudaError_t launch_vc_inject(const double* cf, double* cc, int nc, cudaStream_t s);
+// Apply / residual / smoother on the stencil arrays (modes as launch_ho).
+template <typename T>
+cudaError_t launch_vc(int mode, VcArgsT<T> a, cudaStream_t s);
+// x = Ainv b with a dense FP64 N x N inverse (row-major).
+template <typename T>
+cudaError_t launch_dense_gemv(const double* Ainv, const T* b, T* x, int N, const SolveState* st,
+                              cudaStream_t s);
 
 // y = A x for a CSR matrix with nrows rows (64-bit row pointers).
 cudaError_t launch_csr_spmv(long long nrows, const long long* row_ptr, const int* col,

@@ -1,0 +1,307 @@
+// Variable-coefficient (div(c grad u)) second-order SBP-SAT kernels.
+//
+// - k_vc_apply_c: -A u straight from the nodal coefficients.  It is the
+//   standalone apply and reads u, c and writes out: 24 bytes per point in
+//   FP64.
+// - k_vc_stencil: the per-point stencil arrays E, N, D and the boundary
+//   couplings Flo / Fhi of sbp_varcoef.cuh, computed once per level from c.
+// - k_vc<MODE>: the solver's apply / residual / Jacobi sweep on those
+//   arrays, in FP64 or FP32.  Five multiply-adds per point instead of the
+//   face averages.
+// - k_vc_inject: the coarse coefficients, by injection.
+// - k_dense_gemv: the coarse direct solve, x = A^-1 b with a dense inverse.
+// The access pattern is that of the other stencil kernels: a row per thread,
+// a march along j with the row's own values in registers, and i-neighbours
+// from the cache (a warp covers 32 consecutive rows of a column).
+#include <algorithm>
+
+#include "sbp_kernels.cuh"
+#include "sbp_launch.h"
+#include "sbp_varcoef.cuh"
+
+namespace sbp {
+
+namespace {
+
+__device__ __forceinline__ double fmaT(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fmaT(float a, float b, float c) { return fmaf(a, b, c); }
+
+int vc_cols(int n) {
+  const long long nrb = (n + kThreads - 1) / kThreads;
+  const long long c = (long long)n * nrb / (2LL * 152);
+  return (int)std::max(1LL, std::min(32LL, c));
+}
+
+dim3 vc_grid(int n, int cols) {
+  const long long nrb = (n + kThreads - 1) / kThreads;
+  const long long items = nrb * ((n + cols - 1) / cols);
+  return dim3((unsigned)std::min<long long>(items, kMaxPersistCtas));
+}
+
+// out = sign * A u from nodal c (FP64); dot: u . out.
+template <bool DOT>
+__global__ void __launch_bounds__(kThreads)
+    k_vc_apply_c(const double* __restrict__ u, const double* __restrict__ c,
+                 double* __restrict__ out, int n, int sign, int cols, ReduceBuf rb,
+                 double* dot_out) {
+  pdl_begin();
+  const int nrb = (n + kThreads - 1) / kThreads;
+  const int items = nrb * ((n + cols - 1) / cols);
+  double acc = 0.0;
+  for (int w = blockIdx.x; w < items; w += gridDim.x) {
+    const int i = (w % nrb) * kThreads + threadIdx.x;
+    if (i >= n) continue;
+    const int j0 = (w / nrb) * cols;
+    const int j1 = min(n, j0 + cols);
+    const double wi = vc::weight(i, n);
+    auto U = [&](int ii, int jj) { return __ldg(u + (size_t)jj * n + ii); };
+    auto Cf = [&](int ii, int jj) { return __ldg(c + (size_t)jj * n + ii); };
+    // register window along j: u and c at j-1, j, j+1
+    double um = j0 > 0 ? U(i, j0 - 1) : 0.0, u0 = U(i, j0);
+    double cm = j0 > 0 ? Cf(i, j0 - 1) : 0.0, c0 = Cf(i, j0);
+    for (int j = j0; j < j1; ++j) {
+      const double up = j + 1 < n ? U(i, j + 1) : 0.0;
+      const double cp = j + 1 < n ? Cf(i, j + 1) : 0.0;
+      double x = 0.0;
+      if (i > 0) x = fma(0.5 * (Cf(i - 1, j) + c0), U(i - 1, j) - u0, x);
+      if (i < n - 1) x = fma(0.5 * (c0 + Cf(i + 1, j)), U(i + 1, j) - u0, x);
+      double y = 0.0;
+      if (j > 0) y = fma(0.5 * (cm + c0), um - u0, y);
+      if (j < n - 1) y = fma(0.5 * (c0 + cp), up - u0, y);
+      if (j <= 2 || j >= n - 3) {   // Dirichlet closure, scaled by the boundary c
+        if (j == 0)
+          y += c0 * (vc::kBs0 * u0 + vc::kBs1 * up + vc::kBs2 * U(i, 2) +
+                     (vc::kTauDh + vc::kBs0) * u0);
+        if (j == n - 1)
+          y += c0 * (vc::kBs0 * u0 + vc::kBs1 * um + vc::kBs2 * U(i, n - 3) +
+                     (vc::kTauDh + vc::kBs0) * u0);
+        if (j == 1) y += vc::kBs1 * Cf(i, 0) * U(i, 0);
+        if (j == 2) y += vc::kBs2 * Cf(i, 0) * U(i, 0);
+        if (j == n - 2) y += vc::kBs1 * Cf(i, n - 1) * U(i, n - 1);
+        if (j == n - 3) y += vc::kBs2 * Cf(i, n - 1) * U(i, n - 1);
+      }
+      const double na = fma(vc::weight(j, n), x, wi * y);   // (-A u)(i, j)
+      const double v = sign > 0 ? -na : na;
+      out[(size_t)j * n + i] = v;
+      if (DOT) acc = fma(u0, v, acc);
+      um = u0;
+      u0 = up;
+      cm = c0;
+      c0 = cp;
+    }
+  }
+  if (DOT) grid_reduce(acc, rb, [&](double tot) { *dot_out = tot; });
+}
+
+// Stencil arrays of one level from its nodal coefficients.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    k_vc_stencil(const double* __restrict__ c, T* __restrict__ E, T* __restrict__ N,
+                 T* __restrict__ D, T* __restrict__ flo, T* __restrict__ fhi, int n) {
+  const long long total = (long long)n * n;
+  struct Acc {
+    const double* c;
+    int n;
+    __device__ double operator()(int i, int j) const { return __ldg(c + (size_t)j * n + i); }
+  } acc{c, n};
+  for (long long k = (long long)blockIdx.x * kThreads + threadIdx.x; k < total;
+       k += (long long)gridDim.x * kThreads) {
+    const int i = (int)(k % n), j = (int)(k / n);
+    double e, nn, d;
+    vc::coefficients(acc, i, j, n, e, nn, d);
+    E[k] = (T)e;
+    N[k] = (T)nn;
+    D[k] = (T)d;
+    if (j == 0) flo[i] = (T)vc::f_lo(acc(i, 0), i, n);
+    if (j == n - 1) fhi[i] = (T)vc::f_hi(acc(i, n - 1), i, n);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads)
+    k_vc_inject(const double* __restrict__ cf, double* __restrict__ cc, int nc) {
+  const int nf = 2 * nc - 1;
+  const long long total = (long long)nc * nc;
+  for (long long k = (long long)blockIdx.x * kThreads + threadIdx.x; k < total;
+       k += (long long)gridDim.x * kThreads) {
+    const int I = (int)(k % nc), J = (int)(k / nc);
+    cc[k] = __ldg(cf + (size_t)(2 * J) * nf + 2 * I);
+  }
+}
+
+template <int MODE, bool DOT, typename T>
+__global__ void __launch_bounds__(kThreads) k_vc(const VcArgsT<T> a) {
+  pdl_begin();
+  if (a.st && a.st->done) return;
+  const int n = a.n, cols = a.cols;
+  const int nrb = (n + kThreads - 1) / kThreads;
+  const int items = nrb * ((n + cols - 1) / cols);
+  const T* __restrict__ u = a.u;
+  const T* __restrict__ b = a.b;
+  const T* __restrict__ E = a.E;
+  const T* __restrict__ Nc = a.N;
+  const T* __restrict__ D = a.D;
+  T* __restrict__ out = a.out;
+  const T omega = T(a.omega);
+  DotAcc<T> acc;
+  for (int w = blockIdx.x; w < items; w += gridDim.x) {
+    const int i = (w % nrb) * kThreads + threadIdx.x;
+    if (i >= n) continue;
+    const int j0 = (w / nrb) * cols;
+    const int j1 = min(n, j0 + cols);
+    if (MODE == kHoJacobi && a.zero_in) {   // first sweep from v = 0
+      for (int j = j0; j < j1; ++j) {
+        const size_t k = (size_t)j * n + i;
+        const T d = __ldg(D + k);
+        out[k] = a.richardson ? omega * __ldg(b + k) : omega * __ldg(b + k) / d;
+      }
+      continue;
+    }
+    const T flo = __ldg(a.flo + i), fhi = __ldg(a.fhi + i);
+    auto U = [&](int ii, int jj) { return __ldg(u + (size_t)jj * n + ii); };
+    T um = j0 > 0 ? U(i, j0 - 1) : T(0), u0 = U(i, j0);
+    T nm = j0 > 0 ? __ldg(Nc + (size_t)(j0 - 1) * n + i) : T(0);
+    for (int j = j0; j < j1; ++j) {
+      const size_t k = (size_t)j * n + i;
+      const T up = j + 1 < n ? U(i, j + 1) : T(0);
+      const T n0 = __ldg(Nc + k);
+      const T d = __ldg(D + k);
+      T na = -d * u0;
+      na = fmaT(nm, um, na);
+      na = fmaT(n0, up, na);
+      if (i > 0) na = fmaT(__ldg(E + k - 1), U(i - 1, j), na);
+      if (i < n - 1) na = fmaT(__ldg(E + k), U(i + 1, j), na);
+      if (j <= 2 || j >= n - 3) {
+        if (j == 0) na = fmaT(flo, U(i, 2), na);
+        if (j == 2) na = fmaT(flo, U(i, 0), na);
+        if (j == n - 1) na = fmaT(fhi, U(i, n - 3), na);
+        if (j == n - 3) na = fmaT(fhi, U(i, n - 1), na);
+      }
+      T v;
+      if (MODE == kHoApply) {
+        v = a.sign > 0 ? -na : na;
+      } else if (MODE == kHoResid) {
+        v = __ldg(b + k) + (a.sign > 0 ? na : -na);
+      } else {
+        const T r = __ldg(b + k) + na;
+        v = a.richardson ? fmaT(omega, r, u0) : fmaT(omega, r / d, u0);
+      }
+      out[k] = v;
+      if (DOT) acc.add_prod(MODE == kHoApply ? u0 : v, v);
+      um = u0;
+      u0 = up;
+      nm = n0;
+    }
+  }
+  if (DOT)
+    grid_reduce(acc.value(), a.rb, [&](double tot) {
+      if (a.dot_out) *a.dot_out = tot;
+      SolveState* st = a.st;
+      if (!st) return;
+      if (MODE == kHoApply) {
+        st->pAp = tot;
+        if (!isfinite(tot) || tot == 0.0)
+          st->done = kDoneBreakdown;
+        else
+          st->alpha = st->rz / tot;
+      } else if (MODE == kHoResid && a.init) {
+        st->rr0 = st->rr = tot;
+        st->rz = tot;
+        st->thresh2 = a.abstol > 0.0 ? a.abstol * a.abstol : a.reltol * a.reltol * tot;
+        st->iter = 0;
+        if (a.norms) a.norms[0] = sqrt(tot);
+        if (!isfinite(tot))
+          st->done = kDoneBreakdown;
+        else if (tot < st->thresh2 || tot == 0.0)
+          st->done = kDoneConverged;
+        else if (st->maxiter <= 0)
+          st->done = kDoneMaxIter;
+      }
+    });
+}
+
+// x = Ainv b on the coarse grid: one warp per row, FP64 accumulation.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    k_dense_gemv(const double* __restrict__ Ainv, const T* __restrict__ b, T* __restrict__ x,
+                 int N, const SolveState* st) {
+  pdl_begin();
+  if (st && st->done) return;
+  const int lane = threadIdx.x & 31;
+  const int warps = gridDim.x * kWarps;
+  for (int r = blockIdx.x * kWarps + (threadIdx.x >> 5); r < N; r += warps) {
+    const double* row = Ainv + (size_t)r * N;
+    double s = 0.0;
+    for (int k = lane; k < N; k += 32) s = fma(__ldg(row + k), (double)__ldg(b + k), s);
+    s = warp_sum(s);
+    if (lane == 0) x[r] = (T)s;
+  }
+}
+
+template <int MODE, typename T>
+cudaError_t launch_vc_mode(const VcArgsT<T>& a, dim3 grid, cudaStream_t s) {
+  if (a.rb.partials) return launch_pdl(k_vc<MODE, true, T>, grid, dim3(kThreads), 0, s, a);
+  return launch_pdl(k_vc<MODE, false, T>, grid, dim3(kThreads), 0, s, a);
+}
+
+}  // namespace
+
+cudaError_t launch_vc_apply_c(const double* u, const double* c, double* out, int n, int sign,
+                              ReduceBuf rb, double* dot_out, cudaStream_t s) {
+  if (n < 3) return cudaErrorInvalidValue;
+  const int cols = vc_cols(n);
+  const dim3 g = vc_grid(n, cols);
+  if (dot_out)
+    return launch_pdl(k_vc_apply_c<true>, g, dim3(kThreads), 0, s, u, c, out, n, sign, cols, rb,
+                      dot_out);
+  return launch_pdl(k_vc_apply_c<false>, g, dim3(kThreads), 0, s, u, c, out, n, sign, cols, rb,
+                    dot_out);
+}
+
+template <typename T>
+cudaError_t launch_vc_stencil(const double* c, T* E, T* N, T* D, T* flo, T* fhi, int n,
+                              cudaStream_t s) {
+  const long long total = (long long)n * n;
+  const int g = (int)std::max(1LL, std::min<long long>((total + kThreads - 1) / kThreads, 4096));
+  k_vc_stencil<T><<<g, kThreads, 0, s>>>(c, E, N, D, flo, fhi, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_vc_inject(const double* cf, double* cc, int nc, cudaStream_t s) {
+  const long long total = (long long)nc * nc;
+  const int g = (int)std::max(1LL, std::min<long long>((total + kThreads - 1) / kThreads, 4096));
+  k_vc_inject<<<g, kThreads, 0, s>>>(cf, cc, nc);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_vc(int mode, VcArgsT<T> a, cudaStream_t s) {
+  if (a.n < 3 || !a.out) return cudaErrorInvalidValue;
+  if (a.cols <= 0) a.cols = vc_cols(a.n);
+  const dim3 g = vc_grid(a.n, a.cols);
+  switch (mode) {
+    case kHoApply: return launch_vc_mode<kHoApply>(a, g, s);
+    case kHoResid: return launch_vc_mode<kHoResid>(a, g, s);
+    case kHoJacobi: return launch_vc_mode<kHoJacobi>(a, g, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <typename T>
+cudaError_t launch_dense_gemv(const double* Ainv, const T* b, T* x, int N, const SolveState* st,
+                              cudaStream_t s) {
+  const int g = std::max(1, std::min((N + kWarps - 1) / kWarps, 1024));
+  return launch_pdl(k_dense_gemv<T>, dim3(g), dim3(kThreads), 0, s, Ainv, b, x, N, st);
+}
+
+template cudaError_t launch_vc_stencil<double>(const double*, double*, double*, double*, double*,
+                                               double*, int, cudaStream_t);
+template cudaError_t launch_vc_stencil<float>(const double*, float*, float*, float*, float*,
+                                              float*, int, cudaStream_t);
+template cudaError_t launch_vc<double>(int, VcArgsT<double>, cudaStream_t);
+template cudaError_t launch_vc<float>(int, VcArgsT<float>, cudaStream_t);
+template cudaError_t launch_dense_gemv<double>(const double*, const double*, double*, int,
+                                               const SolveState*, cudaStream_t);
+template cudaError_t launch_dense_gemv<float>(const double*, const float*, float*, int,
+                                              const SolveState*, cudaStream_t);
+
+}  // namespace sbp

@@ -94,3 +94,22 @@ def test_csr_assembly_equals_oracle_matrix(lib, n):
     assert np.array_equal(A.indptr, rp)
     assert np.array_equal(A.indices, col)
     assert np.array_equal(A.data, val)
+
+
+@pytest.mark.parametrize("n,kind", [(3, "smooth"), (4, "layered"), (9, "smooth"), (17, "layered"),
+                                    (33, "smooth")])
+def test_variable_assembly_equals_oracle_matrix(n, kind):
+    # the library's per-point variable-coefficient stencil, as CSR, against
+    # the oracle's assembly of variable_diagonal_sbp_D2 per grid line
+    import sc_2022_gb300 as sbp
+    from oracle import sbp_oracle as o
+    import scipy.sparse as sp
+    c = o.coefficient_field(n, kind)
+    rp, col, val = sbp.assemble_variable_host(n, c)
+    A = sp.csr_matrix((val, col, rp), shape=(n * n, n * n))
+    ref = o.assemble_variable(n, c).A
+    assert abs(A - ref).max() <= 1e-13 * abs(ref).max()
+    # c = 1: the constant-coefficient matrix
+    rp1, col1, val1 = sbp.assemble_variable_host(n, np.ones(n * n))
+    A1 = sp.csr_matrix((val1, col1, rp1), shape=(n * n, n * n))
+    assert abs(A1 - o.assemble(n).A).max() == 0.0
