@@ -103,50 +103,66 @@ __global__ void __launch_bounds__(kThreads) k_ho(const HoArgsT<T> a) {
     T c[W];
 #pragma unroll
     for (int k = 0; k < W - 1; ++k) c[k] = col(j0 - R + k);
-    for (int j = j0; j < j1; ++j) {
-      c[W - 1] = col(j + R);
-      T xi;
-      if (xin) {
-        xi = kD0 * c[R];
-#pragma unroll
-        for (int k = 1; k <= R; ++k) xi = fmaT(dk(k), at(i - k, j) + at(i + k, j), xi);
-      } else {
-        xi = T(0);
-#pragma unroll
-        for (int q = 0; q < BN; ++q) xi = fmaT(tx[xr * BN + q], at(xlo ? q : n - 1 - q, j), xi);
+    // chunks of kHoChunk columns: the chunk's window columns and right-hand
+    // sides are loaded together, so a warp keeps several DRAM lines in flight
+    // (p = 6: the wider window and closures leave no registers for it;
+    // measured slower)
+    constexpr int kHoChunk = P == 4 ? 4 : 1;
+    for (int jc = j0; jc < j1; jc += kHoChunk) {
+      T cn[kHoChunk], bn[kHoChunk];
+  #pragma unroll
+      for (int q = 0; q < kHoChunk; ++q) {
+        cn[q] = col(jc + q + R);
+        bn[q] = (MODE != kHoApply && jc + q < j1) ? __ldg(b + (size_t)(jc + q) * n + i) : T(0);
       }
-      const bool yin = j >= BM && j <= n - 1 - BM;
-      const bool ylo = j < BM;
-      const int yr = ylo ? j : n - 1 - j;
-      T yj;
-      if (yin) {
-        yj = kD0 * c[R];
-#pragma unroll
-        for (int k = 1; k <= R; ++k) yj = fmaT(dk(k), c[R - k] + c[R + k], yj);
-      } else {
-        yj = T(0);
-#pragma unroll
-        for (int q = 0; q < BN; ++q) yj = fmaT(ty[yr * BN + q], col(ylo ? q : n - 1 - q), yj);
-      }
-      const T wj = T(ho::weight<P>(j, n));
-      const T na = fmaT(wj, xi, wi * yj);   // (-A u)(i, j)
-      T v;
-      if (MODE == kHoApply) {
-        v = a.sign > 0 ? -na : na;
-      } else if (MODE == kHoResid) {
-        v = __ldg(b + (size_t)j * n + i) + (a.sign > 0 ? na : -na);
-      } else {
-        T inv = T(1);
-        if (!a.richardson) {
-          const T dyy = yin ? kD0 : ty[yr * BN + yr];
-          inv = (xin && yin) ? kInvDiagIn : T(-1) / (wj * dxx + wi * dyy);
+  #pragma unroll
+      for (int q = 0; q < kHoChunk; ++q) {
+        const int j = jc + q;
+        if (j >= j1) break;
+        c[W - 1] = cn[q];
+        T xi;
+        if (xin) {
+          xi = kD0 * c[R];
+  #pragma unroll
+          for (int k = 1; k <= R; ++k) xi = fmaT(dk(k), at(i - k, j) + at(i + k, j), xi);
+        } else {
+          xi = T(0);
+  #pragma unroll
+          for (int q = 0; q < BN; ++q) xi = fmaT(tx[xr * BN + q], at(xlo ? q : n - 1 - q, j), xi);
         }
-        v = fmaT(omega * inv, __ldg(b + (size_t)j * n + i) + na, c[R]);
+        const bool yin = j >= BM && j <= n - 1 - BM;
+        const bool ylo = j < BM;
+        const int yr = ylo ? j : n - 1 - j;
+        T yj;
+        if (yin) {
+          yj = kD0 * c[R];
+  #pragma unroll
+          for (int k = 1; k <= R; ++k) yj = fmaT(dk(k), c[R - k] + c[R + k], yj);
+        } else {
+          yj = T(0);
+  #pragma unroll
+          for (int q = 0; q < BN; ++q) yj = fmaT(ty[yr * BN + q], col(ylo ? q : n - 1 - q), yj);
+        }
+        const T wj = T(ho::weight<P>(j, n));
+        const T na = fmaT(wj, xi, wi * yj);   // (-A u)(i, j)
+        T v;
+        if (MODE == kHoApply) {
+          v = a.sign > 0 ? -na : na;
+        } else if (MODE == kHoResid) {
+          v = bn[q] + (a.sign > 0 ? na : -na);
+        } else {
+          T inv = T(1);
+          if (!a.richardson) {
+            const T dyy = yin ? kD0 : ty[yr * BN + yr];
+            inv = (xin && yin) ? kInvDiagIn : T(-1) / (wj * dxx + wi * dyy);
+          }
+          v = fmaT(omega * inv, bn[q] + na, c[R]);
+        }
+        out[(size_t)j * n + i] = v;
+        if (DOT) acc.add_prod(MODE == kHoApply ? c[R] : v, v);
+  #pragma unroll
+        for (int k = 0; k < W - 1; ++k) c[k] = c[k + 1];
       }
-      out[(size_t)j * n + i] = v;
-      if (DOT) acc.add_prod(MODE == kHoApply ? c[R] : v, v);
-#pragma unroll
-      for (int k = 0; k < W - 1; ++k) c[k] = c[k + 1];
     }
   }
   if (DOT)

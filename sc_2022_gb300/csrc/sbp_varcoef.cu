@@ -160,36 +160,56 @@ __global__ void __launch_bounds__(kThreads) k_vc(const VcArgsT<T> a) {
     auto U = [&](int ii, int jj) { return __ldg(u + (size_t)jj * n + ii); };
     T um = j0 > 0 ? U(i, j0 - 1) : T(0), u0 = U(i, j0);
     T nm = j0 > 0 ? __ldg(Nc + (size_t)(j0 - 1) * n + i) : T(0);
-    for (int j = j0; j < j1; ++j) {
-      const size_t k = (size_t)j * n + i;
-      const T up = j + 1 < n ? U(i, j + 1) : T(0);
-      const T n0 = __ldg(Nc + k);
-      const T d = __ldg(D + k);
-      T na = -d * u0;
-      na = fmaT(nm, um, na);
-      na = fmaT(n0, up, na);
-      if (i > 0) na = fmaT(__ldg(E + k - 1), U(i - 1, j), na);
-      if (i < n - 1) na = fmaT(__ldg(E + k), U(i + 1, j), na);
-      if (j <= 2 || j >= n - 3) {
-        if (j == 0) na = fmaT(flo, U(i, 2), na);
-        if (j == 2) na = fmaT(flo, U(i, 0), na);
-        if (j == n - 1) na = fmaT(fhi, U(i, n - 3), na);
-        if (j == n - 3) na = fmaT(fhi, U(i, n - 1), na);
+    // chunks of kVcChunk columns: the chunk's own-row loads are issued
+    // together, so a warp keeps several DRAM lines in flight
+    constexpr int kVcChunk = 4;
+    for (int jc = j0; jc < j1; jc += kVcChunk) {
+      T upc[kVcChunk], nc[kVcChunk], dc[kVcChunk], ec[kVcChunk], bc[kVcChunk];
+  #pragma unroll
+      for (int q = 0; q < kVcChunk; ++q) {
+        const int j = jc + q;
+        const bool in = j < j1;
+        const size_t k = (size_t)j * n + i;
+        upc[q] = (in && j + 1 < n) ? U(i, j + 1) : T(0);
+        nc[q] = in ? __ldg(Nc + k) : T(0);
+        dc[q] = in ? __ldg(D + k) : T(0);
+        ec[q] = (in && i < n - 1) ? __ldg(E + k) : T(0);
+        bc[q] = (in && MODE != kHoApply) ? __ldg(b + k) : T(0);
       }
-      T v;
-      if (MODE == kHoApply) {
-        v = a.sign > 0 ? -na : na;
-      } else if (MODE == kHoResid) {
-        v = __ldg(b + k) + (a.sign > 0 ? na : -na);
-      } else {
-        const T r = __ldg(b + k) + na;
-        v = a.richardson ? fmaT(omega, r, u0) : fmaT(omega, r / d, u0);
+  #pragma unroll
+      for (int q = 0; q < kVcChunk; ++q) {
+        const int j = jc + q;
+        if (j >= j1) break;
+        const size_t k = (size_t)j * n + i;
+        const T up = upc[q];
+        const T n0 = nc[q];
+        const T d = dc[q];
+        T na = -d * u0;
+        na = fmaT(nm, um, na);
+        na = fmaT(n0, up, na);
+        if (i > 0) na = fmaT(__ldg(E + k - 1), U(i - 1, j), na);
+        if (i < n - 1) na = fmaT(ec[q], U(i + 1, j), na);
+        if (j <= 2 || j >= n - 3) {
+          if (j == 0) na = fmaT(flo, U(i, 2), na);
+          if (j == 2) na = fmaT(flo, U(i, 0), na);
+          if (j == n - 1) na = fmaT(fhi, U(i, n - 3), na);
+          if (j == n - 3) na = fmaT(fhi, U(i, n - 1), na);
+        }
+        T v;
+        if (MODE == kHoApply) {
+          v = a.sign > 0 ? -na : na;
+        } else if (MODE == kHoResid) {
+          v = bc[q] + (a.sign > 0 ? na : -na);
+        } else {
+          const T r = bc[q] + na;
+          v = a.richardson ? fmaT(omega, r, u0) : fmaT(omega, r / d, u0);
+        }
+        out[k] = v;
+        if (DOT) acc.add_prod(MODE == kHoApply ? u0 : v, v);
+        um = u0;
+        u0 = up;
+        nm = n0;
       }
-      out[k] = v;
-      if (DOT) acc.add_prod(MODE == kHoApply ? u0 : v, v);
-      um = u0;
-      u0 = up;
-      nm = n0;
     }
   }
   if (DOT)
