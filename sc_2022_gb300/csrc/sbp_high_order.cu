@@ -225,6 +225,133 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// Mixed-precision CG direction for the order-p operator (z = the FP32
+// V-cycle output, p and Ap FP64, both updated in place):
+//   p  = z + beta p          Ap = A z + beta Ap          p.Ap -> alpha
+// A p by linearity, so the FP64 apply (12 to 16 FP64 instructions per
+// point) becomes A z on the FP32 pipe plus three FP64 instructions.  At
+// interior points A z is summed in float-float: each coefficient d_k is an
+// unevaluated float pair, the products are exact on the high part, and the
+// sums use two_sum.  The result is within about 2^-45 of the largest term.
+// Closure rows and columns (2 bm of n each way) use FP64 on the exact FP32
+// values.  p.Ap comes from the FP32 roundings with compensated accumulation
+// (alpha needs ~1e-7; the FP64 recurrences keep their accuracy).
+template <int P>
+__global__ void __launch_bounds__(kThreads)
+    k_ho_dir_mixed(const float* __restrict__ z, double* __restrict__ p, double* __restrict__ ap,
+                   int n, int cols, SolveState* st, ReduceBuf rb) {
+  using O = ho::Order<P>;
+  constexpr int R = O::kHalf, W = 2 * R + 1, BM = O::kBm, BN = O::kBn;
+  pdl_begin();
+  if (st->done) return;
+  const bool first = st->iter == 0;
+  const double beta = st->beta;
+  const int nrb = (n + kThreads - 1) / kThreads;
+  const int items = nrb * ((n + cols - 1) / cols);
+  const double* tx = tab<P, double>(0);
+  const double* ty = tab<P, double>(1);
+  // d_k as float pairs (folded at compile time); the centre weight is 2 d_0
+  auto dhi = [](int k) { return k == 0 ? (float)(2.0 * O::d(0)) : (float)O::d(k); };
+  auto dlo = [](int k) {
+    const double d = k == 0 ? 2.0 * O::d(0) : O::d(k);
+    return (float)(d - (double)(float)d);
+  };
+  DotAcc<float> acc;
+  for (int w = blockIdx.x; w < items; w += gridDim.x) {
+    const int i = (w % nrb) * kThreads + threadIdx.x;
+    if (i >= n) continue;
+    const int j0 = (w / nrb) * cols;
+    const int j1 = min(n, j0 + cols);
+    const double wi = ho::weight<P>(i, n);
+    const bool xin = i >= BM && i <= n - 1 - BM;
+    const bool xlo = i < BM;
+    const int xr = xlo ? i : n - 1 - i;
+    const float* row = z + i;
+    auto at = [&](int ii, int jj) { return __ldg(z + (size_t)jj * n + ii); };
+    auto col = [&](int jj) { return (jj >= 0 && jj < n) ? __ldg(row + (size_t)jj * n) : 0.0f; };
+    float c[W];
+#pragma unroll
+    for (int k = 0; k < W - 1; ++k) c[k] = col(j0 - R + k);
+    for (int j = j0; j < j1; ++j) {
+      c[W - 1] = col(j + R);
+      const bool yin = j >= BM && j <= n - 1 - BM;
+      double azd;   // (A z)(i, j)
+      if (xin && yin) {
+        // sum_k d_k (z(i-k) + z(i+k) + z(j-k) + z(j+k)) + 2 d_0 z, float-float
+        float hi, lo;
+        {
+          const float z0 = c[R];
+          hi = dhi(0) * z0;
+          lo = fmaf(dhi(0), z0, -hi);
+          lo = fmaf(dlo(0), z0, lo);
+        }
+#pragma unroll
+        for (int k = 1; k <= R; ++k) {
+          float a, ea, b, eb, sk, es;
+          two_sum(at(i - k, j), at(i + k, j), a, ea);
+          two_sum(c[R - k], c[R + k], b, eb);
+          two_sum(a, b, sk, es);
+          const float sl = es + (ea + eb);
+          const float pr = dhi(k) * sk;
+          float e = fmaf(dhi(k), sk, -pr);
+          e = fmaf(dhi(k), sl, e);
+          e = fmaf(dlo(k), sk, e);
+          float t, te;
+          two_sum(hi, pr, t, te);
+          hi = t;
+          lo += te + e;
+        }
+        azd = -(f32_to_f64(hi) + f32_to_f64(lo));   // A z = -(-A z)
+      } else {
+        // closure rows / columns: the FP64 formula on the exact FP32 values
+        double xi;
+        if (xin) {
+          xi = O::d(0) * f32_to_f64(c[R]);
+#pragma unroll
+          for (int k = 1; k <= R; ++k)
+            xi = fma(O::d(k), f32_to_f64(at(i - k, j)) + f32_to_f64(at(i + k, j)), xi);
+        } else {
+          xi = 0.0;
+#pragma unroll
+          for (int q = 0; q < BN; ++q)
+            xi = fma(tx[xr * BN + q], f32_to_f64(at(xlo ? q : n - 1 - q, j)), xi);
+        }
+        const bool ylo = j < BM;
+        const int yr = ylo ? j : n - 1 - j;
+        double yj;
+        if (yin) {
+          yj = O::d(0) * f32_to_f64(c[R]);
+#pragma unroll
+          for (int k = 1; k <= R; ++k)
+            yj = fma(O::d(k), f32_to_f64(c[R - k]) + f32_to_f64(c[R + k]), yj);
+        } else {
+          yj = 0.0;
+#pragma unroll
+          for (int q = 0; q < BN; ++q)
+            yj = fma(ty[yr * BN + q], f32_to_f64(col(ylo ? q : n - 1 - q)), yj);
+        }
+        azd = -fma(ho::weight<P>(j, n), xi, wi * yj);
+      }
+      const size_t k = (size_t)j * n + i;
+      const double zd = f32_to_f64(c[R]);
+      const double pv = first ? zd : fma(beta, p[k], zd);
+      const double av = first ? azd : fma(beta, ap[k], azd);
+      p[k] = pv;
+      ap[k] = av;
+      acc.add_prod(f64_to_f32(pv), f64_to_f32(av));
+#pragma unroll
+      for (int q = 0; q < W - 1; ++q) c[q] = c[q + 1];
+    }
+  }
+  grid_reduce(acc.value(), rb, [&](double tot) {
+    st->pAp = tot;
+    if (!isfinite(tot) || tot == 0.0)
+      st->done = kDoneBreakdown;
+    else
+      st->alpha = st->rz / tot;
+  });
+}
+
 int flat_ctas(long long N) {
   const long long want = (N + (long long)kThreads * 4 - 1) / ((long long)kThreads * 4);
   return (int)std::max(1LL, std::min<long long>(want, kMaxPersistCtas));
@@ -312,6 +439,18 @@ template <typename Tz>
 cudaError_t launch_ho_dir(const Tz* z, double* p, long long N, const SolveState* st,
                           int first, cudaStream_t s) {
   return launch_pdl(k_ho_dir<Tz>, dim3(flat_ctas(N)), dim3(kThreads), 0, s, z, p, N, st, first);
+}
+
+cudaError_t launch_ho_dir_mixed(int p, const float* z, double* pd, double* ap, int n,
+                                SolveState* st, ReduceBuf rb, cudaStream_t s) {
+  if (ho_min_n(p) == 0 || n < ho_min_n(p) || !rb.partials) return cudaErrorInvalidValue;
+  const int cols = ho_cols(n);
+  const long long nrb = (n + kThreads - 1) / kThreads;
+  const long long items = nrb * ((n + cols - 1) / cols);
+  const dim3 grid((unsigned)std::min<long long>(items, kMaxPersistCtas));
+  if (p == 4)
+    return launch_pdl(k_ho_dir_mixed<4>, grid, dim3(kThreads), 0, s, z, pd, ap, n, cols, st, rb);
+  return launch_pdl(k_ho_dir_mixed<6>, grid, dim3(kThreads), 0, s, z, pd, ap, n, cols, st, rb);
 }
 
 template cudaError_t launch_ho<double>(int, int, HoArgsT<double>, cudaStream_t);

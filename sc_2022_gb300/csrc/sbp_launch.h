@@ -254,6 +254,11 @@ cudaError_t launch_ho_rz(const double* r, const Tz* z, long long N, SolveState* 
 template <typename Tz>
 cudaError_t launch_ho_dir(const Tz* z, double* p, long long N, const SolveState* st,
                           int first, cudaStream_t s);
+// Mixed-precision order-p CG direction, in place: p = z + beta p,
+// Ap = A z + beta Ap (A z on the FP32 pipe), p.Ap -> alpha; the first
+// direction (state iteration 0) takes p = z, Ap = A z.
+cudaError_t launch_ho_dir_mixed(int p, const float* z, double* pd, double* ap, int n,
+                                SolveState* st, ReduceBuf rb, cudaStream_t s);
 
 // ---- variable-coefficient operator (sbp_varcoef.cuh), contiguous grids ----
 // out = sign * A u straight from the nodal coefficients c (FP64; dot_out: u . out).

@@ -226,11 +226,34 @@ cudaError_t precondition(OpSolver* s, int first, cudaStream_t q) {
   return launch_ho_dir<T>(z, s->pd, N, s->st, first, q);
 }
 
+// Mixed-precision order-p MGCG forms Ap with the direction: z = V(r),
+// beta, then p = z + beta p and Ap = A z + beta Ap with p.Ap -> alpha in one
+// kernel (A z on the FP32 pipe), so an iteration has no FP64 apply.
+bool fused_direction(const OpSolver* s) { return s->mixed && s->kind == kOpHighOrder; }
+
+cudaError_t precondition_fused(OpSolver* s, int first, cudaStream_t q) {
+  cudaError_t err = cudaSuccess;
+  const long long N = (long long)s->n * s->n;
+  float* z = vcycle<float>(s, 0, q, err);
+  if (err != cudaSuccess) return err;
+  err = launch_ho_rz<float>(s->r, z, N, s->st, s->rb[2], first, q);
+  if (err != cudaSuccess) return err;
+  return launch_ho_dir_mixed(s->p, z, s->pd, s->ap, s->n, s->st, s->rb[0], q);
+}
+
 // The iteration body: Ap and alpha, x/r update and ||r||^2, then the new
 // direction (MGCG: z = V(r), beta = r.z / r.z_old; CG: beta from ||r||^2).
 cudaError_t enqueue_iteration(OpSolver* s, int kind, int sign, cudaStream_t q) {
   const int n = s->n;
   const long long N = (long long)n * n;
+  if (kind == 0 && fused_direction(s)) {   // update, V-cycle, beta, direction + Ap + alpha
+    cudaError_t err = launch_cg_update<double>(
+        Grid<double>{s->x, n}, Grid<double>{s->r, n}, Grid<const double>{s->pd, n},
+        Grid<const double>{s->ap, n}, Grid<float>{s->r_lo, n}, n, 0, s->st, s->norms, s->rb[1],
+        q);
+    if (err != cudaSuccess) return err;
+    return precondition_fused(s, 0, q);
+  }
   HoArgs a = op_args(n);
   a.u = s->pd;
   a.out = s->ap;
@@ -322,7 +345,10 @@ int solve(OpSolver* s, int kind, const double* b, double* x, int sign, double ab
   } else if (s->mixed) {
     SBP_CUDA(launch_copy<double, float>(Grid<const double>{s->r, n}, Grid<float>{s->r_lo, n}, n,
                                         q));
-    SBP_CUDA(precondition<float>(s, 1, q));
+    if (fused_direction(s))
+      SBP_CUDA(precondition_fused(s, 1, q));
+    else
+      SBP_CUDA(precondition<float>(s, 1, q));
   } else {
     SBP_CUDA(precondition<double>(s, 1, q));
   }
