@@ -238,6 +238,7 @@ struct VcArgsT : HoArgsT<T> {
   const T* D;
   const T* flo;
   const T* fhi;
+  const T* Dinv;   // 1 / D (Jacobi sweeps)
 };
 // Smallest grid of order p (0 if p is not 4 or 6).
 int ho_min_n(int p);
@@ -266,7 +267,7 @@ cudaError_t launch_vc_apply_c(const double* u, const double* c, double* out, int
                               ReduceBuf rb, double* dot_out, cudaStream_t s);
 // The level's stencil arrays from its nodal coefficients.
 template <typename T>
-cudaError_t launch_vc_stencil(const double* c, T* E, T* N, T* D, T* flo, T* fhi, int n,
+cudaError_t launch_vc_stencil(const double* c, T* E, T* N, T* D, T* flo, T* fhi, T* Dinv, int n,
                               cudaStream_t s);
 // Coarse nodal coefficients by injection: cc(I, J) = cf(2I, 2J).
 cudaError_t launch_vc_inject(const double* cf, double* cc, int nc, cudaStream_t s);

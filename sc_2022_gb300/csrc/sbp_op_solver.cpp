@@ -58,7 +58,7 @@ struct OpSolver {
     // variable coefficients: nodal c (FP64) and the stencil arrays in the
     // V-cycle's precision
     double* c = nullptr;
-    void* st[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};   // E, N, D, flo, fhi
+    void* st[6] = {};   // E, N, D, flo, fhi, 1/D
   };
   int kind = kOpHighOrder;
   int n = 0, p = 0, device = 0;
@@ -69,7 +69,7 @@ struct OpSolver {
   CoarseDev coarse{};          // order p: fast-diagonalisation factors
   double* ainv = nullptr;      // variable: dense coarse inverse
   int ainv_n = 0;              // its order (nc^2)
-  double* st64[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};   // level-0 FP64 stencil
+  double* st64[6] = {};        // level-0 FP64 stencil arrays
   double* c0 = nullptr;        // variable: the caller's coefficients (device copy)
   float* r_lo = nullptr;       // mixed: FP32 copy of r, written by the update
   double *x = nullptr, *r = nullptr, *pd = nullptr, *ap = nullptr;
@@ -134,7 +134,7 @@ cudaError_t op_launch(OpSolver* s, size_t l, int mode, const HoArgsT<T>& a, cuda
   VcArgsT<T> v;
   static_cast<HoArgsT<T>&>(v) = a;
   const bool fp64_level0 = sizeof(T) == sizeof(double) && l == 0;
-  for (int k = 0; k < 5; ++k) {
+  for (int k = 0; k < 6; ++k) {
     const void* arr = fp64_level0 ? (const void*)s->st64[k] : s->lv[l].st[k];
     const T* pa = static_cast<const T*>(arr);
     if (k == 0) v.E = pa;
@@ -142,6 +142,7 @@ cudaError_t op_launch(OpSolver* s, size_t l, int mode, const HoArgsT<T>& a, cuda
     if (k == 2) v.D = pa;
     if (k == 3) v.flo = pa;
     if (k == 4) v.fhi = pa;
+    if (k == 5) v.Dinv = pa;
   }
   return launch_vc<T>(mode, v, q);
 }
@@ -574,12 +575,12 @@ int build_variable(OpSolver* s, const double* c) {
   if (rc) return rc;
   SBP_CUDA(cudaMemcpy(s->c0, c, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToDevice));
   // level-0 FP64 stencil (the Krylov apply)
-  for (int k = 0; k < 5; ++k) {
-    rc = dalloc(s, &s->st64[k], k < 3 ? (size_t)n * n : (size_t)n);
+  for (int k = 0; k < 6; ++k) {
+    rc = dalloc(s, &s->st64[k], (k < 3 || k == 5) ? (size_t)n * n : (size_t)n);
     if (rc) return rc;
   }
   SBP_CUDA(launch_vc_stencil<double>(s->c0, s->st64[0], s->st64[1], s->st64[2], s->st64[3],
-                                     s->st64[4], n, nullptr));
+                                     s->st64[4], s->st64[5], n, nullptr));
   if (!s->mg) return SBP_OK;
   for (size_t l = 0; l < s->lv.size(); ++l) {
     auto& L = s->lv[l];
@@ -592,11 +593,11 @@ int build_variable(OpSolver* s, const double* c) {
       SBP_CUDA(launch_vc_inject(s->lv[l - 1].c, L.c, m, nullptr));
     }
     if (!s->mixed && l == 0) {
-      for (int k = 0; k < 5; ++k) L.st[k] = s->st64[k];
+      for (int k = 0; k < 6; ++k) L.st[k] = s->st64[k];
       continue;
     }
-    for (int k = 0; k < 5; ++k) {
-      const size_t cnt = k < 3 ? (size_t)m * m : (size_t)m;
+    for (int k = 0; k < 6; ++k) {
+      const size_t cnt = (k < 3 || k == 5) ? (size_t)m * m : (size_t)m;
       if (s->mixed) {
         float* p = nullptr;
         rc = dalloc(s, &p, cnt);
@@ -612,12 +613,12 @@ int build_variable(OpSolver* s, const double* c) {
     cudaError_t e;
     if (s->mixed)
       e = launch_vc_stencil<float>(L.c, as<float>(L.st[0]), as<float>(L.st[1]),
-                                   as<float>(L.st[2]), as<float>(L.st[3]), as<float>(L.st[4]), m,
-                                   nullptr);
+                                   as<float>(L.st[2]), as<float>(L.st[3]), as<float>(L.st[4]),
+                                   as<float>(L.st[5]), m, nullptr);
     else
       e = launch_vc_stencil<double>(L.c, as<double>(L.st[0]), as<double>(L.st[1]),
                                     as<double>(L.st[2]), as<double>(L.st[3]),
-                                    as<double>(L.st[4]), m, nullptr);
+                                    as<double>(L.st[4]), as<double>(L.st[5]), m, nullptr);
     SBP_CUDA(e);
   }
   // dense inverse of the coarsest operator

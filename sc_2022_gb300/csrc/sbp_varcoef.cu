@@ -3,8 +3,9 @@
 // - k_vc_apply_c: -A u straight from the nodal coefficients.  It is the
 //   standalone apply and reads u, c and writes out: 24 bytes per point in
 //   FP64.
-// - k_vc_stencil: the per-point stencil arrays E, N, D and the boundary
-//   couplings Flo / Fhi of sbp_varcoef.cuh, computed once per level from c.
+// - k_vc_stencil: the per-point stencil arrays E, N, D (and 1/D for the
+//   Jacobi sweeps) and the boundary couplings Flo / Fhi of sbp_varcoef.cuh,
+//   computed once per level from c.
 // - k_vc<MODE>: the solver's apply / residual / Jacobi sweep on those
 //   arrays, in FP64 or FP32.  Five multiply-adds per point instead of the
 //   face averages.
@@ -97,7 +98,8 @@ __global__ void __launch_bounds__(kThreads)
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
     k_vc_stencil(const double* __restrict__ c, T* __restrict__ E, T* __restrict__ N,
-                 T* __restrict__ D, T* __restrict__ flo, T* __restrict__ fhi, int n) {
+                 T* __restrict__ D, T* __restrict__ flo, T* __restrict__ fhi,
+                 T* __restrict__ Dinv, int n) {
   const long long total = (long long)n * n;
   struct Acc {
     const double* c;
@@ -112,6 +114,7 @@ __global__ void __launch_bounds__(kThreads)
     E[k] = (T)e;
     N[k] = (T)nn;
     D[k] = (T)d;
+    Dinv[k] = (T)(1.0 / d);
     if (j == 0) flo[i] = (T)vc::f_lo(acc(i, 0), i, n);
     if (j == n - 1) fhi[i] = (T)vc::f_hi(acc(i, n - 1), i, n);
   }
@@ -140,6 +143,9 @@ __global__ void __launch_bounds__(kThreads) k_vc(const VcArgsT<T> a) {
   const T* __restrict__ E = a.E;
   const T* __restrict__ Nc = a.N;
   const T* __restrict__ D = a.D;
+  const T* __restrict__ Dinv = a.Dinv;
+  // a Jacobi sweep reads 1/D instead of D: (1 - omega) u + omega D^-1 (b + neighbours)
+  const bool jac = MODE == kHoJacobi && !a.richardson;
   T* __restrict__ out = a.out;
   const T omega = T(a.omega);
   DotAcc<T> acc;
@@ -151,8 +157,7 @@ __global__ void __launch_bounds__(kThreads) k_vc(const VcArgsT<T> a) {
     if (MODE == kHoJacobi && a.zero_in) {   // first sweep from v = 0
       for (int j = j0; j < j1; ++j) {
         const size_t k = (size_t)j * n + i;
-        const T d = __ldg(D + k);
-        out[k] = a.richardson ? omega * __ldg(b + k) : omega * __ldg(b + k) / d;
+        out[k] = a.richardson ? omega * __ldg(b + k) : omega * __ldg(b + k) * __ldg(Dinv + k);
       }
       continue;
     }
@@ -172,7 +177,7 @@ __global__ void __launch_bounds__(kThreads) k_vc(const VcArgsT<T> a) {
         const size_t k = (size_t)j * n + i;
         upc[q] = (in && j + 1 < n) ? U(i, j + 1) : T(0);
         nc[q] = in ? __ldg(Nc + k) : T(0);
-        dc[q] = in ? __ldg(D + k) : T(0);
+        dc[q] = in ? __ldg((jac ? Dinv : D) + k) : T(0);
         ec[q] = (in && i < n - 1) ? __ldg(E + k) : T(0);
         bc[q] = (in && MODE != kHoApply) ? __ldg(b + k) : T(0);
       }
@@ -184,7 +189,8 @@ __global__ void __launch_bounds__(kThreads) k_vc(const VcArgsT<T> a) {
         const T up = upc[q];
         const T n0 = nc[q];
         const T d = dc[q];
-        T na = -d * u0;
+        // neighbours; the diagonal term joins below (d holds 1/D on a Jacobi sweep)
+        T na = jac ? T(0) : -d * u0;
         na = fmaT(nm, um, na);
         na = fmaT(n0, up, na);
         if (i > 0) na = fmaT(__ldg(E + k - 1), U(i - 1, j), na);
@@ -200,9 +206,10 @@ __global__ void __launch_bounds__(kThreads) k_vc(const VcArgsT<T> a) {
           v = a.sign > 0 ? -na : na;
         } else if (MODE == kHoResid) {
           v = bc[q] + (a.sign > 0 ? na : -na);
+        } else if (jac) {
+          v = fmaT(omega * d, bc[q] + na, (T(1) - omega) * u0);
         } else {
-          const T r = bc[q] + na;
-          v = a.richardson ? fmaT(omega, r, u0) : fmaT(omega, r / d, u0);
+          v = fmaT(omega, bc[q] + na, u0);
         }
         out[k] = v;
         if (DOT) acc.add_prod(MODE == kHoApply ? u0 : v, v);
@@ -278,11 +285,11 @@ cudaError_t launch_vc_apply_c(const double* u, const double* c, double* out, int
 }
 
 template <typename T>
-cudaError_t launch_vc_stencil(const double* c, T* E, T* N, T* D, T* flo, T* fhi, int n,
+cudaError_t launch_vc_stencil(const double* c, T* E, T* N, T* D, T* flo, T* fhi, T* Dinv, int n,
                               cudaStream_t s) {
   const long long total = (long long)n * n;
   const int g = (int)std::max(1LL, std::min<long long>((total + kThreads - 1) / kThreads, 4096));
-  k_vc_stencil<T><<<g, kThreads, 0, s>>>(c, E, N, D, flo, fhi, n);
+  k_vc_stencil<T><<<g, kThreads, 0, s>>>(c, E, N, D, flo, fhi, Dinv, n);
   return cudaGetLastError();
 }
 
@@ -314,9 +321,9 @@ cudaError_t launch_dense_gemv(const double* Ainv, const T* b, T* x, int N, const
 }
 
 template cudaError_t launch_vc_stencil<double>(const double*, double*, double*, double*, double*,
-                                               double*, int, cudaStream_t);
+                                               double*, double*, int, cudaStream_t);
 template cudaError_t launch_vc_stencil<float>(const double*, float*, float*, float*, float*,
-                                              float*, int, cudaStream_t);
+                                              float*, float*, int, cudaStream_t);
 template cudaError_t launch_vc<double>(int, VcArgsT<double>, cudaStream_t);
 template cudaError_t launch_vc<float>(int, VcArgsT<float>, cudaStream_t);
 template cudaError_t launch_dense_gemv<double>(const double*, const double*, double*, int,
