@@ -754,11 +754,10 @@ struct CgDirJob {
 // ---------------------------------------------------------------------------
 template <bool TMA>
 struct CgDirMixedJob {
-  // one stage: the z box (FP32, 72 x 37) and the p_old, Ap_old tiles (FP64,
-  // 68 x 33 at (64 ti, j_lo)), all three prefetched one tile ahead
-  static constexpr int kOffP = align128(box_bytes<float, BI, BJ>());
-  static constexpr int kOffA = kOffP + align128(box_bytes<double, QI, QJ>());
-  static constexpr int kStage = kOffA + align128(box_bytes<double, QI, QJ>());
+  // one stage: the z box (FP32, 72 x 37), prefetched one tile ahead; p_old
+  // and Ap_old are read pointwise from global memory, which keeps the stage
+  // small enough for five CTAs per SM
+  static constexpr int kStage = align128(box_bytes<float, BI, BJ>());
   static constexpr int kScratch = 0;
   static constexpr bool kReduce = true;
   // p.Ap from the FP32 roundings of p and Ap, accumulated with the
@@ -780,29 +779,23 @@ struct CgDirMixedJob {
     return false;
   }
   __device__ int tiles() const { return ntot; }
-  __device__ unsigned tx_bytes(int) const {
-    return TMA ? box_bytes<float, BI, BJ>() + 2u * box_bytes<double, QI, QJ>() : 0u;
-  }
+  __device__ unsigned tx_bytes(int) const { return TMA ? box_bytes<float, BI, BJ>() : 0u; }
   __device__ void issue(unsigned char* buf, unsigned long long* bar, int id, const Ctx&) const {
     const TileBoxes bx(id % ntx, tile_at<TI, TJ>(id, ntx, n).j_lo);
     stage_box<TMA, BI, BJ>(reinterpret_cast<float*>(buf), z, &z.box, bx.x0, bx.y0, n, bar);
-    stage_box<TMA, QI, QJ>(reinterpret_cast<double*>(buf + kOffP), pold, &pold.inner, bx.xi,
-                           bx.yi, n, bar);
-    stage_box<TMA, QI, QJ>(reinterpret_cast<double*>(buf + kOffA), apold, &apold.inner, bx.xi,
-                           bx.yi, n, bar);
   }
   __device__ void compute(unsigned char* buf, int id, Acc& acc, const Ctx& c, unsigned char*) const {
     const TileT t = tile_at<TI, TJ>(id, ntx, n);
     const TileBoxes bx(id % ntx, t.j_lo);
     const float* s = reinterpret_cast<const float*>(buf);
-    const double* sp = reinterpret_cast<const double*>(buf + kOffP);
-    const double* sa = reinterpret_cast<const double*>(buf + kOffA);
     const double beta = c.beta;
     const bool first = c.first;
-    auto emit = [&](int i, int j, int k, float zc, double az) {
+    auto emit = [&](int i, int j, int, float zc, double az) {
       const double zd = f32_to_f64(zc);
-      const double pv = first ? zd : fma(beta, sp[k], zd);
-      const double ap = first ? az : fma(beta, sa[k], az);
+      const double pv =
+          first ? zd : fma(beta, __ldg(pold.p + (size_t)j * (size_t)pold.ld + i), zd);
+      const double ap =
+          first ? az : fma(beta, __ldg(apold.p + (size_t)j * (size_t)apold.ld + i), az);
       pnew.at(i, j) = pv;
       Ap.at(i, j) = ap;
       acc.add_prod(f64_to_f32(pv), f64_to_f32(ap));
