@@ -113,3 +113,35 @@ def test_variable_assembly_equals_oracle_matrix(n, kind):
     rp1, col1, val1 = sbp.assemble_variable_host(n, np.ones(n * n))
     A1 = sp.csr_matrix((val1, col1, rp1), shape=(n * n, n * n))
     assert abs(A1 - o.assemble(n).A).max() == 0.0
+
+
+def test_new_entry_points_reject_bad_arguments_without_gpu():
+    # argument checks run before any CUDA call
+    import sc_2022_gb300 as sbp
+    from sc_2022_gb300 import _lib as L
+    lib = sbp.load_library()
+    h = C.c_void_p()
+    assert lib.sbp_ho_solver_create(C.byref(h), 65, 3, None) == L.SBP_ERR_ARGS   # p = 3
+    assert lib.sbp_ho_solver_create(C.byref(h), 7, 4, None) == L.SBP_ERR_ARGS    # n < 8
+    assert lib.sbp_ho_solver_create(C.byref(h), 11, 6, None) == L.SBP_ERR_ARGS   # n < 12
+    assert lib.sbp_ho_solver_create(None, 65, 4, None) == L.SBP_ERR_ARGS
+    assert lib.sbp_apply_ho_f64(None, None, 65, 4, 1, None) == L.SBP_ERR_ARGS
+    assert lib.sbp_apply_ho_f64(C.c_void_p(8), C.c_void_p(8), 65, 5, 1, None) == L.SBP_ERR_ARGS
+    assert lib.sbp_apply_ho_f64(C.c_void_p(8), C.c_void_p(8), 65, 4, 0, None) == L.SBP_ERR_ARGS
+    assert lib.sbp_vc_solver_create(C.byref(h), 65, None, None) == L.SBP_ERR_ARGS   # no c
+    assert lib.sbp_vc_solver_create(C.byref(h), 2, C.c_void_p(8), None) == L.SBP_ERR_ARGS
+    assert lib.sbp_apply_vc_f64(C.c_void_p(8), None, C.c_void_p(8), 65, 1, None) == L.SBP_ERR_ARGS
+    assert lib.sbp_apply_vc_f64(C.c_void_p(8), C.c_void_p(8), C.c_void_p(8), 2, 1,
+                                None) == L.SBP_ERR_ARGS
+    for f in (lib.sbp_ho_mgcg_solve, lib.sbp_vc_mgcg_solve):
+        assert f(None, None, None, 0.0, 1e-8, 10, None, None, 0, None) == L.SBP_ERR_ARGS
+    assert lib.sbp_ho_solver_destroy(None) == 0 and lib.sbp_vc_solver_destroy(None) == 0
+    assert lib.sbp_ho_solver_levels(None) == L.SBP_ERR_ARGS
+    # host CSR assembly: too small a capacity reports the needed count
+    nnz = C.c_longlong()
+    c = np.ones(9 * 9)
+    rp = np.zeros(82, dtype=np.int64)
+    assert lib.sbp_vc_assemble_host(9, c.ctypes.data_as(C.POINTER(C.c_double)),
+                                    rp.ctypes.data_as(C.POINTER(C.c_longlong)), None, None, 0,
+                                    C.byref(nnz)) == L.SBP_ERR_ARGS
+    assert nnz.value > 81
