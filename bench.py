@@ -38,6 +38,13 @@ WORKLOAD = ("plain/mixed matrix-free MGCG, N=4097 (16.8M unknowns), u=sin(pi x)c
             "bilinear prolongation, FP64 direct coarse solve, tol 1e-10")
 
 
+def workload(n: int) -> str:
+    """The workload string for grid n (the headline configuration is N = 4097)."""
+    if n == 4097:
+        return WORKLOAD
+    return WORKLOAD.replace("N=4097 (16.8M unknowns)", f"N={n} ({n * n / 1e6:.1f}M unknowns)")
+
+
 def parse_args():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -51,7 +58,7 @@ def parse_args():
     p.add_argument("--dtype", choices=["f64", "f32"], default="f64",
                    help="operand type of --mode apply")
     p.add_argument("--mode", choices=["full", "apply", "solve-fp64", "solve-mixed", "vcycle",
-                                      "high-order", "variable",
+                                      "high-order", "variable", "adjoint",
                                       "batch", "spmv"],
                    default="full", help="profiling modes run one part only and print a "
                    "short line (not the benchmark line)")
@@ -200,7 +207,7 @@ def run_reference(args, d: Dist):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(val, 3), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (manufactured solution)",
-        "config": {"workload": WORKLOAD + " [CPU: C restatement of the reference's sparse "
+        "config": {"workload": workload(n) + " [CPU: C restatement of the reference's sparse "
                    "CSR path, same V-cycle]", "n": n, "parallelism": "replicas"},
         "cpu_baseline": {"value": round(val, 3), "unit": "ms", "cores": cores, "kind": "port",
                          "sample": f"{r['solves']} full FP64 MGCG solves at N={n} "
@@ -350,9 +357,10 @@ def run_ours(args, d: Dist):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms32, 4),
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
         "data": "synthetic (manufactured solution u=sin(pi x)cos(pi y), b resident in HBM)",
-        "config": {"workload": WORKLOAD, "n": n, "unknowns": n * n,
+        "config": {"workload": workload(n), "n": n, "unknowns": n * n,
                    "parallelism": "replicas" if args.gpus > 1 else "single GPU",
-                   "l2": "inputs larger than L2 (b, x, r, p, Ap: 134 MB each)"},
+                   "l2": f"inputs {'larger' if 8 * n * n > 129e6 else 'smaller'} than L2 "
+                         f"(b, x, r, p, Ap: {8 * n * n / 1e6:.0f} MB each)"},
         "fp64_ms_per_solve": round(ms64, 4),
         "mixed_speedup_vs_fp64": round(ms64 / ms32, 3),
         "solves_per_s_all_gpus": round(args.gpus * 1e3 / ms32, 2),
@@ -586,6 +594,57 @@ def run_part(args):
             out[f"mgcg_{tag}_converged"] = r.converged
             out["levels"] = s.levels
             s.close()
+        print(json.dumps(out))
+        return
+    if args.mode == "adjoint":
+        # the gradient of L = sum_k 1/2 (u_k - t_k)' H~ (u_k - t_k) with respect
+        # to the sources f_k and the boundary data g_k, for a batch of 16 bump
+        # problems at --grid, through torch autograd: forward MGCG solves, the
+        # H-misfit, then the adjoint MGCG solves and the transposed right-hand
+        # side map, all to 1e-10
+        import time
+
+        import numpy as np
+
+        from sc_2022_gb300 import adjoint as adj
+        B = 16
+        fs, gs = [], {side: [] for side in "WESN"}
+        for k in range(B):
+            f, g = problems.bump_problem(n, 5000 + k)
+            fs.append(np.asarray(f).reshape(n, n))
+            for side in "WESN":
+                gs[side].append(np.asarray(g[side]))
+        f0 = torch.tensor(np.stack(fs), dtype=torch.float64, device=dev)
+        g0 = [torch.tensor(np.stack(gs[side]), dtype=torch.float64, device=dev)
+              for side in "WESN"]
+        targets = 1e-3 * torch.randn((B, n, n), dtype=torch.float64, device=dev,
+                                     generator=torch.Generator(device=dev).manual_seed(3))
+        out = {"mode": "adjoint", "n": n, "batch": B, "reltol": 1e-10}
+        grads = {}
+        for tag, prec in (("fp64", _lib.SBP_PREC_FP64), ("mixed", _lib.SBP_PREC_MIXED)):
+            s = sbp.Solver(n, sbp.default_options(prec))
+
+            def gradient():
+                f = f0.clone().requires_grad_(True)
+                g = [t.clone().requires_grad_(True) for t in g0]
+                u = adj.PoissonSolve.apply(f, *g, s, 1e-10)
+                loss = adj.HMisfit.apply(u, targets)
+                loss.backward()
+                return loss, f.grad
+
+            for _ in range(args.warmup):
+                gradient()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                loss, df = gradient()
+            torch.cuda.synchronize()
+            out[f"{tag}_ms_per_gradient"] = round(1e3 * (time.perf_counter() - t0) / args.steps, 2)
+            out[f"{tag}_loss"] = float(loss.detach())
+            grads[tag] = df.detach().clone()
+            s.close()
+        out["mixed_vs_fp64_df_rel_diff"] = float((grads["mixed"] - grads["fp64"]).norm() /
+                                                 grads["fp64"].norm())
         print(json.dumps(out))
         return
     if args.mode == "vcycle":
