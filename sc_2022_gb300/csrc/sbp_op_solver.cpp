@@ -829,7 +829,6 @@ int sbp_vc_assemble_host(int n, const double* c, long long* row_ptr, int* col, d
     int n;
     double operator()(int i, int j) const { return c[(size_t)j * n + i]; }
   } acc{c, n};
-  const long long N = (long long)n * n;
   long long k = 0;
   row_ptr[0] = 0;
   for (int j = 0; j < n; ++j)
@@ -853,8 +852,8 @@ int sbp_vc_assemble_host(int n, const double* c, long long* row_ptr, int* col, d
         return e2;
       };
       const long long row = (long long)j * n + i;
-      if (j >= 2 && j == 2) ent[m++] = {row - 2LL * n, -vc::f_lo(acc(i, 0), i, n)};
-      if (j == n - 1 && n - 3 >= 0) ent[m++] = {row - 2LL * n, -vc::f_hi(acc(i, n - 1), i, n)};
+      if (j == 2) ent[m++] = {row - 2LL * n, -vc::f_lo(acc(i, 0), i, n)};
+      if (j == n - 1) ent[m++] = {row - 2LL * n, -vc::f_hi(acc(i, n - 1), i, n)};
       if (j > 0) ent[m++] = {row - n, -coupling_n(j - 1)};
       if (i > 0) ent[m++] = {row - 1, -coupling_e(i - 1)};
       ent[m++] = {row, d};
@@ -878,7 +877,6 @@ int sbp_vc_assemble_host(int n, const double* c, long long* row_ptr, int* col, d
       row_ptr[row + 1] = k;
     }
   *nnz = k;
-  (void)N;
   return k <= cap ? SBP_OK : SBP_ERR_ARGS;
 }
 
