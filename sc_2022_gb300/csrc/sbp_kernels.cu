@@ -809,12 +809,14 @@ struct CgDirMixedJob {
       });
     } else {
       visit_generic(s, t, bx, [&](int i, int j, const SAcc<float>& a, int k) {
-        // boundary rows/columns: the SAT stencil in FP64 on the exact FP32 values
+        // boundary rows/columns: the SAT stencil of the exact FP32 values in
+        // float-float on the FP32 pipe
         struct D {
           const SAcc<float>* a;
-          __device__ double operator()(int di, int dj) const { return f32_to_f64((*a)(di, dj)); }
+          __device__ FF operator()(int di, int dj) const { return FF((*a)(di, dj), 0.0f); }
         } d{&a};
-        emit(i, j, k, a(0, 0), -negA<double>(d, i, j, n));
+        const FF na = negA<FF>(d, i, j, n);
+        emit(i, j, k, a(0, 0), -(f32_to_f64(na.hi) + f32_to_f64(na.lo)));
       });
     }
   }

@@ -326,6 +326,40 @@ __device__ __forceinline__ void stencil_ff(float uw, float ue, float um, float u
 }
 
 // ---------------------------------------------------------------------------
+// FF: an unevaluated float pair hi + lo with the arithmetic negA needs, for
+// evaluating the SAT stencil of FP32 values on the FP32 pipe.  Sums use
+// two_sum and products the FMA split, so results carry about 48 bits.  The
+// constructor from double takes the stencil's constants, all exact in FP32.
+// ---------------------------------------------------------------------------
+struct FF {
+  float hi, lo;
+  __device__ FF() {}
+  __device__ FF(float h, float l) : hi(h), lo(l) {}
+  __device__ explicit FF(double c) : hi((float)c), lo(0.0f) {}
+};
+__device__ __forceinline__ FF ff_norm(float s, float e) {
+  const float h = s + e;
+  return FF(h, e - (h - s));
+}
+__device__ __forceinline__ FF operator+(FF a, FF b) {
+  float s, e;
+  two_sum(a.hi, b.hi, s, e);
+  return ff_norm(s, e + (a.lo + b.lo));
+}
+__device__ __forceinline__ FF operator-(FF a, FF b) { return a + FF(-b.hi, -b.lo); }
+__device__ __forceinline__ FF operator*(FF a, FF b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return ff_norm(p, e);
+}
+__device__ __forceinline__ FF& operator+=(FF& a, FF b) {
+  a = a + b;
+  return a;
+}
+
+// ---------------------------------------------------------------------------
 // Dot-product accumulators.  FP64 data: an FP64 FMA per term.  FP32 data:
 // each product is split exactly into p + e (FMA) and summed with a
 // compensated (TwoSum) float-float accumulator, converted to FP64 once per
