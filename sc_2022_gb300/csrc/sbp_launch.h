@@ -274,6 +274,14 @@ cudaError_t launch_vc_inject(const double* cf, double* cc, int nc, cudaStream_t 
 // Apply / residual / smoother on the stencil arrays (modes as launch_ho).
 template <typename T>
 cudaError_t launch_vc(int mode, VcArgsT<T> a, cudaStream_t s);
+// FP64 values as float pairs (hi = nearest float, lo = the remainder's).
+cudaError_t launch_split_pairs(const double* in, float2* out, long long count, cudaStream_t s);
+// Mixed-precision CG direction of the variable-coefficient operator, in
+// place: p = z + beta p, Ap = A z + beta Ap (A z in float-float from the
+// level-0 stencil as float pairs st = {E, N, D, flo, fhi}), p.Ap -> alpha;
+// the first direction (state iteration 0) takes p = z, Ap = A z.
+cudaError_t launch_vc_dir_mixed(const float* z, const float2* const* st, double* pd, double* ap,
+                                int n, SolveState* state, ReduceBuf rb, cudaStream_t s);
 // x = Ainv b with a dense FP64 N x N inverse (row-major).
 template <typename T>
 cudaError_t launch_dense_gemv(const double* Ainv, const T* b, T* x, int N, const SolveState* st,

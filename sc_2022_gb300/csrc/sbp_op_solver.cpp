@@ -70,6 +70,7 @@ struct OpSolver {
   double* ainv = nullptr;      // variable: dense coarse inverse
   int ainv_n = 0;              // its order (nc^2)
   double* st64[6] = {};        // level-0 FP64 stencil arrays
+  float2* pairs[5] = {};       // mixed: level-0 E, N, D, flo, fhi as float pairs
   double* c0 = nullptr;        // variable: the caller's coefficients (device copy)
   float* r_lo = nullptr;       // mixed: FP32 copy of r, written by the update
   double *x = nullptr, *r = nullptr, *pd = nullptr, *ap = nullptr;
@@ -227,10 +228,10 @@ cudaError_t precondition(OpSolver* s, int first, cudaStream_t q) {
   return launch_ho_dir<T>(z, s->pd, N, s->st, first, q);
 }
 
-// Mixed-precision order-p MGCG forms Ap with the direction: z = V(r),
-// beta, then p = z + beta p and Ap = A z + beta Ap with p.Ap -> alpha in one
-// kernel (A z on the FP32 pipe), so an iteration has no FP64 apply.
-bool fused_direction(const OpSolver* s) { return s->mixed && s->kind == kOpHighOrder; }
+// Mixed-precision MGCG forms Ap with the direction: z = V(r), beta, then
+// p = z + beta p and Ap = A z + beta Ap with p.Ap -> alpha in one kernel
+// (A z on the FP32 pipe), so an iteration has no FP64 apply.
+bool fused_direction(const OpSolver* s) { return s->mixed; }
 
 cudaError_t precondition_fused(OpSolver* s, int first, cudaStream_t q) {
   cudaError_t err = cudaSuccess;
@@ -239,7 +240,9 @@ cudaError_t precondition_fused(OpSolver* s, int first, cudaStream_t q) {
   if (err != cudaSuccess) return err;
   err = launch_ho_rz<float>(s->r, z, N, s->st, s->rb[2], first, q);
   if (err != cudaSuccess) return err;
-  return launch_ho_dir_mixed(s->p, z, s->pd, s->ap, s->n, s->st, s->rb[0], q);
+  if (s->kind == kOpHighOrder)
+    return launch_ho_dir_mixed(s->p, z, s->pd, s->ap, s->n, s->st, s->rb[0], q);
+  return launch_vc_dir_mixed(z, s->pairs, s->pd, s->ap, s->n, s->st, s->rb[0], q);
 }
 
 // The iteration body: Ap and alpha, x/r update and ||r||^2, then the new
@@ -582,6 +585,14 @@ int build_variable(OpSolver* s, const double* c) {
   SBP_CUDA(launch_vc_stencil<double>(s->c0, s->st64[0], s->st64[1], s->st64[2], s->st64[3],
                                      s->st64[4], s->st64[5], n, nullptr));
   if (!s->mg) return SBP_OK;
+  if (s->mixed) {   // the fused CG direction's coefficients
+    for (int k = 0; k < 5; ++k) {
+      const size_t cnt = k < 3 ? (size_t)n * n : (size_t)n;
+      rc = dalloc(s, &s->pairs[k], cnt);
+      if (rc) return rc;
+      SBP_CUDA(launch_split_pairs(s->st64[k], s->pairs[k], (long long)cnt, nullptr));
+    }
+  }
   for (size_t l = 0; l < s->lv.size(); ++l) {
     auto& L = s->lv[l];
     const int m = L.n;

@@ -246,6 +246,101 @@ __global__ void __launch_bounds__(kThreads) k_vc(const VcArgsT<T> a) {
     });
 }
 
+// Split FP64 stencil coefficients into float pairs (hi = nearest float, lo =
+// the nearest float of the remainder): the coefficients of the mixed CG
+// direction, to about 2^-48.
+__global__ void __launch_bounds__(kThreads)
+    k_split_pairs(const double* __restrict__ in, float2* __restrict__ out, long long count) {
+  for (long long k = (long long)blockIdx.x * kThreads + threadIdx.x; k < count;
+       k += (long long)gridDim.x * kThreads) {
+    const double d = in[k];
+    const float hi = __double2float_rn(d);
+    out[k] = make_float2(hi, __double2float_rn(d - (double)hi));
+  }
+}
+
+// acc += c * z for a coefficient pair c and an FP32 value z, in float-float.
+__device__ __forceinline__ void ff_fma(float2 c, float z, float& hi, float& lo) {
+  const float p = c.x * z;
+  const float e = fmaf(c.y, z, fmaf(c.x, z, -p));
+  float s, t;
+  two_sum(hi, p, s, t);
+  hi = s;
+  lo += t + e;
+}
+
+// Mixed-precision CG direction of the variable-coefficient operator, in
+// place (z the FP32 V-cycle output, p and Ap FP64):
+//   p = z + beta p,  Ap = A z + beta Ap,  p.Ap -> alpha
+// A z = D z - (the couplings of z) from the stencil as float pairs, summed in
+// float-float on the FP32 pipe; three FP64 instructions per point.
+__global__ void __launch_bounds__(kThreads)
+    k_vc_dir_mixed(const float* __restrict__ z, const float2* __restrict__ E,
+                   const float2* __restrict__ Nc, const float2* __restrict__ D,
+                   const float2* __restrict__ flo_p, const float2* __restrict__ fhi_p,
+                   double* __restrict__ p, double* __restrict__ ap, int n, int cols,
+                   SolveState* st, ReduceBuf rb) {
+  pdl_begin();
+  if (st->done) return;
+  const bool first = st->iter == 0;
+  const double beta = st->beta;
+  const int nrb = (n + kThreads - 1) / kThreads;
+  const int items = nrb * ((n + cols - 1) / cols);
+  DotAcc<float> acc;
+  for (int w = blockIdx.x; w < items; w += gridDim.x) {
+    const int i = (w % nrb) * kThreads + threadIdx.x;
+    if (i >= n) continue;
+    const int j0 = (w / nrb) * cols;
+    const int j1 = min(n, j0 + cols);
+    const float2 flo = __ldg(flo_p + i), fhi = __ldg(fhi_p + i);
+    auto Z = [&](int ii, int jj) { return __ldg(z + (size_t)jj * n + ii); };
+    float um = j0 > 0 ? Z(i, j0 - 1) : 0.0f, u0 = Z(i, j0);
+    float2 nm = j0 > 0 ? __ldg(Nc + (size_t)(j0 - 1) * n + i) : make_float2(0.0f, 0.0f);
+    for (int j = j0; j < j1; ++j) {
+      const size_t k = (size_t)j * n + i;
+      const float up = j + 1 < n ? Z(i, j + 1) : 0.0f;
+      const float2 n0 = __ldg(Nc + k);
+      // -A z = couplings - D z; accumulate A z = D z - couplings
+      float hi = 0.0f, lo = 0.0f;
+      ff_fma(__ldg(D + k), u0, hi, lo);
+      ff_fma(make_float2(-nm.x, -nm.y), um, hi, lo);
+      ff_fma(make_float2(-n0.x, -n0.y), up, hi, lo);
+      if (i > 0) {
+        const float2 e = __ldg(E + k - 1);
+        ff_fma(make_float2(-e.x, -e.y), Z(i - 1, j), hi, lo);
+      }
+      if (i < n - 1) {
+        const float2 e = __ldg(E + k);
+        ff_fma(make_float2(-e.x, -e.y), Z(i + 1, j), hi, lo);
+      }
+      if (j <= 2 || j >= n - 3) {
+        const float2 fl = make_float2(-flo.x, -flo.y), fh = make_float2(-fhi.x, -fhi.y);
+        if (j == 0) ff_fma(fl, Z(i, 2), hi, lo);
+        if (j == 2) ff_fma(fl, Z(i, 0), hi, lo);
+        if (j == n - 1) ff_fma(fh, Z(i, n - 3), hi, lo);
+        if (j == n - 3) ff_fma(fh, Z(i, n - 1), hi, lo);
+      }
+      const double azd = f32_to_f64(hi) + f32_to_f64(lo);
+      const double zd = f32_to_f64(u0);
+      const double pv = first ? zd : fma(beta, p[k], zd);
+      const double av = first ? azd : fma(beta, ap[k], azd);
+      p[k] = pv;
+      ap[k] = av;
+      acc.add_prod(f64_to_f32(pv), f64_to_f32(av));
+      um = u0;
+      u0 = up;
+      nm = n0;
+    }
+  }
+  grid_reduce(acc.value(), rb, [&](double tot) {
+    st->pAp = tot;
+    if (!isfinite(tot) || tot == 0.0)
+      st->done = kDoneBreakdown;
+    else
+      st->alpha = st->rz / tot;
+  });
+}
+
 // x = Ainv b on the coarse grid: one warp per row, FP64 accumulation.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
@@ -318,6 +413,20 @@ cudaError_t launch_dense_gemv(const double* Ainv, const T* b, T* x, int N, const
                               cudaStream_t s) {
   const int g = std::max(1, std::min((N + kWarps - 1) / kWarps, 1024));
   return launch_pdl(k_dense_gemv<T>, dim3(g), dim3(kThreads), 0, s, Ainv, b, x, N, st);
+}
+
+cudaError_t launch_split_pairs(const double* in, float2* out, long long count, cudaStream_t s) {
+  const int g = (int)std::max(1LL, std::min<long long>((count + kThreads - 1) / kThreads, 4096));
+  k_split_pairs<<<g, kThreads, 0, s>>>(in, out, count);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_vc_dir_mixed(const float* z, const float2* const* st, double* pd, double* ap,
+                                int n, SolveState* state, ReduceBuf rb, cudaStream_t s) {
+  if (n < 3 || !rb.partials) return cudaErrorInvalidValue;
+  const int cols = vc_cols(n);
+  return launch_pdl(k_vc_dir_mixed, vc_grid(n, cols), dim3(kThreads), 0, s, z, st[0], st[1],
+                    st[2], st[3], st[4], pd, ap, n, cols, state, rb);
 }
 
 template cudaError_t launch_vc_stencil<double>(const double*, double*, double*, double*, double*,
