@@ -306,15 +306,27 @@ int capture(OpSolver* s, int kind, int sign) {
   return SBP_OK;
 }
 
+// The residual-norm history holds maxiter + 1 entries.  A larger request
+// replaces the array; the iteration graphs that point at the old one are
+// dropped (every solve has finished before the next one starts).
 int ensure_norms(OpSolver* s, int maxiter) {
   if (maxiter + 1 <= s->norms_cap) return SBP_OK;
   double* p = nullptr;
   const int cap = std::max(maxiter + 1, 1024);
   const int rc = dalloc(s, &p, (size_t)cap);
   if (rc) return rc;
-  s->norms = p;   // the old array stays owned by allocs until destroy
+  if (s->norms) {
+    destroy_graphs(s);
+    for (auto it = s->allocs.begin(); it != s->allocs.end(); ++it)
+      if (*it == s->norms) {
+        cudaFree(*it);
+        s->allocs.erase(it);
+        s->dev_bytes -= (long long)std::max<size_t>((size_t)s->norms_cap * sizeof(double), 256);
+        break;
+      }
+  }
+  s->norms = p;
   s->norms_cap = cap;
-  destroy_graphs(s);
   return SBP_OK;
 }
 
