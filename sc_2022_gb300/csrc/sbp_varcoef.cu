@@ -57,18 +57,23 @@ __global__ void __launch_bounds__(kThreads)
     const double wi = vc::weight(i, n);
     auto U = [&](int ii, int jj) { return __ldg(u + (size_t)jj * n + ii); };
     auto Cf = [&](int ii, int jj) { return __ldg(c + (size_t)jj * n + ii); };
-    // register window along j: u and c at j-1, j, j+1
+    // register window along j: u and c at j-1, j, j+1; the face sum
+    // c(j) + c(j+1) is carried to the next column as c(j-1) + c(j).  Face
+    // sums enter unhalved and the 1/2 is applied once per direction.
     double um = j0 > 0 ? U(i, j0 - 1) : 0.0, u0 = U(i, j0);
-    double cm = j0 > 0 ? Cf(i, j0 - 1) : 0.0, c0 = Cf(i, j0);
+    double c0 = Cf(i, j0);
+    double sm = j0 > 0 ? Cf(i, j0 - 1) + c0 : 0.0;   // c(j-1) + c(j)
     for (int j = j0; j < j1; ++j) {
       const double up = j + 1 < n ? U(i, j + 1) : 0.0;
       const double cp = j + 1 < n ? Cf(i, j + 1) : 0.0;
+      const double sp = c0 + cp;                       // c(j) + c(j+1)
       double x = 0.0;
-      if (i > 0) x = fma(0.5 * (Cf(i - 1, j) + c0), U(i - 1, j) - u0, x);
-      if (i < n - 1) x = fma(0.5 * (c0 + Cf(i + 1, j)), U(i + 1, j) - u0, x);
+      if (i > 0) x = (Cf(i - 1, j) + c0) * (U(i - 1, j) - u0);
+      if (i < n - 1) x = fma(c0 + Cf(i + 1, j), U(i + 1, j) - u0, x);
       double y = 0.0;
-      if (j > 0) y = fma(0.5 * (cm + c0), um - u0, y);
-      if (j < n - 1) y = fma(0.5 * (c0 + cp), up - u0, y);
+      if (j > 0) y = sm * (um - u0);
+      if (j < n - 1) y = fma(sp, up - u0, y);
+      y *= 0.5;
       if (j <= 2 || j >= n - 3) {   // Dirichlet closure, scaled by the boundary c
         if (j == 0)
           y += c0 * (vc::kBs0 * u0 + vc::kBs1 * up + vc::kBs2 * U(i, 2) +
@@ -81,14 +86,14 @@ __global__ void __launch_bounds__(kThreads)
         if (j == n - 2) y += vc::kBs1 * Cf(i, n - 1) * U(i, n - 1);
         if (j == n - 3) y += vc::kBs2 * Cf(i, n - 1) * U(i, n - 1);
       }
-      const double na = fma(vc::weight(j, n), x, wi * y);   // (-A u)(i, j)
+      const double na = fma(0.5 * vc::weight(j, n), x, wi * y);   // (-A u)(i, j)
       const double v = sign > 0 ? -na : na;
       out[(size_t)j * n + i] = v;
       if (DOT) acc = fma(u0, v, acc);
       um = u0;
       u0 = up;
-      cm = c0;
       c0 = cp;
+      sm = sp;
     }
   }
   if (DOT) grid_reduce(acc, rb, [&](double tot) { *dot_out = tot; });
