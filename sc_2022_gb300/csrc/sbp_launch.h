@@ -238,7 +238,7 @@ struct VcArgsT : HoArgsT<T> {
   const T* D;
   const T* flo;
   const T* fhi;
-  const T* Dinv;   // 1 / D (Jacobi sweeps)
+  const T* Dinv;   // omega / D (Jacobi sweeps)
 };
 // Smallest grid of order p (0 if p is not 4 or 6).
 int ho_min_n(int p);
@@ -265,10 +265,11 @@ cudaError_t launch_ho_dir_mixed(int p, const float* z, double* pd, double* ap, i
 // out = sign * A u straight from the nodal coefficients c (FP64; dot_out: u . out).
 cudaError_t launch_vc_apply_c(const double* u, const double* c, double* out, int n, int sign,
                               ReduceBuf rb, double* dot_out, cudaStream_t s);
-// The level's stencil arrays from its nodal coefficients.
+// The level's stencil arrays from its nodal coefficients; Dinv = wscale / D
+// (the Jacobi weight over the diagonal).
 template <typename T>
-cudaError_t launch_vc_stencil(const double* c, T* E, T* N, T* D, T* flo, T* fhi, T* Dinv, int n,
-                              cudaStream_t s);
+cudaError_t launch_vc_stencil(const double* c, T* E, T* N, T* D, T* flo, T* fhi, T* Dinv,
+                              double wscale, int n, cudaStream_t s);
 // Coarse nodal coefficients by injection: cc(I, J) = cf(2I, 2J).
 cudaError_t launch_vc_inject(const double* cf, double* cc, int nc, cudaStream_t s);
 // Apply / residual / smoother on the stencil arrays (modes as launch_ho).

@@ -586,6 +586,8 @@ int dense_inverse(int nc, const std::vector<double>& c, std::vector<double>& inv
 // the dense coarse inverse.
 int build_variable(OpSolver* s, const double* c) {
   const int n = s->n;
+  // the Jacobi weight, folded into the stored inverse diagonal
+  const double jw = s->opts.omega > 0.0 ? s->opts.omega : 2.0 / 3.0;
   int rc = dalloc(s, &s->c0, (size_t)n * n);
   if (rc) return rc;
   SBP_CUDA(cudaMemcpy(s->c0, c, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToDevice));
@@ -595,7 +597,7 @@ int build_variable(OpSolver* s, const double* c) {
     if (rc) return rc;
   }
   SBP_CUDA(launch_vc_stencil<double>(s->c0, s->st64[0], s->st64[1], s->st64[2], s->st64[3],
-                                     s->st64[4], s->st64[5], n, nullptr));
+                                     s->st64[4], s->st64[5], jw, n, nullptr));
   if (!s->mg) return SBP_OK;
   if (s->mixed) {   // the fused CG direction's coefficients
     for (int k = 0; k < 5; ++k) {
@@ -637,11 +639,11 @@ int build_variable(OpSolver* s, const double* c) {
     if (s->mixed)
       e = launch_vc_stencil<float>(L.c, as<float>(L.st[0]), as<float>(L.st[1]),
                                    as<float>(L.st[2]), as<float>(L.st[3]), as<float>(L.st[4]),
-                                   as<float>(L.st[5]), m, nullptr);
+                                   as<float>(L.st[5]), jw, m, nullptr);
     else
       e = launch_vc_stencil<double>(L.c, as<double>(L.st[0]), as<double>(L.st[1]),
                                     as<double>(L.st[2]), as<double>(L.st[3]),
-                                    as<double>(L.st[4]), as<double>(L.st[5]), m, nullptr);
+                                    as<double>(L.st[4]), as<double>(L.st[5]), jw, m, nullptr);
     SBP_CUDA(e);
   }
   // dense inverse of the coarsest operator

@@ -3,8 +3,8 @@
 // - k_vc_apply_c: -A u straight from the nodal coefficients.  It is the
 //   standalone apply and reads u, c and writes out: 24 bytes per point in
 //   FP64.
-// - k_vc_stencil: the per-point stencil arrays E, N, D (and 1/D for the
-//   Jacobi sweeps) and the boundary couplings Flo / Fhi of sbp_varcoef.cuh,
+// - k_vc_stencil: the per-point stencil arrays E, N, D (and omega / D for
+//   the Jacobi sweeps) and the boundary couplings Flo / Fhi of sbp_varcoef.cuh,
 //   computed once per level from c.
 // - k_vc<MODE>: the solver's apply / residual / Jacobi sweep on those
 //   arrays, in FP64 or FP32.  Five multiply-adds per point instead of the
@@ -104,7 +104,7 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads)
     k_vc_stencil(const double* __restrict__ c, T* __restrict__ E, T* __restrict__ N,
                  T* __restrict__ D, T* __restrict__ flo, T* __restrict__ fhi,
-                 T* __restrict__ Dinv, int n) {
+                 T* __restrict__ Dinv, double wscale, int n) {
   const long long total = (long long)n * n;
   struct Acc {
     const double* c;
@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(kThreads)
     E[k] = (T)e;
     N[k] = (T)nn;
     D[k] = (T)d;
-    Dinv[k] = (T)(1.0 / d);
+    Dinv[k] = (T)(wscale / d);
     if (j == 0) flo[i] = (T)vc::f_lo(acc(i, 0), i, n);
     if (j == n - 1) fhi[i] = (T)vc::f_hi(acc(i, n - 1), i, n);
   }
@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(kThreads) k_vc(const VcArgsT<T> a) {
   const T* __restrict__ Nc = a.N;
   const T* __restrict__ D = a.D;
   const T* __restrict__ Dinv = a.Dinv;
-  // a Jacobi sweep reads 1/D instead of D: (1 - omega) u + omega D^-1 (b + neighbours)
+  // a Jacobi sweep reads omega / D instead of D: (1 - omega) u + omega D^-1 (b + neighbours)
   const bool jac = MODE == kHoJacobi && !a.richardson;
   T* __restrict__ out = a.out;
   const T omega = T(a.omega);
@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(kThreads) k_vc(const VcArgsT<T> a) {
     if (MODE == kHoJacobi && a.zero_in) {   // first sweep from v = 0
       for (int j = j0; j < j1; ++j) {
         const size_t k = (size_t)j * n + i;
-        out[k] = a.richardson ? omega * __ldg(b + k) : omega * __ldg(b + k) * __ldg(Dinv + k);
+        out[k] = a.richardson ? omega * __ldg(b + k) : __ldg(b + k) * __ldg(Dinv + k);
       }
       continue;
     }
@@ -194,7 +194,7 @@ __global__ void __launch_bounds__(kThreads) k_vc(const VcArgsT<T> a) {
         const T up = upc[q];
         const T n0 = nc[q];
         const T d = dc[q];
-        // neighbours; the diagonal term joins below (d holds 1/D on a Jacobi sweep)
+        // neighbours; the diagonal term joins below (d holds omega / D on a Jacobi sweep)
         T na = jac ? T(0) : -d * u0;
         na = fmaT(nm, um, na);
         na = fmaT(n0, up, na);
@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(kThreads) k_vc(const VcArgsT<T> a) {
         } else if (MODE == kHoResid) {
           v = bc[q] + (a.sign > 0 ? na : -na);
         } else if (jac) {
-          v = fmaT(omega * d, bc[q] + na, (T(1) - omega) * u0);
+          v = fmaT(d, bc[q] + na, (T(1) - omega) * u0);   // d = omega / D
         } else {
           v = fmaT(omega, bc[q] + na, u0);
         }
@@ -385,11 +385,11 @@ cudaError_t launch_vc_apply_c(const double* u, const double* c, double* out, int
 }
 
 template <typename T>
-cudaError_t launch_vc_stencil(const double* c, T* E, T* N, T* D, T* flo, T* fhi, T* Dinv, int n,
-                              cudaStream_t s) {
+cudaError_t launch_vc_stencil(const double* c, T* E, T* N, T* D, T* flo, T* fhi, T* Dinv,
+                              double wscale, int n, cudaStream_t s) {
   const long long total = (long long)n * n;
   const int g = (int)std::max(1LL, std::min<long long>((total + kThreads - 1) / kThreads, 4096));
-  k_vc_stencil<T><<<g, kThreads, 0, s>>>(c, E, N, D, flo, fhi, Dinv, n);
+  k_vc_stencil<T><<<g, kThreads, 0, s>>>(c, E, N, D, flo, fhi, Dinv, wscale, n);
   return cudaGetLastError();
 }
 
@@ -435,9 +435,9 @@ cudaError_t launch_vc_dir_mixed(const float* z, const float2* const* st, double*
 }
 
 template cudaError_t launch_vc_stencil<double>(const double*, double*, double*, double*, double*,
-                                               double*, double*, int, cudaStream_t);
+                                               double*, double*, double, int, cudaStream_t);
 template cudaError_t launch_vc_stencil<float>(const double*, float*, float*, float*, float*,
-                                              float*, float*, int, cudaStream_t);
+                                              float*, float*, double, int, cudaStream_t);
 template cudaError_t launch_vc<double>(int, VcArgsT<double>, cudaStream_t);
 template cudaError_t launch_vc<float>(int, VcArgsT<float>, cudaStream_t);
 template cudaError_t launch_dense_gemv<double>(const double*, const double*, double*, int,
