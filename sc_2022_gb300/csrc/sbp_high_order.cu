@@ -73,6 +73,7 @@ __global__ void __launch_bounds__(kThreads) k_ho(const HoArgsT<T> a) {
   const T* tx = tab<P, T>(0);
   const T* ty = tab<P, T>(1);
   const T omega = T(a.omega);
+  const T winv_in = omega * kInvDiagIn;   // the interior Jacobi factor
   DotAcc<T> acc;
   for (int w = blockIdx.x; w < items; w += gridDim.x) {
     const int i = (w % nrb) * kThreads + threadIdx.x;
@@ -90,10 +91,11 @@ __global__ void __launch_bounds__(kThreads) k_ho(const HoArgsT<T> a) {
         const bool yin = j >= BM && j <= n - 1 - BM;
         const int yr = j < BM ? j : n - 1 - j;
         const T dyy = yin ? kD0 : ty[yr * BN + yr];
-        const T inv = a.richardson ? T(1)
-                      : (xin && yin) ? kInvDiagIn
-                                     : T(-1) / (T(ho::weight<P>(j, n)) * dxx + wi * dyy);
-        out[(size_t)j * n + i] = omega * __ldg(b + (size_t)j * n + i) * inv;
+        const T winv =
+            a.richardson ? omega
+            : (xin && yin) ? winv_in
+                           : omega * (T(-1) / (T(ho::weight<P>(j, n)) * dxx + wi * dyy));
+        out[(size_t)j * n + i] = winv * __ldg(b + (size_t)j * n + i);
       }
       continue;
     }
@@ -164,12 +166,12 @@ __global__ void __launch_bounds__(kThreads) k_ho(const HoArgsT<T> a) {
         } else if (MODE == kHoResid) {
           v = bn[q] + (a.sign > 0 ? na : -na);
         } else {
-          T inv = T(1);
+          T winv = omega;   // omega D^-1 (Jacobi) or omega (Richardson)
           if (!a.richardson) {
             const T dyy = yin ? kD0 : ty[yr * BN + yr];
-            inv = (xin && yin) ? kInvDiagIn : T(-1) / (wj * dxx + wi * dyy);
+            winv = (xin && yin) ? winv_in : omega * (T(-1) / (wj * dxx + wi * dyy));
           }
-          v = fmaT(omega * inv, bn[q] + na, c[R]);
+          v = fmaT(winv, bn[q] + na, c[R]);
         }
         out[(size_t)j * n + i] = v;
         if (DOT) acc.add_prod(MODE == kHoApply ? c[R] : v, v);
