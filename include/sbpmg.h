@@ -377,6 +377,11 @@ int sbp_batch_mgcg_solve(sbp_batch* b, const double* const* bs, double* const* x
  * reference's per-V-cycle host LU solve (matrix_free_mg_cg.jl:166).  `cap`
  * is the capacity of `out` in doubles.  Needs no GPU. */
 int sbp_coarse_inverse_host(int nc, double* out, long long cap);
+/* The same for the operator of SBP order p (2, 4 or 6) on any nc x nc grid
+ * (nc <= 129, at least 3 for p = 2, 8 for p = 4 and 12 for p = 6), from the
+ * fast-diagonalisation factors that the order-p solver's coarse level uses.
+ * Needs no GPU. */
+int sbp_coarse_inverse_order_host(int nc, int p, double* out, long long cap);
 
 /* Message of the last SBP_ERR_CUDA / SBP_ERR_NOMEM on this host thread. */
 const char* sbp_last_error(void);

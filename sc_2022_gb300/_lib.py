@@ -86,6 +86,7 @@ SIGNATURES = {
     "sbp_mgcg_adjoint_f64": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _d, _d, _d, _i,
                                   C.POINTER(sbp_result), _vp]),
     "sbp_coarse_inverse_host": (_i, [_i, _dp, C.c_longlong]),
+    "sbp_coarse_inverse_order_host": (_i, [_i, _i, _dp, C.c_longlong]),
     "sbp_apply_ho_f64": (_i, [_vp, _vp, _i, _i, _i, _vp]),
     "sbp_ho_solver_create": (_i, [C.POINTER(_vp), _i, _i, C.POINTER(sbp_options)]),
     "sbp_ho_solver_destroy": (_i, [_vp]),

@@ -477,6 +477,21 @@ int sbp_coarse_inverse_host(int nc, double* out, long long cap) {
   return SBP_OK;
 }
 
+int sbp_coarse_inverse_order_host(int nc, int p, double* out, long long cap) {
+  if (!out || nc > 129 || (p != 2 && p != 4 && p != 6)) return SBP_ERR_ARGS;
+  if (nc < (p == 2 ? 3 : ho_min_points(p))) return SBP_ERR_ARGS;
+  const long long N = (long long)nc * nc;
+  if (cap < N * N) return SBP_ERR_ARGS;
+  try {
+    auto X = coarse_inverse(nc, p);
+    std::memcpy(out, X->data(), (size_t)(N * N) * sizeof(double));
+  } catch (const std::exception& ex) {
+    g_last_error = ex.what();
+    return SBP_ERR_ARGS;
+  }
+  return SBP_OK;
+}
+
 const char* sbp_status_string(int status) {
   switch (status) {
     case SBP_OK: return "ok";

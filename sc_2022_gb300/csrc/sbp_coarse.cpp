@@ -290,8 +290,8 @@ int ho_min_points(int p) {
   return p == 4 ? ho::Order<4>::kMinN : (p == 6 ? ho::Order<6>::kMinN : 0);
 }
 
-std::shared_ptr<const std::vector<double>> coarse_inverse(int nc) {
-  auto f = coarse_factors(nc);
+std::shared_ptr<const std::vector<double>> coarse_inverse(int nc, int p) {
+  auto f = coarse_factors(nc, p);
   const int N = nc * nc;
   auto X = std::make_shared<std::vector<double>>((size_t)N * N, 0.0);
   unsigned nt = std::max(1u, std::thread::hardware_concurrency());

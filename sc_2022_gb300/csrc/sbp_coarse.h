@@ -34,8 +34,8 @@ int ho_min_points(int p);
 // x = A^{-1} b on the host with the factors (column-major nc x nc grids).
 void coarse_solve_host(const CoarseFactors& f, const double* b, double* x);
 
-// Row-major (= column-major, it is symmetric) nc^2 x nc^2 inverse of A,
-// column by column from the factors.
-std::shared_ptr<const std::vector<double>> coarse_inverse(int nc);
+// Row-major (= column-major, it is symmetric) nc^2 x nc^2 inverse of the
+// order-p operator A, column by column from the factors.
+std::shared_ptr<const std::vector<double>> coarse_inverse(int nc, int p = 2);
 
 }  // namespace sbp

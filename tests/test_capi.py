@@ -145,3 +145,21 @@ def test_new_entry_points_reject_bad_arguments_without_gpu():
                                     rp.ctypes.data_as(C.POINTER(C.c_longlong)), None, None, 0,
                                     C.byref(nnz)) == L.SBP_ERR_ARGS
     assert nnz.value > 81
+
+
+@pytest.mark.parametrize("p,nc", [(2, 17), (4, 8), (4, 17), (4, 33), (6, 12), (6, 17), (6, 33)])
+def test_order_p_coarse_inverse_equals_oracle(p, nc):
+    # the order-p fast-diagonalisation factors (the order-p solver's coarse
+    # solve) against the inverse of the oracle's assembled operator
+    import sc_2022_gb300 as sbp
+    lib = sbp.load_library()
+    N = nc * nc
+    out = np.zeros(N * N)
+    assert lib.sbp_coarse_inverse_order_host(nc, p, out.ctypes.data_as(C.POINTER(C.c_double)),
+                                             N * N) == 0
+    A = o.assemble(nc, p).A.toarray()
+    Ainv = out.reshape(N, N)
+    assert np.abs(Ainv @ A - np.eye(N)).max() < 1e-9
+    assert np.abs(Ainv - Ainv.T).max() == 0.0
+    assert lib.sbp_coarse_inverse_order_host(7, 4, out.ctypes.data_as(C.POINTER(C.c_double)),
+                                             N * N) != 0   # below the minimum grid
