@@ -262,6 +262,10 @@ int sbp_vc_vcycle_apply(sbp_vc_solver* s, const double* b, double* v, void* stre
  * Needs no GPU.  Returns SBP_ERR_ARGS with *nnz set when cap is too small. */
 int sbp_vc_assemble_host(int n, const double* c, long long* row_ptr, int* col, double* val,
                          long long cap, long long* nnz);
+/* The dense inverse the variable-coefficient solver uses on its coarse grid
+ * (nc <= 33; c a host array of nc * nc coefficients), row-major, by the same
+ * host Cholesky.  Needs no GPU. */
+int sbp_vc_coarse_inverse_host(int nc, const double* c, double* out, long long cap);
 
 /* ---- assembled-operator comparator ------------------------------------ */
 

@@ -846,6 +846,17 @@ int sbp_vc_vcycle_apply(sbp_vc_solver* s, const double* b, double* v, void* stre
   return vcycle_apply(s, b, v, (cudaStream_t)stream);
 }
 
+int sbp_vc_coarse_inverse_host(int nc, const double* c, double* out, long long cap) {
+  if (nc < 3 || nc > kVcMaxCoarse || !c || !out) return SBP_ERR_ARGS;
+  const long long N = (long long)nc * nc;
+  if (cap < N * N) return SBP_ERR_ARGS;
+  std::vector<double> ch(c, c + N), inv;
+  const int rc = dense_inverse(nc, ch, inv);
+  if (rc) return rc;
+  std::copy(inv.begin(), inv.end(), out);
+  return SBP_OK;
+}
+
 int sbp_vc_assemble_host(int n, const double* c, long long* row_ptr, int* col, double* val,
                          long long cap, long long* nnz) {
   if (n < 3 || !c || !row_ptr || !nnz) return SBP_ERR_ARGS;

@@ -163,3 +163,19 @@ def test_order_p_coarse_inverse_equals_oracle(p, nc):
     assert np.abs(Ainv - Ainv.T).max() == 0.0
     assert lib.sbp_coarse_inverse_order_host(7, 4, out.ctypes.data_as(C.POINTER(C.c_double)),
                                              N * N) != 0   # below the minimum grid
+
+
+@pytest.mark.parametrize("nc,kind", [(5, "smooth"), (9, "layered"), (17, "smooth")])
+def test_variable_coarse_inverse_equals_oracle(nc, kind):
+    # the dense coarse inverse of the variable-coefficient solver (host
+    # Cholesky) against the inverse of the oracle's assembled operator
+    import sc_2022_gb300 as sbp
+    lib = sbp.load_library()
+    c = np.ascontiguousarray(o.coefficient_field(nc, kind))
+    N = nc * nc
+    out = np.zeros(N * N)
+    dp = C.POINTER(C.c_double)
+    assert lib.sbp_vc_coarse_inverse_host(nc, c.ctypes.data_as(dp), out.ctypes.data_as(dp),
+                                          N * N) == 0
+    A = o.assemble_variable(nc, c).A.toarray()
+    assert np.abs(out.reshape(N, N) @ A - np.eye(N)).max() < 1e-10
