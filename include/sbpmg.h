@@ -241,8 +241,10 @@ int sbp_apply_vc_f64(const double* u, const double* c, double* out, int n, int s
 
 /* Variable-coefficient solver handle for the coefficient field c (copied
  * at creation).  opts (NULL = sbp_options_default) as for sbp_ho_solver_create.
- * - V-cycle levels re-discretise the operator with the coefficients
- *   injected to each coarse grid.
+ * - V-cycle levels re-discretise the operator.  Coarse coefficients are
+ *   the harmonic mean of the fine ones over the full-weighting stencil,
+ *   1 / sum_ab w_a w_b / c(2I+a, 2J+b), w = (1/4, 1/2, 1/4), clamped at
+ *   the edges.
  * - The coarse level is solved exactly with a dense inverse; coarse_n is
  *   capped at 33.
  * - Any n >= 3 gets plain CG; multigrid needs n = 2^k + 1 or n <= 33. */

@@ -270,8 +270,9 @@ cudaError_t launch_vc_apply_c(const double* u, const double* c, double* out, int
 template <typename T>
 cudaError_t launch_vc_stencil(const double* c, T* E, T* N, T* D, T* flo, T* fhi, T* Dinv,
                               double wscale, int n, cudaStream_t s);
-// Coarse nodal coefficients by injection: cc(I, J) = cf(2I, 2J).
-cudaError_t launch_vc_inject(const double* cf, double* cc, int nc, cudaStream_t s);
+// Coarse nodal coefficients (nc x nc) of the fine field cf ((2nc-1)^2): the
+// harmonic mean of cf over the full-weighting stencil of (2I, 2J).
+cudaError_t launch_vc_coarsen(const double* cf, double* cc, int nc, cudaStream_t s);
 // Apply / residual / smoother on the stencil arrays (modes as launch_ho).
 template <typename T>
 cudaError_t launch_vc(int mode, VcArgsT<T> a, cudaStream_t s);

@@ -12,8 +12,9 @@
 // Its preconditioner is weighted Jacobi (omega = 2/3, m = 3 sweeps) with
 // standard transfers and the re-discretised coarse operator.  Here the same
 // V-cycle runs on the GPU over any number of levels:
-// - each level re-discretises the operator (variable coefficients are
-//   injected to the coarse grid);
+// - each level re-discretises the operator; the coarse coefficients are the
+//   full-weighting harmonic mean of the fine ones (injection under-samples
+//   thin layers and costs iterations);
 // - the smoother is Jacobi or Richardson;
 // - the transfers are the second-order path's restriction and prolongation
 //   kernels;
@@ -615,7 +616,7 @@ int build_variable(OpSolver* s, const double* c) {
     } else {
       rc = dalloc(s, &L.c, (size_t)m * m);
       if (rc) return rc;
-      SBP_CUDA(launch_vc_inject(s->lv[l - 1].c, L.c, m, nullptr));
+      SBP_CUDA(launch_vc_coarsen(s->lv[l - 1].c, L.c, m, nullptr));
     }
     if (!s->mixed && l == 0) {
       for (int k = 0; k < 6; ++k) L.st[k] = s->st64[k];

@@ -9,7 +9,7 @@
 // - k_vc<MODE>: the solver's apply / residual / Jacobi sweep on those
 //   arrays, in FP64 or FP32.  Five multiply-adds per point instead of the
 //   face averages.
-// - k_vc_inject: the coarse coefficients, by injection.
+// - k_vc_coarsen: the coarse coefficients, a full-weighting harmonic mean.
 // - k_dense_gemv: the coarse direct solve, x = A^-1 b with a dense inverse.
 // The access pattern is that of the other stencil kernels: a row per thread,
 // a march along j with the row's own values in registers, and i-neighbours
@@ -125,14 +125,31 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// cc(I, J) = 1 / sum_ab w_a w_b / cf(2I + a, 2J + b), a, b in {-1, 0, 1},
+// w = (1/4, 1/2, 1/4), fine indices clamped to the grid.  Sums run along j
+// first, then along i, each left to right with separate roundings (no FMA
+// contraction), so the result is the same double as the oracle's.
 __global__ void __launch_bounds__(kThreads)
-    k_vc_inject(const double* __restrict__ cf, double* __restrict__ cc, int nc) {
+    k_vc_coarsen(const double* __restrict__ cf, double* __restrict__ cc, int nc) {
   const int nf = 2 * nc - 1;
+  const double w[3] = {0.25, 0.5, 0.25};
   const long long total = (long long)nc * nc;
   for (long long k = (long long)blockIdx.x * kThreads + threadIdx.x; k < total;
        k += (long long)gridDim.x * kThreads) {
     const int I = (int)(k % nc), J = (int)(k / nc);
-    cc[k] = __ldg(cf + (size_t)(2 * J) * nf + 2 * I);
+    double both = 0.0;
+    for (int a = 0; a < 3; ++a) {
+      const int i = min(max(2 * I + a - 1, 0), nf - 1);
+      double col = 0.0;
+      for (int b = 0; b < 3; ++b) {
+        const int j = min(max(2 * J + b - 1, 0), nf - 1);
+        const double t = __dmul_rn(w[b], 1.0 / __ldg(cf + (size_t)j * nf + i));
+        col = b == 0 ? t : __dadd_rn(col, t);
+      }
+      const double t = __dmul_rn(w[a], col);
+      both = a == 0 ? t : __dadd_rn(both, t);
+    }
+    cc[k] = 1.0 / both;
   }
 }
 
@@ -393,10 +410,11 @@ cudaError_t launch_vc_stencil(const double* c, T* E, T* N, T* D, T* flo, T* fhi,
   return cudaGetLastError();
 }
 
-cudaError_t launch_vc_inject(const double* cf, double* cc, int nc, cudaStream_t s) {
+cudaError_t launch_vc_coarsen(const double* cf, double* cc, int nc, cudaStream_t s) {
+  if (nc < 2) return cudaErrorInvalidValue;
   const long long total = (long long)nc * nc;
   const int g = (int)std::max(1LL, std::min<long long>((total + kThreads - 1) / kThreads, 4096));
-  k_vc_inject<<<g, kThreads, 0, s>>>(cf, cc, nc);
+  k_vc_coarsen<<<g, kThreads, 0, s>>>(cf, cc, nc);
   return cudaGetLastError();
 }
 

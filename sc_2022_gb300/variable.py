@@ -10,7 +10,7 @@ operator with any nodal field c > 0 is matrix-free on the GPU:
 - the SATs are those of ``Assembling_matrix``, with the boundary flux and
   the Dirichlet penalty scaled by c at the boundary point.
 It comes with CG and a multigrid-preconditioned CG whose coarse levels
-re-discretise the operator with injected coefficients.  c = 1 gives the
+re-discretise the operator with harmonic-mean coarse coefficients.  c = 1 gives the
 constant-coefficient operator exactly.
 """
 from __future__ import annotations

@@ -1,6 +1,6 @@
 """GPU parity of the variable-coefficient operator (div(c grad u)) and its
 solvers against the oracle's assembly of variable_diagonal_sbp_D2 per grid
-line and the oracle's multigrid with injected coefficients."""
+line and the oracle's multigrid with harmonic-mean coarse coefficients."""
 import numpy as np
 import pytest
 import scipy.sparse.linalg as spla

@@ -164,6 +164,29 @@ def test_vcycle_galerkin_h_independent():
     assert max(its) <= 8 and max(its) - min(its) <= 1
 
 
+def test_coarsen_coefficients_harmonic_full_weighting():
+    # constant fields stay constant; a mean lies within the fine values it
+    # averages; on the layered field the harmonic coarse coefficients keep
+    # MGCG at 10 iterations at N = 129 (injection: 11)
+    c = np.full((17, 17), 2.5)
+    np.testing.assert_array_equal(o.coarsen_coefficients(c), np.full((9, 9), 2.5))
+    f = o.coefficient_field(65, "layered").reshape(65, 65)
+    cc = o.coarsen_coefficients(f)
+    assert cc.shape == (33, 33)
+    assert cc.min() >= f.min() * (1 - 1e-15) and cc.max() <= f.max() * (1 + 1e-15)
+    # at a coarse point away from the edges, by the definition
+    w = np.array([0.25, 0.5, 0.25])
+    I, J = 7, 11
+    blk = 1.0 / f[2 * J - 1:2 * J + 2, 2 * I - 1:2 * I + 2]
+    assert cc[J, I] == pytest.approx(1.0 / (w @ blk @ w), rel=1e-15)
+    n = 129
+    c = o.coefficient_field(n, "layered")
+    b = np.random.default_rng(4).standard_normal(n * n)
+    hier = o.Hierarchy(n, o.MGOptions(restriction="galerkin", coarse_n=17), coef=c)
+    _, it, _ = o.mgcg(hier, b, reltol=1e-10)
+    assert it <= 10
+
+
 def test_adjoint_oracle_matches_finite_differences():
     # The oracle gradient of L = 1/2 |u - ut|_H^2 along seeded directions in
     # (f, gW, gE, gS, gN): central differences are exact for a quadratic loss
