@@ -170,7 +170,8 @@ struct TileBoxes {
   }
 };
 
-__device__ __forceinline__ bool tile_interior(const TileT& t, int n) {
+template <int A, int B>
+__device__ __forceinline__ bool tile_interior(const Tile<A, B>& t, int n) {
   return t.i_lo > 0 && t.i_hi < n && t.j_lo > 2 && t.j_hi < n - 3;
 }
 
@@ -1305,20 +1306,34 @@ __device__ __forceinline__ void region_for(int i0, int i1, int j0, int j1, Fn&& 
 }
 
 // Pre-smoothing (S sweeps from zero) + residual + restriction.  Tiles are
-// 32 x 16 coarse points; the fine box (76 x 41 at (64 ti - 4, 32 tj - 4))
-// holds b around the residual region with a halo of S <= 3.
-constexpr int PBI = 76, PBJ = 41;
+// RI x RJ coarse points; the fine box (BI x BJ at (2 RI ti - 4, 2 RJ tj - 4))
+// holds b around the residual region with a halo of S <= 3.  The residual
+// region of a tile spans box indices 5 .. 2R + 5 in each direction, so a box
+// needs 2R + 9 points; BI is rounded up for 16-byte TMA rows.
+// - PreLarge: 32 x 16 tiles (76 x 41 boxes), with the unrolled interior path.
+// - PreSmall: 16 x 8 tiles (44 x 25 boxes), for levels with fewer large
+//   tiles than SMs: a quarter of the serial work per CTA on four times the
+//   CTAs.  Every tile takes the generic path.
+template <int RI_, int RJ_, int BI_, int BJ_, bool LEAN_>
+struct PreGeom {
+  static constexpr int RI = RI_, RJ = RJ_, BI = BI_, BJ = BJ_;
+  static constexpr bool kLean = LEAN_;
+  static_assert(BI >= 2 * RI + 9 && BJ >= 2 * RJ + 9 && BI % 4 == 0, "pre-smoothing box");
+};
+using PreLarge = PreGeom<RTI, RTJ, 76, 41, true>;
+using PreSmall = PreGeom<16, 8, 44, 25, false>;
+constexpr int PBI = PreLarge::BI;
 
-template <typename T, bool TMA>
+template <typename T, bool TMA, class Geo = PreLarge>
 struct PreFusedJob {
-  static constexpr int kBox = align128(box_bytes<T, PBI, PBJ>());
+  static constexpr int kBox = align128(box_bytes<T, Geo::BI, Geo::BJ>());
   static constexpr int kStage = kBox;
   static constexpr int kScratch = 2 * kBox;
   static constexpr bool kReduce = false;
   using Acc = DotAcc<double>;
   using Ctx = NoCtx;
   DevOperand<T> b;
-  CUtensorMap bmap;    // PBI x PBJ box of b
+  CUtensorMap bmap;    // BI x BJ box of b
   Grid<T> vout, f;
   int nf, nc, ntx, ntot, sweeps, smoother, kind;
   T omega;
@@ -1326,10 +1341,11 @@ struct PreFusedJob {
   ReduceBuf rb;
   __device__ bool prepare(Ctx&) const { return st && st->done; }
   __device__ int tiles() const { return ntot; }
-  __device__ unsigned tx_bytes(int) const { return TMA ? box_bytes<T, PBI, PBJ>() : 0u; }
+  __device__ unsigned tx_bytes(int) const { return TMA ? box_bytes<T, Geo::BI, Geo::BJ>() : 0u; }
   __device__ void issue(unsigned char* buf, unsigned long long* bar, int id, const Ctx&) const {
     const int ti = id % ntx, tj = id / ntx;
-    stage_box<TMA, PBI, PBJ>(reinterpret_cast<T*>(buf), b, &bmap, 64 * ti - 4, 32 * tj - 4, nf, bar);
+    stage_box<TMA, Geo::BI, Geo::BJ>(reinterpret_cast<T*>(buf), b, &bmap, 2 * Geo::RI * ti - 4,
+                                 2 * Geo::RJ * tj - 4, nf, bar);
   }
   // Interior tile (full 32 x 16 coarse tile; every swept fine point has the
   // plain 5-point stencil and the constant smoother weight m).  Box offsets:
@@ -1407,17 +1423,20 @@ struct PreFusedJob {
   }
 
   __device__ void compute(unsigned char* buf, int id, Acc&, const Ctx&, unsigned char* scr) const {
+    constexpr int BW = Geo::BI;   // box row length
     const int ti = id % ntx, tj = id / ntx;
-    const Tile<RTI, RTJ> t = tile_at<RTI, RTJ>(id, ntx, nc);
-    const int X0 = 64 * ti - 4, Y0 = 32 * tj - 4;
+    const Tile<Geo::RI, Geo::RJ> t = tile_at<Geo::RI, Geo::RJ>(id, ntx, nc);
+    const int X0 = 2 * Geo::RI * ti - 4, Y0 = 2 * Geo::RJ * tj - 4;
     const T* B = reinterpret_cast<const T*>(buf);
     T* const V0 = reinterpret_cast<T*>(scr);
     T* const V1 = reinterpret_cast<T*>(scr + kBox);
-    if (lean_ok(t)) {
-      if (sweeps == 3) compute_lean<3>(t, X0, Y0, B, V0, V1);
-      else if (sweeps == 2) compute_lean<2>(t, X0, Y0, B, V0, V1);
-      else compute_lean<1>(t, X0, Y0, B, V0, V1);
-      return;
+    if constexpr (Geo::kLean) {
+      if (lean_ok(t)) {
+        if (sweeps == 3) compute_lean<3>(t, X0, Y0, B, V0, V1);
+        else if (sweeps == 2) compute_lean<2>(t, X0, Y0, B, V0, V1);
+        else compute_lean<1>(t, X0, Y0, B, V0, V1);
+        return;
+      }
     }
     const bool jac = (smoother == kSmoothJacobi);
     // residual region and its expansions, clipped to the domain
@@ -1429,7 +1448,7 @@ struct PreFusedJob {
     {
       const int h = sweeps;
       region_for(lo(ri0, h), hi(ri1, h), lo(rj0, h), hi(rj1, h), [&](int i, int j) {
-        const int k = (j - Y0) * PBI + (i - X0);
+        const int k = (j - Y0) * BW + (i - X0);
         V0[k] = (jac ? omega * inv_diagA<T>(i, j, nf) : omega) * B[k];
       });
     }
@@ -1437,7 +1456,7 @@ struct PreFusedJob {
     bool cur1 = false;   // v_k lives in V1 (else V0)
     for (int sw = 2; sw <= sweeps; ++sw) {
       const int h = sweeps - sw + 1;
-      box_sweep<T, PBI>(cur1 ? V0 : V1, cur1 ? V1 : V0, B, X0, Y0, lo(ri0, h), hi(ri1, h),
+      box_sweep<T, BW>(cur1 ? V0 : V1, cur1 ? V1 : V0, B, X0, Y0, lo(ri0, h), hi(ri1, h),
                         lo(rj0, h), hi(rj1, h), nf, jac, omega);
       __syncthreads();
       cur1 = !cur1;
@@ -1447,20 +1466,20 @@ struct PreFusedJob {
     const T* const VS = cur1 ? V1 : V0;
     region_for(max(2 * t.i_lo, 0), min(2 * t.i_hi - 1, nf - 1), max(2 * t.j_lo, 0),
                min(2 * t.j_hi - 1, nf - 1), [&](int i, int j) {
-                 vout.at(i, j) = VS[(j - Y0) * PBI + (i - X0)];
+                 vout.at(i, j) = VS[(j - Y0) * BW + (i - X0)];
                });
     {
       const int i0 = max(ri0, 0), i1 = min(ri1, nf - 1), j0 = max(rj0, 0), j1 = min(rj1, nf - 1);
       const bool interior = i0 > 0 && i1 < nf - 1 && j0 > 2 && j1 < nf - 3;
       if (interior) {
-        march_region<T, PBI>(VS, X0, Y0, i0, i1, j0, j1,
+        march_region<T, BW>(VS, X0, Y0, i0, i1, j0, j1,
                              [&](int, int, int k, T um, T u0, T up, T uw, T ue) {
                                R[k] = B[k] + (((uw + ue) + (um + up)) - T(4) * u0);
                              });
       } else {
         region_for(i0, i1, j0, j1, [&](int i, int j) {
-          const int k = (j - Y0) * PBI + (i - X0);
-          R[k] = B[k] + negA<T>(SAcc<T>{VS + k, PBI}, i, j, nf);
+          const int k = (j - Y0) * BW + (i - X0);
+          R[k] = B[k] + negA<T>(SAcc<T>{VS + k, BW}, i, j, nf);
         });
       }
     }
@@ -1483,7 +1502,7 @@ struct PreFusedJob {
           for (int ai = -1; ai <= 1; ++ai) {
             const T wi = restrict_w1<T>(kind, I, nc, ai);
             if (wi == T(0)) continue;
-            acc = fma(wi * wj, R[(2 * J + bj - Y0) * PBI + (2 * I + ai - X0)], acc);
+            acc = fma(wi * wj, R[(2 * J + bj - Y0) * BW + (2 * I + ai - X0)], acc);
           }
         }
         f.at(I, J) = acc;
@@ -1493,24 +1512,38 @@ struct PreFusedJob {
   __device__ void finish(double) const {}
 };
 
-// Prolongation + post-smoothing (S sweeps).  Fine tiles 64 x 32; boxes of
-// v_in and b: 72 x 41 at (64 ti - 4, j_lo - 4); coarse e: 40 x 22 at
-// (32 ti - 4, (j_lo - 4) >> 1).
-constexpr int QBI = 72, QBJ = 41;
-constexpr int QCI = 40, QCJ = 22;
+// Prolongation + post-smoothing (S sweeps).  Fine tiles TI x TJ; boxes of
+// v_in and b: BI x BJ at (TI ti - 4, j_lo - 4); coarse e: CI x CJ at
+// (TI/2 ti - 4, (j_lo - 4) >> 1).  With S <= 3 the swept region reaches box
+// index TI + 6 in i and TJ + 7 in j, and the coarse values it interpolates
+// reach TI/2 + 6 and TJ/2 + 4.
+// - PostLarge: 64 x 32 tiles, with the unrolled interior path.
+// - PostSmall: 32 x 16 tiles, for levels with fewer large tiles than SMs;
+//   every tile takes the generic path.
+template <int TI_, int TJ_, int BI_, int BJ_, int CI_, int CJ_, bool LEAN_>
+struct PostGeom {
+  static constexpr int TI = TI_, TJ = TJ_, BI = BI_, BJ = BJ_, CI = CI_, CJ = CJ_;
+  static constexpr bool kLean = LEAN_;
+  static_assert(BI >= TI + 7 && BJ >= TJ + 8 && CI >= TI / 2 + 7 && CJ >= TJ / 2 + 5 &&
+                    BI % 4 == 0 && CI % 4 == 0,
+                "post-smoothing boxes");
+};
+using PostLarge = PostGeom<TI, TJ, 72, 41, 40, 22, true>;
+using PostSmall = PostGeom<32, 16, 40, 25, 24, 14, false>;
+constexpr int QBI = PostLarge::BI, QCI = PostLarge::CI;
 
-template <typename T, bool DOT, bool TMA>
+template <typename T, bool DOT, bool TMA, class Geo = PostLarge>
 struct PostFusedJob {
-  static constexpr int kBox = align128(box_bytes<T, QBI, QBJ>());
+  static constexpr int kBox = align128(box_bytes<T, Geo::BI, Geo::BJ>());
   static constexpr int kOffB = kBox;
   static constexpr int kOffE = 2 * kBox;
-  static constexpr int kStage = kOffE + align128(box_bytes<T, QCI, QCJ>());
+  static constexpr int kStage = kOffE + align128(box_bytes<T, Geo::CI, Geo::CJ>());
   static constexpr int kScratch = kBox;
   static constexpr bool kReduce = DOT;
   using Acc = DotAcc<T>;
   using Ctx = NoCtx;
   DevOperand<T> vin, e, b;
-  CUtensorMap vmap, bmap, emap;   // QBI x QBJ boxes of v_in and b, QCI x QCJ of e
+  CUtensorMap vmap, bmap, emap;   // BI x BJ boxes of v_in and b, CI x CJ of e
   Grid<T> vout;
   int n, ntx, ntot, sweeps, smoother;
   T omega;
@@ -1519,16 +1552,17 @@ struct PostFusedJob {
   __device__ bool prepare(Ctx&) const { return st && st->done; }
   __device__ int tiles() const { return ntot; }
   __device__ unsigned tx_bytes(int) const {
-    return TMA ? 2u * box_bytes<T, QBI, QBJ>() + box_bytes<T, QCI, QCJ>() : 0u;
+    return TMA ? 2u * box_bytes<T, Geo::BI, Geo::BJ>() + box_bytes<T, Geo::CI, Geo::CJ>() : 0u;
   }
   __device__ void issue(unsigned char* buf, unsigned long long* bar, int id, const Ctx&) const {
     const int ti = id % ntx;
-    const int jl = tile_at<TI, TJ>(id, ntx, n).j_lo;
-    stage_box<TMA, QBI, QBJ>(reinterpret_cast<T*>(buf), vin, &vmap, 64 * ti - 4, jl - 4, n, bar);
-    stage_box<TMA, QBI, QBJ>(reinterpret_cast<T*>(buf + kOffB), b, &bmap, 64 * ti - 4, jl - 4, n,
-                             bar);
-    stage_box<TMA, QCI, QCJ>(reinterpret_cast<T*>(buf + kOffE), e, &emap, 32 * ti - 4,
-                             (jl - 4) >> 1, (n + 1) / 2, bar);
+    const int jl = tile_at<Geo::TI, Geo::TJ>(id, ntx, n).j_lo;
+    const int x0 = Geo::TI * ti - 4;
+    stage_box<TMA, Geo::BI, Geo::BJ>(reinterpret_cast<T*>(buf), vin, &vmap, x0, jl - 4, n, bar);
+    stage_box<TMA, Geo::BI, Geo::BJ>(reinterpret_cast<T*>(buf + kOffB), b, &bmap, x0, jl - 4, n,
+                                 bar);
+    stage_box<TMA, Geo::CI, Geo::CJ>(reinterpret_cast<T*>(buf + kOffE), e, &emap,
+                                 (Geo::TI / 2) * ti - 4, (jl - 4) >> 1, (n + 1) / 2, bar);
   }
   // Interior tile (full 64 x 32 fine tile, every swept point with the plain
   // stencil and constant weight m).  Box offsets: the tile Rt starts at box
@@ -1616,19 +1650,22 @@ struct PostFusedJob {
 
   __device__ void compute(unsigned char* buf, int id, Acc& acc, const Ctx&,
                           unsigned char* scr) const {
-    const TileT t = tile_at<TI, TJ>(id, ntx, n);
+    constexpr int BW = Geo::BI, CW = Geo::CI;   // box row lengths
+    const Tile<Geo::TI, Geo::TJ> t = tile_at<Geo::TI, Geo::TJ>(id, ntx, n);
     const int ti = id % ntx;
-    const int X0 = 64 * ti - 4, Y0 = t.j_lo - 4;
-    const int XC = 32 * ti - 4, YC = (t.j_lo - 4) >> 1;
+    const int X0 = Geo::TI * ti - 4, Y0 = t.j_lo - 4;
+    const int XC = (Geo::TI / 2) * ti - 4, YC = (t.j_lo - 4) >> 1;
     T* const V0 = reinterpret_cast<T*>(buf);
     T* const V1 = reinterpret_cast<T*>(scr);
     const T* B = reinterpret_cast<const T*>(buf + kOffB);
     const T* E = reinterpret_cast<const T*>(buf + kOffE);
-    if (lean_ok(t)) {
-      if (sweeps == 3) compute_lean<3>(t, V0, V1, B, E, acc);
-      else if (sweeps == 2) compute_lean<2>(t, V0, V1, B, E, acc);
-      else compute_lean<1>(t, V0, V1, B, E, acc);
-      return;
+    if constexpr (Geo::kLean) {
+      if (lean_ok(t)) {
+        if (sweeps == 3) compute_lean<3>(t, V0, V1, B, E, acc);
+        else if (sweeps == 2) compute_lean<2>(t, V0, V1, B, E, acc);
+        else compute_lean<1>(t, V0, V1, B, E, acc);
+        return;
+      }
     }
     const bool jac = (smoother == kSmoothJacobi);
     auto lo = [](int v, int h) { return max(v - h, 0); };
@@ -1637,22 +1674,22 @@ struct PostFusedJob {
     // F0 = v_in + P e on the tile + S
     region_for(lo(ti0, sweeps), hi(ti1, sweeps), lo(tj0, sweeps), hi(tj1, sweeps),
                [&](int i, int j) {
-                 const T* q = E + ((j >> 1) - YC) * QCI + ((i >> 1) - XC);
+                 const T* q = E + ((j >> 1) - YC) * CW + ((i >> 1) - XC);
                  const bool oi = i & 1, oj = j & 1;
                  T pe = q[0];
                  if (oi) pe += q[1];
                  if (oj) {
-                   pe += q[QCI];
-                   if (oi) pe += q[QCI + 1];
+                   pe += q[CW];
+                   if (oi) pe += q[CW + 1];
                  }
-                 V0[(j - Y0) * QBI + (i - X0)] +=
+                 V0[(j - Y0) * BW + (i - X0)] +=
                      pe * ((oi && oj) ? T(0.25) : ((oi || oj) ? T(0.5) : T(1)));
                });
     __syncthreads();
     bool cur1 = false;
     for (int sw = 1; sw < sweeps; ++sw) {
       const int h = sweeps - sw;
-      box_sweep<T, QBI>(cur1 ? V0 : V1, cur1 ? V1 : V0, B, X0, Y0, lo(ti0, h), hi(ti1, h),
+      box_sweep<T, BW>(cur1 ? V0 : V1, cur1 ? V1 : V0, B, X0, Y0, lo(ti0, h), hi(ti1, h),
                         lo(tj0, h), hi(tj1, h), n, jac, omega);
       __syncthreads();
       cur1 = !cur1;
@@ -1662,7 +1699,7 @@ struct PostFusedJob {
     const bool interior = tile_interior(t, n);
     if (interior && sweeps > 0) {
       const T m = jac ? omega * T(0.25) : omega;
-      march_region<T, QBI>(in, X0, Y0, ti0, ti1, tj0, tj1,
+      march_region<T, BW>(in, X0, Y0, ti0, ti1, tj0, tj1,
                            [&](int i, int j, int k, T um, T u0, T up, T uw, T ue) {
                              const T bb = B[k];
                              const T vn = fma(m, bb + (((uw + ue) + (um + up)) - T(4) * u0), u0);
@@ -1671,12 +1708,12 @@ struct PostFusedJob {
                            });
     } else {
       region_for(ti0, ti1, tj0, tj1, [&](int i, int j) {
-        const int k = (j - Y0) * QBI + (i - X0);
+        const int k = (j - Y0) * BW + (i - X0);
         const T* a = in + k;
         const T bb = B[k];
         T vn = a[0];
         if (sweeps > 0) {
-          const T na = negA<T>(SAcc<T>{a, QBI}, i, j, n);
+          const T na = negA<T>(SAcc<T>{a, BW}, i, j, n);
           const T m = jac ? omega * inv_diagA<T>(i, j, n) : omega;
           vn = fma(m, bb + na, a[0]);
         }
@@ -1975,41 +2012,62 @@ cudaError_t launch_resrestrict(Grid<const T> v, Grid<const T> b, Grid<T> f, int 
                                   s);
 }
 
+// Levels with fewer than four large tiles per SM take the small tiles.
+// Below one tile per SM a launch is bound by the serial work of one tile per
+// CTA, not by HBM.  Between one and four, whole tiles balance badly over the
+// resident CTAs: 512 large tiles of the N = 1025 level on 456 CTAs leave 56
+// CTAs a second tile.  Mixed V-cycle at N = 4097: 454 us with large tiles
+// everywhere, 432 us with small tiles below 152 large ones, 430 us below 608.
+static bool small_fused_tiles(int ncoarse) {
+  return ntiles(ncoarse, RTI) * ntiles(ncoarse, RTJ) < 4 * sm_count();
+}
+
+template <typename T, class G>
+static cudaError_t launch_pre_fused_geom(const Operand& b, Grid<T> vout, Grid<T> f, int nf,
+                                         int sweeps, int smoother, double omega, int kind,
+                                         const SolveState* st, cudaStream_t s) {
+  const int nc = (nf + 1) / 2;
+  const int ntx = ntiles(nc, G::RI), nty = ntiles(nc, G::RJ);
+  const int total = ntx * nty;
+  const DevOperand<T> db = dev_operand<T>(b);
+  CUtensorMap bm{};
+  const bool tma = b.tma && make_box_map(bm, b, sizeof(T) == 8, G::BI, G::BJ);
+  if (tma)
+    return launch_persist(PreFusedJob<T, true, G>{db, bm, vout, f, nf, nc, ntx, total, sweeps,
+                                                  smoother, kind, T(omega), st, ReduceBuf{}},
+                          total, s);
+  return launch_persist(PreFusedJob<T, false, G>{db, bm, vout, f, nf, nc, ntx, total, sweeps,
+                                                 smoother, kind, T(omega), st, ReduceBuf{}},
+                        total, s);
+}
+
 template <typename T>
 cudaError_t launch_pre_fused(const Operand& b, Grid<T> vout, Grid<T> f, int nf, int sweeps,
                              int smoother, double omega, int kind, const SolveState* st,
                              cudaStream_t s) {
   if (sweeps < 1 || sweeps > kMaxFusedSweeps) return cudaErrorInvalidValue;
-  const int nc = (nf + 1) / 2;
-  const int ntx = ntiles(nc, RTI), nty = ntiles(nc, RTJ);
-  const int total = ntx * nty;
-  const DevOperand<T> db = dev_operand<T>(b);
-  CUtensorMap bm{};
-  const bool tma = b.tma && make_box_map(bm, b, sizeof(T) == 8, PBI, PBJ);
-  if (tma)
-    return launch_persist(PreFusedJob<T, true>{db, bm, vout, f, nf, nc, ntx, total, sweeps,
-                                               smoother, kind, T(omega), st, ReduceBuf{}},
-                          total, s);
-  return launch_persist(PreFusedJob<T, false>{db, bm, vout, f, nf, nc, ntx, total, sweeps,
-                                              smoother, kind, T(omega), st, ReduceBuf{}},
-                        total, s);
+  if (small_fused_tiles((nf + 1) / 2))
+    return launch_pre_fused_geom<T, PreSmall>(b, vout, f, nf, sweeps, smoother, omega, kind, st,
+                                              s);
+  return launch_pre_fused_geom<T, PreLarge>(b, vout, f, nf, sweeps, smoother, omega, kind, st,
+                                            s);
 }
 
-template <typename T>
-cudaError_t launch_post_fused(const Operand& vin, const Operand& e, const Operand& b, Grid<T> vout,
-                              int n, int sweeps, int smoother, double omega, int dot,
-                              SolveState* st, ReduceBuf rb, cudaStream_t s) {
-  if (sweeps < 0 || sweeps > kMaxFusedSweeps || (dot && !st)) return cudaErrorInvalidValue;
-  const dim3 g = tile_grid(n);
-  const int total = (int)(g.x * g.y);
+template <typename T, class G>
+static cudaError_t launch_post_fused_geom(const Operand& vin, const Operand& e, const Operand& b,
+                                          Grid<T> vout, int n, int sweeps, int smoother,
+                                          double omega, int dot, SolveState* st, ReduceBuf rb,
+                                          cudaStream_t s) {
+  const int ntx = ntiles(n, G::TI), nty = ntiles(n, G::TJ);
+  const int total = ntx * nty;
   const bool f64 = sizeof(T) == 8;
   CUtensorMap vm{}, bm{}, em{};
-  const bool tma = vin.tma && b.tma && e.tma && make_box_map(vm, vin, f64, QBI, QBJ) &&
-                   make_box_map(bm, b, f64, QBI, QBJ) && make_box_map(em, e, f64, QCI, QCJ);
+  const bool tma = vin.tma && b.tma && e.tma && make_box_map(vm, vin, f64, G::BI, G::BJ) &&
+                   make_box_map(bm, b, f64, G::BI, G::BJ) && make_box_map(em, e, f64, G::CI, G::CJ);
   const DevOperand<T> dv = dev_operand<T>(vin), de = dev_operand<T>(e), db = dev_operand<T>(b);
 #define SBP_POST(D, M)                                                                           \
-  return launch_persist(PostFusedJob<T, D, M>{dv, de, db, vm, bm, em, vout, n, (int)g.x, total,  \
-                                              sweeps, smoother, T(omega), st, rb},               \
+  return launch_persist(PostFusedJob<T, D, M, G>{dv, de, db, vm, bm, em, vout, n, ntx, total,   \
+                                                 sweeps, smoother, T(omega), st, rb},            \
                         total, s)
   if (dot) {
     if (tma) SBP_POST(true, true);
@@ -2018,6 +2076,18 @@ cudaError_t launch_post_fused(const Operand& vin, const Operand& e, const Operan
   if (tma) SBP_POST(false, true);
   SBP_POST(false, false);
 #undef SBP_POST
+}
+
+template <typename T>
+cudaError_t launch_post_fused(const Operand& vin, const Operand& e, const Operand& b, Grid<T> vout,
+                              int n, int sweeps, int smoother, double omega, int dot,
+                              SolveState* st, ReduceBuf rb, cudaStream_t s) {
+  if (sweeps < 0 || sweeps > kMaxFusedSweeps || (dot && !st)) return cudaErrorInvalidValue;
+  if (small_fused_tiles((n + 1) / 2))
+    return launch_post_fused_geom<T, PostSmall>(vin, e, b, vout, n, sweeps, smoother, omega, dot,
+                                                st, rb, s);
+  return launch_post_fused_geom<T, PostLarge>(vin, e, b, vout, n, sweeps, smoother, omega, dot,
+                                              st, rb, s);
 }
 
 // Resolve the launch configuration of every persistent kernel up front
@@ -2070,6 +2140,18 @@ cudaError_t prepare_kernels() {
   persist_ctas_per_sm<PostFusedJob<double, true, true>>();
   persist_ctas_per_sm<PostFusedJob<double, false, false>>();
   persist_ctas_per_sm<PostFusedJob<double, true, false>>();
+  persist_ctas_per_sm<PreFusedJob<float, true, PreSmall>>();
+  persist_ctas_per_sm<PreFusedJob<float, false, PreSmall>>();
+  persist_ctas_per_sm<PreFusedJob<double, true, PreSmall>>();
+  persist_ctas_per_sm<PreFusedJob<double, false, PreSmall>>();
+  persist_ctas_per_sm<PostFusedJob<float, false, true, PostSmall>>();
+  persist_ctas_per_sm<PostFusedJob<float, true, true, PostSmall>>();
+  persist_ctas_per_sm<PostFusedJob<float, false, false, PostSmall>>();
+  persist_ctas_per_sm<PostFusedJob<float, true, false, PostSmall>>();
+  persist_ctas_per_sm<PostFusedJob<double, false, true, PostSmall>>();
+  persist_ctas_per_sm<PostFusedJob<double, true, true, PostSmall>>();
+  persist_ctas_per_sm<PostFusedJob<double, false, false, PostSmall>>();
+  persist_ctas_per_sm<PostFusedJob<double, true, false, PostSmall>>();
   persist_ctas_per_sm<CgDirMixedJob<true>>();
   return cudaGetLastError();
 }
