@@ -264,6 +264,14 @@ int sbp_vc_vcycle_apply(sbp_vc_solver* s, const double* b, double* v, void* stre
  * Needs no GPU.  Returns SBP_ERR_ARGS with *nnz set when cap is too small. */
 int sbp_vc_assemble_host(int n, const double* c, long long* row_ptr, int* col, double* val,
                          long long cap, long long* nnz);
+/* The coarse coefficients the variable-coefficient multigrid derives from a
+ * fine field: cc (nc x nc) from cf ((2nc - 1) x (2nc - 1)), host arrays,
+ * i fast, with the arithmetic of the solver's device kernel (the same bits).
+ * The reference samples its coefficient function on each grid
+ * (diagonal_sbp.jl:462-465); a nodal field is averaged instead, as the
+ * solver handle describes.  Needs no GPU. */
+int sbp_vc_coarsen_host(int nc, const double* cf, double* cc);
+
 /* The dense inverse the variable-coefficient solver uses on its coarse grid
  * (nc <= 33; c a host array of nc * nc coefficients), row-major, by the same
  * host Cholesky.  Needs no GPU. */

@@ -105,6 +105,7 @@ SIGNATURES = {
     "sbp_vc_cg_solve": (_i, [_vp, _vp, _vp, _i, _d, _d, _i, C.POINTER(sbp_result), _dp, _i,
                              _vp]),
     "sbp_vc_vcycle_apply": (_i, [_vp, _vp, _vp, _vp]),
+    "sbp_vc_coarsen_host": (_i, [_i, _dp, _dp]),
     "sbp_vc_coarse_inverse_host": (_i, [_i, _dp, _dp, C.c_longlong]),
     "sbp_vc_assemble_host": (_i, [_i, _dp, C.POINTER(C.c_longlong), C.POINTER(_i), _dp,
                                   C.c_longlong, C.POINTER(C.c_longlong)]),

@@ -858,6 +858,13 @@ int sbp_vc_coarse_inverse_host(int nc, const double* c, double* out, long long c
   return SBP_OK;
 }
 
+int sbp_vc_coarsen_host(int nc, const double* cf, double* cc) {
+  if (nc < 1 || nc > (1 << 15) || !cf || !cc) return SBP_ERR_ARGS;
+  for (int J = 0; J < nc; ++J)
+    for (int I = 0; I < nc; ++I) cc[(size_t)J * nc + I] = vc::coarse_coefficient(cf, nc, I, J);
+  return SBP_OK;
+}
+
 int sbp_vc_assemble_host(int n, const double* c, long long* row_ptr, int* col, double* val,
                          long long cap, long long* nnz) {
   if (n < 3 || !c || !row_ptr || !nnz) return SBP_ERR_ARGS;

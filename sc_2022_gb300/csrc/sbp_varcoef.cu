@@ -125,31 +125,15 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-// cc(I, J) = 1 / sum_ab w_a w_b / cf(2I + a, 2J + b), a, b in {-1, 0, 1},
-// w = (1/4, 1/2, 1/4), fine indices clamped to the grid.  Sums run along j
-// first, then along i, each left to right with separate roundings (no FMA
-// contraction), so the result is the same double as the oracle's.
+// cc(I, J) = vc::coarse_coefficient(cf, nc, I, J); the host entry point
+// sbp_vc_coarsen_host gives the same bits.
 __global__ void __launch_bounds__(kThreads)
     k_vc_coarsen(const double* __restrict__ cf, double* __restrict__ cc, int nc) {
-  const int nf = 2 * nc - 1;
-  const double w[3] = {0.25, 0.5, 0.25};
   const long long total = (long long)nc * nc;
   for (long long k = (long long)blockIdx.x * kThreads + threadIdx.x; k < total;
        k += (long long)gridDim.x * kThreads) {
     const int I = (int)(k % nc), J = (int)(k / nc);
-    double both = 0.0;
-    for (int a = 0; a < 3; ++a) {
-      const int i = min(max(2 * I + a - 1, 0), nf - 1);
-      double col = 0.0;
-      for (int b = 0; b < 3; ++b) {
-        const int j = min(max(2 * J + b - 1, 0), nf - 1);
-        const double t = __dmul_rn(w[b], 1.0 / __ldg(cf + (size_t)j * nf + i));
-        col = b == 0 ? t : __dadd_rn(col, t);
-      }
-      const double t = __dmul_rn(w[a], col);
-      both = a == 0 ? t : __dadd_rn(both, t);
-    }
-    cc[k] = 1.0 / both;
+    cc[k] = vc::coarse_coefficient(cf, nc, I, J);
   }
 }
 

@@ -36,6 +36,53 @@ namespace vc {
 constexpr double kTauDh = -13.0;   // h tau_D
 constexpr double kBs0 = 1.5, kBs1 = -2.0, kBs2 = 0.5;
 
+// Separately rounded product and sum (no FMA contraction), so that host and
+// device code give the same bits.
+__host__ __device__ inline double mul_rn(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __dmul_rn(a, b);
+#else
+  volatile double t = a * b;
+  return t;
+#endif
+}
+__host__ __device__ inline double add_rn(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __dadd_rn(a, b);
+#else
+  volatile double t = a + b;
+  return t;
+#endif
+}
+
+__host__ __device__ inline int clamp_index(int k, int n) { return k < 0 ? 0 : (k >= n ? n - 1 : k); }
+
+// Coarse nodal coefficient (I, J) of the nc x nc grid below the fine field cf
+// ((2nc - 1)^2 values, i fast): the harmonic mean of cf over the
+// full-weighting stencil of (2I, 2J),
+//   1 / sum_ab w_a w_b / cf(2I + a, 2J + b),  a, b in {-1, 0, 1},
+// w = (1/4, 1/2, 1/4), fine indices clamped to the grid.  The sums run along
+// j first, then along i, left to right.  Injection (cf(2I, 2J)) under-samples
+// layers thinner than the coarse spacing; the harmonic mean keeps their
+// conductance.
+__host__ __device__ inline double coarse_coefficient(const double* cf, int nc, int I, int J) {
+  const int nf = 2 * nc - 1;
+  const double w[3] = {0.25, 0.5, 0.25};
+  double both = 0.0;
+  for (int a = 0; a < 3; ++a) {
+    const int i = clamp_index(2 * I + a - 1, nf);
+    double col = 0.0;
+    for (int b = 0; b < 3; ++b) {
+      const int j = clamp_index(2 * J + b - 1, nf);
+      const double t = mul_rn(w[b], 1.0 / cf[(size_t)j * nf + i]);
+      col = b == 0 ? t : add_rn(col, t);
+    }
+    const double t = mul_rn(w[a], col);
+    both = a == 0 ? t : add_rn(both, t);
+  }
+  return 1.0 / both;
+}
+
 __host__ __device__ inline double weight(int k, int n) {
   return (k == 0 || k == n - 1) ? 0.5 : 1.0;
 }

@@ -63,6 +63,22 @@ def assemble_variable_host(n: int, coef) -> tuple:
     return row_ptr, col[:nnz.value].copy(), val[:nnz.value].copy()
 
 
+def coarsen_coefficients_host(coef) -> np.ndarray:
+    """The coarse coefficients ((n+1)/2 x (n+1)/2) the solver's next level
+    uses below the n x n field ``coef`` (n odd): the full-weighting harmonic
+    mean, computed on the host with the device kernel's arithmetic."""
+    c = np.ascontiguousarray(np.asarray(coef, dtype=np.float64))
+    n = int(round(np.sqrt(c.size)))
+    if n * n != c.size or n % 2 == 0:
+        raise ValueError("coef must be an n x n field with n odd")
+    nc = (n + 1) // 2
+    out = np.empty(nc * nc, dtype=np.float64)
+    L.check(L.load().sbp_vc_coarsen_host(nc, c.ctypes.data_as(C.POINTER(C.c_double)),
+                                         out.ctypes.data_as(C.POINTER(C.c_double))),
+            "sbp_vc_coarsen_host")
+    return out.reshape(nc, nc)
+
+
 class VariableCoefficientSolver:
     """Solver handle for div(c grad u) with the coefficient field ``coef``
     (an n x n float64 device grid, copied at creation).  Plain CG on any

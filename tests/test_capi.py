@@ -165,6 +165,33 @@ def test_order_p_coarse_inverse_equals_oracle(p, nc):
                                              N * N) != 0   # below the minimum grid
 
 
+@pytest.mark.parametrize("n,kind", [(3, "smooth"), (9, "layered"), (33, "smooth"),
+                                    (65, "layered"), (129, "random")])
+def test_variable_coarse_coefficients_equal_oracle_bitwise(n, kind):
+    # the coarse coefficients of the variable-coefficient multigrid (the
+    # device kernel's arithmetic, run on the host) are the oracle's doubles
+    import sc_2022_gb300 as sbp
+    if kind == "random":
+        c = np.exp(np.random.default_rng(5).uniform(-3.0, 3.0, n * n))
+    else:
+        c = o.coefficient_field(n, kind)
+    got = sbp.coarsen_coefficients_host(c)
+    ref = o.coarsen_coefficients(c.reshape(n, n))
+    assert got.shape == ref.shape
+    np.testing.assert_array_equal(got, ref)
+
+
+def test_variable_coarse_coefficients_arguments():
+    import sc_2022_gb300 as sbp
+    lib = sbp.load_library()
+    dp = C.POINTER(C.c_double)
+    buf = np.ones(9)
+    assert lib.sbp_vc_coarsen_host(0, buf.ctypes.data_as(dp), buf.ctypes.data_as(dp)) < 0
+    assert lib.sbp_vc_coarsen_host(2, None, buf.ctypes.data_as(dp)) < 0
+    with pytest.raises(ValueError):
+        sbp.coarsen_coefficients_host(np.ones(16))
+
+
 @pytest.mark.parametrize("nc,kind", [(5, "smooth"), (9, "layered"), (17, "smooth")])
 def test_variable_coarse_inverse_equals_oracle(nc, kind):
     # the dense coarse inverse of the variable-coefficient solver (host
