@@ -272,6 +272,24 @@ int sbp_vc_assemble_host(int n, const double* c, long long* row_ptr, int* col, d
  * solver handle describes.  Needs no GPU. */
 int sbp_vc_coarsen_host(int nc, const double* cf, double* cc);
 
+/* Galerkin coarse operators A_c = P' A P of the variable-coefficient
+ * operator (P: the bilinear prolongation of sbp_prolong_f64), the set-up
+ * arithmetic of a Galerkin multigrid hierarchy.  A_c is a symmetric 9-point
+ * stencil at every point, stored as five host arrays of nc x nc (i fast):
+ * D = A_c(p, p) and the couplings of -A_c to (i+1, j), (i, j+1), (i+1, j+1)
+ * and (i-1, j+1): E, N, NE, NW (zero where the neighbour is outside).
+ * sbp_vc_galerkin_coarse_host takes the fine operator from the nodal field c
+ * on n x n points (n odd); sbp_galerkin9_coarse_host takes a 9-point level
+ * in the same five-array form.  nc = (n + 1) / 2.  Needs no GPU.
+ * The reference re-discretises each level instead (get_operators,
+ * legacy_functions.jl:100-174); for a layered field the Galerkin operators
+ * keep the MGCG iteration count independent of N. */
+int sbp_vc_galerkin_coarse_host(int n, const double* c, double* D, double* E, double* N,
+                                double* NE, double* NW);
+int sbp_galerkin9_coarse_host(int n, const double* D, const double* E, const double* N,
+                              const double* NE, const double* NW, double* Dc, double* Ec,
+                              double* Nc, double* NEc, double* NWc);
+
 /* The dense inverse the variable-coefficient solver uses on its coarse grid
  * (nc <= 33; c a host array of nc * nc coefficients), row-major, by the same
  * host Cholesky.  Needs no GPU. */

@@ -740,10 +740,11 @@ class Hierarchy:
     (``matrix_free_mg_cg.jl:455``), coarse level solved by a sparse LU
     (``:460``, ``A_2h \\ f`` at :166)."""
 
-    def __init__(self, n: int, opts: MGOptions, p: int = 2, coef=None):
+    def __init__(self, n: int, opts: MGOptions, p: int = 2, coef=None, galerkin: bool = False):
         """p: SBP order of every level.  coef (flat n x n, i fast): nodal
         coefficients of the variable-coefficient operator, carried to each
-        coarse grid by :func:`coarsen_coefficients`."""
+        coarse grid by :func:`coarsen_coefficients`.  galerkin: coarse
+        operators P' A P instead of the re-discretised ones."""
         self.opts = opts
         self.p = p
         self.ns = [n]
@@ -763,9 +764,13 @@ class Hierarchy:
             self.coefs = [c.ravel() for c in cs]
             self.asm = [assemble_variable(m, c) for m, c in zip(self.ns, self.coefs)]
         self.A = [a.A for a in self.asm]
-        self.diag = [A.diagonal() for A in self.A]
         self.R = [restriction_2d(m, opts.restriction) for m in self.ns[:-1]]
         self.P = [prolongation_2d(m) for m in self.ns[1:]]
+        if galerkin:
+            self.A = [self.A[0]]
+            for P in self.P:
+                self.A.append((P.T @ self.A[-1] @ P).tocsr())
+        self.diag = [A.diagonal() for A in self.A]
         self.lu = spla.splu(self.A[-1].tocsc())
 
     def smooth(self, l, v, b, iters):

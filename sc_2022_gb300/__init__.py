@@ -16,7 +16,8 @@ from .matrix_free import (CG_Matrix_Free_GPU_v2, CG_full_GPU, initial_guess_inte
                           matrix_free_prolongation_2d_GPU, matrix_free_restriction_2d_GPU,
                           matrix_free_richardson, matrix_free_Two_level_multigrid)
 from .variable import (MGCG_variable_GPU, VariableCoefficientSolver, assemble_variable_host,
-                       coarsen_coefficients_host, matrix_free_A_variable_GPU)
+                       coarsen_coefficients_host, galerkin_coarse_host,
+                       matrix_free_A_variable_GPU)
 from .solver import (BatchSolver, Options, SolveResult, Solver, default_options,
                      reference_two_level_options)
 
@@ -30,7 +31,7 @@ __all__ = [
     "initial_guess_interpolation_three_level_CG_GPU", "CG_p4_GPU", "matrix_free_A_p4_GPU",
     "CG_high_order_GPU", "HighOrderSolver", "MGCG_high_order_GPU", "matrix_free_A_high_order_GPU",
     "MGCG_variable_GPU", "VariableCoefficientSolver", "assemble_variable_host",
-    "coarsen_coefficients_host", "matrix_free_A_variable_GPU",
+    "coarsen_coefficients_host", "galerkin_coarse_host", "matrix_free_A_variable_GPU",
 ]
 
 

@@ -106,6 +106,8 @@ SIGNATURES = {
                              _vp]),
     "sbp_vc_vcycle_apply": (_i, [_vp, _vp, _vp, _vp]),
     "sbp_vc_coarsen_host": (_i, [_i, _dp, _dp]),
+    "sbp_vc_galerkin_coarse_host": (_i, [_i, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "sbp_galerkin9_coarse_host": (_i, [_i] + [_dp] * 10),
     "sbp_vc_coarse_inverse_host": (_i, [_i, _dp, _dp, C.c_longlong]),
     "sbp_vc_assemble_host": (_i, [_i, _dp, C.POINTER(C.c_longlong), C.POINTER(_i), _dp,
                                   C.c_longlong, C.POINTER(C.c_longlong)]),

@@ -865,6 +865,54 @@ int sbp_vc_coarsen_host(int nc, const double* cf, double* cc) {
   return SBP_OK;
 }
 
+namespace {
+void store9(const vc::Stencil9& s, size_t k, double* D, double* E, double* N, double* NE,
+            double* NW) {
+  D[k] = s.d;
+  E[k] = s.e;
+  N[k] = s.n;
+  NE[k] = s.ne;
+  NW[k] = s.nw;
+}
+}  // namespace
+
+int sbp_vc_galerkin_coarse_host(int n, const double* c, double* D, double* E, double* N,
+                                double* NE, double* NW) {
+  if (n < 3 || n % 2 == 0 || n > (1 << 15) || !c || !D || !E || !N || !NE || !NW)
+    return SBP_ERR_ARGS;
+  struct Acc {
+    const double* c;
+    int n;
+    double operator()(int i, int j) const { return c[(size_t)j * n + i]; }
+  } acc{c, n};
+  const vc::FineVc<Acc> A{acc, n};
+  const int nc = (n + 1) / 2;
+  double r[3][3];
+  for (int J = 0; J < nc; ++J)
+    for (int I = 0; I < nc; ++I) {
+      vc::galerkin_row(A, nc, I, J, r);
+      store9(vc::stencil9_of(r), (size_t)J * nc + I, D, E, N, NE, NW);
+    }
+  return SBP_OK;
+}
+
+int sbp_galerkin9_coarse_host(int n, const double* D, const double* E, const double* N,
+                              const double* NE, const double* NW, double* Dc, double* Ec,
+                              double* Nc, double* NEc, double* NWc) {
+  if (n < 3 || n % 2 == 0 || n > (1 << 15) || !D || !E || !N || !NE || !NW || !Dc || !Ec ||
+      !Nc || !NEc || !NWc)
+    return SBP_ERR_ARGS;
+  const vc::FineNine A{D, E, N, NE, NW, n};
+  const int nc = (n + 1) / 2;
+  double r[3][3];
+  for (int J = 0; J < nc; ++J)
+    for (int I = 0; I < nc; ++I) {
+      vc::galerkin_row(A, nc, I, J, r);
+      store9(vc::stencil9_of(r), (size_t)J * nc + I, Dc, Ec, Nc, NEc, NWc);
+    }
+  return SBP_OK;
+}
+
 int sbp_vc_assemble_host(int n, const double* c, long long* row_ptr, int* col, double* val,
                          long long cap, long long* nnz) {
   if (n < 3 || !c || !row_ptr || !nnz) return SBP_ERR_ARGS;

@@ -116,5 +116,115 @@ __host__ __device__ inline double f_hi(double c_in, int i, int n) {
   return weight(i, n) * kBs2 * c_in;
 }
 
+// ---------------------------------------------------------------------------
+// Galerkin coarse operators A_c = P' A P (P: bilinear prolongation, nc ->
+// 2nc - 1 per direction).  For the variable-coefficient operator A_c is a
+// symmetric 9-point stencil at every coarse point, and P' A_c P stays one.
+// A 9-point level stores per point D (the diagonal of A) and the couplings
+// of -A to (i+1, j), (i, j+1), (i+1, j+1) and (i-1, j+1): E, N, NE, NW.
+// ---------------------------------------------------------------------------
+struct Stencil9 {
+  double d, e, n, ne, nw;
+};
+
+// A(p, p + (di, dj)) of the fine operator at p = (i, j) on n x n points, for
+// the offsets of `galerkin_row` (|di| <= 1, |dj| <= 2).
+// FineVc: the variable-coefficient operator from nodal c (c(i, j) accessor).
+template <typename C>
+struct FineVc {
+  const C& c;
+  int n;
+  __host__ __device__ double operator()(int i, int j, int di, int dj) const {
+    double e, nn, d;
+    if (di == 0 && dj == 0) {
+      coefficients(c, i, j, n, e, nn, d);
+      return d;
+    }
+    if (dj == 0) {   // E(min(i, i + di), j)
+      coefficients(c, di > 0 ? i : i - 1, j, n, e, nn, d);
+      return -e;
+    }
+    if (di != 0) return 0.0;
+    if (dj == 1 || dj == -1) {   // N(i, min(j, j + dj))
+      coefficients(c, i, dj > 0 ? j : j - 1, n, e, nn, d);
+      return -nn;
+    }
+    // the couplings two columns apart next to the Dirichlet sides
+    const int a = dj > 0 ? j : j - 2;   // the pair (a, a + 2)
+    double v = 0.0;
+    if (a == 0) v -= f_lo(c(i, 0), i, n);
+    if (a + 2 == n - 1) v -= f_hi(c(i, n - 1), i, n);
+    return v;
+  }
+};
+
+// A 9-point level (arrays of n x n points, i fast) as the same accessor.
+struct FineNine {
+  const double *d, *e, *n_, *ne, *nw;
+  int n;
+  __host__ __device__ double operator()(int i, int j, int di, int dj) const {
+    if (di < -1 || di > 1 || dj < -1 || dj > 1) return 0.0;
+    const auto at = [&](const double* a, int ii, int jj) { return a[(size_t)jj * n + ii]; };
+    if (di == 0 && dj == 0) return at(d, i, j);
+    if (dj == 0) return -at(e, di > 0 ? i : i - 1, j);
+    if (di == 0) return -at(n_, i, dj > 0 ? j : j - 1);
+    if (di == dj) return -at(ne, di > 0 ? i : i - 1, di > 0 ? j : j - 1);
+    return -at(nw, di < 0 ? i : i + 1, dj > 0 ? j : j - 1);   // (-1, 1) or (1, -1)
+  }
+};
+
+// Row (I, J) of P' A P on the nc x nc coarse grid: out[1 + dJ][1 + dI] =
+// A_c((I, J), (I + dI, J + dJ)).  Each fine point p of P(:, (I, J)) (the
+// 3 x 3 block around (2I, 2J), weights 1, 1/2, 1/4) meets each fine
+// neighbour q it couples to (offsets up to 1 in i, 2 in j), and q passes
+// A(p, q) P(p, K) on to its coarse parents (one, two or four points, weights
+// 1, 1/2, 1/4), all within one coarse point of (I, J).  Fixed loop order:
+// deterministic.
+template <typename Fine>
+__host__ __device__ inline void galerkin_row(const Fine& A, int nc, int I, int J,
+                                             double out[3][3]) {
+  const int nf = 2 * nc - 1;
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) out[a][b] = 0.0;
+  for (int pb = -1; pb <= 1; ++pb) {
+    const int pj = 2 * J + pb;
+    if (pj < 0 || pj >= nf) continue;
+    const double wpj = pb == 0 ? 1.0 : 0.5;
+    for (int pa = -1; pa <= 1; ++pa) {
+      const int pi = 2 * I + pa;
+      if (pi < 0 || pi >= nf) continue;
+      const double wp = wpj * (pa == 0 ? 1.0 : 0.5);
+      for (int dj = -2; dj <= 2; ++dj) {
+        const int qj = pj + dj;
+        if (qj < 0 || qj >= nf) continue;
+        for (int di = -1; di <= 1; ++di) {
+          const int qi = pi + di;
+          if (qi < 0 || qi >= nf) continue;
+          const double apq = A(pi, pj, di, dj);
+          if (apq == 0.0) continue;
+          const double v = wp * apq;
+          // coarse parents of q
+          const int i0 = qi >> 1, j0 = qj >> 1;
+          const bool oi = qi & 1, oj = qj & 1;
+          for (int sj = 0; sj <= (oj ? 1 : 0); ++sj)
+            for (int si = 0; si <= (oi ? 1 : 0); ++si) {
+              const double w = (oi ? 0.5 : 1.0) * (oj ? 0.5 : 1.0);
+              const int dI = i0 + si - I, dJ = j0 + sj - J;
+              // always within one point (the two-apart couplings join even
+              // columns); the bound only guards the array
+              if (dI < -1 || dI > 1 || dJ < -1 || dJ > 1) continue;
+              out[1 + dJ][1 + dI] += w * v;
+            }
+        }
+      }
+    }
+  }
+}
+
+// The stored form of a Galerkin row.
+__host__ __device__ inline Stencil9 stencil9_of(const double r[3][3]) {
+  return Stencil9{r[1][1], -r[1][2], -r[2][1], -r[2][2], -r[2][0]};
+}
+
 }  // namespace vc
 }  // namespace sbp

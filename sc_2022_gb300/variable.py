@@ -79,6 +79,39 @@ def coarsen_coefficients_host(coef) -> np.ndarray:
     return out.reshape(nc, nc)
 
 
+def galerkin_coarse_host(coef, levels: int = 1) -> list:
+    """Galerkin coarse operators P' A P of the variable-coefficient operator
+    with the n x n nodal field ``coef`` (n odd), ``levels`` levels down, built
+    on the host by the library.  Returns one dict per coarse level with the
+    9-point stencil arrays 'D', 'E', 'N', 'NE', 'NW' (each m x m, indexed
+    [j, i]): D the diagonal of A_c, the others the couplings of -A_c to
+    (i+1, j), (i, j+1), (i+1, j+1) and (i-1, j+1)."""
+    c = np.ascontiguousarray(np.asarray(coef, dtype=np.float64))
+    n = int(round(np.sqrt(c.size)))
+    if n * n != c.size or n % 2 == 0 or n < 3:
+        raise ValueError("coef must be an n x n field with n odd and n >= 3")
+    lib = L.load()
+    dp = C.POINTER(C.c_double)
+    out = []
+    for lev in range(levels):
+        if n < 3 or n % 2 == 0:
+            raise ValueError(f"level {lev}: {n} points cannot be coarsened")
+        m = (n + 1) // 2
+        arrs = {k: np.zeros(m * m) for k in ("D", "E", "N", "NE", "NW")}
+        ptrs = [arrs[k].ctypes.data_as(dp) for k in ("D", "E", "N", "NE", "NW")]
+        if lev == 0:
+            L.check(lib.sbp_vc_galerkin_coarse_host(n, c.ctypes.data_as(dp), *ptrs),
+                    "sbp_vc_galerkin_coarse_host")
+        else:
+            prev = out[-1]
+            fine = [np.ascontiguousarray(prev[k]).ravel() for k in ("D", "E", "N", "NE", "NW")]
+            L.check(lib.sbp_galerkin9_coarse_host(n, *[f.ctypes.data_as(dp) for f in fine],
+                                                  *ptrs), "sbp_galerkin9_coarse_host")
+        out.append({k: v.reshape(m, m) for k, v in arrs.items()})
+        n = m
+    return out
+
+
 class VariableCoefficientSolver:
     """Solver handle for div(c grad u) with the coefficient field ``coef``
     (an n x n float64 device grid, copied at creation).  Plain CG on any

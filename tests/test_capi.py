@@ -181,6 +181,45 @@ def test_variable_coarse_coefficients_equal_oracle_bitwise(n, kind):
     np.testing.assert_array_equal(got, ref)
 
 
+def _nine_point_matrix(st):
+    """The symmetric matrix of a stored 9-point level (arrays [j, i])."""
+    import scipy.sparse as sps
+    m = st["D"].shape[0]
+    rows, cols, vals = [], [], []
+    for j in range(m):
+        for i in range(m):
+            k = j * m + i
+            rows.append(k); cols.append(k); vals.append(st["D"][j, i])
+            for key, di, dj in (("E", 1, 0), ("N", 0, 1), ("NE", 1, 1), ("NW", -1, 1)):
+                ii, jj = i + di, j + dj
+                if 0 <= ii < m and 0 <= jj < m:
+                    q = jj * m + ii
+                    rows += [k, q]; cols += [q, k]; vals += [-st[key][j, i]] * 2
+                else:
+                    assert st[key][j, i] == 0.0
+    return sps.csr_matrix((vals, (rows, cols)), shape=(m * m, m * m))
+
+
+@pytest.mark.parametrize("n,kind", [(3, "smooth"), (9, "layered"), (17, "smooth"),
+                                    (33, "layered")])
+def test_galerkin_coarse_operators_equal_oracle(n, kind):
+    # P' A P of the variable-coefficient operator, level after level, built
+    # by the library's set-up arithmetic, against the oracle's sparse products
+    import sc_2022_gb300 as sbp
+    c = o.coefficient_field(n, kind)
+    levels = max(1, int(np.log2(n - 1)) - 1)
+    got = sbp.galerkin_coarse_host(c, levels=levels)
+    A = o.assemble_variable(n, c).A
+    m = n
+    for st in got:
+        m = (m + 1) // 2
+        P = o.prolongation_2d(m)
+        A = (P.T @ A @ P).tocsr()
+        B = _nine_point_matrix(st)
+        scale = abs(A).max()
+        assert abs(B - A).max() <= 1e-14 * scale
+
+
 def test_variable_coarse_coefficients_arguments():
     import sc_2022_gb300 as sbp
     lib = sbp.load_library()
@@ -190,6 +229,11 @@ def test_variable_coarse_coefficients_arguments():
     assert lib.sbp_vc_coarsen_host(2, None, buf.ctypes.data_as(dp)) < 0
     with pytest.raises(ValueError):
         sbp.coarsen_coefficients_host(np.ones(16))
+    five = [buf.ctypes.data_as(dp)] * 5
+    assert lib.sbp_vc_galerkin_coarse_host(4, buf.ctypes.data_as(dp), *five) < 0
+    assert lib.sbp_galerkin9_coarse_host(1, *[buf.ctypes.data_as(dp)] * 10) < 0
+    with pytest.raises(ValueError):
+        sbp.galerkin_coarse_host(np.ones(16))
 
 
 @pytest.mark.parametrize("nc,kind", [(5, "smooth"), (9, "layered"), (17, "smooth")])

@@ -187,6 +187,19 @@ def test_coarsen_coefficients_harmonic_full_weighting():
     assert it <= 10
 
 
+def test_galerkin_coarse_operators_keep_iterations_flat():
+    # P' A P coarse operators on the layered field: 8 MGCG iterations at
+    # N = 65 and 129 (the re-discretised hierarchy needs 9 and 10)
+    its = []
+    for n in (65, 129):
+        c = o.coefficient_field(n, "layered")
+        b = np.random.default_rng(0).standard_normal(n * n)
+        hier = o.Hierarchy(n, o.MGOptions(restriction="galerkin", coarse_n=17), coef=c,
+                           galerkin=True)
+        its.append(o.mgcg(hier, b, reltol=1e-10)[1])
+    assert max(its) <= 8
+
+
 def test_adjoint_oracle_matches_finite_differences():
     # The oracle gradient of L = 1/2 |u - ut|_H^2 along seeded directions in
     # (f, gW, gE, gS, gN): central differences are exact for a quadratic loss
