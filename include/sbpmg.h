@@ -23,6 +23,11 @@
  *  - Every function returns 0 (SBP_OK) or a negative sbp_status; no
  *    exceptions cross the ABI.  A handle may be used by one host thread at a
  *    time.
+ *  - Kernels that wait on asynchronous copies wait a bounded time.  If a
+ *    wait gives up, the kernel ends (its results are non-finite) and sets a
+ *    device flag; the next call that waits for the GPU (the solve entry
+ *    points, sbp_residual_norm_f64) reads and clears it and returns
+ *    SBP_ERR_TIMEOUT.
  */
 #ifndef SBPMG_H_
 #define SBPMG_H_
@@ -38,7 +43,9 @@ typedef enum sbp_status {
   SBP_ERR_NOMEM = -3,       /* device or host allocation failed */
   SBP_ERR_MAXITER = -4,     /* solver stopped at maxiter without converging */
   SBP_ERR_BREAKDOWN = -5,   /* p'Ap == 0 or a non-finite residual */
-  SBP_ERR_UNSUPPORTED = -6  /* option combination not supported */
+  SBP_ERR_UNSUPPORTED = -6, /* option combination not supported */
+  SBP_ERR_TIMEOUT = -7      /* a kernel's bounded wait on an asynchronous copy gave up: the
+                               call's results are void; the library stays usable */
 } sbp_status;
 
 typedef enum sbp_smoother { SBP_SMOOTH_JACOBI = 0, SBP_SMOOTH_RICHARDSON = 1 } sbp_smoother;

@@ -18,6 +18,7 @@ SBP_ERR_NOMEM = -3
 SBP_ERR_MAXITER = -4
 SBP_ERR_BREAKDOWN = -5
 SBP_ERR_UNSUPPORTED = -6
+SBP_ERR_TIMEOUT = -7
 
 SBP_SMOOTH_JACOBI = 0
 SBP_SMOOTH_RICHARDSON = 1

@@ -32,6 +32,13 @@ int fail_cuda(cudaError_t e, const char* what) {
   return SBP_ERR_CUDA;
 }
 
+int check_device_fault(const char* what) {
+  if (take_device_fault() == 0u) return SBP_OK;
+  g_last_error = std::string(what) +
+                 ": a kernel's bounded wait on an asynchronous copy gave up; results are void";
+  return SBP_ERR_TIMEOUT;
+}
+
 int finish_result(const SolveState& fs, sbp_result* res) {
   int status;
   if (fs.done == kDoneConverged)
@@ -400,10 +407,7 @@ int run_krylov(sbp_solver* s, int kind, const double* b, double* x, int sign, do
   SBP_CUDA(copy_grid(x, n, s->x, ld, n, q));
   SBP_CUDA(cudaMemcpyAsync(&s->st_host[0], s->st, sizeof(SolveState), cudaMemcpyDeviceToHost, q));
   SBP_CUDA(cudaStreamSynchronize(q));
-  if (read_device_fault() != 0u) {
-    g_last_error = "a kernel's bounded wait on an asynchronous copy gave up";
-    return SBP_ERR_CUDA;
-  }
+  if (const int fr = check_device_fault("solve")) return fr;
   const SolveState fs = s->st_host[0];
   s->last_launches = launches;
   if (norms_out && norms_cap > 0) {
@@ -501,6 +505,8 @@ const char* sbp_status_string(int status) {
     case SBP_ERR_MAXITER: return "maximum iterations reached";
     case SBP_ERR_BREAKDOWN: return "breakdown (p'Ap == 0 or non-finite residual)";
     case SBP_ERR_UNSUPPORTED: return "unsupported option combination";
+    case SBP_ERR_TIMEOUT:
+      return "a kernel's bounded wait on an asynchronous copy gave up (results void)";
     default: return "unknown status";
   }
 }
@@ -556,8 +562,9 @@ int sbp_apply_dot_f64(const double* u, double* out, int n, int sign, double* dot
 
 int sbp_apply_dot_f64_noalloc(const double* u, double* out, int n, int sign, double* dot,
                               void* stream) {
-  const int rc = apply_dot_f64_noalloc(u, out, n, sign, dot, (cudaStream_t)stream);
-  if (rc == SBP_ERR_CUDA) g_last_error = cudaGetErrorString(cudaGetLastError());
+  cudaError_t err = cudaSuccess;
+  const int rc = apply_dot_f64_noalloc(u, out, n, sign, dot, (cudaStream_t)stream, &err);
+  if (rc == SBP_ERR_CUDA) g_last_error = cudaGetErrorString(err);
   if (rc == SBP_ERR_UNSUPPORTED)
     g_last_error = "sbp_apply_dot_f64_noalloc: the launch needs more than the 1024 partial-sum "
                    "slots of the static scratch";
@@ -581,6 +588,7 @@ int sbp_residual_norm_f64(const double* x, const double* b, int n, int sign, dou
   cudaFreeAsync(r, q);
   if (e == cudaSuccess) e = cudaStreamSynchronize(q);
   if (e != cudaSuccess) return fail_cuda(e, "sbp_residual_norm_f64");
+  if (const int fr = check_device_fault("sbp_residual_norm_f64")) return fr;
   *norm_host = std::sqrt(v);
   return SBP_OK;
 }
@@ -1197,10 +1205,7 @@ int sbp_batch_autotune(sbp_batch* B, const double* const* b, double* const* x, i
   cudaEventDestroy(t1);
   if (rc) return rc;
   SBP_CUDA(cudaStreamSynchronize(q));
-  if (read_device_fault() != 0u) {
-    g_last_error = "a kernel's bounded wait on an asynchronous copy gave up";
-    return SBP_ERR_CUDA;
-  }
+  if (const int fr = check_device_fault("sbp_batch_autotune")) return fr;
   B->iter_valid = false;  // recapture with the chosen launch shapes
   return batch_capture(B, q);
 }
@@ -1272,10 +1277,7 @@ int sbp_batch_mgcg_solve(sbp_batch* B, const double* const* b, double* const* x,
   for (BatchClass& c : B->classes) launches += (long long)c.finish.groups.size();
   SBP_CUDA(cudaMemcpyAsync(B->states_host, B->states, sb, cudaMemcpyDeviceToHost, q));
   SBP_CUDA(cudaStreamSynchronize(q));
-  if (read_device_fault() != 0u) {
-    g_last_error = "a kernel's bounded wait on an asynchronous copy gave up";
-    return SBP_ERR_CUDA;
-  }
+  if (const int fr = check_device_fault("sbp_batch_mgcg_solve")) return fr;
   B->last_launches = launches;
   int status = SBP_OK;
   for (int m = 0; m < B->count; ++m) {

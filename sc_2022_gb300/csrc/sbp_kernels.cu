@@ -288,17 +288,31 @@ __global__ void __launch_bounds__(kThreads) k_persist(const __grid_constant__ Jo
     cp_async_commit();
     cp_async_wait<1>();
     // TMA stages: one thread observes the transaction barrier, the block
-    // barrier then orders the staged data for every thread
-    if (threadIdx.x == 0) ok = mbar_wait_bounded(&bar[k & 1], (k >> 1) & 1);
-    if (!__syncthreads_and(ok)) break;
+    // barrier then orders the staged data for every thread (and gives every
+    // thread the same verdict)
+    bool arrived = true;
+    if (threadIdx.x == 0) arrived = mbar_wait_bounded(&bar[k & 1], (k >> 1) & 1);
+    ok = __syncthreads_and(arrived);
+    if (!ok) {
+      // the copy of `next` into the other buffer may still be in flight:
+      // wait for it (bounded) so that no copy lands after the CTA has left
+      if (threadIdx.x == 0 && next < total) mbar_wait_bounded(&bar[nb], ((k + 1) >> 1) & 1);
+      __syncthreads();
+      break;
+    }
     job.compute((k & 1) ? buf1 : buf0, tile, acc, ctx, scratch);
     // this buffer is refilled by TMA (async proxy) after the barrier
     fence_proxy_async_smem();
     __syncthreads();
   }
   cp_async_wait<0>();
-  if (!ok) return;  // a copy never arrived: the fault flag is set, results are void
-  if (Job::kReduce) grid_reduce(acc.value(), job.rb, [&](double tot) { job.finish(tot); });
+  // A CTA whose copy never arrived still takes part in the reduction, with a
+  // NaN partial: the ticket count stays whole (the last CTA resets it for the
+  // next launch) and the result is non-finite, which the solver reports as a
+  // breakdown; the fault flag is set as well.
+  if (Job::kReduce)
+    grid_reduce(ok ? acc.value() : __longlong_as_double(0x7ff8000000000000LL), job.rb,
+                [&](double tot) { job.finish(tot); });
 }
 
 // ---------------------------------------------------------------------------
@@ -372,8 +386,15 @@ __global__ void __launch_bounds__(kThreads)
     if (next < total) stage(next, nb ? buf1 : buf0, &bar[nb], true);
     cp_async_commit();
     cp_async_wait<1>();
-    if (threadIdx.x == 0) ok = mbar_wait_bounded(&bar[k & 1], (k >> 1) & 1);
-    if (!__syncthreads_and(ok)) break;
+    bool arrived = true;
+    if (threadIdx.x == 0) arrived = mbar_wait_bounded(&bar[k & 1], (k >> 1) & 1);
+    ok = __syncthreads_and(arrived);
+    if (!ok) {
+      // drain the copy of `next` (bounded) before the CTA leaves
+      if (threadIdx.x == 0 && next < total) mbar_wait_bounded(&bar[nb], ((k + 1) >> 1) & 1);
+      __syncthreads();
+      break;
+    }
     const int slot = tile / tpp;
     if (Job::kReduce && slot != cur) {
       if (cur >= 0) flush();
@@ -387,9 +408,14 @@ __global__ void __launch_bounds__(kThreads)
     __syncthreads();
   }
   cp_async_wait<0>();
-  if (!ok) return;  // a copy never arrived: the fault flag is set, results are void
   if (!Job::kReduce) return;
   if (cur >= 0) flush();
+  __syncthreads();
+  // a copy never arrived: every problem gets a NaN partial from this CTA (the
+  // ticket count stays whole; the results are non-finite, the fault flag set)
+  if (!ok)
+    for (int k = threadIdx.x; k < count; k += kThreads)
+      slot_part[k] = __longlong_as_double(0x7ff8000000000000LL);
   __syncthreads();
   for (int k = threadIdx.x; k < count; k += kThreads)
     partials[(size_t)blockIdx.x * count + k] = slot_part[k];
@@ -2162,6 +2188,15 @@ unsigned int read_device_fault() {
   return v;
 }
 
+unsigned int take_device_fault() {
+  const unsigned int v = read_device_fault();
+  if (v != 0u) {
+    const unsigned int zero = 0u;
+    cudaMemcpyToSymbol(g_sbp_fault, &zero, sizeof(zero));
+  }
+  return v;
+}
+
 // ---------------------------------------------------------------------------
 // Standalone prolongation out (+)= P e.
 // ---------------------------------------------------------------------------
@@ -2709,12 +2744,14 @@ cudaError_t noalloc_scratch(void** out) {
 
 }  // namespace
 
-// Returns 0, or -1 (arguments), -2 (CUDA error), -6 (scratch too small).
+// Returns 0, or -1 (arguments), -2 (CUDA error, kept in *err), -6 (scratch
+// too small).
 int apply_dot_f64_noalloc(const double* u, double* out, int n, int sign, double* dot,
-                          cudaStream_t s) {
+                          cudaStream_t s, cudaError_t* err) {
+  *err = cudaSuccess;
   if (!u || !out || !dot || n < 3 || (sign != 1 && sign != -1)) return -1;
   void* scratch = nullptr;
-  if (noalloc_scratch(&scratch) != cudaSuccess) return -2;
+  if ((*err = noalloc_scratch(&scratch)) != cudaSuccess) return -2;
   using Job = ApplyJob<double, true, false>;
   const dim3 g = tile_grid(n);
   const int total = (int)(g.x * g.y);
@@ -2726,11 +2763,12 @@ int apply_dot_f64_noalloc(const double* u, double* out, int n, int sign, double*
                reinterpret_cast<unsigned*>(base + kNoAllocTicketOffset)};
   // the ticket must start at zero; the partial slots are overwritten by
   // every launch before they are read
-  if (cudaMemsetAsync(rb.ticket, 0, sizeof(unsigned), s) != cudaSuccess) return -2;
+  if ((*err = cudaMemsetAsync(rb.ticket, 0, sizeof(unsigned), s)) != cudaSuccess) return -2;
   const Operand uo = raw_operand(u, n, n);
   const Job job{dev_operand<double>(uo), Grid<double>{out, n}, n, (int)g.x, total, sign, rb, dot};
   k_persist<Job><<<grid, kThreads, 2 * Job::kStage + Job::kScratch + 128, s>>>(job);
-  return cudaGetLastError() == cudaSuccess ? 0 : -2;
+  *err = cudaGetLastError();
+  return *err == cudaSuccess ? 0 : -2;
 }
 
 }  // namespace sbp

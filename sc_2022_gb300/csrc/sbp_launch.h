@@ -53,12 +53,14 @@ cudaError_t launch_resrestrict_op(const Operand* v, const Operand& b, Grid<T> f,
 
 // Allocation-free apply + dot with the reduction scratch in a static device
 // array (see sbp_apply_dot_f64_noalloc in sbpmg.h).  Returns 0 or a negative
-// sbp_status value.
+// sbp_status value; on a CUDA error (-2) *err holds the error that caused it.
 int apply_dot_f64_noalloc(const double* u, double* out, int n, int sign, double* dot,
-                          cudaStream_t s);
+                          cudaStream_t s, cudaError_t* err);
 
 // Non-zero once a kernel's bounded wait on an asynchronous copy gave up.
 unsigned int read_device_fault();
+// The same, clearing the flag (the current device's copy).
+unsigned int take_device_fault();
 
 // Upper bound on the CTAs any reducing launch uses for an n x n grid; the
 // partials buffer of a ReduceBuf must hold this many doubles.

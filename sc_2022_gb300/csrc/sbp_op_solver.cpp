@@ -390,6 +390,7 @@ int solve(OpSolver* s, int kind, const double* b, double* x, int sign, double ab
   SBP_CUDA(cudaMemcpyAsync(x, s->x, (size_t)N * sizeof(double), cudaMemcpyDeviceToDevice, q));
   SBP_CUDA(cudaMemcpyAsync(&s->st_host[0], s->st, sizeof(SolveState), cudaMemcpyDeviceToHost, q));
   SBP_CUDA(cudaStreamSynchronize(q));
+  if (const int fr = check_device_fault("solve")) return fr;
   const SolveState fs = s->st_host[0];
   if (norms_out && norms_cap > 0) {
     const int cnt = std::min(norms_cap, fs.iter + 1);
@@ -421,7 +422,7 @@ int vcycle_apply(OpSolver* s, const double* b, double* v, cudaStream_t q) {
     SBP_CUDA(cudaMemcpyAsync(v, z, bytes, cudaMemcpyDeviceToDevice, q));
   }
   SBP_CUDA(cudaStreamSynchronize(q));
-  return SBP_OK;
+  return check_device_fault("vcycle");
 }
 
 // ---- creation ----------------------------------------------------------

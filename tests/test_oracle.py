@@ -189,9 +189,9 @@ def test_coarsen_coefficients_harmonic_full_weighting():
 
 def test_galerkin_coarse_operators_keep_iterations_flat():
     # P' A P coarse operators on the layered field: 8 MGCG iterations at
-    # N = 65 and 129 (the re-discretised hierarchy needs 9 and 10)
+    # N = 65, 129 and 257 (the re-discretised hierarchy needs 9, 10 and 11)
     its = []
-    for n in (65, 129):
+    for n in (65, 129, 257):
         c = o.coefficient_field(n, "layered")
         b = np.random.default_rng(0).standard_normal(n * n)
         hier = o.Hierarchy(n, o.MGOptions(restriction="galerkin", coarse_n=17), coef=c,
