@@ -5,10 +5,16 @@ precision vs FP64, and the operator apply's HBM bandwidth.
 One "step" is one complete MGCG solve of the N = 4097 manufactured problem
 (u = sin(pi x) cos(pi y), SBP-SAT, V-cycle to 65^2, Jacobi 3+3) from x0 = 0
 to ||b - A x|| <= 1e-10 ||b||, with b resident in HBM.  `value` is the
-mixed-precision time per solve (ms, lower is better); the FP64 time, the
-end-to-end time through the C ABI with host buffers, the apply roofline and
-a CPU baseline (the reference's sparse CPU path restated in C, OpenMP, on
-this machine's host cores) are reported beside it.
+mixed-precision time per solve (ms, lower is better).  Beside it the line
+carries the FP64 time, the end-to-end time through the C ABI with host
+buffers, the per-kernel times of the solve and the roofline of its dominant
+kernel, the operator applies against HBM (and the FP64 apply against the
+measured FP64 rate), the solution's distance from the C oracle's solve of
+the same problem, plain FP64 CG at the same size, a CPU baseline (the
+reference's sparse CPU path restated in C, OpenMP, on this machine's host
+cores), and one timing of each further configuration (N = 8193 mixed, the
+256-problem batch, the N = 2049 x 16 adjoint gradient, the p = 4 / 6 and
+variable-coefficient solvers, assembled SpMV against the matrix-free apply).
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 For N > 1 launch under torch.distributed.run: every rank solves its own
@@ -25,17 +31,23 @@ import subprocess
 import sys
 import tempfile
 import time
+import traceback
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "MGCG time to 1e-10 rel. residual at N=4097²: mixed vs FP64; apply GB/s vs HBM"
-# DRAM bytes (read + write) of one sbp_apply_f64 launch at N = 4097, measured
-# with ncu (dram__bytes_read.sum + dram__bytes_write.sum).
-APPLY_F64_TRAFFIC = 222.6e6
 WORKLOAD = ("plain/mixed matrix-free MGCG, N=4097 (16.8M unknowns), u=sin(pi x)cos(pi y), "
             "V-cycle to 65^2, weighted Jacobi 2/3 3+3, SBP-compatible restriction, "
             "bilinear prolongation, FP64 direct coarse solve, tol 1e-10")
+
+# Algorithmic bytes per fine-grid point of the solver kernels that run on the
+# finest level once per iteration (unique arrays read + written once).
+KERNEL_BYTES_PER_POINT = {
+    "CgDirMixedJob": 36,      # z (f32), p_old, Ap_old read; p, Ap written
+    "CgDirJob<double, double": 32,   # z, p_old read; p, Ap written
+    "k_cg_update<": 52,       # x, p, r, Ap read; x, r written; r_lo (f32) written
+}
 
 
 def workload(n: int) -> str:
@@ -55,11 +67,13 @@ def parse_args():
                    help="points per side (use --grid under torch.distributed.run)")
     p.add_argument("--apply-iters", type=int, default=50)
     p.add_argument("--cpu-baseline", type=int, default=1, help="time the CPU baseline leg")
+    p.add_argument("--extras", type=int, default=1,
+                   help="time the further configurations after the headline (1 GPU only)")
     p.add_argument("--dtype", choices=["f64", "f32"], default="f64",
                    help="operand type of --mode apply")
     p.add_argument("--mode", choices=["full", "apply", "solve-fp64", "solve-mixed", "vcycle",
-                                      "high-order", "variable", "adjoint",
-                                      "batch", "spmv"],
+                                      "cg", "n8193", "high-order", "variable", "adjoint",
+                                      "batch", "spmv", "profile"],
                    default="full", help="profiling modes run one part only and print a "
                    "short line (not the benchmark line)")
     return p.parse_args()
@@ -167,6 +181,8 @@ class ClockSampler:
 # CPU baseline: the reference's sparse CPU path restated in C (OpenMP)
 # ---------------------------------------------------------------------------
 def cpu_mgcg_timing(n: int, b_host, steps: int, warmup: int, threads: int | None = None):
+    """Median time of `steps` FP64 MGCG solves (after `warmup`) with the C
+    restatement; also returns the last solution (the oracle's x)."""
     from oracle import cpu_path
     import numpy as np
     threads = threads or os.cpu_count() or 1
@@ -175,7 +191,7 @@ def cpu_mgcg_timing(n: int, b_host, steps: int, warmup: int, threads: int | None
     m = cpu_path.CpuMG(n, smoother="jacobi", restriction="galerkin", coarse_n=65)
     setup = time.perf_counter() - t0
     abstol = 1e-10 * float(np.linalg.norm(b_host))
-    times, iters = [], None
+    times, iters, x = [], None, None
     for k in range(warmup + steps):
         x0 = np.zeros_like(b_host)
         t = time.perf_counter()
@@ -186,14 +202,19 @@ def cpu_mgcg_timing(n: int, b_host, steps: int, warmup: int, threads: int | None
         iters = it
     m.close()
     return {"ms_per_solve": 1e3 * statistics.median(times), "threads": threads, "iters": iters,
-            "setup_s": setup, "solves": len(times)}
+            "setup_s": setup, "solves": len(times), "warmup": warmup, "x": x}
+
+
+def cpu_sample_text(r, n, extra=""):
+    return (f"median of {r['solves']} full FP64 MGCG solves at N={n} ({r['iters']} iterations "
+            f"each) after {r['warmup']} warm-up, with the C restatement of the reference's sparse "
+            f"CPU path (CSR SpMV, same V-cycle), setup excluded{extra}")
 
 
 # ---------------------------------------------------------------------------
 def run_reference(args, d: Dist):
     if d.rank != 0:
         return
-    import numpy as np
     from sc_2022_gb300 import problems
     n = args.n
     # host-side problem (no GPU work on this arm)
@@ -207,16 +228,22 @@ def run_reference(args, d: Dist):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(val, 3), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (manufactured solution)",
-        "config": {"workload": workload(n) + " [CPU: C restatement of the reference's sparse "
-                   "CSR path, same V-cycle]", "n": n, "parallelism": "replicas"},
+        "config": config_block(args, n),
         "cpu_baseline": {"value": round(val, 3), "unit": "ms", "cores": cores, "kind": "port",
-                         "sample": f"{r['solves']} full FP64 MGCG solves at N={n} "
-                                   f"({r['iters']} iterations each), setup excluded"},
+                         "sample": cpu_sample_text(r, n, "; the reference itself is Julia, "
+                                                   "which this machine cannot run")},
         "e2e": {"value": round(val, 3), "unit": "ms", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "detail": {"iters": r["iters"], "setup_s": round(r["setup_s"], 2)},
     }
     print(json.dumps(line), flush=True)
+
+
+def config_block(args, n):
+    return {"workload": workload(n), "n": n, "unknowns": n * n,
+            "parallelism": "replicas" if args.gpus > 1 else "single GPU",
+            "l2": f"inputs {'larger' if 8 * n * n > 129e6 else 'smaller'} than L2 "
+                  f"(b, x, r, p, Ap: {8 * n * n / 1e6:.0f} MB each)"}
 
 
 def _host_rhs(n, f, g):
@@ -236,9 +263,369 @@ def _host_rhs(n, f, g):
     return np.ascontiguousarray((-B).ravel())
 
 
-def run_ours(args, d: Dist):
-    import ctypes as C
+# ---------------------------------------------------------------------------
+# timing helpers
+# ---------------------------------------------------------------------------
+def event_time(fn, steps, warmup=0, stream=None):
+    """ms per call of fn over `steps` calls, CUDA events on the stream."""
+    import torch
+    stream = stream or torch.cuda.current_stream()
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    out = None
+    for _ in range(steps):
+        out = fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps, out
 
+
+def true_rel_residual(lib, x, b, n, sign=1):
+    import ctypes as C
+    import torch
+    out = C.c_double()
+    rc = lib.sbp_residual_norm_f64(C.c_void_p(x.data_ptr()), C.c_void_p(b.data_ptr()), n, sign,
+                                   C.byref(out),
+                                   C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == 0, rc
+    return out.value / b.norm().item()
+
+
+def short_name(k: str) -> str:
+    """Kernel name without the namespace and template noise."""
+    k = k.replace("sbp::", "").replace("void ", "")
+    return k.split("(")[0] if not k.startswith("k_persist") else k.split(">(")[0] + ">"
+
+
+def apply_timing(n, dtype, iters, dev, sign=-1):
+    """ms per launch of sbp_apply_f64 / _f32 over two alternated inputs
+    (4 arrays larger than L2 at N = 4097)."""
+    import ctypes as C
+    import torch
+    import sc_2022_gb300 as sbp
+    lib = sbp.load_library()
+    stream = torch.cuda.current_stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    gen = torch.Generator(device=dev).manual_seed(0)
+    dt = torch.float64 if dtype == "f64" else torch.float32
+    fn = lib.sbp_apply_f64 if dtype == "f64" else lib.sbp_apply_f32
+    us = [torch.randn(n * n, generator=gen, device=dev, dtype=torch.float64).to(dt)
+          for _ in range(2)]
+    outs = [torch.empty_like(us[0]) for _ in range(2)]
+
+    def pair():
+        for k in range(2):
+            rc = fn(C.c_void_p(us[k].data_ptr()), C.c_void_p(outs[k].data_ptr()), n, sign, sp)
+            assert rc == 0, rc
+
+    ms2, _ = event_time(pair, iters, warmup=3, stream=stream)
+    return ms2 / 2.0
+
+
+# ---------------------------------------------------------------------------
+# further configurations (one timing each; also the --mode parts)
+# ---------------------------------------------------------------------------
+def part_cg(n, dev, steps=1):
+    """Plain FP64 matrix-free CG on A x = b (CG_CPU semantics) from zero to
+    1e-10 relative residual, manufactured problem."""
+    import sc_2022_gb300 as sbp
+    import torch
+    from sc_2022_gb300 import problems
+    lib = sbp.load_library()
+    f, g, _ = problems.manufactured(n, "baseline")
+    b = problems.assemble_rhs(f, g, device=dev).reshape(-1)
+    s = sbp.Solver(n)
+    x = torch.zeros_like(b)
+    s.cg(b, x, sign=1, reltol=1e-10, maxiter=20)   # captures the iteration graphs
+
+    def solve():
+        x.zero_()
+        return s.cg(b, x, sign=1, reltol=1e-10, maxiter=200000)
+
+    ms, r = event_time(solve, steps)
+    out = {"n": n, "iters": r.iters, "converged": r.converged, "ms_per_solve": round(ms, 2),
+           "us_per_iteration": round(1e3 * ms / max(r.iters, 1), 2),
+           "true_rel_residual": true_rel_residual(lib, x, b, n), "reltol": 1e-10,
+           "launches_per_solve": s.last_launches}
+    s.close()
+    return out
+
+
+def part_n8193(dev, warmup=1, steps=3):
+    """Config 3: N = 8193 bump/trig problem, mixed and FP64 MGCG to 1e-10."""
+    import sc_2022_gb300 as sbp
+    import torch
+    from sc_2022_gb300 import _lib, problems
+    lib = sbp.load_library()
+    n = 8193
+    f, g = problems.bump_problem(n, seed=3)
+    b = problems.assemble_rhs(f, g, device=dev).reshape(-1)
+    del f
+    out = {"n": n, "problem": "8 Gaussian bumps + 6-mode trig boundary data, seed 3"}
+    xs = {}
+    for tag, prec in (("mixed", _lib.SBP_PREC_MIXED), ("fp64", _lib.SBP_PREC_FP64)):
+        s = sbp.Solver(n, sbp.default_options(prec))
+        x = torch.zeros_like(b)
+
+        def solve():
+            x.zero_()
+            return s.mgcg(b, x, reltol=1e-10)
+
+        ms, r = event_time(solve, steps, warmup=warmup)
+        out[f"{tag}_ms"] = round(ms, 3)
+        out[f"{tag}_iters"] = r.iters
+        out[f"{tag}_true_rel_residual"] = true_rel_residual(lib, x, b, n)
+        xs[tag] = x
+        s.close()
+    out["mixed_speedup_vs_fp64"] = round(out["fp64_ms"] / out["mixed_ms"], 3)
+    out["mixed_vs_fp64_solution_rel_diff"] = ((xs["mixed"] - xs["fp64"]).norm() /
+                                              xs["fp64"].norm()).item()
+    return out
+
+
+def part_batch(dev, warmup=1, steps=2):
+    """Config 4: 256 problems, N log-uniform over {65..1025}, bump/trig data,
+    FP64 MGCG to 1e-10: batched vs one solve at a time."""
+    import sc_2022_gb300 as sbp
+    import torch
+    from sc_2022_gb300 import problems
+    ns, bs = problems.batch_problems(256, seed=4, device=dev)
+    opts = sbp.default_options()
+    B = sbp.BatchSolver(ns, opts)
+    xs = [torch.zeros_like(b) for b in bs]
+    t0 = time.perf_counter()
+    budgets = B.autotune(bs, xs)
+    tune_s = time.perf_counter() - t0
+    solvers = {m: sbp.Solver(m, opts) for m in sorted(set(ns))}
+
+    def batched():
+        for x in xs:
+            x.zero_()
+        return B.mgcg(bs, xs, reltol=1e-10, maxiter=200)
+
+    def sequential():
+        out = []
+        for m, b, x in zip(ns, bs, xs):
+            x.zero_()
+            out.append(solvers[m].mgcg(b, x, reltol=1e-10, maxiter=200))
+        return out
+
+    res = {}
+    for name, fn in (("batched", batched), ("sequential", sequential)):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            r = fn()
+        torch.cuda.synchronize()
+        res[name + "_ms"] = round(1e3 * (time.perf_counter() - t0) / steps, 3)
+        res[name + "_iters"] = sum(x.iters for x in r)
+        res[name + "_all_converged"] = all(x.converged for x in r)
+    res.update({"problems": len(ns), "sizes": {str(m): ns.count(m) for m in sorted(set(ns))},
+                "speedup": round(res["sequential_ms"] / res["batched_ms"], 3),
+                "launches_batched": B.last_launches, "autotune": budgets,
+                "autotune_s": round(tune_s, 2), "timing": "host wall clock around synchronised "
+                "solves (the batch spans several streams)"})
+    B.close()
+    for s in solvers.values():
+        s.close()
+    return res
+
+
+def part_adjoint(n, dev, warmup=1, steps=2):
+    """Config 5: gradient of L = sum_k 1/2 (u_k - t_k)' H~ (u_k - t_k) with
+    respect to the 16 sources and boundary data through torch autograd:
+    forward MGCG solves, the H-misfit, the adjoint MGCG solves and the
+    transposed right-hand-side map, all to 1e-10."""
+    import numpy as np
+    import sc_2022_gb300 as sbp
+    import torch
+    from sc_2022_gb300 import _lib, problems
+    from sc_2022_gb300 import adjoint as adj
+    B = 16
+    fs, gs = [], {side: [] for side in "WESN"}
+    for k in range(B):
+        f, g = problems.bump_problem(n, 5000 + k)
+        fs.append(np.asarray(f).reshape(n, n))
+        for side in "WESN":
+            gs[side].append(np.asarray(g[side]))
+    f0 = torch.tensor(np.stack(fs), dtype=torch.float64, device=dev)
+    g0 = [torch.tensor(np.stack(gs[side]), dtype=torch.float64, device=dev) for side in "WESN"]
+    targets = 1e-3 * torch.randn((B, n, n), dtype=torch.float64, device=dev,
+                                 generator=torch.Generator(device=dev).manual_seed(3))
+    out = {"n": n, "batch": B, "reltol": 1e-10}
+    grads = {}
+    for tag, prec in (("fp64", _lib.SBP_PREC_FP64), ("mixed", _lib.SBP_PREC_MIXED)):
+        s = sbp.Solver(n, sbp.default_options(prec))
+
+        def gradient():
+            f = f0.clone().requires_grad_(True)
+            g = [t.clone().requires_grad_(True) for t in g0]
+            u = adj.PoissonSolve.apply(f, *g, s, 1e-10)
+            loss = adj.HMisfit.apply(u, targets)
+            loss.backward()
+            return loss, f.grad
+
+        for _ in range(warmup):
+            gradient()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            loss, df = gradient()
+        torch.cuda.synchronize()
+        out[f"{tag}_ms_per_gradient"] = round(1e3 * (time.perf_counter() - t0) / steps, 2)
+        out[f"{tag}_loss"] = float(loss.detach())
+        grads[tag] = df.detach().clone()
+        s.close()
+    out["mixed_vs_fp64_df_rel_diff"] = float((grads["mixed"] - grads["fp64"]).norm() /
+                                             grads["fp64"].norm())
+    return out
+
+
+def part_high_order(n, dev, warmup=1, steps=3):
+    """p = 4 and p = 6 operators: the FP64 apply (16 B per point moved) and
+    MGCG to 1e-10 from zero on a seeded random right-hand side."""
+    import sc_2022_gb300 as sbp
+    import torch
+    from sc_2022_gb300 import _lib
+    out = {"n": n}
+    gen = torch.Generator(device=dev).manual_seed(0)
+    us = [torch.randn(n * n, generator=gen, device=dev, dtype=torch.float64) for _ in range(2)]
+    outs = [torch.empty_like(us[0]) for _ in range(2)]
+    hbm, _ = measured_peaks()
+    for p in (4, 6):
+        k = [0]
+
+        def app():
+            sbp.matrix_free_A_high_order_GPU(us[k[0] % 2], outs[k[0] % 2], p=p)
+            k[0] += 1
+
+        ms, _ = event_time(app, 10 * steps, warmup=warmup)
+        out[f"p{p}_apply_us"] = round(1e3 * ms, 2)
+        out[f"p{p}_apply_frac_of_hbm"] = round(16.0 * n * n / (ms * 1e-3) / 1e9 / hbm, 3)
+        for tag, prec in (("fp64", _lib.SBP_PREC_FP64), ("mixed", _lib.SBP_PREC_MIXED)):
+            s = sbp.HighOrderSolver(n, p, sbp.default_options(prec))
+            x = torch.zeros_like(us[0])
+
+            def solve():
+                x.zero_()
+                return s.mgcg(us[0], x, reltol=1e-10, maxiter=200)
+
+            ms, r = event_time(solve, steps, warmup=warmup)
+            out[f"p{p}_mgcg_{tag}_ms"] = round(ms, 3)
+            out[f"p{p}_mgcg_{tag}_iters"] = r.iters
+            out[f"p{p}_mgcg_{tag}_converged"] = r.converged
+            s.close()
+    return out
+
+
+def part_variable(n, dev, warmup=1, steps=3):
+    """div(c grad u) with the seeded layered coefficient (c from 1 to 10
+    across y = 1/2): the FP64 apply from nodal c (u, c read, out written:
+    24 B per point) and MGCG to 1e-10 from zero."""
+    import sc_2022_gb300 as sbp
+    import torch
+    from sc_2022_gb300 import _lib
+    out = {"n": n, "coefficient": "layered 1..10"}
+    x1 = torch.linspace(0.0, 1.0, n, device=dev, dtype=torch.float64)
+    coef = (1.0 + 4.5 * (1.0 + torch.tanh((x1 - 0.5) * (n - 1) / 2.0)))[:, None].expand(
+        n, n).contiguous().reshape(-1)
+    gen = torch.Generator(device=dev).manual_seed(0)
+    us = [torch.randn(n * n, generator=gen, device=dev, dtype=torch.float64) for _ in range(2)]
+    outs = [torch.empty_like(us[0]) for _ in range(2)]
+    hbm, _ = measured_peaks()
+    k = [0]
+
+    def app():
+        sbp.matrix_free_A_variable_GPU(us[k[0] % 2], coef, outs[k[0] % 2])
+        k[0] += 1
+
+    ms, _ = event_time(app, 10 * steps, warmup=warmup)
+    out.update({"apply_us": round(1e3 * ms, 2),
+                "apply_frac_of_hbm": round(24.0 * n * n / (ms * 1e-3) / 1e9 / hbm, 3)})
+    for tag, prec in (("fp64", _lib.SBP_PREC_FP64), ("mixed", _lib.SBP_PREC_MIXED)):
+        s = sbp.VariableCoefficientSolver(n, coef, sbp.default_options(prec))
+        x = torch.zeros_like(us[0])
+
+        def solve():
+            x.zero_()
+            return s.mgcg(us[0], x, reltol=1e-10, maxiter=200)
+
+        ms, r = event_time(solve, steps, warmup=warmup)
+        out[f"mgcg_{tag}_ms"] = round(ms, 3)
+        out[f"mgcg_{tag}_iters"] = r.iters
+        out[f"mgcg_{tag}_converged"] = r.converged
+        out["levels"] = s.levels
+        s.close()
+    return out
+
+
+def part_spmv(n, dev, warmup=3, steps=20):
+    """The reference's matrix-free vs assembled-SpMV comparison at n: FP64
+    y = A x with this project's CSR SpMV and with the matrix-free apply."""
+    import ctypes as C
+    import sc_2022_gb300 as sbp
+    import torch
+    from sc_2022_gb300 import csr
+    lib = sbp.load_library()
+    sp = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    A = csr.CsrOperator(n, device=dev)
+    gen = torch.Generator(device=dev).manual_seed(0)
+    xs = [torch.randn(n * n, generator=gen, device=dev, dtype=torch.float64) for _ in range(2)]
+    ys = [torch.empty_like(xs[0]) for _ in range(2)]
+    out = {"n": n, "nnz": A.nnz}
+    k = [0]
+
+    def run_spmv():
+        A.matvec(xs[k[0] % 2], ys[k[0] % 2])
+        k[0] += 1
+
+    def run_mf():
+        assert lib.sbp_apply_f64(C.c_void_p(xs[k[0] % 2].data_ptr()),
+                                 C.c_void_p(ys[k[0] % 2].data_ptr()), n, 1, sp) == 0
+        k[0] += 1
+
+    for name, fn, nbytes in (("spmv", run_spmv, A.device_bytes + 16 * n * n),
+                             ("matrix_free", run_mf, 16 * n * n)):
+        ms, _ = event_time(fn, steps, warmup=warmup)
+        out[name + "_us"] = round(1e3 * ms, 2)
+        out[name + "_gbs"] = round(nbytes / (ms * 1e-3) / 1e9, 1)
+    out["matrix_free_speedup"] = round(out["spmv_us"] / out["matrix_free_us"], 3)
+    del A
+    return out
+
+
+def part_profile(s, b, x, n):
+    """Per-kernel times of one mixed solve (uncaptured, CUDA events around
+    every launch) and the roofline of the dominant kernel."""
+    res, rows = s.profile(b, x, kind="mgcg", reltol=1e-10)
+    tot = sum(r["total_ms"] for r in rows)
+    kernels = [{"kernel": short_name(r["kernel"]), "launches": r["launches"],
+                "us_per_launch": round(1e3 * r["ms_per_launch"], 2),
+                "share": round(r["total_ms"] / tot, 4)} for r in rows[:10]]
+    top = rows[0]
+    bpp = None
+    for key, v in KERNEL_BYTES_PER_POINT.items():
+        if key in top["kernel"]:
+            bpp = v
+    return res, rows, kernels, top, bpp, tot
+
+
+def fp64_rate(lib):
+    import ctypes as C
+    import torch
+    g = C.c_double()
+    rc = lib.sbp_fp64_fma_rate(C.byref(g), C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    return g.value if rc == 0 else None
+
+
+# ---------------------------------------------------------------------------
+def run_ours(args, d: Dist):
     import numpy as np
     import torch
 
@@ -250,7 +637,6 @@ def run_ours(args, d: Dist):
     n = args.n
     f, g, U = problems.manufactured(n, "baseline")
     b = problems.assemble_rhs(f, g, device=dev).reshape(-1)
-    bnorm = b.norm().item()
     s64 = sbp.Solver(n, sbp.default_options(_lib.SBP_PREC_FP64))
     s32 = sbp.Solver(n, sbp.default_options(_lib.SBP_PREC_MIXED))
     x = torch.zeros_like(b)
@@ -301,350 +687,186 @@ def run_ours(args, d: Dist):
     for _ in range(2):
         e2e()
     ms_e2e, _ = timed(e2e, args.steps)
-    # operator apply roofline (two inputs alternated: 4 x 134 MB > L2)
-    gen = torch.Generator(device=dev).manual_seed(0)
-    us = [torch.randn(n * n, generator=gen, device=dev, dtype=torch.float64) for _ in range(2)]
-    outs = [torch.empty_like(us[0]) for _ in range(2)]
-    sp = C.c_void_p(stream.cuda_stream)
-
-    def apply_pair():
-        for k in range(2):
-            rc = lib.sbp_apply_f64(C.c_void_p(us[k].data_ptr()), C.c_void_p(outs[k].data_ptr()),
-                                   n, -1, sp)
-            assert rc == 0
-
-    for _ in range(3):
-        apply_pair()
-    ms_apply2, _ = timed(apply_pair, args.apply_iters)
-    # the FP32 apply of the mixed V-cycle's operator (4 x 67 MB inputs/outputs)
-    us32 = [u.float() for u in us]
-    outs32 = [torch.empty_like(us32[0]) for _ in range(2)]
-
-    def apply_pair32():
-        for k in range(2):
-            rc = lib.sbp_apply_f32(C.c_void_p(us32[k].data_ptr()),
-                                   C.c_void_p(outs32[k].data_ptr()), n, -1, sp)
-            assert rc == 0
-
-    for _ in range(3):
-        apply_pair32()
-    ms_apply32_2, _ = timed(apply_pair32, args.apply_iters)
+    # operator applies (two inputs alternated: 4 x 134 MB > L2 for FP64)
+    ms_apply = d.max(apply_timing(n, "f64", args.apply_iters, dev))
+    ms_apply32 = d.max(apply_timing(n, "f32", args.apply_iters, dev))
     clocks = sampler.stop()
-    ms_apply = ms_apply2 / 2.0
-    ms_apply32 = d.max(ms_apply32_2 / 2.0)
-
     ms32 = d.max(ms32)
     ms64 = d.max(ms64)
     ms_e2e = d.max(ms_e2e)
-    ms_apply = d.max(ms_apply)
 
-    # accuracy of the timed solves
-    def true_rel(xv):
-        out = C.c_double()
-        rc = lib.sbp_residual_norm_f64(C.c_void_p(xv.data_ptr()), C.c_void_p(b.data_ptr()), n, 1,
-                                       C.byref(out), sp)
-        assert rc == 0
-        return out.value / bnorm
+    # per-kernel times of one mixed solve and the dominant kernel's roofline
+    xp = torch.zeros_like(b)
+    rp, prof_rows, kernels, top, bpp, prof_total = part_profile(s32, b, xp, n)
+    del xp
 
-    rel32, rel64 = true_rel(x32), true_rel(x64)
+    rel32, rel64 = true_rel_residual(lib, x32, b, n), true_rel_residual(lib, x64, b, n)
     err_vs_fp64 = ((x32 - x64).norm() / x64.norm()).item()
 
     peak, peak_kind = measured_peaks()
+    gfma = fp64_rate(lib)
     apply_bytes = 16.0 * n * n
-    achieved = apply_bytes / (ms_apply * 1e-3) / 1e9
+    achieved64 = apply_bytes / (ms_apply * 1e-3) / 1e9
+    achieved32 = 8.0 * n * n / (ms_apply32 * 1e-3) / 1e9
+    top_ms = top["ms_per_launch"]
+    roof = {"kernel": short_name(top["kernel"]), "bound": "hbm", "peak": peak, "unit": "GB/s",
+            "peak_kind": peak_kind, "traffic": None,
+            "ms_per_launch": round(top_ms, 5), "launches_per_solve": top["launches"],
+            "share_of_solve": round(top["total_ms"] / prof_total, 4),
+            "timing": "CUDA events around each launch of one mixed solve launched without "
+                      "graphs (sbp_solver_profile), on the launching stream"}
+    if bpp is not None:
+        achieved = bpp * n * n / (top_ms * 1e-3) / 1e9
+        roof.update({"achieved": round(achieved, 1), "frac": round(achieved / peak, 4),
+                     "algorithmic_bytes_per_launch": bpp * n * n,
+                     "bytes_per_point": bpp})
     line = {
         "metric": METRIC, "value": round(ms32, 4), "unit": "ms", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms32, 4),
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
         "data": "synthetic (manufactured solution u=sin(pi x)cos(pi y), b resident in HBM)",
-        "config": {"workload": workload(n), "n": n, "unknowns": n * n,
-                   "parallelism": "replicas" if args.gpus > 1 else "single GPU",
-                   "l2": f"inputs {'larger' if 8 * n * n > 129e6 else 'smaller'} than L2 "
-                         f"(b, x, r, p, Ap: {8 * n * n / 1e6:.0f} MB each)"},
+        "config": config_block(args, n),
         "fp64_ms_per_solve": round(ms64, 4),
         "mixed_speedup_vs_fp64": round(ms64 / ms32, 3),
         "solves_per_s_all_gpus": round(args.gpus * 1e3 / ms32, 2),
         "e2e": {"value": round(ms_e2e, 4), "unit": "ms", "h2d_bytes_per_step": 8 * n * n,
                 "d2h_bytes_per_step": 8 * n * n, "path": "sbp_mgcg_solve (mixed) with pinned "
                 "host b/x copied in and out every step"},
-        "roofline": {"kernel": "k_apply<double> (operator apply, FP64)", "bound": "hbm",
-                     "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                     "algorithmic_bytes_per_launch": apply_bytes,
-                     # DRAM read + write of one launch at N = 4097 from a single ncu
-                     # capture (profiles/apply_f64_n4097.md); part of the output stays in L2
-                     "traffic": APPLY_F64_TRAFFIC if n == 4097 else None,
-                     "ms_per_launch": round(ms_apply, 5)},
-        "apply_f32": {"kernel": "sbp_apply_f32 (operator apply, FP32)", "achieved_gbs":
-                      round(8.0 * n * n / (ms_apply32 * 1e-3) / 1e9, 1),
-                      "frac": round(8.0 * n * n / (ms_apply32 * 1e-3) / 1e9 / peak, 4),
-                      "algorithmic_bytes_per_launch": 8.0 * n * n,
+        "roofline": roof,
+        "solve_kernels": kernels,
+        "apply_f32": {"kernel": "sbp_apply_f32 (operator apply, FP32, caller layout)",
+                      "achieved_gbs": round(achieved32, 1), "frac": round(achieved32 / peak, 4),
+                      "peak": peak, "algorithmic_bytes_per_launch": 8.0 * n * n,
                       "ms_per_launch": round(ms_apply32, 5)},
+        "apply_f64": {"kernel": "sbp_apply_f64 (operator apply, FP64, caller layout)",
+                      "achieved_gbs": round(achieved64, 1), "frac": round(achieved64 / peak, 4),
+                      "peak": peak, "algorithmic_bytes_per_launch": apply_bytes,
+                      "ms_per_launch": round(ms_apply, 5),
+                      "fp64_pipe": None if not gfma else {
+                          "ops_per_point": 4,
+                          "achieved_gops": round(4.0 * n * n / (ms_apply * 1e-3) / 1e9, 1),
+                          "peak_gops": round(gfma, 1),
+                          "frac": round(4.0 * n * n / (ms_apply * 1e-3) / 1e9 / gfma, 4),
+                          "peak_kind": "measured (sbp_fp64_fma_rate, this run)",
+                          "note": "4 = the stencil's minimum FP64 operations per point (3 adds, "
+                                  "1 FMA); half the warps form the sum exactly on the integer "
+                                  "pipe instead, so the FP64-equivalent rate can exceed the "
+                                  "FP64 pipe's own"}},
         "clocks": clocks,
         "gpu_launches": int(launches32 * args.steps),
         "detail": {"iters_mixed": r32.iters, "iters_fp64": r64.iters,
                    "true_rel_residual_mixed": rel32, "true_rel_residual_fp64": rel64,
                    "mixed_vs_fp64_solution_rel_diff": err_vs_fp64,
                    "launches_per_solve": launches32,
+                   "profiled_solve_iters": rp.iters,
+                   "profiled_solve_kernel_ms": round(prof_total, 3),
                    "device_bytes": s32.device_bytes + s64.device_bytes},
     }
-    if d.rank == 0 and args.cpu_baseline:
-        bh = b.detach().cpu().numpy()
-        r = cpu_mgcg_timing(n, bh, steps=1, warmup=0)
-        r1 = cpu_mgcg_timing(n, bh, steps=1, warmup=0, threads=1)
-        line["cpu_baseline"] = {
-            "value": round(r["ms_per_solve"], 2), "unit": "ms", "cores": r["threads"],
-            "kind": "port", "sample": f"1 full FP64 MGCG solve at N={n} ({r['iters']} iterations) "
-                                      "with the C restatement of the reference's sparse CPU path "
-                                      "(CSR SpMV, same V-cycle), setup excluded",
-            "value_1_core": round(r1["ms_per_solve"], 2)}
-    if d.rank == 0:
-        print(json.dumps(line), flush=True)
     s32.close()
     s64.close()
+    if d.rank == 0 and args.cpu_baseline:
+        bh = b.detach().cpu().numpy()
+        r = cpu_mgcg_timing(n, bh, steps=3, warmup=1)
+        xo = r.pop("x")
+        # the oracle pin: the GPU solutions against the C oracle's FP64 solve
+        line["detail"]["oracle_iters"] = r["iters"]
+        on = float(np.linalg.norm(xo))
+        line["detail"]["fp64_vs_oracle_rel"] = float(
+            np.linalg.norm(x64.cpu().numpy() - xo) / on)
+        line["detail"]["mixed_vs_oracle_rel"] = float(
+            np.linalg.norm(x32.cpu().numpy() - xo) / on)
+        r1 = cpu_mgcg_timing(n, bh, steps=1, warmup=0, threads=1)
+        r1.pop("x")
+        line["cpu_baseline"] = {
+            "value": round(r["ms_per_solve"], 2), "unit": "ms", "cores": r["threads"],
+            "kind": "port", "sample": cpu_sample_text(r, n),
+            "value_1_core": round(r1["ms_per_solve"], 2)}
+    if d.rank == 0 and args.extras and d.world == 1:
+        extras = {}
+        for name, fn in (("cg_fp64", lambda: part_cg(n, dev)),
+                         ("n8193", lambda: part_n8193(dev)),
+                         ("batch256", lambda: part_batch(dev)),
+                         ("adjoint_2049x16", lambda: part_adjoint(2049, dev)),
+                         ("high_order", lambda: part_high_order(n, dev)),
+                         ("variable", lambda: part_variable(n, dev)),
+                         ("spmv", lambda: part_spmv(n, dev))):
+            t0 = time.perf_counter()
+            try:
+                extras[name] = fn()
+            except Exception as exc:   # one failing extra must not lose the line
+                extras[name] = {"error": f"{type(exc).__name__}: {exc}"[:300]}
+                traceback.print_exc(file=sys.stderr)
+            extras[name]["wall_s"] = round(time.perf_counter() - t0, 1)
+            torch.cuda.empty_cache()
+        line["cg_fp64"] = extras.pop("cg_fp64")
+        line["configs"] = extras
+    if d.rank == 0:
+        print(json.dumps(line), flush=True)
 
 
 def run_part(args):
     """Profiling helper: one part of the benchmark on a single GPU."""
-    import ctypes as C
-
     import torch
 
     import sc_2022_gb300 as sbp
     from sc_2022_gb300 import _lib, problems
     n = args.n
     dev = torch.device("cuda", 0)
-    stream = torch.cuda.current_stream()
-    sp = C.c_void_p(stream.cuda_stream)
     lib = sbp.load_library()
     if args.mode == "apply":
+        import ctypes as C
+        sp = C.c_void_p(torch.cuda.current_stream().cuda_stream)
         gen = torch.Generator(device=dev).manual_seed(0)
         dt = torch.float64 if args.dtype == "f64" else torch.float32
         fn = lib.sbp_apply_f64 if args.dtype == "f64" else lib.sbp_apply_f32
-        us = [torch.randn(n * n, generator=gen, device=dev, dtype=dt) for _ in range(2)]
+        us = [torch.randn(n * n, generator=gen, device=dev, dtype=torch.float64).to(dt)
+              for _ in range(2)]
         outs = [torch.empty_like(us[0]) for _ in range(2)]
         for k in range(args.warmup + args.steps):
             rc = fn(C.c_void_p(us[k % 2].data_ptr()), C.c_void_p(outs[k % 2].data_ptr()), n, -1, sp)
             assert rc == 0
         torch.cuda.synchronize()
         print(json.dumps({"mode": "apply", "dtype": args.dtype, "n": n,
-                          "launches": args.warmup + args.steps}))
+                          "launches": args.warmup + args.steps,
+                          "us_per_launch_timed": round(
+                              1e3 * apply_timing(n, args.dtype, max(args.steps, 1), dev), 2)}))
+        return
+    if args.mode == "cg":
+        print(json.dumps({"mode": "cg", **part_cg(n, dev, steps=max(args.steps, 1))}))
+        return
+    if args.mode == "n8193":
+        print(json.dumps({"mode": "n8193", **part_n8193(dev, args.warmup, max(args.steps, 1))}))
         return
     if args.mode == "spmv":
-        # the reference's matrix-free vs assembled-SpMV comparison at --n:
-        # FP64 y = A x with this project's CSR SpMV and with the matrix-free apply
-        from sc_2022_gb300 import csr
-        A = csr.CsrOperator(n, device=dev)
-        gen = torch.Generator(device=dev).manual_seed(0)
-        xs = [torch.randn(n * n, generator=gen, device=dev, dtype=torch.float64) for _ in range(2)]
-        ys = [torch.empty_like(xs[0]) for _ in range(2)]
-        out = {"mode": "spmv", "n": n, "nnz": A.nnz}
-
-        def run_spmv(k):
-            A.matvec(xs[k % 2], ys[k % 2])
-
-        def run_mf(k):
-            assert lib.sbp_apply_f64(C.c_void_p(xs[k % 2].data_ptr()),
-                                     C.c_void_p(ys[k % 2].data_ptr()), n, 1, sp) == 0
-
-        for name, fn, nbytes in (("spmv", run_spmv, A.device_bytes + 16 * n * n),
-                                 ("matrix_free", run_mf, 16 * n * n)):
-            for k in range(args.warmup):
-                fn(k)
-            torch.cuda.synchronize()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record()
-            for k in range(args.steps):
-                fn(k)
-            e1.record()
-            torch.cuda.synchronize()
-            ms = e0.elapsed_time(e1) / args.steps
-            out[name + "_us"] = round(1e3 * ms, 2)
-            out[name + "_gbs"] = round(nbytes / (ms * 1e-3) / 1e9, 1)
-        out["matrix_free_speedup"] = round(out["spmv_us"] / out["matrix_free_us"], 3)
-        print(json.dumps(out))
+        print(json.dumps({"mode": "spmv", **part_spmv(n, dev, args.warmup, max(args.steps, 1))}))
         return
     if args.mode == "batch":
-        # 256 problems, N log-uniform over {65..1025}, bump/trig data, FP64
-        # MGCG to 1e-10: batched vs one solve at a time
-        import time
-        ns, bs = problems.batch_problems(256, seed=4, device=dev)
-        opts = sbp.default_options()
-        B = sbp.BatchSolver(ns, opts)
-        xs = [torch.zeros_like(b) for b in bs]
-        budgets = B.autotune(bs, xs)
-        solvers = {m: sbp.Solver(m, opts) for m in sorted(set(ns))}
-
-        def batched():
-            for x in xs:
-                x.zero_()
-            return B.mgcg(bs, xs, reltol=1e-10, maxiter=200)
-
-        def sequential():
-            out = []
-            for m, b, x in zip(ns, bs, xs):
-                x.zero_()
-                out.append(solvers[m].mgcg(b, x, reltol=1e-10, maxiter=200))
-            return out
-
-        res = {}
-        for name, fn in (("batched", batched), ("sequential", sequential)):
-            for _ in range(args.warmup):
-                fn()
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            for _ in range(args.steps):
-                r = fn()
-            torch.cuda.synchronize()
-            res[name + "_ms"] = round(1e3 * (time.perf_counter() - t0) / args.steps, 3)
-            res[name + "_iters"] = sum(x.iters for x in r)
-        res.update({"mode": "batch", "problems": len(ns),
-                    "sizes": {str(m): ns.count(m) for m in sorted(set(ns))},
-                    "speedup": round(res["sequential_ms"] / res["batched_ms"], 3),
-                    "launches_batched": B.last_launches, "cta_budgets": budgets})
-        print(json.dumps(res))
+        print(json.dumps({"mode": "batch", **part_batch(dev, args.warmup, max(args.steps, 1))}))
         return
     if args.mode == "high-order":
-        # p = 4 and p = 6 operators at --n: the FP64 apply (16 B per point
-        # moved) and MGCG to 1e-10 from zero on a seeded random right-hand side
-        out = {"mode": "high-order", "n": n}
-        gen = torch.Generator(device=dev).manual_seed(0)
-        us = [torch.randn(n * n, generator=gen, device=dev, dtype=torch.float64) for _ in range(2)]
-        outs = [torch.empty_like(us[0]) for _ in range(2)]
-        hbm, hbm_src = measured_peaks()
-        out["hbm_peak_gbs"] = hbm
-        out["hbm_peak_source"] = hbm_src
-        for p in (4, 6):
-            for k in range(args.warmup):
-                sbp.matrix_free_A_high_order_GPU(us[k % 2], outs[k % 2], p=p)
-            torch.cuda.synchronize()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record()
-            for k in range(args.steps):
-                sbp.matrix_free_A_high_order_GPU(us[k % 2], outs[k % 2], p=p)
-            e1.record()
-            torch.cuda.synchronize()
-            ms = e0.elapsed_time(e1) / args.steps
-            gbs = 16.0 * n * n / (ms * 1e-3) / 1e9
-            out[f"p{p}_apply_us"] = round(1e3 * ms, 2)
-            out[f"p{p}_apply_gbs"] = round(gbs, 1)
-            out[f"p{p}_apply_frac_of_hbm"] = round(gbs / hbm, 3)
-            for tag, prec in (("fp64", _lib.SBP_PREC_FP64), ("mixed", _lib.SBP_PREC_MIXED)):
-                s = sbp.HighOrderSolver(n, p, sbp.default_options(prec))
-                x = torch.zeros_like(us[0])
-                for _ in range(args.warmup):
-                    x.zero_()
-                    s.mgcg(us[0], x, reltol=1e-10, maxiter=200)
-                torch.cuda.synchronize()
-                e0.record()
-                for _ in range(args.steps):
-                    x.zero_()
-                    r = s.mgcg(us[0], x, reltol=1e-10, maxiter=200)
-                e1.record()
-                torch.cuda.synchronize()
-                out[f"p{p}_mgcg_{tag}_ms"] = round(e0.elapsed_time(e1) / args.steps, 3)
-                out[f"p{p}_mgcg_{tag}_iters"] = r.iters
-                out[f"p{p}_mgcg_{tag}_converged"] = r.converged
-                s.close()
-        print(json.dumps(out))
+        print(json.dumps({"mode": "high-order",
+                          **part_high_order(n, dev, args.warmup, max(args.steps, 1))}))
         return
     if args.mode == "variable":
-        # div(c grad u) at --n with the seeded layered coefficient (c from 1
-        # to 10 across y = 1/2): the FP64 apply from nodal c (u, c read, out
-        # written: 24 B per point) and MGCG to 1e-10 from zero
-        out = {"mode": "variable", "n": n, "coefficient": "layered 1..10"}
-        x1 = torch.linspace(0.0, 1.0, n, device=dev, dtype=torch.float64)
-        coef = (1.0 + 4.5 * (1.0 + torch.tanh((x1 - 0.5) * (n - 1) / 2.0)))[:, None].expand(
-            n, n).contiguous().reshape(-1)
-        gen = torch.Generator(device=dev).manual_seed(0)
-        us = [torch.randn(n * n, generator=gen, device=dev, dtype=torch.float64) for _ in range(2)]
-        outs = [torch.empty_like(us[0]) for _ in range(2)]
-        hbm, hbm_src = measured_peaks()
-        for k in range(args.warmup):
-            sbp.matrix_free_A_variable_GPU(us[k % 2], coef, outs[k % 2])
-        torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for k in range(args.steps):
-            sbp.matrix_free_A_variable_GPU(us[k % 2], coef, outs[k % 2])
-        e1.record()
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / args.steps
-        gbs = 24.0 * n * n / (ms * 1e-3) / 1e9
-        out.update({"apply_us": round(1e3 * ms, 2), "apply_gbs": round(gbs, 1),
-                    "apply_frac_of_hbm": round(gbs / hbm, 3), "hbm_peak_source": hbm_src})
-        for tag, prec in (("fp64", _lib.SBP_PREC_FP64), ("mixed", _lib.SBP_PREC_MIXED)):
-            s = sbp.VariableCoefficientSolver(n, coef, sbp.default_options(prec))
-            x = torch.zeros_like(us[0])
-            for _ in range(args.warmup):
-                x.zero_()
-                s.mgcg(us[0], x, reltol=1e-10, maxiter=200)
-            torch.cuda.synchronize()
-            e0.record()
-            for _ in range(args.steps):
-                x.zero_()
-                r = s.mgcg(us[0], x, reltol=1e-10, maxiter=200)
-            e1.record()
-            torch.cuda.synchronize()
-            out[f"mgcg_{tag}_ms"] = round(e0.elapsed_time(e1) / args.steps, 3)
-            out[f"mgcg_{tag}_iters"] = r.iters
-            out[f"mgcg_{tag}_converged"] = r.converged
-            out["levels"] = s.levels
-            s.close()
-        print(json.dumps(out))
+        print(json.dumps({"mode": "variable",
+                          **part_variable(n, dev, args.warmup, max(args.steps, 1))}))
         return
     if args.mode == "adjoint":
-        # the gradient of L = sum_k 1/2 (u_k - t_k)' H~ (u_k - t_k) with respect
-        # to the sources f_k and the boundary data g_k, for a batch of 16 bump
-        # problems at --grid, through torch autograd: forward MGCG solves, the
-        # H-misfit, then the adjoint MGCG solves and the transposed right-hand
-        # side map, all to 1e-10
-        import time
-
-        import numpy as np
-
-        from sc_2022_gb300 import adjoint as adj
-        B = 16
-        fs, gs = [], {side: [] for side in "WESN"}
-        for k in range(B):
-            f, g = problems.bump_problem(n, 5000 + k)
-            fs.append(np.asarray(f).reshape(n, n))
-            for side in "WESN":
-                gs[side].append(np.asarray(g[side]))
-        f0 = torch.tensor(np.stack(fs), dtype=torch.float64, device=dev)
-        g0 = [torch.tensor(np.stack(gs[side]), dtype=torch.float64, device=dev)
-              for side in "WESN"]
-        targets = 1e-3 * torch.randn((B, n, n), dtype=torch.float64, device=dev,
-                                     generator=torch.Generator(device=dev).manual_seed(3))
-        out = {"mode": "adjoint", "n": n, "batch": B, "reltol": 1e-10}
-        grads = {}
-        for tag, prec in (("fp64", _lib.SBP_PREC_FP64), ("mixed", _lib.SBP_PREC_MIXED)):
+        print(json.dumps({"mode": "adjoint",
+                          **part_adjoint(n, dev, args.warmup, max(args.steps, 1))}))
+        return
+    if args.mode == "profile":
+        f, g, _ = problems.manufactured(n, "baseline")
+        b = problems.assemble_rhs(f, g, device=dev).reshape(-1)
+        out = {"mode": "profile", "n": n}
+        for tag, prec in (("mixed", _lib.SBP_PREC_MIXED), ("fp64", _lib.SBP_PREC_FP64)):
             s = sbp.Solver(n, sbp.default_options(prec))
-
-            def gradient():
-                f = f0.clone().requires_grad_(True)
-                g = [t.clone().requires_grad_(True) for t in g0]
-                u = adj.PoissonSolve.apply(f, *g, s, 1e-10)
-                loss = adj.HMisfit.apply(u, targets)
-                loss.backward()
-                return loss, f.grad
-
-            for _ in range(args.warmup):
-                gradient()
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            for _ in range(args.steps):
-                loss, df = gradient()
-            torch.cuda.synchronize()
-            out[f"{tag}_ms_per_gradient"] = round(1e3 * (time.perf_counter() - t0) / args.steps, 2)
-            out[f"{tag}_loss"] = float(loss.detach())
-            grads[tag] = df.detach().clone()
+            x = torch.zeros_like(b)
+            s.mgcg(b, x, reltol=1e-10)
+            x.zero_()
+            res, rows, kernels, top, bpp, tot = part_profile(s, b, x, n)
+            out[tag] = {"iters": res.iters, "kernel_ms": round(tot, 3), "kernels": kernels}
             s.close()
-        out["mixed_vs_fp64_df_rel_diff"] = float((grads["mixed"] - grads["fp64"]).norm() /
-                                                 grads["fp64"].norm())
         print(json.dumps(out))
         return
     if args.mode == "vcycle":
@@ -655,17 +877,8 @@ def run_part(args):
         v = torch.empty_like(b)
         for name, prec in (("mixed", _lib.SBP_PREC_MIXED), ("fp64", _lib.SBP_PREC_FP64)):
             s = sbp.Solver(n, sbp.default_options(prec))
-            for _ in range(args.warmup):
-                s.vcycle(b, v)
-            torch.cuda.synchronize()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record()
-            for _ in range(args.steps):
-                s.vcycle(b, v)
-            e1.record()
-            torch.cuda.synchronize()
-            out[name + "_us"] = round(1e3 * e0.elapsed_time(e1) / args.steps, 2)
+            ms, _ = event_time(lambda: s.vcycle(b, v), max(args.steps, 1), warmup=args.warmup)
+            out[name + "_us"] = round(1e3 * ms, 2)
             out["levels"] = s.levels
             s.close()
         print(json.dumps(out))

@@ -358,6 +358,34 @@ int sbp_cg_solve(sbp_solver* s, const double* b, double* x, int sign, double abs
  * nu) (matrix_free_mg_cg.jl:143-176) for the two-level options. */
 int sbp_vcycle_apply(sbp_solver* s, const double* b, double* v, void* stream);
 
+/* Measured FP64 FMA rate of the current GPU in 1e9 lane-operations per
+ * second (blocking): eight independent FMA chains per thread over one full
+ * wave of CTAs, best of three CUDA-event timings.  The denominator of the
+ * FP64-pipe roofline of the FP64 kernels.  Diagnostics; no reference
+ * counterpart. */
+int sbp_fp64_fma_rate(double* gfma_per_s, void* stream);
+
+/* Per-kernel time of one solve (diagnostics). */
+typedef struct sbp_kernel_time {
+  char name[160];  /* demangled kernel name, truncated */
+  int launches;    /* launches during the solve */
+  double total_ms; /* sum of the launches' CUDA-event durations */
+} sbp_kernel_time;
+
+/* One solve as sbp_mgcg_solve (kind 0, sign ignored) or sbp_cg_solve
+ * (kind 1) from the caller's x, stopping at reltol, but launched directly
+ * instead of through CUDA graphs, with a pair of CUDA events on `stream`
+ * around every kernel launch.  Per-kernel launch counts and summed
+ * durations, aggregated by kernel and sorted by time, go to out (cap
+ * entries); *count receives the number of distinct kernels.  The events
+ * serialise the launches, so the sum exceeds a graph solve's time by the
+ * launch gaps; each duration is the kernel's own.  The reference measures
+ * this path with nsys and @elapsed around whole calls
+ * (matrix_free_mg_cg.jl:577-597); it has no per-kernel timer of its own. */
+int sbp_solver_profile(sbp_solver* s, int kind, const double* b, double* x, int sign,
+                       double reltol, int maxiter, sbp_result* res, sbp_kernel_time* out,
+                       int cap, int* count, void* stream);
+
 /* Adjoint MGCG: lam = A^-T gu = A^-1 gu (A is SPD) with the handle's MGCG
  * from lam = 0 (tolerances as sbp_mgcg_solve), then the transpose of
  * sbp_rhs_f64's map applied to lam.  For u = A^-1 sbp_rhs_f64(f, g, fsign)

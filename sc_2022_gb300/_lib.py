@@ -52,6 +52,14 @@ class sbp_result(C.Structure):
     ]
 
 
+class sbp_kernel_time(C.Structure):
+    _fields_ = [
+        ("name", C.c_char * 160),
+        ("launches", C.c_int),
+        ("total_ms", C.c_double),
+    ]
+
+
 _vp = C.c_void_p
 _i = C.c_int
 _d = C.c_double
@@ -83,6 +91,9 @@ SIGNATURES = {
     "sbp_mgcg_solve": (_i, [_vp, _vp, _vp, _d, _d, _i, C.POINTER(sbp_result), _dp, _i, _vp]),
     "sbp_cg_solve": (_i, [_vp, _vp, _vp, _i, _d, _d, _i, C.POINTER(sbp_result), _dp, _i, _vp]),
     "sbp_vcycle_apply": (_i, [_vp, _vp, _vp, _vp]),
+    "sbp_fp64_fma_rate": (_i, [_dp, _vp]),
+    "sbp_solver_profile": (_i, [_vp, _i, _vp, _vp, _i, _d, _i, C.POINTER(sbp_result),
+                                C.POINTER(sbp_kernel_time), _i, C.POINTER(_i), _vp]),
     "sbp_h_misfit_f64": (_i, [_vp, _vp, _vp, _i, _vp, _vp]),
     "sbp_mgcg_adjoint_f64": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _d, _d, _d, _i,
                                   C.POINTER(sbp_result), _vp]),

@@ -1,10 +1,12 @@
 // C ABI of libsbpmg: solver handles (multigrid hierarchy, workspace, CUDA
 // graphs of one Krylov iteration) and the single-grid entry points.
 #include <cuda_runtime.h>
+#include <cxxabi.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -813,6 +815,79 @@ int sbp_mgcg_adjoint_f64(sbp_solver* s, const double* gu, double* lam, double* d
     SBP_CUDA(launch_rhs_adjoint(cgrid<double>(lam, n), grid<double>(df, n), dgW, dgE, dgS, dgN,
                                 n, fsign, q));
   return rc;
+}
+
+int sbp_fp64_fma_rate(double* gfma_per_s, void* stream) {
+  if (!gfma_per_s) return SBP_ERR_ARGS;
+  SBP_CUDA(measure_fp64_fma_rate(gfma_per_s, (cudaStream_t)stream));
+  return SBP_OK;
+}
+
+int sbp_solver_profile(sbp_solver* s, int kind, const double* b, double* x, int sign,
+                       double reltol, int maxiter, sbp_result* res, sbp_kernel_time* out,
+                       int cap, int* count, void* stream) {
+  if ((kind != 0 && kind != 1) || (kind == 1 && sign != 1 && sign != -1) || !count ||
+      (cap > 0 && !out) || reltol <= 0.0)
+    return SBP_ERR_ARGS;
+  if (kind == 0) sign = +1;
+  int rc = krylov_prepare(s, kind, b, x, 0.0, reltol, maxiter);
+  if (rc) return rc;
+  cudaStream_t q = (cudaStream_t)stream;
+  const int n = s->n, ld = s->ld;
+  LaunchTimer timer;
+  timer_slot() = &timer;
+  cudaError_t e = enqueue_setup(s, kind, b, x, sign, 0.0, reltol, maxiter, q);
+  for (int k = 0; e == cudaSuccess && k < maxiter; ++k) {
+    e = enqueue_iteration(s, kind, k & 1, sign, q);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(&s->st_host[0], s->st, sizeof(SolveState), cudaMemcpyDeviceToHost, q);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(q);
+    if (e == cudaSuccess && s->st_host[0].done) break;
+  }
+  timer_slot() = nullptr;
+  if (e == cudaSuccess) e = copy_grid(x, n, s->x, ld, n, q);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&s->st_host[0], s->st, sizeof(SolveState), cudaMemcpyDeviceToHost, q);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(q);
+  // aggregate by kernel (first-launch order), then sort by total time
+  struct Agg {
+    const void* fn;
+    int launches;
+    double ms;
+  };
+  std::vector<Agg> agg;
+  for (const LaunchTimer::Rec& r : timer.recs) {
+    float ms = 0.f;
+    if (e == cudaSuccess && r.e1) e = cudaEventElapsedTime(&ms, r.e0, r.e1);
+    size_t k = 0;
+    while (k < agg.size() && agg[k].fn != r.fn) ++k;
+    if (k == agg.size()) agg.push_back({r.fn, 0, 0.0});
+    agg[k].launches += 1;
+    agg[k].ms += ms;
+  }
+  for (const LaunchTimer::Rec& r : timer.recs) {
+    if (r.e0) cudaEventDestroy(r.e0);
+    if (r.e1) cudaEventDestroy(r.e1);
+  }
+  if (e != cudaSuccess) return fail_cuda(e, "sbp_solver_profile");
+  if (timer.failed) return fail_cuda(cudaErrorMemoryAllocation, "sbp_solver_profile (events)");
+  if (const int fr = check_device_fault("sbp_solver_profile")) return fr;
+  std::stable_sort(agg.begin(), agg.end(), [](const Agg& a, const Agg& b) { return a.ms > b.ms; });
+  *count = (int)agg.size();
+  for (int k = 0; k < cap && k < (int)agg.size(); ++k) {
+    const char* mangled = nullptr;
+    std::string name = "?";
+    if (cudaFuncGetName(&mangled, agg[k].fn) == cudaSuccess && mangled) {
+      int st = 0;
+      char* dm = abi::__cxa_demangle(mangled, nullptr, nullptr, &st);
+      name = (st == 0 && dm) ? dm : mangled;
+      std::free(dm);
+    }
+    std::snprintf(out[k].name, sizeof(out[k].name), "%s", name.c_str());
+    out[k].launches = agg[k].launches;
+    out[k].total_ms = agg[k].ms;
+  }
+  return finish_result(s->st_host[0], res);
 }
 
 int sbp_vcycle_apply(sbp_solver* s, const double* b, double* v, void* stream) {

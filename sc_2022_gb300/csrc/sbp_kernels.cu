@@ -476,6 +476,26 @@ Recorder*& recorder_slot() {
   return r;
 }
 
+LaunchTimer*& timer_slot() {
+  static thread_local LaunchTimer* t = nullptr;
+  return t;
+}
+
+void timer_mark(LaunchTimer* t, const void* fn, cudaStream_t s, bool after) {
+  if (!after) {
+    LaunchTimer::Rec r;
+    r.fn = fn;
+    if (cudaEventCreate(&r.e0) != cudaSuccess || cudaEventCreate(&r.e1) != cudaSuccess) {
+      t->failed = true;
+      return;
+    }
+    cudaEventRecord(r.e0, s);
+    t->recs.push_back(r);
+  } else if (!t->recs.empty() && t->recs.back().fn == fn) {
+    cudaEventRecord(t->recs.back().e1, s);
+  }
+}
+
 template <class Args>
 static cudaError_t record_launch(BatchLaunchFn fn, const Args& a, int aux0, int aux1 = 0,
                                  int aux2 = 0, int aux3 = 0) {
@@ -2769,6 +2789,56 @@ int apply_dot_f64_noalloc(const double* u, double* out, int n, int sign, double*
   k_persist<Job><<<grid, kThreads, 2 * Job::kStage + Job::kScratch + 128, s>>>(job);
   *err = cudaGetLastError();
   return *err == cudaSuccess ? 0 : -2;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 FMA issue rate of this GPU (roofline denominator of the FP64-bound
+// kernels): eight independent FMA chains per thread, one full wave of CTAs.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads) k_fp64_fma_rate(double* sink, int iters, double m) {
+  double a[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) a[c] = 1.0 + 1e-3 * (double)(threadIdx.x + 37 * c);
+  const double add = 1e-9;
+  for (int k = 0; k < iters; ++k) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) a[c] = fma(a[c], m, add);
+  }
+  double t = 0.0;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) t += a[c];
+  if (t == -1.0) sink[blockIdx.x] = t;  // never true: keeps the chains live
+}
+
+cudaError_t measure_fp64_fma_rate(double* gfma_per_s, cudaStream_t s) {
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fp64_fma_rate, kThreads, 0);
+  if (e != cudaSuccess) return e;
+  const int grid = sm_count() * std::max(1, per_sm);
+  const int iters = 2048;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if ((e = cudaEventCreate(&e0)) != cudaSuccess) return e;
+  if ((e = cudaEventCreate(&e1)) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return e;
+  }
+  float best = 0.f;
+  for (int rep = 0; rep < 4 && e == cudaSuccess; ++rep) {
+    cudaEventRecord(e0, s);
+    k_fp64_fma_rate<<<grid, kThreads, 0, s>>>(nullptr, iters, 0.9999999);
+    cudaEventRecord(e1, s);
+    e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e == cudaSuccess && rep > 0 && (best == 0.f || ms < best)) best = ms;
+  }
+  if (e == cudaSuccess) e = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (e != cudaSuccess) return e;
+  const double fmas = (double)grid * kThreads * 8.0 * iters;
+  *gfma_per_s = fmas / (best * 1e-3) / 1e9;
+  return cudaSuccess;
 }
 
 }  // namespace sbp

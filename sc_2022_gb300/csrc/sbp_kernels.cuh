@@ -169,10 +169,25 @@ __device__ __forceinline__ void pdl_begin() {
   asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
 }
 
+// Per-launch timing for diagnostics (sbp_solver_profile): while a LaunchTimer
+// is installed on the calling host thread, launch_pdl brackets every launch
+// with a pair of CUDA events on the launching stream.
+struct LaunchTimer;
+LaunchTimer*& timer_slot();
+void timer_mark(LaunchTimer* t, const void* fn, cudaStream_t s, bool after);
+
 // Launch with programmatic dependent launch enabled (see pdl_begin()).
 template <typename... KArgs, typename... Args>
 static cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
                               cudaStream_t s, Args&&... args) {
+  if (LaunchTimer* t = timer_slot()) {
+    timer_mark(t, reinterpret_cast<const void*>(kernel), s, false);
+    timer_slot() = nullptr;
+    const cudaError_t e = launch_pdl(kernel, grid, block, smem, s, std::forward<Args>(args)...);
+    timer_slot() = t;
+    timer_mark(t, reinterpret_cast<const void*>(kernel), s, true);
+    return e;
+  }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = grid;
   cfg.blockDim = block;

@@ -57,6 +57,10 @@ cudaError_t launch_resrestrict_op(const Operand* v, const Operand& b, Grid<T> f,
 int apply_dot_f64_noalloc(const double* u, double* out, int n, int sign, double* dot,
                           cudaStream_t s, cudaError_t* err);
 
+// FP64 FMA lane-operations per second of the current GPU (in units of 1e9),
+// timed with CUDA events on s (blocking).
+cudaError_t measure_fp64_fma_rate(double* gfma_per_s, cudaStream_t s);
+
 // Non-zero once a kernel's bounded wait on an asynchronous copy gave up.
 unsigned int read_device_fault();
 // The same, clearing the flag (the current device's copy).
@@ -197,6 +201,18 @@ struct Recorder {
 };
 // The calling thread's recorder (nullptr: launch normally).
 Recorder*& recorder_slot();
+
+// Per-launch CUDA-event timing (sbp_solver_profile): installed through
+// timer_slot() (sbp_kernels.cuh), filled by launch_pdl.
+struct LaunchTimer {
+  struct Rec {
+    const void* fn = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+  };
+  std::vector<Rec> recs;
+  bool failed = false;
+};
+LaunchTimer*& timer_slot();
 // Most problems one batched launch can carry (per-CTA partials live in
 // shared memory).
 constexpr int kMaxBatchSlots = 512;

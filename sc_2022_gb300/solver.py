@@ -229,6 +229,30 @@ class Solver:
             L.check(st, "sbp_mgcg_adjoint_f64")
         return SolveResult(res.iters, st, [], res.initial_norm, res.final_norm, res.threshold)
 
+    def profile(self, b: torch.Tensor, x: torch.Tensor, kind: str = "mgcg", sign: int = 1,
+                reltol: float = 1e-10, maxiter: int | None = None, stream=None):
+        """One solve (``kind`` "mgcg" or "cg") launched without CUDA graphs,
+        with CUDA events around every kernel launch.  Returns (SolveResult,
+        [{"kernel", "launches", "total_ms", "ms_per_launch"}, ...]) sorted by
+        total time; x is overwritten with the solution."""
+        n = self._check_pair(b, x)
+        maxiter = n * n if maxiter is None else maxiter
+        cap = 64
+        out = (L.sbp_kernel_time * cap)()
+        cnt = C.c_int(0)
+        res = L.sbp_result()
+        st = self._lib.sbp_solver_profile(self._h, 0 if kind == "mgcg" else 1, ptr(b), ptr(x),
+                                          sign, reltol, maxiter, C.byref(res), out, cap,
+                                          C.byref(cnt), _stream_ptr(stream))
+        if st < 0 and st not in (L.SBP_ERR_MAXITER, L.SBP_ERR_BREAKDOWN):
+            L.check(st, "sbp_solver_profile")
+        rows = [{"kernel": out[k].name.decode(), "launches": out[k].launches,
+                 "total_ms": out[k].total_ms,
+                 "ms_per_launch": out[k].total_ms / max(out[k].launches, 1)}
+                for k in range(min(cnt.value, cap))]
+        return SolveResult(res.iters, st, [], res.initial_norm, res.final_norm,
+                           res.threshold), rows
+
     def vcycle(self, b: torch.Tensor, v: torch.Tensor, stream=None) -> torch.Tensor:
         """v = M b, one V-cycle from zero."""
         check_grid(b, name="b")

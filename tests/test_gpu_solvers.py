@@ -248,9 +248,22 @@ def test_mixed_n8193_bump_against_fp64(sbp):
                                      C.byref(out), None) == 0
     assert out.value <= 2e-10 * b.norm().item()
     err = ((x32 - xs[_lib.SBP_PREC_FP64]).norm() / xs[_lib.SBP_PREC_FP64].norm()).item()
-    print(f"N=8193 mixed vs FP64: iterations {its}, relative solution difference {err:.3e}, "
+    # and against the C oracle's FP64 MGCG solve of the same b (67M unknowns)
+    import os
+    from oracle import cpu_path
+    cpu_path.set_threads(os.cpu_count() or 1)
+    bh = host(b)
+    m = cpu_path.CpuMG(n, smoother="jacobi", restriction="galerkin", coarse_n=65)
+    xo, it_o, _ = m.mgcg(bh, np.zeros_like(bh), 1e-10 * float(np.linalg.norm(bh)))
+    m.close()
+    err_o = relerr(host(x32), xo)
+    err_o64 = relerr(host(xs[_lib.SBP_PREC_FP64]), xo)
+    print(f"N=8193 mixed vs FP64: iterations {its} (oracle {it_o}), relative solution "
+          f"difference {err:.3e}, mixed vs oracle {err_o:.3e}, FP64 vs oracle {err_o64:.3e}, "
           f"true relative residual {out.value / b.norm().item():.3e}")
     assert err < 1e-8
+    assert its[_lib.SBP_PREC_FP64] == it_o
+    assert err_o <= 1e-10 and err_o64 <= 1e-10
 
 
 @pytest.mark.parametrize("n", [65, 257])
