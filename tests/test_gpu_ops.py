@@ -253,3 +253,57 @@ def test_csr_spmv_matches_matrix_free(sbp, n):
     if n == 257:
         ref = o.assemble(n).A @ x
         assert np.linalg.norm(host(y) - ref) / np.linalg.norm(ref) < 1e-14
+
+
+@pytest.mark.parametrize("n", [2049, 4097])
+def test_apply_large_vs_oracle(sbp, n):
+    # The caller-layout applies at the benchmark sizes (many column runs and
+    # row blocks per launch, the last row block holding one row), FP64 and
+    # FP32, both signs, and the fused dot, against the oracle's matrix-free
+    # restatement of matrix_free_A_full_GPU (split_matrix_free.jl:444-486).
+    rng = np.random.default_rng(n)
+    u = rng.standard_normal(n * n)
+    ref = o.neg_A_matrix_free(u, n).ravel()
+    lib = sbp.load_library()
+    ud = dev(u)
+    out = torch.empty_like(ud)
+    for sign in (-1, 1):
+        assert lib.sbp_apply_f64(C.c_void_p(ud.data_ptr()), C.c_void_p(out.data_ptr()), n, sign,
+                                 None) == 0
+        assert relerr(host(out), -sign * ref) < APPLY_RTOL
+    u32 = u.astype(np.float32)
+    ref32 = o.neg_A_matrix_free(u32.astype(np.float64), n).ravel()
+    ud32 = dev(u32, torch.float32)
+    out32 = torch.empty_like(ud32)
+    assert lib.sbp_apply_f32(C.c_void_p(ud32.data_ptr()), C.c_void_p(out32.data_ptr()), n, -1,
+                             None) == 0
+    assert relerr(host(out32), ref32) < 1e-6
+    dot = torch.zeros(1, dtype=torch.float64, device="cuda")
+    assert lib.sbp_apply_dot_f64(C.c_void_p(ud.data_ptr()), C.c_void_p(out.data_ptr()), n, 1,
+                                 C.c_void_p(dot.data_ptr()), None) == 0
+    want = -float(u @ ref)
+    assert abs(host(dot)[0] - want) <= 1e-11 * abs(want)
+
+
+@pytest.mark.parametrize("n", [65, 1025])
+def test_apply_unaligned_arrays(sbp, n):
+    # arrays that start 8 (FP64) or 4 (FP32) bytes into a buffer: an offset
+    # view is as valid a caller array as a fresh allocation
+    rng = np.random.default_rng(5)
+    u = rng.standard_normal(n * n)
+    ref = o.neg_A_matrix_free(u, n).ravel()
+    lib = sbp.load_library()
+    buf = torch.zeros(n * n + 1, dtype=torch.float64, device="cuda")
+    buf[1:] = dev(u)
+    outb = torch.zeros(n * n + 1, dtype=torch.float64, device="cuda")
+    assert lib.sbp_apply_f64(C.c_void_p(buf[1:].data_ptr()), C.c_void_p(outb[1:].data_ptr()), n,
+                             -1, None) == 0
+    assert relerr(host(outb[1:]), ref) < APPLY_RTOL
+    assert host(outb)[0] == 0.0
+    buf32 = torch.zeros(n * n + 1, dtype=torch.float32, device="cuda")
+    buf32[1:] = dev(u.astype(np.float32), torch.float32)
+    out32 = torch.zeros(n * n + 1, dtype=torch.float32, device="cuda")
+    assert lib.sbp_apply_f32(C.c_void_p(buf32[1:].data_ptr()), C.c_void_p(out32[1:].data_ptr()),
+                             n, -1, None) == 0
+    ref32 = o.neg_A_matrix_free(u.astype(np.float32).astype(np.float64), n).ravel()
+    assert relerr(host(out32[1:]), ref32) < 1e-6
