@@ -44,9 +44,10 @@ WORKLOAD = ("plain/mixed matrix-free MGCG, N=4097 (16.8M unknowns), u=sin(pi x)c
 # Algorithmic bytes per fine-grid point of the solver kernels that run on the
 # finest level once per iteration (unique arrays read + written once).
 KERNEL_BYTES_PER_POINT = {
+    "CgDirF32Job": 20,        # z, p_old (f32) read; p (f32), Ap written
     "CgDirMixedJob": 36,      # z (f32), p_old, Ap_old read; p, Ap written
     "CgDirJob<double, double": 32,   # z, p_old read; p, Ap written
-    "k_cg_update<": 52,       # x, p, r, Ap read; x, r written; r_lo (f32) written
+    "k_cg_update<": 48,       # x, r, Ap, p (f32) read; x, r, r_lo (f32) written
 }
 
 

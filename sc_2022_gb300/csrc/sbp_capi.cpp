@@ -106,6 +106,8 @@ struct sbp_solver {
   double* Ap = nullptr;
   float* r_lo = nullptr;            // FP32 copy of r (mixed precision)
   Operand ox, orr, op[2], oap, orlo;
+  float* p32[2] = {nullptr, nullptr};   // FP32 direction of mixed MGCG (ping-pong)
+  Operand op32[2];
   SolveState* st = nullptr;
   SolveState* st_host = nullptr;    // pinned, 2 slots
   double* norms = nullptr;
@@ -286,10 +288,9 @@ cudaError_t enqueue_iteration(sbp_solver* s, int kind, int parity, int sign, cud
   const bool mixed = (kind == 0 && s->opts.precision == SBP_PREC_MIXED);
   if (kind == 0) {
     if (mixed)
-      // Ap is updated in place (each point reads its old value, then writes)
-      e = launch_cg_dir_mixed<double>(vcycle_out_op(s), s->op[parity], s->oap,
-                                      grid<double>(pnew, ld), grid<double>(s->Ap, ld), n, s->st,
-                                      s->rb, q);
+      // FP32 direction p~ and Ap = A p~ (exact) in one pass
+      e = launch_cg_dir_f32(vcycle_out_op(s), s->op32[parity], grid<float>(s->p32[1 - parity], ld),
+                            grid<double>(s->Ap, ld), n, s->st, s->rb, q);
     else
       e = launch_cg_dir_op<double, double>(vcycle_out_op(s), s->op[parity], grid<double>(pnew, ld),
                                            grid<double>(s->Ap, ld), n, +1, s->st, s->rb, q);
@@ -301,7 +302,7 @@ cudaError_t enqueue_iteration(sbp_solver* s, int kind, int parity, int sign, cud
   e = launch_cg_update<double>(grid<double>(s->x, ld), grid<double>(s->r, ld),
                                cgrid<double>(pnew, ld), cgrid<double>(s->Ap, ld),
                                Grid<float>{mixed ? s->r_lo : nullptr, ld}, n, kind == 1 ? 1 : 0,
-                               s->st, s->norms, s->rb, q);
+                               s->st, s->norms, s->rb, q, mixed ? s->p32[1 - parity] : nullptr);
   if (e != cudaSuccess) return e;
   if (kind == 0) e = enqueue_vcycle_any(s, true, s->st, q);
   return e;
@@ -715,6 +716,11 @@ int sbp_solver_create(sbp_solver** out, int n, const sbp_options* opts) {
       rc = dalloc(s, &p, nn * sizeof(float)); if (rc) return rc; s->r_lo = (float*)p;
       SBP_CUDA(cudaMemset(s->r_lo, 0, nn * sizeof(float)));
       make_operand(s->orlo, s->r_lo, n, s->ld, false);
+      for (int k = 0; k < 2; ++k) {
+        rc = dalloc(s, &p, nn * sizeof(float)); if (rc) return rc; s->p32[k] = (float*)p;
+        SBP_CUDA(cudaMemset(s->p32[k], 0, nn * sizeof(float)));
+        make_operand(s->op32[k], s->p32[k], n, s->ld, false);
+      }
     }
     int m = n;
     while (true) {

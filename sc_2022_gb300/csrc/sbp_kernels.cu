@@ -892,6 +892,111 @@ cudaError_t launch_cg_dir_mixed(const Operand& z, const Operand& pold, const Ope
 }
 
 // ---------------------------------------------------------------------------
+// Mixed-precision CG direction with an FP32 direction vector:
+//   p~ = fl32(z + beta p~_old)      (z and p~_old FP32, staged with halos)
+//   Ap = A p~                       (exact: float-float stencil of FP32 values)
+//   p~.Ap -> alpha
+// x += alpha p~ and r -= alpha Ap then use the same p~, so the recurrence
+// residual stays the residual of x in FP64; rounding the direction to FP32
+// only perturbs its conjugacy (by ~6e-8, below the FP32 V-cycle's own
+// perturbation of z).  20 bytes per point instead of 36, and no FP64
+// instruction per point besides the conversion of A p~ to FP64.
+// ---------------------------------------------------------------------------
+template <bool TMA>
+struct CgDirF32Job {
+  static constexpr int kOffZ = align128(box_bytes<float, BI, BJ>());
+  static constexpr int kStage = kOffZ + align128(box_bytes<float, BI, BJ>());
+  static constexpr int kScratch = 0;
+  static constexpr bool kReduce = true;
+  // p~.Ap from the FP32 rounding of Ap, accumulated with the compensated
+  // float pair (alpha and beta only need ~1e-7)
+  using Acc = DotAcc<float>;
+  using Ctx = DirCtx;
+  DevOperand<float> z, pold;
+  Grid<float> pnew;
+  Grid<double> Ap;
+  int n, ntx, ntot;
+  SolveState* st;
+  ReduceBuf rb;
+  __device__ bool prepare(Ctx& c) const {
+    if (st->done) return true;
+    c.first = (st->iter == 0);
+    c.beta = st->beta;
+    return false;
+  }
+  __device__ int tiles() const { return ntot; }
+  __device__ unsigned tx_bytes(int) const {
+    // on the first iteration p~_old is not read
+    return TMA ? box_bytes<float, BI, BJ>() + (st->iter == 0 ? 0u : box_bytes<float, BI, BJ>())
+               : 0u;
+  }
+  __device__ void issue(unsigned char* buf, unsigned long long* bar, int id, const Ctx& c) const {
+    const TileBoxes bx(id % ntx, tile_at<TI, TJ>(id, ntx, n).j_lo);
+    stage_box<TMA, BI, BJ>(reinterpret_cast<float*>(buf + kOffZ), z, &z.box, bx.x0, bx.y0, n, bar);
+    if (!c.first)
+      stage_box<TMA, BI, BJ>(reinterpret_cast<float*>(buf), pold, &pold.box, bx.x0, bx.y0, n,
+                             bar);
+  }
+  __device__ void compute(unsigned char* buf, int id, Acc& acc, const Ctx& c, unsigned char*) const {
+    const TileT t = tile_at<TI, TJ>(id, ntx, n);
+    const TileBoxes bx(id % ntx, t.j_lo);
+    float* s = reinterpret_cast<float*>(buf);
+    const float* sz = reinterpret_cast<const float*>(buf + kOffZ);
+    const float beta = (float)c.beta;
+    const bool first = c.first;
+    // p~ on every staged point the stencil reads (each tile computes the
+    // same value for a shared halo point: same inputs, same instruction)
+    transform_box(s, t, bx, n, [&](int, int, float& v) {
+      const float zz = sz[&v - s];
+      v = first ? zz : fmaf(beta, v, zz);
+    });
+    __syncthreads();
+    auto emit = [&](int i, int j, float pv, double ap) {
+      pnew.at(i, j) = pv;
+      Ap.at(i, j) = ap;
+      acc.add_prod(pv, f64_to_f32(ap));
+    };
+    if (tile_interior(t, n)) {
+      visit_interior(s, t, [&](int i, int j, float um, float u0, float up, float uw, float ue,
+                               int) {
+        float hi, lo;
+        stencil_ff(uw, ue, um, up, u0, hi, lo);
+        emit(i, j, u0, -(f32_to_f64(hi) + f32_to_f64(lo)));   // A p~ = -(stencil)
+      });
+    } else {
+      visit_generic(s, t, bx, [&](int i, int j, const SAcc<float>& a, int) {
+        struct D {
+          const SAcc<float>* a;
+          __device__ FF operator()(int di, int dj) const { return FF((*a)(di, dj), 0.0f); }
+        } d{&a};
+        const FF na = negA<FF>(d, i, j, n);
+        emit(i, j, a(0, 0), -(f32_to_f64(na.hi) + f32_to_f64(na.lo)));
+      });
+    }
+  }
+  __device__ void finish(double tot) const {
+    st->pAp = tot;
+    if (!isfinite(tot) || tot == 0.0)
+      st->done = kDoneBreakdown;
+    else
+      st->alpha = st->rz / tot;
+  }
+};
+
+cudaError_t launch_cg_dir_f32(const Operand& z, const Operand& pold, Grid<float> pnew,
+                              Grid<double> Ap, int n, SolveState* st, ReduceBuf rb,
+                              cudaStream_t s) {
+  const dim3 g = tile_grid(n);
+  const int total = (int)(g.x * g.y);
+  const DevOperand<float> dz = dev_operand<float>(z), dp = dev_operand<float>(pold);
+  if (z.tma && pold.tma)
+    return launch_persist(CgDirF32Job<true>{dz, dp, pnew, Ap, n, (int)g.x, total, st, rb}, total,
+                          s);
+  return launch_persist(CgDirF32Job<false>{dz, dp, pnew, Ap, n, (int)g.x, total, st, rb}, total,
+                        s);
+}
+
+// ---------------------------------------------------------------------------
 // CG update (pointwise, flat, 16-byte vectors): x += alpha p; r -= alpha Ap;
 // ||r||^2; convergence test.  The arrays share one layout; padding entries
 // are zero and stay zero.
@@ -907,6 +1012,7 @@ struct CgUpdateArgs {
   double* x;
   double* r;
   const double* p;
+  const float* pf;   // FP32 direction (mixed MGCG); p unused when set
   const double* Ap;
   float* rlo;
   long long N;
@@ -930,6 +1036,7 @@ __device__ __forceinline__ void cg_update_run(const CgUpdateArgs& a, unsigned ct
   double* __restrict__ x = a.x;
   double* __restrict__ r = a.r;
   const double* __restrict__ p = a.p;
+  const float* __restrict__ pf = a.pf;
   const double* __restrict__ Ap = a.Ap;
   float* __restrict__ rlo = a.rlo;
   if (VEC) {
@@ -940,7 +1047,13 @@ __device__ __forceinline__ void cg_update_run(const CgUpdateArgs& a, unsigned ct
     const double2* a2 = reinterpret_cast<const double2*>(Ap);
 #pragma unroll 2
     for (long long k = tid; k < nv; k += stride) {
-      const double2 pv = __ldg(p2 + k);
+      double2 pv;
+      if (pf) {
+        const float2 q = __ldg(reinterpret_cast<const float2*>(pf) + k);
+        pv = make_double2(f32_to_f64(q.x), f32_to_f64(q.y));
+      } else {
+        pv = __ldg(p2 + k);
+      }
       const double2 av = __ldg(a2 + k);
       double2 xv = x2[k];
       double2 rv = r2[k];
@@ -954,7 +1067,7 @@ __device__ __forceinline__ void cg_update_run(const CgUpdateArgs& a, unsigned ct
   }
   for (long long k = done_to + tid; k < N; k += stride) {
     double xv = x[k], rv = r[k];
-    cg_update_pt(xv, rv, p[k], Ap[k], alpha, acc);
+    cg_update_pt(xv, rv, pf ? f32_to_f64(pf[k]) : p[k], Ap[k], alpha, acc);
     x[k] = xv;
     r[k] = rv;
     if (rlo) rlo[k] = f64_to_f32(rv);
@@ -1960,16 +2073,18 @@ cudaError_t launch_cg_dir(Grid<const Tz> z, Grid<const T> pold, Grid<T> pnew, Gr
 template <typename T>
 cudaError_t launch_cg_update(Grid<T> x, Grid<T> r, Grid<const T> p, Grid<const T> Ap,
                              Grid<float> rlo, int n, int plain, SolveState* st, double* norms,
-                             ReduceBuf rb, cudaStream_t s) {
+                             ReduceBuf rb, cudaStream_t s, const float* pf) {
   static_assert(sizeof(T) == 8, "the Krylov vectors are FP64");
   const int ld = x.ld;
-  if (r.ld != ld || p.ld != ld || Ap.ld != ld || (rlo.p && rlo.ld != ld) || ld < n)
+  if (r.ld != ld || (!pf && p.ld != ld) || Ap.ld != ld || (rlo.p && rlo.ld != ld) || ld < n)
     return cudaErrorInvalidValue;
   const long long N = (long long)ld * n;
-  const bool vec = aligned16(x.p) && aligned16(r.p) && aligned16(p.p) && aligned16(Ap.p) &&
-                   (!rlo.p || ((uintptr_t)rlo.p & 7u) == 0) && (ld % 2 == 0 || N % 2 == 0);
+  const bool vec = aligned16(x.p) && aligned16(r.p) && (pf ? ((uintptr_t)pf & 7u) == 0
+                                                           : aligned16(p.p)) &&
+                   aligned16(Ap.p) && (!rlo.p || ((uintptr_t)rlo.p & 7u) == 0) &&
+                   (ld % 2 == 0 || N % 2 == 0);
   const int g = flat_grid(N, vec ? 4 : 2);
-  const CgUpdateArgs a{x.p, r.p, p.p, Ap.p, rlo.p, N, plain, st, norms, rb};
+  const CgUpdateArgs a{x.p, r.p, pf ? nullptr : p.p, pf, Ap.p, rlo.p, N, plain, st, norms, rb};
   if (recorder_slot())
     return vec ? record_launch(&launch_cg_update_batch<true>, a, g)
                : record_launch(&launch_cg_update_batch<false>, a, g);
@@ -2174,6 +2289,7 @@ cudaError_t prepare_kernels() {
   persist_ctas_per_sm<CgDirJob<double, float, false>>();
   persist_ctas_per_sm<CgDirJob<double, float, true>>();
   persist_ctas_per_sm<CgDirMixedJob<false>>();
+  persist_ctas_per_sm<CgDirF32Job<false>>();
   persist_ctas_per_sm<PreFusedJob<float, true>>();
   persist_ctas_per_sm<PreFusedJob<float, false>>();
   persist_ctas_per_sm<PreFusedJob<double, true>>();
@@ -2199,6 +2315,7 @@ cudaError_t prepare_kernels() {
   persist_ctas_per_sm<PostFusedJob<double, false, false, PostSmall>>();
   persist_ctas_per_sm<PostFusedJob<double, true, false, PostSmall>>();
   persist_ctas_per_sm<CgDirMixedJob<true>>();
+  persist_ctas_per_sm<CgDirF32Job<true>>();
   return cudaGetLastError();
 }
 
@@ -2710,7 +2827,8 @@ template cudaError_t launch_cg_dir<double, float>(Grid<const float>, Grid<const 
                                                   SolveState*, ReduceBuf, cudaStream_t);
 template cudaError_t launch_cg_update<double>(Grid<double>, Grid<double>, Grid<const double>,
                                               Grid<const double>, Grid<float>, int, int,
-                                              SolveState*, double*, ReduceBuf, cudaStream_t);
+                                              SolveState*, double*, ReduceBuf, cudaStream_t,
+                                              const float*);
 template cudaError_t launch_copy<double, double>(Grid<const double>, Grid<double>, int,
                                                  cudaStream_t);
 template cudaError_t launch_copy<double, float>(Grid<const double>, Grid<float>, int,

@@ -33,6 +33,12 @@ template <typename T>
 cudaError_t launch_cg_dir_mixed(const Operand& z, const Operand& pold, const Operand& apold,
                                 Grid<double> pnew, Grid<double> Ap, int n, SolveState* st,
                                 ReduceBuf rb, cudaStream_t s);
+// Mixed-precision CG direction kept in FP32: p~ = fl32(z + beta p~_old),
+// Ap = A p~ exactly (float-float stencil), p~.Ap -> alpha.  z and p~_old are
+// staged with their halos (TMA when both allow it).
+cudaError_t launch_cg_dir_f32(const Operand& z, const Operand& pold, Grid<float> pnew,
+                              Grid<double> Ap, int n, SolveState* st, ReduceBuf rb,
+                              cudaStream_t s);
 template <typename T>
 cudaError_t launch_smooth_op(int field, int epi, const Operand& vin, const Operand& e,
                              const Operand& b, Grid<T> vout, int n, int smoother, double omega,
@@ -95,10 +101,11 @@ cudaError_t launch_cg_dir(Grid<const Tz> z, Grid<const T> pold, Grid<T> pnew, Gr
 // x += alpha p, r -= alpha Ap, rlo = float(r) (if rlo.p), rr = r.r,
 // iter += 1, norms[iter] = sqrt(rr), convergence / max-iteration test.
 // `plain`: unpreconditioned CG, also beta = rr/rz and rz = rr.
+// pf (optional): an FP32 direction used in place of p (p is then ignored).
 template <typename T>
 cudaError_t launch_cg_update(Grid<T> x, Grid<T> r, Grid<const T> p, Grid<const T> Ap,
                              Grid<float> rlo, int n, int plain, SolveState* st, double* norms,
-                             ReduceBuf rb, cudaStream_t s);
+                             ReduceBuf rb, cudaStream_t s, const float* pf = nullptr);
 
 // One smoothing pass on level n.  The stencil input ("field") is
 //   kFieldPlain:   vin
