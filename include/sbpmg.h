@@ -358,6 +358,17 @@ int sbp_cg_solve(sbp_solver* s, const double* b, double* x, int sign, double abs
  * nu) (matrix_free_mg_cg.jl:143-176) for the two-level options. */
 int sbp_vcycle_apply(sbp_solver* s, const double* b, double* v, void* stream);
 
+/* Test hook for the failure path of the bounded waits (no counterpart in
+ * the reference).  drop != 0: from the next launch on, CTA 0 of every
+ * persistent stencil launch declares its first staged tile to its mbarrier
+ * but issues no copy, and every bounded wait gives up after wait_polls
+ * try_wait polls (0 = the default of about a second).  The affected calls
+ * end with non-finite results and the solve entry points return
+ * SBP_ERR_TIMEOUT; no memory access goes astray and no wait is unbounded.
+ * drop = 0, wait_polls = 0 restores normal operation.  Synchronises the
+ * device first.  Not for production use. */
+int sbp_test_drop_copy(int drop, unsigned wait_polls);
+
 /* Measured FP64 FMA rate of the current GPU in 1e9 lane-operations per
  * second (blocking): eight independent FMA chains per thread over one full
  * wave of CTAs, best of three CUDA-event timings.  The denominator of the

@@ -92,6 +92,7 @@ SIGNATURES = {
     "sbp_cg_solve": (_i, [_vp, _vp, _vp, _i, _d, _d, _i, C.POINTER(sbp_result), _dp, _i, _vp]),
     "sbp_vcycle_apply": (_i, [_vp, _vp, _vp, _vp]),
     "sbp_fp64_fma_rate": (_i, [_dp, _vp]),
+    "sbp_test_drop_copy": (_i, [_i, C.c_uint]),
     "sbp_solver_profile": (_i, [_vp, _i, _vp, _vp, _i, _d, _i, C.POINTER(sbp_result),
                                 C.POINTER(sbp_kernel_time), _i, C.POINTER(_i), _vp]),
     "sbp_h_misfit_f64": (_i, [_vp, _vp, _vp, _i, _vp, _vp]),
@@ -165,7 +166,7 @@ class SbpError(RuntimeError):
     def __init__(self, status: int, where: str):
         lib = load()
         msg = lib.sbp_status_string(status).decode()
-        if status in (SBP_ERR_CUDA, SBP_ERR_NOMEM):
+        if status in (SBP_ERR_CUDA, SBP_ERR_NOMEM, SBP_ERR_TIMEOUT):
             detail = lib.sbp_last_error().decode()
             if detail:
                 msg = f"{msg} ({detail})"

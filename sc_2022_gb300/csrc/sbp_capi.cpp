@@ -823,6 +823,12 @@ int sbp_mgcg_adjoint_f64(sbp_solver* s, const double* gu, double* lam, double* d
   return rc;
 }
 
+int sbp_test_drop_copy(int drop, unsigned wait_polls) {
+  SBP_CUDA(cudaDeviceSynchronize());
+  SBP_CUDA(set_copy_drop(drop, wait_polls));
+  return SBP_OK;
+}
+
 int sbp_fp64_fma_rate(double* gfma_per_s, void* stream) {
   if (!gfma_per_s) return SBP_ERR_ARGS;
   SBP_CUDA(measure_fp64_fma_rate(gfma_per_s, (cudaStream_t)stream));

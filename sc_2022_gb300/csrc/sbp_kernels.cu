@@ -270,8 +270,11 @@ __global__ void __launch_bounds__(kThreads) k_persist(const __grid_constant__ Jo
   typename Job::Acc acc;
   int tile = blockIdx.x;
   if (tile < total) {
-    if (threadIdx.x == 0) mbar_arrive_expect_tx(&bar[0], job.tx_bytes(tile));
-    job.issue(buf0, &bar[0], tile, ctx);
+    const unsigned tx = job.tx_bytes(tile);
+    if (threadIdx.x == 0) mbar_arrive_expect_tx(&bar[0], tx);
+    // failure test only: the declared copy is never issued (TMA stages)
+    const bool drop = tx != 0u && blockIdx.x == 0 && g_sbp_drop_copy != 0u;
+    if (!drop) job.issue(buf0, &bar[0], tile, ctx);
   }
   cp_async_commit();
   bool ok = true;
@@ -2323,6 +2326,14 @@ unsigned int read_device_fault() {
   unsigned int v = 0;
   cudaMemcpyFromSymbol(&v, g_sbp_fault, sizeof(v));
   return v;
+}
+
+cudaError_t set_copy_drop(int drop, unsigned polls) {
+  const unsigned d = drop ? 1u : 0u;
+  const unsigned p = polls ? polls : kWaitPollsDefault;
+  cudaError_t e = cudaMemcpyToSymbol(g_sbp_drop_copy, &d, sizeof(d));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_sbp_wait_polls, &p, sizeof(p));
+  return e;
 }
 
 unsigned int take_device_fault() {

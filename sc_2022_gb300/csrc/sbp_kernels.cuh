@@ -146,11 +146,22 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned 
 // waits all live in sbp_kernels.cu, whose copy read_device_fault() reads.
 static __device__ unsigned int g_sbp_fault = 0u;
 
+// try_wait polls of a bounded wait before it gives up, and the failure
+// test's switch (sbp_test_drop_copy): while set, CTA 0 of every persistent
+// launch declares its first tile's bytes but issues no copy, so that wait
+// runs out.  Set only through sbp_test_drop_copy (this translation unit's
+// copies, like g_sbp_fault).
+constexpr unsigned kWaitPollsDefault = 1u << 22;
+static __device__ unsigned int g_sbp_wait_polls = kWaitPollsDefault;
+static __device__ unsigned int g_sbp_drop_copy = 0u;
+
 // Bounded wait on an mbarrier phase.  try_wait suspends for a bounded,
-// hardware-defined time per call, so the limit is seconds: far beyond any
-// legitimate TMA latency, short enough that a lost copy cannot hang the GPU.
+// hardware-defined time per call, so the default limit is seconds: far beyond
+// any legitimate TMA latency, short enough that a lost copy cannot hang the
+// GPU.
 __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned phase) {
-  for (unsigned it = 0; it < (1u << 22); ++it)
+  const unsigned polls = *const_cast<volatile unsigned*>(&g_sbp_wait_polls);
+  for (unsigned it = 0; it < polls; ++it)
     if (mbar_try_wait(bar, phase)) return true;
   atomicOr(&g_sbp_fault, 1u);
   return false;

@@ -71,6 +71,10 @@ cudaError_t measure_fp64_fma_rate(double* gfma_per_s, cudaStream_t s);
 unsigned int read_device_fault();
 // The same, clearing the flag (the current device's copy).
 unsigned int take_device_fault();
+// Failure test switch: drop = 1 makes CTA 0 of every persistent launch skip
+// its first TMA copy (its wait then runs out after `polls` try_wait polls);
+// drop = 0, polls = 0 restores normal operation.
+cudaError_t set_copy_drop(int drop, unsigned polls);
 
 // Upper bound on the CTAs any reducing launch uses for an n x n grid; the
 // partials buffer of a ReduceBuf must hold this many doubles.
