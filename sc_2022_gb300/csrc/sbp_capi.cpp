@@ -251,7 +251,8 @@ long long vcycle_launches(const sbp_solver* s, bool dot) {
   for (size_t l = 0; l + 1 < nl; ++l) {
     const int n = s->levels[l].n;
     if (mixed ? use_fused<float>(s, n) : use_fused<double>(s, n)) {
-      c += 2;                             // fused pre-smoothing, fused post-smoothing
+      // fused pre-smoothing (one or two kernels), fused post-smoothing
+      c += pre_fused_launches(n, o.nu_pre, mixed) + 1;
       continue;
     }
     c += (o.nu_pre >= 2) ? 1 + (o.nu_pre - 2) : 1;

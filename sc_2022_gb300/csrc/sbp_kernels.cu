@@ -1501,10 +1501,22 @@ struct PreFusedJob {
   T omega;
   const SolveState* st;
   ReduceBuf rb;
+  // ring > 0: only the boundary ring of tiles (first and last tile row and
+  // column; nty = ring's tile rows) is visited, k -> ring_id(k); the interior
+  // tiles are done by the register wave kernel (k_pre_wave)
+  int ring, nty;
+  __device__ int ring_id(int k) const {
+    if (!ring) return k;
+    if (k < ntx) return k;
+    if (k < 2 * ntx) return (k - ntx) + (nty - 1) * ntx;
+    const int k2 = k - 2 * ntx;
+    return ((k2 & 1) ? ntx - 1 : 0) + (1 + (k2 >> 1)) * ntx;
+  }
   __device__ bool prepare(Ctx&) const { return st && st->done; }
   __device__ int tiles() const { return ntot; }
   __device__ unsigned tx_bytes(int) const { return TMA ? box_bytes<T, Geo::BI, Geo::BJ>() : 0u; }
-  __device__ void issue(unsigned char* buf, unsigned long long* bar, int id, const Ctx&) const {
+  __device__ void issue(unsigned char* buf, unsigned long long* bar, int k, const Ctx&) const {
+    const int id = ring_id(k);
     const int ti = id % ntx, tj = id / ntx;
     stage_box<TMA, Geo::BI, Geo::BJ>(reinterpret_cast<T*>(buf), b, &bmap, 2 * Geo::RI * ti - 4,
                                  2 * Geo::RJ * tj - 4, nf, bar);
@@ -1584,8 +1596,9 @@ struct PreFusedJob {
     f.at(I, J + 1) = sc * fma(T(0.5), cs[2] + cs[4], cs[3]);
   }
 
-  __device__ void compute(unsigned char* buf, int id, Acc&, const Ctx&, unsigned char* scr) const {
+  __device__ void compute(unsigned char* buf, int k, Acc&, const Ctx&, unsigned char* scr) const {
     constexpr int BW = Geo::BI;   // box row length
+    const int id = ring_id(k);
     const int ti = id % ntx, tj = id / ntx;
     const Tile<Geo::RI, Geo::RJ> t = tile_at<Geo::RI, Geo::RJ>(id, ntx, nc);
     const int X0 = 2 * Geo::RI * ti - 4, Y0 = 2 * Geo::RJ * tj - 4;
@@ -2189,20 +2202,211 @@ static bool small_fused_tiles(int ncoarse) {
 template <typename T, class G>
 static cudaError_t launch_pre_fused_geom(const Operand& b, Grid<T> vout, Grid<T> f, int nf,
                                          int sweeps, int smoother, double omega, int kind,
-                                         const SolveState* st, cudaStream_t s) {
+                                         const SolveState* st, cudaStream_t s, int ring = 0) {
   const int nc = (nf + 1) / 2;
   const int ntx = ntiles(nc, G::RI), nty = ntiles(nc, G::RJ);
-  const int total = ntx * nty;
+  const int total = ring ? 2 * ntx + 2 * (nty - 2) : ntx * nty;
   const DevOperand<T> db = dev_operand<T>(b);
   CUtensorMap bm{};
   const bool tma = b.tma && make_box_map(bm, b, sizeof(T) == 8, G::BI, G::BJ);
   if (tma)
     return launch_persist(PreFusedJob<T, true, G>{db, bm, vout, f, nf, nc, ntx, total, sweeps,
-                                                  smoother, kind, T(omega), st, ReduceBuf{}},
+                                                  smoother, kind, T(omega), st, ReduceBuf{},
+                                                  ring, nty},
                           total, s);
   return launch_persist(PreFusedJob<T, false, G>{db, bm, vout, f, nf, nc, ntx, total, sweeps,
-                                                 smoother, kind, T(omega), st, ReduceBuf{}},
+                                                 smoother, kind, T(omega), st, ReduceBuf{},
+                                                 ring, nty},
                         total, s);
+}
+
+// ---------------------------------------------------------------------------
+// Register wave pre-smoothing for the interior of a fine level (FP32, three
+// Jacobi/Richardson sweeps from zero, residual, restriction), the job of
+// PreFusedJob's interior tiles without shared memory or block barriers.
+//
+// A warp owns a strip of 28 coarse rows x up to 32 coarse columns of the
+// interior rectangle [Ia, Ib) x [Ja, Jb) (the union of the PreLarge tiles
+// that are neither in the first nor in the last tile row or column: every
+// point there and in its halo has the plain 5-point stencil and the
+// constant smoother weight).  Lane l holds fine rows 2 I0 - 4 + 2l and the
+// row after it (64 rows: 56 owned plus a 4-row halo on each side), and the
+// warp marches along j with every stage one column behind the previous:
+//   step c: b at column c (loaded D columns ahead as one float2 per lane),
+//           v2 at c - 1 (from b, v1 = m b folded in),
+//           v3 at c - 2, residual r at c - 3,
+//           f(I, J) once r reaches column 2J + 1.
+// The i-neighbours of a lane's two rows are its own other row and one row of
+// the lane above or below (one shuffle per point per stage); the
+// j-neighbours are the stage's previous and next columns, kept in registers.
+// v3 on owned points and f are stored straight from registers.  The sums are
+// formed in the same order as PreFusedJob's interior path.
+// ---------------------------------------------------------------------------
+constexpr int kWaveRows = 28;     // coarse rows of a strip
+constexpr int kWaveCols = 32;     // coarse columns of a strip (at most)
+constexpr int kWaveAhead = 8;     // columns of b loaded ahead
+
+struct PreWaveArgs {
+  const float* b;
+  int ldb;
+  float* vout;
+  int ldv;
+  float* f;
+  int ldf;
+  int nf, Ia, Ib, Ja, Jb, nsi, nsj;
+  float m, k1, m2, sc;
+  const SolveState* st;
+};
+
+__global__ void __launch_bounds__(kThreads) k_pre_wave(const PreWaveArgs a) {
+  pdl_begin();
+  if (a.st && a.st->done) return;
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * kThreads + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * kThreads) >> 5;
+  const int items = a.nsi * a.nsj;
+  const unsigned FULL = 0xffffffffu;
+  for (int it = gw; it < items; it += nw) {
+    const int si = it % a.nsi, sj = it / a.nsi;
+    const int I0 = a.Ia + kWaveRows * si;
+    const int I1 = min(I0 + kWaveRows, a.Ib);
+    const int J0 = a.Ja + kWaveCols * sj;
+    const int J1 = min(J0 + kWaveCols, a.Jb);
+    const int ra = 2 * I0 - 4 + 2 * lane;               // this lane's first fine row
+    const bool own_rows = lane >= 2 && ra + 1 <= 2 * I1 - 1;
+    const int I = I0 + lane - 2;                          // coarse row centred on ra
+    const bool own_f = lane >= 2 && I < I1;
+    const int c_first = 2 * J0 - 4, c_last = 2 * J1 + 2;  // leading columns marched
+    const float* bp = a.b + (size_t)ra;
+    // b queue: q[k] holds column c + k
+    float2 q[kWaveAhead];
+#pragma unroll
+    for (int k = 0; k < kWaveAhead; ++k) {
+      const int c = c_first + k;
+      q[k] = c <= c_last ? __ldg(reinterpret_cast<const float2*>(bp + (size_t)c * a.ldb))
+                         : make_float2(0.f, 0.f);
+    }
+    // stage windows (x = row ra, y = row ra + 1)
+    float2 b1 = make_float2(0.f, 0.f), b2 = b1, b3 = b1;  // b at c-1, c-2, c-3
+    float2 v2a = b1, v2b = b1;                            // v2 at c-2, c-3
+    float2 v3a = b1, v3b = b1;                            // v3 at c-3, c-4
+    float t1 = 0.f, t2 = 0.f;                             // row-combined r at c-4, c-5
+    for (int c = c_first; c <= c_last; ++c) {
+      const float2 b0 = q[0];
+#pragma unroll
+      for (int k = 0; k < kWaveAhead - 1; ++k) q[k] = q[k + 1];
+      {
+        const int cn = c + kWaveAhead;
+        q[kWaveAhead - 1] = cn <= c_last
+                                ? __ldg(reinterpret_cast<const float2*>(bp + (size_t)cn * a.ldb))
+                                : make_float2(0.f, 0.f);
+      }
+      // v2 at column c - 1 from b at c - 2, c - 1, c
+      float2 v2;
+      {
+        const float up = __shfl_up_sync(FULL, b1.y, 1);    // row ra - 1
+        const float dn = __shfl_down_sync(FULL, b1.x, 1);  // row ra + 2
+        v2.x = fmaf(a.m2, (up + b1.y) + (b2.x + b0.x), a.k1 * b1.x);
+        v2.y = fmaf(a.m2, (b1.x + dn) + (b2.y + b0.y), a.k1 * b1.y);
+      }
+      // v3 at column c - 2 from v2 at c - 3, c - 2, c - 1
+      float2 v3;
+      {
+        const float up = __shfl_up_sync(FULL, v2a.y, 1);
+        const float dn = __shfl_down_sync(FULL, v2a.x, 1);
+        v3.x = fmaf(a.m, b2.x + (((up + v2a.y) + (v2b.x + v2.x)) - 4.f * v2a.x), v2a.x);
+        v3.y = fmaf(a.m, b2.y + (((v2a.x + dn) + (v2b.y + v2.y)) - 4.f * v2a.y), v2a.y);
+      }
+      // v3 at column c - 2 is final: store the owned points
+      if (own_rows && c - 2 >= 2 * J0 && c - 2 <= 2 * J1 - 1)
+        *reinterpret_cast<float2*>(a.vout + (size_t)(c - 2) * a.ldv + ra) = v3;
+      // residual at column c - 3 from v3 at c - 4, c - 3, c - 2
+      float2 r;
+      {
+        const float up = __shfl_up_sync(FULL, v3a.y, 1);
+        const float dn = __shfl_down_sync(FULL, v3a.x, 1);
+        const float nbx = (up + v3a.y) + (v3b.x + v3.x);
+        const float nby = (v3a.x + dn) + (v3b.y + v3.y);
+        r.x = b3.x + (nbx - 4.f * v3a.x);
+        r.y = b3.y + (nby - 4.f * v3a.y);
+      }
+      // restriction: row-combine at column c - 3 for the coarse row centred
+      // on ra (rows ra - 1, ra, ra + 1), then f when c - 3 = 2J + 1
+      const float rup = __shfl_up_sync(FULL, r.y, 1);
+      const float t0 = fmaf(0.5f, rup + r.y, r.x);
+      const int cr = c - 3;
+      if (((cr - 1) & 1) == 0 && cr >= 2 * J0 + 1 && cr <= 2 * J1 - 1) {
+        const int J = (cr - 1) >> 1;
+        if (own_f) a.f[(size_t)J * a.ldf + I] = a.sc * fmaf(0.5f, t2 + t0, t1);
+      }
+      // shift the windows
+      t2 = t1;
+      t1 = t0;
+      v3b = v3a;
+      v3a = v3;
+      v2b = v2a;
+      v2a = v2;
+      b3 = b2;
+      b2 = b1;
+      b1 = b0;
+    }
+  }
+}
+
+// Whether the interior rectangle of the PreLarge tiling is non-empty and
+// which coarse range it covers.
+static bool pre_wave_rect(int nc, int& Ia, int& Ib, int& Ja, int& Jb) {
+  const int ntx = ntiles(nc, RTI), nty = ntiles(nc, RTJ);
+  if (ntx < 3 || nty < 3) return false;
+  if ((nc - 1) % RTI != 0 || (nc - 1) % RTJ != 0) return false;   // full tiles only
+  Ia = RTI + 1;
+  Ib = RTI * (ntx - 1) + 1;
+  Ja = RTJ + 1;
+  Jb = RTJ * (nty - 1) + 1;
+  return Ia < Ib && Ja < Jb;
+}
+
+static cudaError_t launch_pre_wave(const Operand& b, Grid<float> vout, Grid<float> f, int nf,
+                                   int Ia, int Ib, int Ja, int Jb, int smoother, double omega,
+                                   int kind, const SolveState* st, cudaStream_t s) {
+  PreWaveArgs a;
+  a.b = static_cast<const float*>(b.p);
+  a.ldb = b.ld;
+  a.vout = vout.p;
+  a.ldv = vout.ld;
+  a.f = f.p;
+  a.ldf = f.ld;
+  a.nf = nf;
+  a.Ia = Ia;
+  a.Ib = Ib;
+  a.Ja = Ja;
+  a.Jb = Jb;
+  a.nsi = (Ib - Ia + kWaveRows - 1) / kWaveRows;
+  a.nsj = (Jb - Ja + kWaveCols - 1) / kWaveCols;
+  const float m = (smoother == kSmoothJacobi) ? (float)omega * 0.25f : (float)omega;
+  a.m = m;
+  a.k1 = 2.f * m - 4.f * m * m;
+  a.m2 = m * m;
+  a.sc = (kind == kRestrictGalerkin) ? 1.f : 0.25f;
+  a.st = st;
+  static const int per_sm = [] {
+    int v = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_pre_wave, kThreads, 0) != cudaSuccess ||
+        v < 1)
+      v = 1;
+    return v;
+  }();
+  const int items = a.nsi * a.nsj;
+  const int grid = std::max(1, std::min((items + kWarps - 1) / kWarps, sm_count() * per_sm));
+  return launch_pdl(k_pre_wave, dim3(grid), dim3(kThreads), 0, s, a);
+}
+
+int pre_fused_launches(int nf, int sweeps, bool f32) {
+  int Ia, Ib, Ja, Jb;
+  if (f32 && sweeps == 3 && !small_fused_tiles((nf + 1) / 2) &&
+      pre_wave_rect((nf + 1) / 2, Ia, Ib, Ja, Jb))
+    return 2;
+  return 1;
 }
 
 template <typename T>
@@ -2213,6 +2417,18 @@ cudaError_t launch_pre_fused(const Operand& b, Grid<T> vout, Grid<T> f, int nf, 
   if (small_fused_tiles((nf + 1) / 2))
     return launch_pre_fused_geom<T, PreSmall>(b, vout, f, nf, sweeps, smoother, omega, kind, st,
                                               s);
+  int Ia, Ib, Ja, Jb;
+  if (std::is_same<T, float>::value && sweeps == 3 && !recorder_slot() &&
+      (b.ld % 2) == 0 && (vout.ld % 2) == 0 && ((uintptr_t)b.p & 7u) == 0 &&
+      ((uintptr_t)vout.p & 7u) == 0 && pre_wave_rect((nf + 1) / 2, Ia, Ib, Ja, Jb)) {
+    // boundary tiles by the staged job, the interior by the register wave
+    cudaError_t e = launch_pre_fused_geom<T, PreLarge>(b, vout, f, nf, sweeps, smoother, omega,
+                                                       kind, st, s, 1);
+    if (e != cudaSuccess) return e;
+    return launch_pre_wave(b, Grid<float>{reinterpret_cast<float*>(vout.p), vout.ld},
+                           Grid<float>{reinterpret_cast<float*>(f.p), f.ld}, nf, Ia, Ib, Ja, Jb,
+                           smoother, omega, kind, st, s);
+  }
   return launch_pre_fused_geom<T, PreLarge>(b, vout, f, nf, sweeps, smoother, omega, kind, st,
                                             s);
 }

@@ -67,6 +67,10 @@ int apply_dot_f64_noalloc(const double* u, double* out, int n, int sign, double*
 // timed with CUDA events on s (blocking).
 cudaError_t measure_fp64_fma_rate(double* gfma_per_s, cudaStream_t s);
 
+// Kernel launches of one launch_pre_fused call on a solver level (the
+// interior of the large FP32 levels takes a second, register-wave kernel).
+int pre_fused_launches(int nf, int sweeps, bool f32);
+
 // Non-zero once a kernel's bounded wait on an asynchronous copy gave up.
 unsigned int read_device_fault();
 // The same, clearing the flag (the current device's copy).

@@ -141,3 +141,26 @@ def test_fp64_fma_rate(sbp):
     assert sbp.load_library().sbp_fp64_fma_rate(C.byref(g), None) == 0
     # GB300: about two FP64 lanes per clock per SM, 152 SMs at up to 2.07 GHz
     assert 50.0 < g.value < 5000.0
+
+
+@pytest.mark.parametrize("n", [2049, 4097])
+def test_vcycle_large_levels_match_c_oracle(sbp, threads, n):
+    # One V-cycle of the benchmark hierarchy (matrix_free_Two_level_multigrid
+    # generalised to 7 levels, matrix_free_mg_cg.jl:143-176) at the sizes
+    # whose fine levels run the register-wave pre-smoothing in the mixed
+    # form: FP64 against the C oracle's V-cycle to 1e-12, mixed to 2e-5
+    from sc_2022_gb300 import _lib
+    rng = np.random.default_rng(n)
+    b = rng.standard_normal(n * n)
+    m = cpu_path.CpuMG(n, smoother="jacobi", restriction="galerkin", coarse_n=65)
+    zo = m.vcycle(b)
+    m.close()
+    bd = torch.tensor(b, dtype=torch.float64, device="cuda")
+    for prec, tol in ((_lib.SBP_PREC_FP64, 1e-12), (_lib.SBP_PREC_MIXED, 2e-5)):
+        s = sbp.Solver(n, sbp.default_options(prec))
+        z = torch.empty_like(bd)
+        s.vcycle(bd, z)
+        err = relerr(host(z), zo)
+        print(f"N={n} V-cycle precision {prec}: vs C oracle {err:.3e}")
+        assert err <= tol
+        s.close()
