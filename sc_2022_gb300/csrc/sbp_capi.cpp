@@ -86,6 +86,7 @@ struct Level {
   Operand ob, ov[2];        // TMA operands of b and v
   int out = 0;              // buffer holding the V-cycle result
   bool own_b = false;
+  cudaEvent_t fork = nullptr, join = nullptr;   // boundary branch of the pre-smoothing
 };
 
 }  // namespace
@@ -116,6 +117,7 @@ struct sbp_solver {
   long long dev_bytes = 0;
   std::vector<void*> allocs;
   cudaStream_t cap = nullptr;       // private stream for graph capture
+  cudaStream_t aux = nullptr;       // forked branch (boundary tiles of the wave levels)
   cudaEvent_t ev[2] = {nullptr, nullptr};
   // cached iteration graphs: [kind][parity]; kind 0 = MGCG, 1 = CG
   cudaGraphExec_t iter_exec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
@@ -201,7 +203,7 @@ cudaError_t enqueue_vcycle(sbp_solver* s, size_t l, bool dot, SolveState* st, cu
   if (use_fused<T>(s, n)) {
     Level& C = s->levels[l + 1];
     e = launch_pre_fused<T>(L.ob, grid<T>(L.v[0], L.ld), grid<T>(C.b, C.ld), n, o.nu_pre, sm, om,
-                            o.restriction, st, q);
+                            o.restriction, st, q, s->aux, L.fork, L.join);
     if (e != cudaSuccess) return e;
     e = enqueue_vcycle<T>(s, l + 1, false, st, q);
     if (e != cudaSuccess) return e;
@@ -744,6 +746,12 @@ int sbp_solver_create(sbp_solver** out, int n, const sbp_options* opts) {
       make_operand(L.ov[0], L.v[0], m, L.ld, f64);
       make_operand(L.ov[1], L.v[1], m, L.ld, f64);
       s->levels.push_back(L);
+      if (mixed && pre_fused_launches(m, s->opts.nu_pre, true) == 2) {
+        Level& B = s->levels.back();
+        SBP_CUDA(cudaEventCreateWithFlags(&B.fork, cudaEventDisableTiming));
+        SBP_CUDA(cudaEventCreateWithFlags(&B.join, cudaEventDisableTiming));
+        if (!s->aux) SBP_CUDA(cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking));
+      }
       if (m == s->opts.coarse_n) break;
       m = (m + 1) / 2;
     }
@@ -778,8 +786,13 @@ int sbp_solver_destroy(sbp_solver* s) {
   for (void* p : s->allocs) cudaFree(p);
   if (s->st_host) cudaFreeHost(s->st_host);
   if (s->cap) cudaStreamDestroy(s->cap);
+  if (s->aux) cudaStreamDestroy(s->aux);
   for (auto& e : s->ev)
     if (e) cudaEventDestroy(e);
+  for (Level& L : s->levels) {
+    if (L.fork) cudaEventDestroy(L.fork);
+    if (L.join) cudaEventDestroy(L.join);
+  }
   delete s;
   return SBP_OK;
 }

@@ -2291,7 +2291,7 @@ __global__ void __launch_bounds__(kThreads) k_pre_wave(const PreWaveArgs a) {
     float2 v2a = b1, v2b = b1;                            // v2 at c-2, c-3
     float2 v3a = b1, v3b = b1;                            // v3 at c-3, c-4
     float t1 = 0.f, t2 = 0.f;                             // row-combined r at c-4, c-5
-    for (int c = c_first; c <= c_last; ++c) {
+    auto step = [&](int c) {
       const float2 b0 = q[0];
 #pragma unroll
       for (int k = 0; k < kWaveAhead - 1; ++k) q[k] = q[k + 1];
@@ -2349,7 +2349,15 @@ __global__ void __launch_bounds__(kThreads) k_pre_wave(const PreWaveArgs a) {
       b3 = b2;
       b2 = b1;
       b1 = b0;
+    };
+    // blocks of kWaveAhead steps, unrolled so that the window shifts are
+    // register renames; then the remaining steps
+    int c = c_first;
+    for (; c + kWaveAhead - 1 <= c_last; c += kWaveAhead) {
+#pragma unroll
+      for (int u = 0; u < kWaveAhead; ++u) step(c + u);
     }
+    for (; c <= c_last; ++c) step(c);
   }
 }
 
@@ -2412,7 +2420,8 @@ int pre_fused_launches(int nf, int sweeps, bool f32) {
 template <typename T>
 cudaError_t launch_pre_fused(const Operand& b, Grid<T> vout, Grid<T> f, int nf, int sweeps,
                              int smoother, double omega, int kind, const SolveState* st,
-                             cudaStream_t s) {
+                             cudaStream_t s, cudaStream_t aux, cudaEvent_t fork,
+                             cudaEvent_t join) {
   if (sweeps < 1 || sweeps > kMaxFusedSweeps) return cudaErrorInvalidValue;
   if (small_fused_tiles((nf + 1) / 2))
     return launch_pre_fused_geom<T, PreSmall>(b, vout, f, nf, sweeps, smoother, omega, kind, st,
@@ -2421,13 +2430,25 @@ cudaError_t launch_pre_fused(const Operand& b, Grid<T> vout, Grid<T> f, int nf, 
   if (std::is_same<T, float>::value && sweeps == 3 && !recorder_slot() &&
       (b.ld % 2) == 0 && (vout.ld % 2) == 0 && ((uintptr_t)b.p & 7u) == 0 &&
       ((uintptr_t)vout.p & 7u) == 0 && pre_wave_rect((nf + 1) / 2, Ia, Ib, Ja, Jb)) {
-    // boundary tiles by the staged job, the interior by the register wave
-    cudaError_t e = launch_pre_fused_geom<T, PreLarge>(b, vout, f, nf, sweeps, smoother, omega,
-                                                       kind, st, s, 1);
+    // boundary tiles by the staged job (on a forked branch when one is
+    // given: it is latency-bound and overlaps the wave), the interior by the
+    // register wave
+    const bool forked = aux && fork && join;
+    cudaError_t e = cudaSuccess;
+    if (forked) {
+      e = cudaEventRecord(fork, s);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(aux, fork, 0);
+    }
+    if (e == cudaSuccess)
+      e = launch_pre_fused_geom<T, PreLarge>(b, vout, f, nf, sweeps, smoother, omega, kind, st,
+                                             forked ? aux : s, 1);
+    if (forked && e == cudaSuccess) e = cudaEventRecord(join, aux);
     if (e != cudaSuccess) return e;
-    return launch_pre_wave(b, Grid<float>{reinterpret_cast<float*>(vout.p), vout.ld},
-                           Grid<float>{reinterpret_cast<float*>(f.p), f.ld}, nf, Ia, Ib, Ja, Jb,
-                           smoother, omega, kind, st, s);
+    e = launch_pre_wave(b, Grid<float>{reinterpret_cast<float*>(vout.p), vout.ld},
+                        Grid<float>{reinterpret_cast<float*>(f.p), f.ld}, nf, Ia, Ib, Ja, Jb,
+                        smoother, omega, kind, st, s);
+    if (forked && e == cudaSuccess) e = cudaStreamWaitEvent(s, join, 0);
+    return e;
   }
   return launch_pre_fused_geom<T, PreLarge>(b, vout, f, nf, sweeps, smoother, omega, kind, st,
                                             s);
@@ -3020,7 +3041,8 @@ SBP_INST_T(float)
 
 #define SBP_INST_OP(T)                                                                         \
   template cudaError_t launch_pre_fused<T>(const Operand&, Grid<T>, Grid<T>, int, int, int,      \
-                                           double, int, const SolveState*, cudaStream_t);        \
+                                           double, int, const SolveState*, cudaStream_t,         \
+                                           cudaStream_t, cudaEvent_t, cudaEvent_t);              \
   template cudaError_t launch_post_fused<T>(const Operand&, const Operand&, const Operand&,      \
                                             Grid<T>, int, int, int, double, int, SolveState*,    \
                                             ReduceBuf, cudaStream_t);                            \

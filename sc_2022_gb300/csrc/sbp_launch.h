@@ -46,9 +46,13 @@ cudaError_t launch_smooth_op(int field, int epi, const Operand& vin, const Opera
 // Fused V-cycle passes (temporal blocking, sweeps <= 3): pre-smoothing from
 // zero + residual + restriction into f, and prolongation + post-smoothing.
 template <typename T>
+// With aux, fork and join given, a level whose interior runs the register
+// wave does its boundary tiles on `aux` concurrently (fork recorded on s,
+// join waited on by s).
 cudaError_t launch_pre_fused(const Operand& b, Grid<T> vout, Grid<T> f, int nf, int sweeps,
                              int smoother, double omega, int kind, const SolveState* st,
-                             cudaStream_t s);
+                             cudaStream_t s, cudaStream_t aux = nullptr,
+                             cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
 template <typename T>
 cudaError_t launch_post_fused(const Operand& vin, const Operand& e, const Operand& b, Grid<T> vout,
                               int n, int sweeps, int smoother, double omega, int dot,
