@@ -2244,7 +2244,8 @@ static cudaError_t launch_pre_fused_geom(const Operand& b, Grid<T> vout, Grid<T>
 // ---------------------------------------------------------------------------
 constexpr int kWaveRows = 28;     // coarse rows of a strip
 constexpr int kWaveCols = 32;     // coarse columns of a strip (at most)
-constexpr int kWaveAhead = 8;     // columns of b loaded ahead
+constexpr int kWaveAhead = 16;    // columns of b in flight per warp
+constexpr int kWaveSlots = kWaveAhead + 1;   // per-warp ring of b columns
 
 struct PreWaveArgs {
   const float* b;
@@ -2258,10 +2259,21 @@ struct PreWaveArgs {
   const SolveState* st;
 };
 
+__device__ __forceinline__ void cp_async8(void* sdst, const void* gsrc) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_u32(sdst)), "l"(gsrc)
+               : "memory");
+}
+
+// b columns come through a per-lane ring in shared memory filled by cp.async
+// kWaveAhead columns ahead (one commit group per column; a lane reads only
+// its own slots, so the wait needs no warp or block barrier).  The slot a
+// copy refills was read one step earlier.
 __global__ void __launch_bounds__(kThreads) k_pre_wave(const PreWaveArgs a) {
+  __shared__ __align__(16) float2 ring[kWarps][kWaveSlots][32];
   pdl_begin();
   if (a.st && a.st->done) return;
   const int lane = threadIdx.x & 31;
+  const int wl = threadIdx.x >> 5;
   const int gw = (blockIdx.x * kThreads + threadIdx.x) >> 5;
   const int nw = (gridDim.x * kThreads) >> 5;
   const int items = a.nsi * a.nsj;
@@ -2278,29 +2290,30 @@ __global__ void __launch_bounds__(kThreads) k_pre_wave(const PreWaveArgs a) {
     const bool own_f = lane >= 2 && I < I1;
     const int c_first = 2 * J0 - 4, c_last = 2 * J1 + 2;  // leading columns marched
     const float* bp = a.b + (size_t)ra;
-    // b queue: q[k] holds column c + k
-    float2 q[kWaveAhead];
+    float2* const mine = &ring[wl][0][lane];
+    // prologue: columns c_first .. c_first + kWaveAhead - 1 (empty groups
+    // past the strip keep the group count per column)
 #pragma unroll
     for (int k = 0; k < kWaveAhead; ++k) {
       const int c = c_first + k;
-      q[k] = c <= c_last ? __ldg(reinterpret_cast<const float2*>(bp + (size_t)c * a.ldb))
-                         : make_float2(0.f, 0.f);
+      if (c <= c_last) cp_async8(mine + k * 32, bp + (size_t)c * a.ldb);
+      cp_async_commit();
     }
-    // stage windows (x = row ra, y = row ra + 1)
+    int slot = 0, fill = kWaveAhead;                      // ring slots of columns c, c + ahead
     float2 b1 = make_float2(0.f, 0.f), b2 = b1, b3 = b1;  // b at c-1, c-2, c-3
     float2 v2a = b1, v2b = b1;                            // v2 at c-2, c-3
     float2 v3a = b1, v3b = b1;                            // v3 at c-3, c-4
     float t1 = 0.f, t2 = 0.f;                             // row-combined r at c-4, c-5
-    auto step = [&](int c) {
-      const float2 b0 = q[0];
-#pragma unroll
-      for (int k = 0; k < kWaveAhead - 1; ++k) q[k] = q[k + 1];
+    for (int c = c_first; c <= c_last; ++c) {
+      cp_async_wait<kWaveAhead - 1>();                    // column c has landed
+      const float2 b0 = mine[slot * 32];
       {
         const int cn = c + kWaveAhead;
-        q[kWaveAhead - 1] = cn <= c_last
-                                ? __ldg(reinterpret_cast<const float2*>(bp + (size_t)cn * a.ldb))
-                                : make_float2(0.f, 0.f);
+        if (cn <= c_last) cp_async8(mine + fill * 32, bp + (size_t)cn * a.ldb);
+        cp_async_commit();
       }
+      slot = slot + 1 == kWaveSlots ? 0 : slot + 1;
+      fill = fill + 1 == kWaveSlots ? 0 : fill + 1;
       // v2 at column c - 1 from b at c - 2, c - 1, c
       float2 v2;
       {
@@ -2349,15 +2362,8 @@ __global__ void __launch_bounds__(kThreads) k_pre_wave(const PreWaveArgs a) {
       b3 = b2;
       b2 = b1;
       b1 = b0;
-    };
-    // blocks of kWaveAhead steps, unrolled so that the window shifts are
-    // register renames; then the remaining steps
-    int c = c_first;
-    for (; c + kWaveAhead - 1 <= c_last; c += kWaveAhead) {
-#pragma unroll
-      for (int u = 0; u < kWaveAhead; ++u) step(c + u);
     }
-    for (; c <= c_last; ++c) step(c);
+    cp_async_wait<0>();   // no copy outlives the strip
   }
 }
 
