@@ -1501,16 +1501,19 @@ struct PreFusedJob {
   T omega;
   const SolveState* st;
   ReduceBuf rb;
-  // ring > 0: only the boundary ring of tiles (first and last tile row and
-  // column; nty = ring's tile rows) is visited, k -> ring_id(k); the interior
-  // tiles are done by the register wave kernel (k_pre_wave)
+  // ring = w > 0: only the boundary ring of tiles w deep (the first and
+  // last w tile rows and columns; nty = tile rows) is visited,
+  // k -> ring_id(k); the interior tiles are done by the register wave kernel
+  // (k_pre_wave)
   int ring, nty;
   __device__ int ring_id(int k) const {
-    if (!ring) return k;
-    if (k < ntx) return k;
-    if (k < 2 * ntx) return (k - ntx) + (nty - 1) * ntx;
-    const int k2 = k - 2 * ntx;
-    return ((k2 & 1) ? ntx - 1 : 0) + (1 + (k2 >> 1)) * ntx;
+    const int w = ring;
+    if (!w) return k;
+    if (k < w * ntx) return k;
+    if (k < 2 * w * ntx) return (k - w * ntx) + (nty - w) * ntx;
+    const int k2 = k - 2 * w * ntx;
+    const int r = k2 % (2 * w);
+    return (r < w ? r : ntx - 2 * w + r) + (w + k2 / (2 * w)) * ntx;
   }
   __device__ bool prepare(Ctx&) const { return st && st->done; }
   __device__ int tiles() const { return ntot; }
@@ -2205,7 +2208,7 @@ static cudaError_t launch_pre_fused_geom(const Operand& b, Grid<T> vout, Grid<T>
                                          const SolveState* st, cudaStream_t s, int ring = 0) {
   const int nc = (nf + 1) / 2;
   const int ntx = ntiles(nc, G::RI), nty = ntiles(nc, G::RJ);
-  const int total = ring ? 2 * ntx + 2 * (nty - 2) : ntx * nty;
+  const int total = ring ? ntx * nty - (ntx - 2 * ring) * (nty - 2 * ring) : ntx * nty;
   const DevOperand<T> db = dev_operand<T>(b);
   CUtensorMap bm{};
   const bool tma = b.tma && make_box_map(bm, b, sizeof(T) == 8, G::BI, G::BJ);
@@ -2445,9 +2448,12 @@ cudaError_t launch_pre_fused(const Operand& b, Grid<T> vout, Grid<T> f, int nf, 
       e = cudaEventRecord(fork, s);
       if (e == cudaSuccess) e = cudaStreamWaitEvent(aux, fork, 0);
     }
+    // the ring is one large tile deep: two of the quarter-size tiles, which
+    // split its serial work four ways
+    static_assert(2 * PreSmall::RI == RTI && 2 * PreSmall::RJ == RTJ, "ring of small tiles");
     if (e == cudaSuccess)
-      e = launch_pre_fused_geom<T, PreLarge>(b, vout, f, nf, sweeps, smoother, omega, kind, st,
-                                             forked ? aux : s, 1);
+      e = launch_pre_fused_geom<T, PreSmall>(b, vout, f, nf, sweeps, smoother, omega, kind, st,
+                                             forked ? aux : s, 2);
     if (forked && e == cudaSuccess) e = cudaEventRecord(join, aux);
     if (e != cudaSuccess) return e;
     e = launch_pre_wave(b, Grid<float>{reinterpret_cast<float*>(vout.p), vout.ld},
