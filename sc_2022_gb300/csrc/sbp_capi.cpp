@@ -87,6 +87,7 @@ struct Level {
   int out = 0;              // buffer holding the V-cycle result
   bool own_b = false;
   cudaEvent_t fork = nullptr, join = nullptr;   // boundary branch of the pre-smoothing
+  cudaEvent_t pfork = nullptr, pjoin = nullptr; // and of the post-smoothing
 };
 
 }  // namespace
@@ -208,7 +209,7 @@ cudaError_t enqueue_vcycle(sbp_solver* s, size_t l, bool dot, SolveState* st, cu
     e = enqueue_vcycle<T>(s, l + 1, false, st, q);
     if (e != cudaSuccess) return e;
     e = launch_post_fused<T>(L.ov[0], C.ov[C.out], L.ob, grid<T>(L.v[1], L.ld), n, o.nu_post, sm,
-                             om, dot ? 1 : 0, st, s->rb, q);
+                             om, dot ? 1 : 0, st, s->rb, q, s->aux, L.pfork, L.pjoin);
     L.out = 1;
     return e;
   }
@@ -254,7 +255,7 @@ long long vcycle_launches(const sbp_solver* s, bool dot) {
     const int n = s->levels[l].n;
     if (mixed ? use_fused<float>(s, n) : use_fused<double>(s, n)) {
       // fused pre-smoothing (one or two kernels), fused post-smoothing
-      c += pre_fused_launches(n, o.nu_pre, mixed) + 1;
+      c += pre_fused_launches(n, o.nu_pre, mixed) + post_fused_launches(n, o.nu_post, mixed);
       continue;
     }
     c += (o.nu_pre >= 2) ? 1 + (o.nu_pre - 2) : 1;
@@ -752,6 +753,12 @@ int sbp_solver_create(sbp_solver** out, int n, const sbp_options* opts) {
         SBP_CUDA(cudaEventCreateWithFlags(&B.join, cudaEventDisableTiming));
         if (!s->aux) SBP_CUDA(cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking));
       }
+      if (mixed && post_fused_launches(m, s->opts.nu_post, true) == 2) {
+        Level& B = s->levels.back();
+        SBP_CUDA(cudaEventCreateWithFlags(&B.pfork, cudaEventDisableTiming));
+        SBP_CUDA(cudaEventCreateWithFlags(&B.pjoin, cudaEventDisableTiming));
+        if (!s->aux) SBP_CUDA(cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking));
+      }
       if (m == s->opts.coarse_n) break;
       m = (m + 1) / 2;
     }
@@ -790,8 +797,8 @@ int sbp_solver_destroy(sbp_solver* s) {
   for (auto& e : s->ev)
     if (e) cudaEventDestroy(e);
   for (Level& L : s->levels) {
-    if (L.fork) cudaEventDestroy(L.fork);
-    if (L.join) cudaEventDestroy(L.join);
+    for (cudaEvent_t ev : {L.fork, L.join, L.pfork, L.pjoin})
+      if (ev) cudaEventDestroy(ev);
   }
   delete s;
   return SBP_OK;

@@ -152,6 +152,7 @@ struct SolveState {
   int done;         // 1 = converged, 2 = breakdown/non-finite, 3 = max iter
   int maxiter;
   int pad;
+  double rz_part;   // r.z over the boundary tiles of a split post-smoothing pass
 };
 
 constexpr int kDoneConverged = 1;

@@ -1727,12 +1727,26 @@ struct PostFusedJob {
   T omega;
   SolveState* st;
   ReduceBuf rb;
+  // ring = w > 0: only the boundary ring of tiles w deep is visited (the
+  // interior is done by k_post_wave); partial: the dot's total goes to
+  // st->rz_part for k_post_wave to finish
+  int ring, nty, partial;
+  __device__ int ring_id(int k) const {
+    const int w = ring;
+    if (!w) return k;
+    if (k < w * ntx) return k;
+    if (k < 2 * w * ntx) return (k - w * ntx) + (nty - w) * ntx;
+    const int k2 = k - 2 * w * ntx;
+    const int r = k2 % (2 * w);
+    return (r < w ? r : ntx - 2 * w + r) + (w + k2 / (2 * w)) * ntx;
+  }
   __device__ bool prepare(Ctx&) const { return st && st->done; }
   __device__ int tiles() const { return ntot; }
   __device__ unsigned tx_bytes(int) const {
     return TMA ? 2u * box_bytes<T, Geo::BI, Geo::BJ>() + box_bytes<T, Geo::CI, Geo::CJ>() : 0u;
   }
-  __device__ void issue(unsigned char* buf, unsigned long long* bar, int id, const Ctx&) const {
+  __device__ void issue(unsigned char* buf, unsigned long long* bar, int k, const Ctx&) const {
+    const int id = ring_id(k);
     const int ti = id % ntx;
     const int jl = tile_at<Geo::TI, Geo::TJ>(id, ntx, n).j_lo;
     const int x0 = Geo::TI * ti - 4;
@@ -1826,9 +1840,10 @@ struct PostFusedJob {
                                              });
   }
 
-  __device__ void compute(unsigned char* buf, int id, Acc& acc, const Ctx&,
+  __device__ void compute(unsigned char* buf, int k, Acc& acc, const Ctx&,
                           unsigned char* scr) const {
     constexpr int BW = Geo::BI, CW = Geo::CI;   // box row lengths
+    const int id = ring_id(k);
     const Tile<Geo::TI, Geo::TJ> t = tile_at<Geo::TI, Geo::TJ>(id, ntx, n);
     const int ti = id % ntx;
     const int X0 = Geo::TI * ti - 4, Y0 = t.j_lo - 4;
@@ -1901,6 +1916,10 @@ struct PostFusedJob {
     }
   }
   __device__ void finish(double tot) const {
+    if (partial) {
+      st->rz_part = tot;
+      return;
+    }
     if (!isfinite(tot)) {
       st->done = kDoneBreakdown;
     } else {
@@ -2470,9 +2489,9 @@ template <typename T, class G>
 static cudaError_t launch_post_fused_geom(const Operand& vin, const Operand& e, const Operand& b,
                                           Grid<T> vout, int n, int sweeps, int smoother,
                                           double omega, int dot, SolveState* st, ReduceBuf rb,
-                                          cudaStream_t s) {
+                                          cudaStream_t s, int ring = 0, int partial = 0) {
   const int ntx = ntiles(n, G::TI), nty = ntiles(n, G::TJ);
-  const int total = ntx * nty;
+  const int total = ring ? ntx * nty - (ntx - 2 * ring) * (nty - 2 * ring) : ntx * nty;
   const bool f64 = sizeof(T) == 8;
   CUtensorMap vm{}, bm{}, em{};
   const bool tma = vin.tma && b.tma && e.tma && make_box_map(vm, vin, f64, G::BI, G::BJ) &&
@@ -2480,7 +2499,8 @@ static cudaError_t launch_post_fused_geom(const Operand& vin, const Operand& e, 
   const DevOperand<T> dv = dev_operand<T>(vin), de = dev_operand<T>(e), db = dev_operand<T>(b);
 #define SBP_POST(D, M)                                                                           \
   return launch_persist(PostFusedJob<T, D, M, G>{dv, de, db, vm, bm, em, vout, n, ntx, total,   \
-                                                 sweeps, smoother, T(omega), st, rb},            \
+                                                 sweeps, smoother, T(omega), st, rb, ring, nty,  \
+                                                 partial},                                      \
                         total, s)
   if (dot) {
     if (tma) SBP_POST(true, true);
@@ -2491,14 +2511,281 @@ static cudaError_t launch_post_fused_geom(const Operand& vin, const Operand& e, 
 #undef SBP_POST
 }
 
+// ---------------------------------------------------------------------------
+// Register wave post-smoothing for the interior of a fine level (FP32,
+// prolongation of the coarse correction + three sweeps, optional b.v dot),
+// the job of PostFusedJob's interior tiles without shared-memory sweeps or
+// block barriers.  A warp owns a strip of up to 56 fine rows x 64 fine
+// columns of the interior rectangle [Ra, Rb) x [Ca, Cb) (the union of the
+// PostLarge tiles outside the first and last tile rows and columns).  Lane l
+// holds fine rows rb0 + 2l (even: coarse row rb0/2 + l) and rb0 + 2l + 1;
+// the warp marches along j:
+//   step c: F0 = v_in + P e at column c, sweep 1 at c - 1, sweep 2 at
+//           c - 2, sweep 3 at c - 3 (final: stored, and b.v accumulated).
+// The odd row of a lane interpolates its coarse row and the next lane's; an
+// odd column averages the coarse columns on either side.  v_in and b come
+// through per-lane cp.async rings kPostAhead columns ahead; e (coarse) is
+// loaded two coarse columns ahead.  Arithmetic order as in the interior
+// path of PostFusedJob.
+// ---------------------------------------------------------------------------
+constexpr int kPostRows = 56;
+constexpr int kPostCols = 64;
+constexpr int kPostAhead = 8;
+constexpr int kPostSlots = kPostAhead + 1;
+
+struct PostWaveArgs {
+  const float* vin;
+  int ldv;
+  const float* b;
+  int ldb;
+  const float* e;
+  int lde;
+  float* vout;
+  int ldo;
+  int n, Ra, Rb, Ca, Cb, nsi, nsj;
+  float m;
+  SolveState* st;
+  ReduceBuf rb;
+};
+
+template <bool DOT>
+__global__ void __launch_bounds__(kThreads) k_post_wave(const PostWaveArgs a) {
+  __shared__ __align__(16) float2 vring[kWarps][kPostSlots][32];
+  __shared__ __align__(16) float2 bring[kWarps][kPostSlots][32];
+  pdl_begin();
+  if (a.st && a.st->done) return;   // uniform: the state was final before this launch
+  const int lane = threadIdx.x & 31;
+  const int wl = threadIdx.x >> 5;
+  const int gw = (blockIdx.x * kThreads + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * kThreads) >> 5;
+  const int items = a.nsi * a.nsj;
+  const unsigned FULL = 0xffffffffu;
+  const float m = a.m;
+  DotAcc<float> acc;
+  for (int it = gw; it < items; it += nw) {
+    const int si = it % a.nsi, sj = it / a.nsi;
+    const int rb0 = (a.Ra & ~1) - 4 + kPostRows * si;   // even
+    const int r_lo = max(rb0 + 4, a.Ra), r_hi = min(rb0 + 4 + kPostRows, a.Rb);
+    const int c0 = a.Ca + kPostCols * sj;
+    const int c1 = min(c0 + kPostCols, a.Cb);
+    const int ra = rb0 + 2 * lane;
+    const bool own_x = ra >= r_lo && ra < r_hi;
+    const bool own_y = ra + 1 >= r_lo && ra + 1 < r_hi;
+    const int er = (rb0 >> 1) + lane;                       // this lane's coarse row
+    const int c_first = c0 - 3, c_last = c1 + 2;
+    const float* vp = a.vin + (size_t)ra;
+    const float* bp = a.b + (size_t)ra;
+    const float* ep = a.e + (size_t)er;
+    float2* const vmine = &vring[wl][0][lane];
+    float2* const bmine = &bring[wl][0][lane];
+#pragma unroll
+    for (int k = 0; k < kPostAhead; ++k) {
+      const int c = c_first + k;
+      if (c <= c_last) {
+        cp_async8(vmine + k * 32, vp + (size_t)c * a.ldv);
+        cp_async8(bmine + k * 32, bp + (size_t)c * a.ldb);
+      }
+      cp_async_commit();
+    }
+    int slot = 0, fill = kPostAhead;
+    // row-interpolated coarse values of columns J = c >> 1 and J + 1
+    auto rv = [&](float ev) {
+      const float en = __shfl_down_sync(FULL, ev, 1);    // coarse row er + 1
+      return make_float2(ev, fmaf(0.5f, en, 0.5f * ev));
+    };
+    int J = c_first >> 1;
+    float2 rvc = rv(__ldg(ep + (size_t)J * a.lde));
+    float2 rvn = rv(__ldg(ep + (size_t)(J + 1) * a.lde));
+    float epre = __ldg(ep + (size_t)(J + 2) * a.lde);
+    float2 f1 = make_float2(0.f, 0.f), f2 = f1;             // F0 at c-1, c-2
+    float2 w1a = f1, w1b = f1;                              // sweep 1 at c-2, c-3
+    float2 w2a = f1, w2b = f1;                              // sweep 2 at c-3, c-4
+    float2 b1 = f1, b2 = f1, b3 = f1;                       // b at c-1, c-2, c-3
+    for (int c = c_first; c <= c_last; ++c) {
+      cp_async_wait<kPostAhead - 1>();                      // column c has landed
+      const float2 vi = vmine[slot * 32];
+      const float2 b0 = bmine[slot * 32];
+      {
+        const int cn = c + kPostAhead;
+        if (cn <= c_last) {
+          cp_async8(vmine + fill * 32, vp + (size_t)cn * a.ldv);
+          cp_async8(bmine + fill * 32, bp + (size_t)cn * a.ldb);
+        }
+        cp_async_commit();
+      }
+      slot = slot + 1 == kPostSlots ? 0 : slot + 1;
+      fill = fill + 1 == kPostSlots ? 0 : fill + 1;
+      if (!(c & 1) && c != c_first) {                       // next coarse column
+        ++J;
+        rvc = rvn;
+        rvn = rv(epre);
+        epre = __ldg(ep + (size_t)(J + 2) * a.lde);
+      }
+      float2 f0;
+      if (c & 1) {
+        f0.x = vi.x + 0.5f * (rvc.x + rvn.x);
+        f0.y = vi.y + 0.5f * (rvc.y + rvn.y);
+      } else {
+        f0.x = vi.x + rvc.x;
+        f0.y = vi.y + rvc.y;
+      }
+      // sweep 1 at column c - 1
+      float2 w1;
+      {
+        const float up = __shfl_up_sync(FULL, f1.y, 1);
+        const float dn = __shfl_down_sync(FULL, f1.x, 1);
+        w1.x = fmaf(m, b1.x + (((up + f1.y) + (f2.x + f0.x)) - 4.f * f1.x), f1.x);
+        w1.y = fmaf(m, b1.y + (((f1.x + dn) + (f2.y + f0.y)) - 4.f * f1.y), f1.y);
+      }
+      // sweep 2 at column c - 2
+      float2 w2;
+      {
+        const float up = __shfl_up_sync(FULL, w1a.y, 1);
+        const float dn = __shfl_down_sync(FULL, w1a.x, 1);
+        w2.x = fmaf(m, b2.x + (((up + w1a.y) + (w1b.x + w1.x)) - 4.f * w1a.x), w1a.x);
+        w2.y = fmaf(m, b2.y + (((w1a.x + dn) + (w1b.y + w1.y)) - 4.f * w1a.y), w1a.y);
+      }
+      // sweep 3 at column c - 3: final
+      {
+        const float up = __shfl_up_sync(FULL, w2a.y, 1);
+        const float dn = __shfl_down_sync(FULL, w2a.x, 1);
+        float2 w3;
+        w3.x = fmaf(m, b3.x + (((up + w2a.y) + (w2b.x + w2.x)) - 4.f * w2a.x), w2a.x);
+        w3.y = fmaf(m, b3.y + (((w2a.x + dn) + (w2b.y + w2.y)) - 4.f * w2a.y), w2a.y);
+        const int cw = c - 3;
+        if (cw >= c0 && cw < c1) {
+          float* o = a.vout + (size_t)cw * a.ldo + ra;
+          if (own_x && own_y) {
+            *reinterpret_cast<float2*>(o) = w3;
+          } else {
+            if (own_x) o[0] = w3.x;
+            if (own_y) o[1] = w3.y;
+          }
+          if (DOT) {
+            if (own_x) acc.add_prod(b3.x, w3.x);
+            if (own_y) acc.add_prod(b3.y, w3.y);
+          }
+        }
+      }
+      w2b = w2a;
+      w2a = w2;
+      w1b = w1a;
+      w1a = w1;
+      f2 = f1;
+      f1 = f0;
+      b3 = b2;
+      b2 = b1;
+      b1 = b0;
+    }
+    cp_async_wait<0>();   // no copy outlives the strip
+  }
+  if (DOT)
+    grid_reduce(acc.value(), a.rb, [&](double tot) {
+      // the boundary tiles' share, left by the staged pass that ran first
+      tot += a.st->rz_part;
+      SolveState* st = a.st;
+      if (!isfinite(tot)) {
+        st->done = kDoneBreakdown;
+      } else {
+        st->rz_new = tot;
+        if (st->iter > 0) st->beta = tot / st->rz;
+        st->rz = tot;
+      }
+    });
+}
+
+// The interior rectangle of the PostLarge tiling (fine coordinates).
+static bool post_wave_rect(int n, int& Ra, int& Rb, int& Ca, int& Cb) {
+  const int ntx = ntiles(n, TI), nty = ntiles(n, TJ);
+  if (ntx < 3 || nty < 3) return false;
+  if ((n - 1) % TI != 0 || (n - 1) % TJ != 0) return false;   // full tiles only
+  Ra = TI + 1;
+  Rb = TI * (ntx - 1) + 1;
+  Ca = TJ + 1;
+  Cb = TJ * (nty - 1) + 1;
+  return Ra < Rb && Ca < Cb;
+}
+
+int post_fused_launches(int n, int sweeps, bool f32) {
+  int Ra, Rb, Ca, Cb;
+  if (f32 && sweeps == 3 && !small_fused_tiles((n + 1) / 2) && post_wave_rect(n, Ra, Rb, Ca, Cb))
+    return 2;
+  return 1;
+}
+
 template <typename T>
 cudaError_t launch_post_fused(const Operand& vin, const Operand& e, const Operand& b, Grid<T> vout,
                               int n, int sweeps, int smoother, double omega, int dot,
-                              SolveState* st, ReduceBuf rb, cudaStream_t s) {
+                              SolveState* st, ReduceBuf rb, cudaStream_t s, cudaStream_t aux,
+                              cudaEvent_t fork, cudaEvent_t join) {
   if (sweeps < 0 || sweeps > kMaxFusedSweeps || (dot && !st)) return cudaErrorInvalidValue;
   if (small_fused_tiles((n + 1) / 2))
     return launch_post_fused_geom<T, PostSmall>(vin, e, b, vout, n, sweeps, smoother, omega, dot,
                                                 st, rb, s);
+  int Ra, Rb, Ca, Cb;
+  if (std::is_same<T, float>::value && sweeps == 3 && !recorder_slot() && vin.ld % 2 == 0 &&
+      b.ld % 2 == 0 && vout.ld % 2 == 0 && ((uintptr_t)vin.p & 7u) == 0 &&
+      ((uintptr_t)b.p & 7u) == 0 && ((uintptr_t)vout.p & 7u) == 0 &&
+      post_wave_rect(n, Ra, Rb, Ca, Cb)) {
+    static_assert(2 * PostSmall::TI == TI && 2 * PostSmall::TJ == TJ, "ring of small tiles");
+    // the boundary ring (two quarter-size tiles deep) by the staged job: on
+    // a forked branch without the dot; before the wave with it (the wave
+    // finishes the reduction with the ring's share)
+    const bool forked = !dot && aux && fork && join;
+    cudaError_t e2 = cudaSuccess;
+    if (forked) {
+      e2 = cudaEventRecord(fork, s);
+      if (e2 == cudaSuccess) e2 = cudaStreamWaitEvent(aux, fork, 0);
+    }
+    if (e2 == cudaSuccess)
+      e2 = launch_post_fused_geom<T, PostSmall>(vin, e, b, vout, n, sweeps, smoother, omega, dot,
+                                                st, rb, forked ? aux : s, 2, dot ? 1 : 0);
+    if (forked && e2 == cudaSuccess) e2 = cudaEventRecord(join, aux);
+    if (e2 != cudaSuccess) return e2;
+    PostWaveArgs a;
+    a.vin = static_cast<const float*>(vin.p);
+    a.ldv = vin.ld;
+    a.b = static_cast<const float*>(b.p);
+    a.ldb = b.ld;
+    a.e = static_cast<const float*>(e.p);
+    a.lde = e.ld;
+    a.vout = reinterpret_cast<float*>(vout.p);
+    a.ldo = vout.ld;
+    a.n = n;
+    a.Ra = Ra;
+    a.Rb = Rb;
+    a.Ca = Ca;
+    a.Cb = Cb;
+    a.nsi = (Rb - (Ra & ~1) + kPostRows - 1) / kPostRows;   // strips own from Ra & ~1 on
+    a.nsj = (Cb - Ca + kPostCols - 1) / kPostCols;
+    a.m = (smoother == kSmoothJacobi) ? (float)omega * 0.25f : (float)omega;
+    a.st = st;
+    a.rb = rb;
+    static const int per_sm[2] = {
+        [] {
+          int v = 0;
+          if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_post_wave<false>, kThreads, 0) !=
+                  cudaSuccess ||
+              v < 1)
+            v = 1;
+          return v;
+        }(),
+        [] {
+          int v = 0;
+          if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_post_wave<true>, kThreads, 0) !=
+                  cudaSuccess ||
+              v < 1)
+            v = 1;
+          return v;
+        }()};
+    const int items = a.nsi * a.nsj;
+    const int grid =
+        std::max(1, std::min((items + kWarps - 1) / kWarps, sm_count() * per_sm[dot ? 1 : 0]));
+    e2 = dot ? launch_pdl(k_post_wave<true>, dim3(grid), dim3(kThreads), 0, s, a)
+             : launch_pdl(k_post_wave<false>, dim3(grid), dim3(kThreads), 0, s, a);
+    if (forked && e2 == cudaSuccess) e2 = cudaStreamWaitEvent(s, join, 0);
+    return e2;
+  }
   return launch_post_fused_geom<T, PostLarge>(vin, e, b, vout, n, sweeps, smoother, omega, dot,
                                               st, rb, s);
 }
@@ -3057,7 +3344,8 @@ SBP_INST_T(float)
                                            cudaStream_t, cudaEvent_t, cudaEvent_t);              \
   template cudaError_t launch_post_fused<T>(const Operand&, const Operand&, const Operand&,      \
                                             Grid<T>, int, int, int, double, int, SolveState*,    \
-                                            ReduceBuf, cudaStream_t);                            \
+                                            ReduceBuf, cudaStream_t, cudaStream_t, cudaEvent_t,  \
+                                            cudaEvent_t);                                        \
   template cudaError_t launch_apply_op<T>(const Operand&, Grid<T>, int, int, ReduceBuf, double*, \
                                           cudaStream_t);                                         \
   template cudaError_t launch_smooth_op<T>(int, int, const Operand&, const Operand&,             \
