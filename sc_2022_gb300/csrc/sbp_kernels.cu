@@ -2265,7 +2265,6 @@ static cudaError_t launch_pre_fused_geom(const Operand& b, Grid<T> vout, Grid<T>
 // formed in the same order as PreFusedJob's interior path.
 // ---------------------------------------------------------------------------
 constexpr int kWaveRows = 28;     // coarse rows of a strip
-constexpr int kWaveCols = 32;     // coarse columns of a strip (at most)
 constexpr int kWaveAhead = 16;    // columns of b in flight per warp
 constexpr int kWaveSlots = kWaveAhead + 1;   // per-warp ring of b columns
 
@@ -2276,10 +2275,30 @@ struct PreWaveArgs {
   int ldv;
   float* f;
   int ldf;
-  int nf, Ia, Ib, Ja, Jb, nsi, nsj;
+  int nf, Ia, Ib, Ja, Jb, nsi, nsj, cols;   // cols: coarse columns of a strip
   float m, k1, m2, sc;
   const SolveState* st;
 };
+
+// Strip width (columns of a strip, from `cands`) that minimises the march
+// steps of the busiest warp: rounds of strips per warp x steps per strip
+// (fill + width x per_col).
+static int best_strip_cols(int rows_strips, int cols_total, int warps, const int* cands, int nc,
+                           int fill, int per_col) {
+  long long best = -1;
+  int pick = cands[0];
+  for (int k = 0; k < nc; ++k) {
+    const int w = cands[k];
+    const long long items = (long long)rows_strips * ((cols_total + w - 1) / w);
+    const long long rounds = (items + warps - 1) / warps;
+    const long long cost = rounds * (fill + (long long)per_col * w);
+    if (best < 0 || cost < best) {
+      best = cost;
+      pick = w;
+    }
+  }
+  return pick;
+}
 
 __device__ __forceinline__ void cp_async8(void* sdst, const void* gsrc) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_u32(sdst)), "l"(gsrc)
@@ -2304,8 +2323,8 @@ __global__ void __launch_bounds__(kThreads) k_pre_wave(const PreWaveArgs a) {
     const int si = it % a.nsi, sj = it / a.nsi;
     const int I0 = a.Ia + kWaveRows * si;
     const int I1 = min(I0 + kWaveRows, a.Ib);
-    const int J0 = a.Ja + kWaveCols * sj;
-    const int J1 = min(J0 + kWaveCols, a.Jb);
+    const int J0 = a.Ja + a.cols * sj;
+    const int J1 = min(J0 + a.cols, a.Jb);
     const int ra = 2 * I0 - 4 + 2 * lane;               // this lane's first fine row
     const bool own_rows = lane >= 2 && ra + 1 <= 2 * I1 - 1;
     const int I = I0 + lane - 2;                          // coarse row centred on ra
@@ -2418,7 +2437,6 @@ static cudaError_t launch_pre_wave(const Operand& b, Grid<float> vout, Grid<floa
   a.Ja = Ja;
   a.Jb = Jb;
   a.nsi = (Ib - Ia + kWaveRows - 1) / kWaveRows;
-  a.nsj = (Jb - Ja + kWaveCols - 1) / kWaveCols;
   const float m = (smoother == kSmoothJacobi) ? (float)omega * 0.25f : (float)omega;
   a.m = m;
   a.k1 = 2.f * m - 4.f * m * m;
@@ -2432,6 +2450,9 @@ static cudaError_t launch_pre_wave(const Operand& b, Grid<float> vout, Grid<floa
       v = 1;
     return v;
   }();
+  static const int cands[] = {8, 12, 16, 24, 32};   // coarse columns
+  a.cols = best_strip_cols(a.nsi, Jb - Ja, sm_count() * per_sm * kWarps, cands, 5, 7, 2);
+  a.nsj = (Jb - Ja + a.cols - 1) / a.cols;
   const int items = a.nsi * a.nsj;
   const int grid = std::max(1, std::min((items + kWarps - 1) / kWarps, sm_count() * per_sm));
   return launch_pdl(k_pre_wave, dim3(grid), dim3(kThreads), 0, s, a);
@@ -2529,7 +2550,6 @@ static cudaError_t launch_post_fused_geom(const Operand& vin, const Operand& e, 
 // path of PostFusedJob.
 // ---------------------------------------------------------------------------
 constexpr int kPostRows = 56;
-constexpr int kPostCols = 64;
 constexpr int kPostAhead = 8;
 constexpr int kPostSlots = kPostAhead + 1;
 
@@ -2542,14 +2562,14 @@ struct PostWaveArgs {
   int lde;
   float* vout;
   int ldo;
-  int n, Ra, Rb, Ca, Cb, nsi, nsj;
+  int n, Ra, Rb, Ca, Cb, nsi, nsj, cols;   // cols: fine columns of a strip
   float m;
   SolveState* st;
   ReduceBuf rb;
 };
 
 template <bool DOT>
-__global__ void __launch_bounds__(kThreads) k_post_wave(const PostWaveArgs a) {
+__global__ void __launch_bounds__(kThreads, 4) k_post_wave(const PostWaveArgs a) {
   __shared__ __align__(16) float2 vring[kWarps][kPostSlots][32];
   __shared__ __align__(16) float2 bring[kWarps][kPostSlots][32];
   pdl_begin();
@@ -2566,8 +2586,8 @@ __global__ void __launch_bounds__(kThreads) k_post_wave(const PostWaveArgs a) {
     const int si = it % a.nsi, sj = it / a.nsi;
     const int rb0 = (a.Ra & ~1) - 4 + kPostRows * si;   // even
     const int r_lo = max(rb0 + 4, a.Ra), r_hi = min(rb0 + 4 + kPostRows, a.Rb);
-    const int c0 = a.Ca + kPostCols * sj;
-    const int c1 = min(c0 + kPostCols, a.Cb);
+    const int c0 = a.Ca + a.cols * sj;
+    const int c1 = min(c0 + a.cols, a.Cb);
     const int ra = rb0 + 2 * lane;
     const bool own_x = ra >= r_lo && ra < r_hi;
     const bool own_y = ra + 1 >= r_lo && ra + 1 < r_hi;
@@ -2757,7 +2777,6 @@ cudaError_t launch_post_fused(const Operand& vin, const Operand& e, const Operan
     a.Ca = Ca;
     a.Cb = Cb;
     a.nsi = (Rb - (Ra & ~1) + kPostRows - 1) / kPostRows;   // strips own from Ra & ~1 on
-    a.nsj = (Cb - Ca + kPostCols - 1) / kPostCols;
     a.m = (smoother == kSmoothJacobi) ? (float)omega * 0.25f : (float)omega;
     a.st = st;
     a.rb = rb;
@@ -2778,6 +2797,10 @@ cudaError_t launch_post_fused(const Operand& vin, const Operand& e, const Operan
             v = 1;
           return v;
         }()};
+    static const int cands[] = {16, 24, 32, 48, 64};   // fine columns
+    a.cols = best_strip_cols(a.nsi, Cb - Ca, sm_count() * per_sm[dot ? 1 : 0] * kWarps, cands, 5,
+                             6, 1);
+    a.nsj = (Cb - Ca + a.cols - 1) / a.cols;
     const int items = a.nsi * a.nsj;
     const int grid =
         std::max(1, std::min((items + kWarps - 1) / kWarps, sm_count() * per_sm[dot ? 1 : 0]));
