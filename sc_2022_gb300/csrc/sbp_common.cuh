@@ -152,7 +152,13 @@ struct SolveState {
   int done;         // 1 = converged, 2 = breakdown/non-finite, 3 = max iter
   int maxiter;
   int pad;
-  double rz_part;   // r.z over the boundary tiles of a split post-smoothing pass
+  // r.z of a post-smoothing pass split between the boundary tiles and the
+  // interior wave (running concurrently): each side leaves its share and
+  // counts in; the second to arrive finishes (ring + wave, in that order)
+  double rz_part;
+  double rz_wave;
+  unsigned join;
+  int pad2;
 };
 
 constexpr int kDoneConverged = 1;

@@ -1690,6 +1690,31 @@ struct PreFusedJob {
   __device__ void finish(double) const {}
 };
 
+// The end of the preconditioner's r.z reduction: beta and rz.
+__device__ __forceinline__ void finish_rz(SolveState* st, double tot) {
+  if (!isfinite(tot)) {
+    st->done = kDoneBreakdown;
+  } else {
+    st->rz_new = tot;
+    if (st->iter > 0) st->beta = tot / st->rz;
+    st->rz = tot;
+  }
+}
+
+// One side of an r.z split between two concurrent kernels (the boundary
+// tiles and the interior wave of a post-smoothing pass): called once by each
+// side after its own reduction; the second side to arrive finishes with
+// ring + wave (fixed order) and re-arms the counter.
+__device__ __forceinline__ void rz_join(SolveState* st, double* mine, double tot) {
+  *mine = tot;
+  __threadfence();
+  if (atomicAdd(&st->join, 1u) == 1u) {
+    __threadfence();
+    finish_rz(st, __ldcg(&st->rz_part) + __ldcg(&st->rz_wave));
+    st->join = 0u;
+  }
+}
+
 // Prolongation + post-smoothing (S sweeps).  Fine tiles TI x TJ; boxes of
 // v_in and b: BI x BJ at (TI ti - 4, j_lo - 4); coarse e: CI x CJ at
 // (TI/2 ti - 4, (j_lo - 4) >> 1).  With S <= 3 the swept region reaches box
@@ -1916,17 +1941,10 @@ struct PostFusedJob {
     }
   }
   __device__ void finish(double tot) const {
-    if (partial) {
-      st->rz_part = tot;
-      return;
-    }
-    if (!isfinite(tot)) {
-      st->done = kDoneBreakdown;
-    } else {
-      st->rz_new = tot;
-      if (st->iter > 0) st->beta = tot / st->rz;
-      st->rz = tot;
-    }
+    if (partial)
+      rz_join(st, &st->rz_part, tot);
+    else
+      finish_rz(st, tot);
   }
 };
 
@@ -2550,6 +2568,8 @@ static cudaError_t launch_post_fused_geom(const Operand& vin, const Operand& e, 
 // path of PostFusedJob.
 // ---------------------------------------------------------------------------
 constexpr int kPostRows = 56;
+constexpr int kRingPartialsOffset = 2080;
+static_assert(kRingPartialsOffset + 2080 <= kMaxPersistCtas + 64, "split partials buffer");
 constexpr int kPostAhead = 8;
 constexpr int kPostSlots = kPostAhead + 1;
 
@@ -2699,19 +2719,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_post_wave(const PostWaveArgs a)
     }
     cp_async_wait<0>();   // no copy outlives the strip
   }
-  if (DOT)
-    grid_reduce(acc.value(), a.rb, [&](double tot) {
-      // the boundary tiles' share, left by the staged pass that ran first
-      tot += a.st->rz_part;
-      SolveState* st = a.st;
-      if (!isfinite(tot)) {
-        st->done = kDoneBreakdown;
-      } else {
-        st->rz_new = tot;
-        if (st->iter > 0) st->beta = tot / st->rz;
-        st->rz = tot;
-      }
-    });
+  // the boundary tiles' share comes from the staged pass running beside
+  if (DOT) grid_reduce(acc.value(), a.rb, [&](double tot) { rz_join(a.st, &a.st->rz_wave, tot); });
 }
 
 // The interior rectangle of the PostLarge tiling (fine coordinates).
@@ -2748,18 +2757,22 @@ cudaError_t launch_post_fused(const Operand& vin, const Operand& e, const Operan
       ((uintptr_t)b.p & 7u) == 0 && ((uintptr_t)vout.p & 7u) == 0 &&
       post_wave_rect(n, Ra, Rb, Ca, Cb)) {
     static_assert(2 * PostSmall::TI == TI && 2 * PostSmall::TJ == TJ, "ring of small tiles");
-    // the boundary ring (two quarter-size tiles deep) by the staged job: on
-    // a forked branch without the dot; before the wave with it (the wave
-    // finishes the reduction with the ring's share)
-    const bool forked = !dot && aux && fork && join;
+    // the boundary ring (two quarter-size tiles deep) by the staged job on a
+    // forked branch; with the dot, the two reductions meet in rz_join
+    const bool forked = aux && fork && join;
     cudaError_t e2 = cudaSuccess;
     if (forked) {
       e2 = cudaEventRecord(fork, s);
       if (e2 == cudaSuccess) e2 = cudaStreamWaitEvent(aux, fork, 0);
     }
+    // the two reductions run at the same time: the ring takes the upper half
+    // of the partials buffer (a solver's holds max_reduce_ctas(n) + 64 >=
+    // 4160 slots; neither grid exceeds SMs x 8 = 1216 CTAs) and its own ticket
+    const ReduceBuf rb_ring{rb.partials ? rb.partials + kRingPartialsOffset : nullptr,
+                            rb.ticket ? rb.ticket + 8 : nullptr};
     if (e2 == cudaSuccess)
       e2 = launch_post_fused_geom<T, PostSmall>(vin, e, b, vout, n, sweeps, smoother, omega, dot,
-                                                st, rb, forked ? aux : s, 2, dot ? 1 : 0);
+                                                st, rb_ring, forked ? aux : s, 2, dot ? 1 : 0);
     if (forked && e2 == cudaSuccess) e2 = cudaEventRecord(join, aux);
     if (e2 != cudaSuccess) return e2;
     PostWaveArgs a;
