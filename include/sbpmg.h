@@ -75,7 +75,7 @@ typedef struct sbp_options {
   int nu_pre;       /* pre-smoothing sweeps */
   int nu_post;      /* post-smoothing sweeps */
   int restriction;  /* sbp_restriction */
-  int coarse_n;     /* grid size of the direct coarse solve (<= 257) */
+  int coarse_n;     /* grid size of the direct coarse solve (<= 1025) */
   int precision;    /* sbp_precision */
   int reserved[5];
 } sbp_options;
@@ -102,7 +102,8 @@ void sbp_options_default(sbp_options* opts);
 /* The reference's own two-level GPU preconditioner
  * (matrix_free_Two_level_multigrid, matrix_free_mg_cg.jl:143-176):
  * Richardson omega = 0.15, nu = 3 + 3, NORMAL restriction, exact coarse
- * solve at (n+1)/2.  Requires (n+1)/2 <= 257. */
+ * solve at (n+1)/2.  Requires (n+1)/2 <= 1025 (n <= 2049); coarse grids
+ * above 257 compute their eigenbases on the GPU at handle creation. */
 void sbp_options_reference_two_level(sbp_options* opts, int n);
 
 /* ---- single-grid operators (no handle) ------------------------------- */

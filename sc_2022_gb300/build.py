@@ -73,7 +73,8 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         raise RuntimeError("nvcc failed:\n" + "\n".join(errors))
     if force or procs or not LIB.exists() or any(o.stat().st_mtime > LIB.stat().st_mtime for o in objs):
         tmp = LIB.with_suffix(".so.tmp")
-        cmd = [cc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart", "-lpthread",
+        cmd = [cc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart", "-lcusolver",
+               "-lpthread",
                "-Xlinker", "--no-undefined"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

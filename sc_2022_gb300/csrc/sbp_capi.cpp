@@ -680,7 +680,7 @@ int sbp_solver_create(sbp_solver** out, int n, const sbp_options* opts) {
     sbp_options& o = s->opts;
     if (o.omega <= 0.0) o.omega = (o.smoother == SBP_SMOOTH_JACOBI) ? 2.0 / 3.0 : 0.15;
     if (!valid_mg_n(n) || !valid_mg_n(o.coarse_n) || o.coarse_n > n) return SBP_ERR_ARGS;
-    if (o.coarse_n > 257) return SBP_ERR_UNSUPPORTED;  // limit of the coarse factors
+    if (o.coarse_n > kCoarseMaxN) return SBP_ERR_UNSUPPORTED;  // limit of the coarse factors
     if (o.nu_pre < 1 || o.nu_post < 0 || o.nu_pre > 64 || o.nu_post > 64) return SBP_ERR_UNSUPPORTED;
     if (o.smoother != SBP_SMOOTH_JACOBI && o.smoother != SBP_SMOOTH_RICHARDSON) return SBP_ERR_ARGS;
     if (o.restriction < 0 || o.restriction > 2) return SBP_ERR_ARGS;

@@ -6,6 +6,9 @@
 // GPU solve is four small matrix products instead of a sparse triangular
 // solve.  The 1D operators are checked, coefficient by coefficient, against
 // the stencil negA that every kernel applies.
+#include <cuda_runtime.h>
+#include <cusolverDn.h>
+
 #include <algorithm>
 #include <cmath>
 #include <map>
@@ -134,6 +137,64 @@ void jacobi_eigen(int n, std::vector<double>& S, std::vector<double>& Q, std::ve
   for (int k = 0; k < n; ++k) lam[k] = s(k, k);
 }
 
+// Eigenpairs of a dense symmetric n x n matrix S (row-major = column-major)
+// on the current GPU with cuSOLVER's divide-and-conquer solver (set-up of the
+// large coarse grids, where the O(n^3)-per-sweep Jacobi method takes seconds
+// to minutes).  Q row-major with the eigenvectors in its columns.
+void gpu_eigen(int n, const std::vector<double>& S, std::vector<double>& Q,
+               std::vector<double>& lam) {
+  cusolverDnHandle_t h = nullptr;
+  double *dA = nullptr, *dW = nullptr, *dwork = nullptr;
+  int* dinfo = nullptr;
+  std::string err;
+  auto cuda_ok = [&](cudaError_t e, const char* what) {
+    if (e != cudaSuccess && err.empty()) err = std::string(what) + ": " + cudaGetErrorString(e);
+    return err.empty();
+  };
+  auto solver_ok = [&](cusolverStatus_t st, const char* what) {
+    if (st != CUSOLVER_STATUS_SUCCESS && err.empty())
+      err = std::string(what) + " failed (status " + std::to_string((int)st) + ")";
+    return err.empty();
+  };
+  const size_t bytes = (size_t)n * n * sizeof(double);
+  int lwork = 0, info = -1;
+  if (solver_ok(cusolverDnCreate(&h), "cusolverDnCreate") &&
+      cuda_ok(cudaMalloc((void**)&dA, bytes), "cudaMalloc") &&
+      cuda_ok(cudaMalloc((void**)&dW, (size_t)n * sizeof(double)), "cudaMalloc") &&
+      cuda_ok(cudaMalloc((void**)&dinfo, sizeof(int)), "cudaMalloc") &&
+      cuda_ok(cudaMemcpy(dA, S.data(), bytes, cudaMemcpyHostToDevice), "cudaMemcpy") &&
+      solver_ok(cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n,
+                                            dA, n, dW, &lwork),
+                "cusolverDnDsyevd_bufferSize") &&
+      cuda_ok(cudaMalloc((void**)&dwork, (size_t)std::max(lwork, 1) * sizeof(double)),
+              "cudaMalloc") &&
+      solver_ok(cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, dA, n, dW,
+                                 dwork, lwork, dinfo),
+                "cusolverDnDsyevd") &&
+      cuda_ok(cudaMemcpy(&info, dinfo, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy")) {
+    std::vector<double> A((size_t)n * n);
+    lam.resize(n);
+    if (cuda_ok(cudaMemcpy(A.data(), dA, bytes, cudaMemcpyDeviceToHost), "cudaMemcpy") &&
+        cuda_ok(cudaMemcpy(lam.data(), dW, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost),
+                "cudaMemcpy")) {
+      Q.resize((size_t)n * n);
+      for (int r = 0; r < n; ++r)   // column-major eigenvectors -> row-major Q
+        for (int c = 0; c < n; ++c) Q[(size_t)r * n + c] = A[(size_t)c * n + r];
+    }
+  }
+  if (dwork) cudaFree(dwork);
+  if (dinfo) cudaFree(dinfo);
+  if (dW) cudaFree(dW);
+  if (dA) cudaFree(dA);
+  if (h) cusolverDnDestroy(h);
+  if (!err.empty()) throw std::runtime_error("coarse eigen-decomposition: " + err);
+  if (info != 0) throw std::runtime_error("coarse eigen-decomposition did not converge");
+}
+
+// Grids up to this size take the host Jacobi eigen-solver (also used by the
+// host-only entry points); larger ones the GPU solver.
+constexpr int kJacobiMaxN = 257;
+
 // Generalised eigenvectors of K v = l W v (K = -M, M row-major, W = diag(w)):
 // V column-major with V^T W V = I.
 void pencil_eigen(int n, const std::vector<double>& M, const std::vector<double>& w,
@@ -151,7 +212,10 @@ void pencil_eigen(int n, const std::vector<double>& M, const std::vector<double>
       S[(size_t)r * n + c] = S[(size_t)c * n + r] = 0.5 * (a + b);
     }
   std::vector<double> Q;
-  jacobi_eigen(n, S, Q, lam);
+  if (n <= kJacobiMaxN)
+    jacobi_eigen(n, S, Q, lam);
+  else
+    gpu_eigen(n, S, Q, lam);
   V.resize((size_t)n * n);
   for (int r = 0; r < n; ++r)
     for (int c = 0; c < n; ++c) V[(size_t)c * n + r] = Q[(size_t)r * n + c] / std::sqrt(w[r]);
@@ -216,6 +280,39 @@ std::shared_ptr<const CoarseFactors> build_factors(int nc, int p) {
       if (!(d > 0.0)) throw std::runtime_error("coarse operator is not positive definite");
       f->dinv[(size_t)j * nc + i] = 1.0 / d;
     }
+  if (nc > kJacobiMaxN) {
+    // large grids: the eigen-residuals K v = l W v of every pair and the
+    // W-orthonormality of a sample of pairs (O(n^2) each; the full check
+    // below is O(n^3))
+    auto pencil_check = [&](const std::vector<double>& M, const std::vector<double>& V,
+                            const std::vector<double>& lam) {
+      double worst = 0.0;
+      for (int k = 0; k < nc; ++k) {
+        const double* v = V.data() + (size_t)k * nc;
+        for (int r = 0; r < nc; ++r) {
+          double kv = 0.0;
+          for (int c = std::max(0, r - 3); c < std::min(nc, r + 4); ++c)
+            kv -= M[(size_t)r * nc + c] * v[c];
+          worst = std::max(worst, std::fabs(kv - lam[k] * w[r] * v[r]) /
+                                      (1.0 + std::fabs(lam[k])));
+        }
+      }
+      for (int t = 0; t < 64; ++t) {
+        const int a = (int)((37u * (unsigned)t + 11u) % (unsigned)nc);
+        const int c = (int)((101u * (unsigned)t + 5u) % (unsigned)nc);
+        double dot = 0.0;
+        for (int r = 0; r < nc; ++r)
+          dot += V[(size_t)a * nc + r] * w[r] * V[(size_t)c * nc + r];
+        worst = std::max(worst, std::fabs(dot - (a == c ? 1.0 : 0.0)));
+      }
+      return worst;
+    };
+    if (p != 2) throw std::runtime_error("coarse size out of range for SBP order p");
+    const double ex = pencil_check(X, f->Vx, lx), ey = pencil_check(Y, f->Vy, ly);
+    if (!(ex <= 1e-9) || !(ey <= 1e-9))
+      throw std::runtime_error("coarse fast-diagonalisation self-check failed");
+    return f;
+  }
   // Self-check: A (A^{-1} b) == b on a fixed vector.
   std::vector<double> b(N), x(N);
   for (size_t k = 0; k < N; ++k) b[k] = std::sin(0.37 * (double)k + 0.11) + 0.25;
@@ -275,7 +372,8 @@ void coarse_solve_host(const CoarseFactors& f, const double* b, double* x) {
 
 std::shared_ptr<const CoarseFactors> coarse_factors(int nc, int p) {
   const int lo = p == 2 ? 3 : ho_min_points(p);
-  if (lo == 0 || nc < lo || nc > 257) throw std::runtime_error("coarse size out of range");
+  if (lo == 0 || nc < lo || nc > kCoarseMaxN || (p != 2 && nc > kJacobiMaxN))
+    throw std::runtime_error("coarse size out of range");
   static std::mutex mu;
   static std::map<std::pair<int, int>, std::shared_ptr<const CoarseFactors>> cache;
   std::lock_guard<std::mutex> lock(mu);

@@ -22,8 +22,14 @@ struct CoarseFactors {
   std::vector<double> dinv;  // 1 / (lx_i + ly_j) at i + j * nc
 };
 
+// Largest coarse grid of the fast-diagonalisation solve (p = 2; 257 for
+// p = 4, 6).  Grids above 257 take the GPU eigen-solver at set-up, so they
+// need a current CUDA device.
+constexpr int kCoarseMaxN = 1025;
+
 // Factors of the coarse operator of SBP order p (2, 4 or 6) on an nc x nc
-// grid (nc <= 257 and at least 3 for p = 2, ho_min_points(p) otherwise).  For
+// grid (3 <= nc <= kCoarseMaxN for p = 2; ho_min_points(p) <= nc <= 257
+// otherwise).  For
 // p = 2 the Kronecker structure is checked against the kernels' own stencil
 // coefficients.  Throws std::runtime_error on failure.
 std::shared_ptr<const CoarseFactors> coarse_factors(int nc, int p = 2);

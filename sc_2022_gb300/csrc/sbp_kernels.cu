@@ -10,6 +10,7 @@
 #include <mutex>
 #include <utility>
 
+#include "sbp_coarse.h"
 #include "sbp_kernels.cuh"
 #include "sbp_launch.h"
 #include "sbp_tma.h"
@@ -3068,9 +3069,18 @@ cudaError_t allow_fd_smem() {
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)fd_smem_bytes(kFdStageMaxN, true));
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_coarse_fd_batch<Tin, Tout, true>,
+  e = cudaFuncSetAttribute(k_coarse_fd_batch<Tin, Tout, true>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)fd_smem_bytes(kFdStageMaxN, true));
+  if (e != cudaSuccess) return e;
+  // the unstaged pass of the largest coarse grids (1025: 49 KB)
+  e = cudaFuncSetAttribute(k_coarse_fd<Tin, Tout, false>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)fd_smem_bytes(kCoarseMaxN, false));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_coarse_fd_batch<Tin, Tout, false>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)fd_smem_bytes(kFdStageMaxN, true));
+                              (int)fd_smem_bytes(kCoarseMaxN, false));
 }
 
 // The staged coarse kernels need more than the default 48 KB of dynamic

@@ -23,6 +23,9 @@ SQRT_EPS = math.sqrt(2.220446049250313e-16)
 _solver_cache: dict = {}
 
 
+# Largest grid of the direct (fast-diagonalisation) coarse solve.
+COARSE_MAX_N = 1025
+
 def _cached_solver(n: int, options: Options | None) -> Solver:
     key = (n, None if options is None else tuple(vars(options).items()),
            torch.cuda.current_device())
@@ -86,11 +89,11 @@ def CG_Matrix_Free_GPU_v2(x_GPU, Ap_GPU, b_reshaped_GPU, Nx, Ny, abstol: float =
 def _mg_options(n: int, nu: int, A_2h) -> Options:
     if isinstance(A_2h, Options):
         return A_2h
-    if (n + 1) // 2 <= 257:
+    if (n + 1) // 2 <= COARSE_MAX_N:
         o = reference_two_level_options(n)
     else:
         # The reference's exact coarse LU at (n+1)/2 is replaced by the
-        # multi-level V-cycle beyond a 257^2 coarse grid.
+        # multi-level V-cycle beyond the largest direct coarse grid.
         o = default_options()
     o.nu_pre = o.nu_post = nu
     return o
@@ -106,7 +109,7 @@ def matrix_free_MGCG(b_GPU: torch.Tensor, x_GPU: torch.Tensor, A_2h=None,
     ``A_2h`` is the reference's coarse LU factor; here it may be a
     :class:`Solver` (reused), an :class:`Options`, or None: the reference's
     two-level Richardson preconditioner with an exact coarse solve when
-    (n+1)/2 <= 257, else the default V-cycle.  NUM_V_CYCLES, use_galerkin,
+    (n+1)/2 <= 1025 (N <= 2049), else the default V-cycle.  NUM_V_CYCLES, use_galerkin,
     direct_sol and H_tilde are accepted for signature compatibility; the
     reference ignores them as well (SBPp must be 2).
     """
@@ -183,10 +186,10 @@ def matrix_free_prolongation_2d_GPU(idata: torch.Tensor, odata: torch.Tensor,
 # ---------------------------------------------------------------------------
 def _coarse_exact(b_2h: torch.Tensor) -> torch.Tensor:
     """x = A^-1 b on the grid of b: the fast-diagonalisation direct solve of a
-    one-level handle (coarse grids up to 257^2), else MGCG to 1e-14."""
+    one-level handle (coarse grids up to 1025^2), else MGCG to 1e-14."""
     n = check_grid(b_2h, name="b_2h")
     x = torch.zeros_like(b_2h)
-    if n <= 257:
+    if n <= COARSE_MAX_N:
         o = default_options()
         o.coarse_n = n
         _cached_solver(n, o).vcycle(b_2h, x)

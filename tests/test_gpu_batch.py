@@ -111,6 +111,29 @@ def test_batch_config_256_problems(sbp):
           f"({t_seq / t_batch:.2f}x), launches {B.last_launches}, worst rel. diff {worst:.2e}, "
           f"CTA budgets {budgets}")
     assert worst < 1e-8
+    # every problem with N <= 257 against the C oracle's MGCG (same V-cycle,
+    # same stopping rule): iterations within one, solutions to 1e-9
+    import os
+    from oracle import cpu_path
+    cpu_path.set_threads(os.cpu_count() or 1)
+    oracles = {n: cpu_path.CpuMG(n, smoother="jacobi", restriction="galerkin", coarse_n=65)
+               for n in sorted(set(ns)) if n <= 257}
+    checked, worst_o = 0, 0.0
+    for k, n in enumerate(ns):
+        if n not in oracles:
+            continue
+        bh = host(bs[k])
+        xo, ito, _ = oracles[n].mgcg(bh, np.zeros_like(bh), 1e-10 * float(np.linalg.norm(bh)),
+                                     maxiter=100)
+        assert abs(rb[k].iters - ito) <= 1, (k, n, rb[k].iters, ito)
+        err = relerr(host(xs[k]), xo)
+        worst_o = max(worst_o, err)
+        assert err < 1e-9, (k, n, err)
+        checked += 1
+    for m in oracles.values():
+        m.close()
+    print(f"{checked} problems with N <= 257 against the C oracle: worst rel. diff {worst_o:.2e}")
+    assert checked == sum(1 for n in ns if n <= 257) and checked > 100
 
 
 def test_batch_maxiter_then_larger_maxiter(sbp):

@@ -59,8 +59,12 @@ def test_cg_full_gpu_reference_semantics(sbp):
     assert relerr(host(x), xr) < 1e-8
 
 
-@pytest.mark.parametrize("n,expect", [(33, 18), (65, 19), (129, 18), (257, 17), (513, 17)])
+@pytest.mark.parametrize("n,expect", [(33, 18), (65, 19), (129, 18), (257, 17), (513, 17),
+                                      (1025, 15), (2049, 15)])
 def test_mgcg_reference_two_level(sbp, n, expect):
+    # the reference's matrix_free_MGCG with its two-level preconditioner and an
+    # exact coarse solve at (n+1)/2 (coarse grids above 257 get their
+    # fast-diagonalisation eigenbases from the GPU eigen-solver)
     a, b, U = ref_problem(n)
     hier = o.Hierarchy(n, o.MGOptions.reference_two_level(n))
     xr, itr, nr = o.mgcg(hier, b)
