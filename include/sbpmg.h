@@ -370,6 +370,14 @@ int sbp_vcycle_apply(sbp_solver* s, const double* b, double* v, void* stream);
  * device first.  Not for production use. */
 int sbp_test_drop_copy(int drop, unsigned wait_polls);
 
+/* Test hook for the direction pass's FP64 conversion (no counterpart in the
+ * reference): out[k] = -(hi[k] + lo[k]) for float pairs, formed as the mixed
+ * MGCG direction forms A p~ in FP64, off the FP64 pipe (an FP32 two-sum and
+ * an integer step on the FP64 bit pattern).  Must equal
+ * -((double)hi + (double)lo) bit for bit.  Device arrays of length n. */
+int sbp_test_pair_to_f64(const float* hi, const float* lo, double* out, long long n,
+                         void* stream);
+
 /* Measured FP64 FMA rate of the current GPU in 1e9 lane-operations per
  * second (blocking): eight independent FMA chains per thread over one full
  * wave of CTAs, best of three CUDA-event timings.  The denominator of the

@@ -93,6 +93,7 @@ SIGNATURES = {
     "sbp_vcycle_apply": (_i, [_vp, _vp, _vp, _vp]),
     "sbp_fp64_fma_rate": (_i, [_dp, _vp]),
     "sbp_test_drop_copy": (_i, [_i, C.c_uint]),
+    "sbp_test_pair_to_f64": (_i, [_vp, _vp, _vp, C.c_longlong, _vp]),
     "sbp_solver_profile": (_i, [_vp, _i, _vp, _vp, _i, _d, _i, C.POINTER(sbp_result),
                                 C.POINTER(sbp_kernel_time), _i, C.POINTER(_i), _vp]),
     "sbp_h_misfit_f64": (_i, [_vp, _vp, _vp, _i, _vp, _vp]),

@@ -119,6 +119,7 @@ struct sbp_solver {
   std::vector<void*> allocs;
   cudaStream_t cap = nullptr;       // private stream for graph capture
   cudaStream_t aux = nullptr;       // forked branch (boundary tiles of the wave levels)
+  cudaEvent_t dfork = nullptr, djoin = nullptr;   // and of the FP32 direction pass
   cudaEvent_t ev[2] = {nullptr, nullptr};
   // cached iteration graphs: [kind][parity]; kind 0 = MGCG, 1 = CG
   cudaGraphExec_t iter_exec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
@@ -267,6 +268,13 @@ long long vcycle_launches(const sbp_solver* s, bool dot) {
   return c;
 }
 
+// Kernel launches of one Krylov iteration (mirrors enqueue_iteration).
+long long iteration_launches(const sbp_solver* s, int kind) {
+  if (kind != 0) return 2;
+  const bool mixed = (s->opts.precision == SBP_PREC_MIXED);
+  return (mixed ? cg_dir_f32_launches(s->n) : 1) + 1 + vcycle_launches(s, true);
+}
+
 cudaError_t enqueue_vcycle_any(sbp_solver* s, bool dot, SolveState* st, cudaStream_t q) {
   if (s->opts.precision == SBP_PREC_MIXED) return enqueue_vcycle<float>(s, 0, dot, st, q);
   return enqueue_vcycle<double>(s, 0, dot, st, q);
@@ -294,7 +302,8 @@ cudaError_t enqueue_iteration(sbp_solver* s, int kind, int parity, int sign, cud
     if (mixed)
       // FP32 direction p~ and Ap = A p~ (exact) in one pass
       e = launch_cg_dir_f32(vcycle_out_op(s), s->op32[parity], grid<float>(s->p32[1 - parity], ld),
-                            grid<double>(s->Ap, ld), n, s->st, s->rb, q);
+                            grid<double>(s->Ap, ld), n, s->st, s->rb, q, s->aux, s->dfork,
+                            s->djoin);
     else
       e = launch_cg_dir_op<double, double>(vcycle_out_op(s), s->op[parity], grid<double>(pnew, ld),
                                            grid<double>(s->Ap, ld), n, +1, s->st, s->rb, q);
@@ -344,7 +353,7 @@ int capture_iteration(sbp_solver* s, int kind, int sign) {
   }
   s->iter_valid[kind] = true;
   s->iter_key_sign[kind] = sign;
-  s->launches_per_iter[kind] = 2 + (kind == 0 ? vcycle_launches(s, true) : 0);
+  s->launches_per_iter[kind] = iteration_launches(s, kind);
   return SBP_OK;
 }
 
@@ -394,7 +403,7 @@ int run_krylov(sbp_solver* s, int kind, const double* b, double* x, int sign, do
     if (rc) return rc;
   }
   // Iterate: keep one iteration queued ahead of the one being checked.
-  long long launches = 2 + (kind == 0 ? vcycle_launches(s, true) : 0);
+  long long launches = 2 + (kind == 0 ? vcycle_launches(s, true) : 0);   // set-up + V-cycle
   int k = 0;
   bool finished = false;
   if (maxiter == 0) finished = true;
@@ -725,6 +734,11 @@ int sbp_solver_create(sbp_solver** out, int n, const sbp_options* opts) {
         SBP_CUDA(cudaMemset(s->p32[k], 0, nn * sizeof(float)));
         make_operand(s->op32[k], s->p32[k], n, s->ld, false);
       }
+      if (cg_dir_f32_launches(n) == 2) {
+        SBP_CUDA(cudaEventCreateWithFlags(&s->dfork, cudaEventDisableTiming));
+        SBP_CUDA(cudaEventCreateWithFlags(&s->djoin, cudaEventDisableTiming));
+        if (!s->aux) SBP_CUDA(cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking));
+      }
     }
     int m = n;
     while (true) {
@@ -796,6 +810,8 @@ int sbp_solver_destroy(sbp_solver* s) {
   if (s->aux) cudaStreamDestroy(s->aux);
   for (auto& e : s->ev)
     if (e) cudaEventDestroy(e);
+  for (cudaEvent_t ev : {s->dfork, s->djoin})
+    if (ev) cudaEventDestroy(ev);
   for (Level& L : s->levels) {
     for (cudaEvent_t ev : {L.fork, L.join, L.pfork, L.pjoin})
       if (ev) cudaEventDestroy(ev);
@@ -847,6 +863,13 @@ int sbp_mgcg_adjoint_f64(sbp_solver* s, const double* gu, double* lam, double* d
 int sbp_test_drop_copy(int drop, unsigned wait_polls) {
   SBP_CUDA(cudaDeviceSynchronize());
   SBP_CUDA(set_copy_drop(drop, wait_polls));
+  return SBP_OK;
+}
+
+int sbp_test_pair_to_f64(const float* hi, const float* lo, double* out, long long n,
+                         void* stream) {
+  if (n < 0 || (n > 0 && (!hi || !lo || !out))) return SBP_ERR_ARGS;
+  SBP_CUDA(launch_pair_to_f64(hi, lo, out, n, (cudaStream_t)stream));
   return SBP_OK;
 }
 

@@ -906,6 +906,37 @@ cudaError_t launch_cg_dir_mixed(const Operand& z, const Operand& pold, const Ope
 // perturbation of z).  20 bytes per point instead of 36, and no FP64
 // instruction per point besides the conversion of A p~ to FP64.
 // ---------------------------------------------------------------------------
+// A p~ at one point from the float pair hi + lo of -A p~ (negA; the plain
+// 5-point stencil in the interior): FP64 for the Krylov vectors (rounded
+// once, off the FP64 pipe), and in apf its FP32 rounding for p~.Ap.
+__device__ __forceinline__ double dir_ap(float hi, float lo, float& apf) {
+  apf = -(hi + lo);
+  return ff_neg_f64(hi, lo);
+}
+
+// The end of the direction pass's p.Ap reduction: pAp and alpha.
+__device__ __forceinline__ void finish_pap(SolveState* st, double tot) {
+  st->pAp = tot;
+  if (!isfinite(tot) || tot == 0.0)
+    st->done = kDoneBreakdown;
+  else
+    st->alpha = st->rz / tot;
+}
+
+// One side of a p.Ap split between the boundary tiles and the interior wave
+// of the FP32 direction pass (running concurrently): each side leaves its
+// share and counts in; the second to arrive finishes with ring + wave (fixed
+// order) and re-arms the counter.
+__device__ __forceinline__ void pap_join(SolveState* st, double* mine, double tot) {
+  *mine = tot;
+  __threadfence();
+  if (atomicAdd(&st->pap_join, 1u) == 1u) {
+    __threadfence();
+    finish_pap(st, __ldcg(&st->pap_part) + __ldcg(&st->pap_wave));
+    st->pap_join = 0u;
+  }
+}
+
 template <bool TMA>
 struct CgDirF32Job {
   static constexpr int kOffZ = align128(box_bytes<float, BI, BJ>());
@@ -922,6 +953,18 @@ struct CgDirF32Job {
   int n, ntx, ntot;
   SolveState* st;
   ReduceBuf rb;
+  // ring = 1: only the first and last tile rows and columns (nty = tile
+  // columns) are visited, k -> ring_id(k); the interior tiles are done by
+  // the register wave kernel (k_dir_wave), and p.Ap meets its share in
+  // pap_join
+  int ring, nty;
+  __device__ int ring_id(int k) const {
+    if (!ring) return k;
+    if (k < ntx) return k;
+    if (k < 2 * ntx) return (k - ntx) + (nty - 1) * ntx;
+    const int k2 = k - 2 * ntx;
+    return ((k2 & 1) ? ntx - 1 : 0) + (1 + (k2 >> 1)) * ntx;
+  }
   __device__ bool prepare(Ctx& c) const {
     if (st->done) return true;
     c.first = (st->iter == 0);
@@ -934,14 +977,16 @@ struct CgDirF32Job {
     return TMA ? box_bytes<float, BI, BJ>() + (st->iter == 0 ? 0u : box_bytes<float, BI, BJ>())
                : 0u;
   }
-  __device__ void issue(unsigned char* buf, unsigned long long* bar, int id, const Ctx& c) const {
+  __device__ void issue(unsigned char* buf, unsigned long long* bar, int k, const Ctx& c) const {
+    const int id = ring_id(k);
     const TileBoxes bx(id % ntx, tile_at<TI, TJ>(id, ntx, n).j_lo);
     stage_box<TMA, BI, BJ>(reinterpret_cast<float*>(buf + kOffZ), z, &z.box, bx.x0, bx.y0, n, bar);
     if (!c.first)
       stage_box<TMA, BI, BJ>(reinterpret_cast<float*>(buf), pold, &pold.box, bx.x0, bx.y0, n,
                              bar);
   }
-  __device__ void compute(unsigned char* buf, int id, Acc& acc, const Ctx& c, unsigned char*) const {
+  __device__ void compute(unsigned char* buf, int k, Acc& acc, const Ctx& c, unsigned char*) const {
+    const int id = ring_id(k);
     const TileT t = tile_at<TI, TJ>(id, ntx, n);
     const TileBoxes bx(id % ntx, t.j_lo);
     float* s = reinterpret_cast<float*>(buf);
@@ -955,17 +1000,18 @@ struct CgDirF32Job {
       v = first ? zz : fmaf(beta, v, zz);
     });
     __syncthreads();
-    auto emit = [&](int i, int j, float pv, double ap) {
+    auto emit = [&](int i, int j, float pv, float hi, float lo) {
+      float apf;
       pnew.at(i, j) = pv;
-      Ap.at(i, j) = ap;
-      acc.add_prod(pv, f64_to_f32(ap));
+      Ap.at(i, j) = dir_ap(hi, lo, apf);
+      acc.add_prod(pv, apf);
     };
     if (tile_interior(t, n)) {
       visit_interior(s, t, [&](int i, int j, float um, float u0, float up, float uw, float ue,
                                int) {
         float hi, lo;
         stencil_ff(uw, ue, um, up, u0, hi, lo);
-        emit(i, j, u0, -(f32_to_f64(hi) + f32_to_f64(lo)));   // A p~ = -(stencil)
+        emit(i, j, u0, hi, lo);
       });
     } else {
       visit_generic(s, t, bx, [&](int i, int j, const SAcc<float>& a, int) {
@@ -974,30 +1020,33 @@ struct CgDirF32Job {
           __device__ FF operator()(int di, int dj) const { return FF((*a)(di, dj), 0.0f); }
         } d{&a};
         const FF na = negA<FF>(d, i, j, n);
-        emit(i, j, a(0, 0), -(f32_to_f64(na.hi) + f32_to_f64(na.lo)));
+        emit(i, j, a(0, 0), na.hi, na.lo);
       });
     }
   }
   __device__ void finish(double tot) const {
-    st->pAp = tot;
-    if (!isfinite(tot) || tot == 0.0)
-      st->done = kDoneBreakdown;
+    if (ring)
+      pap_join(st, &st->pap_part, tot);
     else
-      st->alpha = st->rz / tot;
+      finish_pap(st, tot);
   }
 };
 
-cudaError_t launch_cg_dir_f32(const Operand& z, const Operand& pold, Grid<float> pnew,
-                              Grid<double> Ap, int n, SolveState* st, ReduceBuf rb,
-                              cudaStream_t s) {
+// The staged direction pass over every tile (ring = 0) or over the first
+// and last tile rows and columns only (ring = 1, beside k_dir_wave).
+static cudaError_t launch_cg_dir_f32_staged(const Operand& z, const Operand& pold,
+                                            Grid<float> pnew, Grid<double> Ap, int n,
+                                            SolveState* st, ReduceBuf rb, cudaStream_t s,
+                                            int ring) {
   const dim3 g = tile_grid(n);
-  const int total = (int)(g.x * g.y);
+  const int ntx = (int)g.x, nty = (int)g.y;
+  const int total = ring ? ntx * nty - (ntx - 2) * (nty - 2) : ntx * nty;
   const DevOperand<float> dz = dev_operand<float>(z), dp = dev_operand<float>(pold);
   if (z.tma && pold.tma)
-    return launch_persist(CgDirF32Job<true>{dz, dp, pnew, Ap, n, (int)g.x, total, st, rb}, total,
-                          s);
-  return launch_persist(CgDirF32Job<false>{dz, dp, pnew, Ap, n, (int)g.x, total, st, rb}, total,
-                        s);
+    return launch_persist(
+        CgDirF32Job<true>{dz, dp, pnew, Ap, n, ntx, total, st, rb, ring, nty}, total, s);
+  return launch_persist(CgDirF32Job<false>{dz, dp, pnew, Ap, n, ntx, total, st, rb, ring, nty},
+                        total, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -1123,6 +1172,22 @@ cudaError_t launch_cg_update_batch(const unsigned char* blobs, int stride, int c
 }
 
 static inline bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+// CTAs of one resident wave of k_cg_update: the grid-stride loop gives every
+// CTA the same share, so a grid beyond one wave leaves a partial second wave
+// running alone at the end (1216 CTAs at 6 resident per SM: 1.33 waves).
+template <bool VEC>
+static int cg_update_wave() {
+  static const int v = [] {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_cg_update<VEC>, kThreads, 0) !=
+            cudaSuccess ||
+        b < 1)
+      b = 1;
+    return b * sm_count();
+  }();
+  return v;
+}
 
 // ---------------------------------------------------------------------------
 // Smoothing pass (Jacobi / Richardson) with the field variants.
@@ -2140,7 +2205,8 @@ cudaError_t launch_cg_update(Grid<T> x, Grid<T> r, Grid<const T> p, Grid<const T
                                                            : aligned16(p.p)) &&
                    aligned16(Ap.p) && (!rlo.p || ((uintptr_t)rlo.p & 7u) == 0) &&
                    (ld % 2 == 0 || N % 2 == 0);
-  const int g = flat_grid(N, vec ? 4 : 2);
+  const int g =
+      std::min(flat_grid(N, vec ? 4 : 2), vec ? cg_update_wave<true>() : cg_update_wave<false>());
   const CgUpdateArgs a{x.p, r.p, pf ? nullptr : p.p, pf, Ap.p, rlo.p, N, plain, st, norms, rb};
   if (recorder_slot())
     return vec ? record_launch(&launch_cg_update_batch<true>, a, g)
@@ -2827,6 +2893,207 @@ cudaError_t launch_post_fused(const Operand& vin, const Operand& e, const Operan
                                               st, rb, s);
 }
 
+// ---------------------------------------------------------------------------
+// Register wave of the FP32 CG direction for the interior of the fine grid
+// (mixed MGCG), the job of CgDirF32Job's interior tiles without staging or
+// block barriers.  A warp owns a strip of 62 rows x `cols` columns of the
+// interior rectangle [Ra, Rb) x [Ca, Cb) (the union of the 64 x 32 tiles
+// outside the first and last tile rows and columns: every point there has
+// the plain 5-point stencil).  Lane l holds rows rb0 + 2l and rb0 + 2l + 1
+// (64 rows: the 62 owned and one halo row on either side), and the warp
+// marches along j:
+//   step c: p~ = fl32(z + beta p~_old) at column c (stored where owned);
+//           A p~ at column c - 1 in float-float from the p~ of columns
+//           c - 2, c - 1, c and of the lanes above and below (one shuffle
+//           each way), stored in FP64, and p~ . fl32(A p~) accumulated.
+// z and p~_old come through per-lane cp.async rings kDirAhead columns ahead;
+// a lane reads only its own slots, so no barrier is needed.  The arithmetic
+// per point is that of CgDirF32Job's interior path.
+// ---------------------------------------------------------------------------
+constexpr int kDirRows = 62;
+constexpr int kDirAhead = 8;
+constexpr int kDirSlots = kDirAhead + 1;
+constexpr int kDirWaveMinN = 1025;
+
+struct DirWaveArgs {
+  const float* z;
+  int ldz;
+  const float* pold;
+  int ldp;
+  float* pnew;
+  int ldn;
+  double* Ap;
+  int lda;
+  int Ra, Rb, Ca, Cb, nsi, nsj, cols;
+  SolveState* st;
+  ReduceBuf rb;
+};
+
+__global__ void __launch_bounds__(kThreads) k_dir_wave(const DirWaveArgs a) {
+  __shared__ __align__(16) float2 zring[kWarps][kDirSlots][32];
+  __shared__ __align__(16) float2 pring[kWarps][kDirSlots][32];
+  pdl_begin();
+  SolveState* st = a.st;
+  if (st->done) return;   // uniform: the state was final before this launch
+  const bool first = (st->iter == 0);   // p~_old is not read
+  const float beta = (float)st->beta;
+  const int lane = threadIdx.x & 31;
+  const int wl = threadIdx.x >> 5;
+  const int gw = (blockIdx.x * kThreads + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * kThreads) >> 5;
+  const int items = a.nsi * a.nsj;
+  const unsigned FULL = 0xffffffffu;
+  float2* const zmine = &zring[wl][0][lane];
+  float2* const pmine = &pring[wl][0][lane];
+  DotAcc<float> acc;
+  for (int it = gw; it < items; it += nw) {
+    const int si = it % a.nsi, sj = it / a.nsi;
+    const int rb0 = a.Ra - 1 + kDirRows * si;             // even: Ra is odd
+    const int r_hi = min(rb0 + 1 + kDirRows, a.Rb);       // owned rows [rb0 + 1, r_hi)
+    const int c0 = a.Ca + a.cols * sj;
+    const int c1 = min(c0 + a.cols, a.Cb);
+    const int ra = rb0 + 2 * lane;
+    const bool own_x = lane > 0 && ra < r_hi;
+    const bool own_y = lane < 31 && ra + 1 < r_hi;
+    const int c_first = c0 - 1, c_last = c1;
+    const float* zp = a.z + (size_t)ra;
+    const float* pp = a.pold + (size_t)ra;
+#pragma unroll
+    for (int k = 0; k < kDirAhead; ++k) {
+      const int c = c_first + k;
+      if (c <= c_last) {
+        cp_async8(zmine + k * 32, zp + (size_t)c * a.ldz);
+        if (!first) cp_async8(pmine + k * 32, pp + (size_t)c * a.ldp);
+      }
+      cp_async_commit();
+    }
+    int slot = 0, fill = kDirAhead;
+    float2 q1 = make_float2(0.f, 0.f), q2 = q1;             // p~ at c - 1, c - 2
+    for (int c = c_first; c <= c_last; ++c) {
+      cp_async_wait<kDirAhead - 1>();                       // column c has landed
+      const float2 zv = zmine[slot * 32];
+      float2 q0 = zv;
+      if (!first) {
+        const float2 pv = pmine[slot * 32];
+        q0.x = fmaf(beta, pv.x, zv.x);
+        q0.y = fmaf(beta, pv.y, zv.y);
+      }
+      {
+        const int cn = c + kDirAhead;
+        if (cn <= c_last) {
+          cp_async8(zmine + fill * 32, zp + (size_t)cn * a.ldz);
+          if (!first) cp_async8(pmine + fill * 32, pp + (size_t)cn * a.ldp);
+        }
+        cp_async_commit();
+      }
+      slot = slot + 1 == kDirSlots ? 0 : slot + 1;
+      fill = fill + 1 == kDirSlots ? 0 : fill + 1;
+      if (c >= c0 && c < c1) {
+        float* o = a.pnew + (size_t)c * a.ldn + ra;
+        if (own_x && own_y) {
+          *reinterpret_cast<float2*>(o) = q0;
+        } else {
+          if (own_x) o[0] = q0.x;
+          if (own_y) o[1] = q0.y;
+        }
+      }
+      const float above = __shfl_up_sync(FULL, q1.y, 1);    // row ra - 1, column c - 1
+      const float below = __shfl_down_sync(FULL, q1.x, 1);  // row ra + 2, column c - 1
+      if (c > c0) {                                         // column c - 1 is in [c0, c1)
+        float hx, lx, hy, ly, fx, fy;
+        stencil_ff(above, q1.y, q2.x, q0.x, q1.x, hx, lx);
+        stencil_ff(q1.x, below, q2.y, q0.y, q1.y, hy, ly);
+        const double ax = dir_ap(hx, lx, fx), ay = dir_ap(hy, ly, fy);
+        double* o = a.Ap + (size_t)(c - 1) * a.lda + ra;
+        if (own_x && own_y) {
+          *reinterpret_cast<double2*>(o) = make_double2(ax, ay);
+        } else {
+          if (own_x) o[0] = ax;
+          if (own_y) o[1] = ay;
+        }
+        if (own_x) acc.add_prod(q1.x, fx);
+        if (own_y) acc.add_prod(q1.y, fy);
+      }
+      q2 = q1;
+      q1 = q0;
+    }
+    cp_async_wait<0>();   // no copy outlives the strip
+  }
+  // the boundary tiles' share comes from the staged pass running beside
+  grid_reduce(acc.value(), a.rb, [&](double tot) { pap_join(st, &st->pap_wave, tot); });
+}
+
+int cg_dir_f32_launches(int n) {
+  int Ra, Rb, Ca, Cb;
+  return (n >= kDirWaveMinN && post_wave_rect(n, Ra, Rb, Ca, Cb)) ? 2 : 1;
+}
+
+static int dir_wave_per_sm() {
+  static const int v = [] {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_dir_wave, kThreads, 0) !=
+            cudaSuccess ||
+        b < 1)
+      b = 1;
+    return b;
+  }();
+  return v;
+}
+
+cudaError_t launch_cg_dir_f32(const Operand& z, const Operand& pold, Grid<float> pnew,
+                              Grid<double> Ap, int n, SolveState* st, ReduceBuf rb,
+                              cudaStream_t s, cudaStream_t aux, cudaEvent_t fork,
+                              cudaEvent_t join) {
+  int Ra, Rb, Ca, Cb;
+  const bool wave = cg_dir_f32_launches(n) == 2 && !recorder_slot() && z.ld % 2 == 0 &&
+                    pold.ld % 2 == 0 && pnew.ld % 2 == 0 && Ap.ld % 2 == 0 &&
+                    ((uintptr_t)z.p & 7u) == 0 && ((uintptr_t)pold.p & 7u) == 0 &&
+                    ((uintptr_t)pnew.p & 7u) == 0 && aligned16(Ap.p) &&
+                    post_wave_rect(n, Ra, Rb, Ca, Cb);
+  if (!wave) return launch_cg_dir_f32_staged(z, pold, pnew, Ap, n, st, rb, s, 0);
+  // the boundary tiles by the staged job on a forked branch (or before the
+  // wave on the same stream); the two p.Ap shares meet in pap_join
+  const bool forked = aux && fork && join;
+  cudaError_t e = cudaSuccess;
+  if (forked) {
+    e = cudaEventRecord(fork, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(aux, fork, 0);
+  }
+  // concurrent reductions: the ring takes the upper half of the partials
+  // buffer and its own ticket, as in the post-smoothing split
+  const ReduceBuf rb_ring{rb.partials ? rb.partials + kRingPartialsOffset : nullptr,
+                          rb.ticket ? rb.ticket + 8 : nullptr};
+  if (e == cudaSuccess)
+    e = launch_cg_dir_f32_staged(z, pold, pnew, Ap, n, st, rb_ring, forked ? aux : s, 1);
+  if (forked && e == cudaSuccess) e = cudaEventRecord(join, aux);
+  if (e != cudaSuccess) return e;
+  DirWaveArgs a;
+  a.z = static_cast<const float*>(z.p);
+  a.ldz = z.ld;
+  a.pold = static_cast<const float*>(pold.p);
+  a.ldp = pold.ld;
+  a.pnew = pnew.p;
+  a.ldn = pnew.ld;
+  a.Ap = Ap.p;
+  a.lda = Ap.ld;
+  a.Ra = Ra;
+  a.Rb = Rb;
+  a.Ca = Ca;
+  a.Cb = Cb;
+  a.nsi = (Rb - Ra + kDirRows - 1) / kDirRows;
+  a.st = st;
+  a.rb = rb;
+  const int warps = sm_count() * dir_wave_per_sm() * kWarps;
+  static const int cands[] = {16, 24, 32, 40, 48, 64, 96};
+  a.cols = best_strip_cols(a.nsi, Cb - Ca, warps, cands, 7, 8, 1);
+  a.nsj = (Cb - Ca + a.cols - 1) / a.cols;
+  const int items = a.nsi * a.nsj;
+  const int grid = std::max(1, std::min((items + kWarps - 1) / kWarps, sm_count() * dir_wave_per_sm()));
+  e = launch_pdl(k_dir_wave, dim3(grid), dim3(kThreads), 0, s, a);
+  if (forked && e == cudaSuccess) e = cudaStreamWaitEvent(s, join, 0);
+  return e;
+}
+
 // Resolve the launch configuration of every persistent kernel up front
 // (shared-memory attribute and occupancy), outside any stream capture.
 template <typename T, int F, int E, bool M>
@@ -2892,6 +3159,9 @@ cudaError_t prepare_kernels() {
   persist_ctas_per_sm<PostFusedJob<double, true, false, PostSmall>>();
   persist_ctas_per_sm<CgDirMixedJob<true>>();
   persist_ctas_per_sm<CgDirF32Job<true>>();
+  cg_update_wave<true>();
+  cg_update_wave<false>();
+  dir_wave_per_sm();
   return cudaGetLastError();
 }
 
@@ -2899,6 +3169,20 @@ unsigned int read_device_fault() {
   unsigned int v = 0;
   cudaMemcpyFromSymbol(&v, g_sbp_fault, sizeof(v));
   return v;
+}
+
+__global__ void k_pair_to_f64(const float* __restrict__ hi, const float* __restrict__ lo,
+                              double* __restrict__ out, long long n) {
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (long long)gridDim.x * blockDim.x)
+    out[k] = ff_neg_f64(hi[k], lo[k]);
+}
+
+cudaError_t launch_pair_to_f64(const float* hi, const float* lo, double* out, long long n,
+                               cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  k_pair_to_f64<<<flat_grid(n, 4), kThreads, 0, s>>>(hi, lo, out, n);
+  return cudaGetLastError();
 }
 
 cudaError_t set_copy_drop(int drop, unsigned polls) {

@@ -351,6 +351,34 @@ __device__ __forceinline__ void stencil_ff(float uw, float ue, float um, float u
   lo = (ea + eb) + (ec + ed);
 }
 
+// -(hi + lo) of two floats rounded to nearest-even in FP64, with an FP64
+// instruction only in rare cases.  two_sum gives s + e == hi + lo with |e| at
+// most half an FP32 ulp of s, so the sum stays in the binade of s (unless s
+// is a power of two and e points down) and is s plus k FP64 ulps of s, k =
+// rn(e * 2^(179 - E)) with E the biased exponent of s (|k| < 2^29): an exact
+// power-of-two scaling and one float -> int conversion, whose ties-to-even
+// is the parity of the FP64 result.  Adding k to the bit pattern of (double)s
+// gives the FP64 sum.  |s| < 2^-75, zero, non-finite s and the binade
+// crossing take the FP64 add, which returns the same bits.
+__device__ __forceinline__ double ff_neg_f64(float hi, float lo) {
+  float s, e;
+  two_sum(hi, lo, s, e);
+  const unsigned u = __float_as_uint(s);
+  const unsigned E = (u >> 23) & 0xFFu;
+  const unsigned neg = u & 0x80000000u;
+  if (E >= 52u && E != 255u &&
+      ((u & 0x7FFFFFu) != 0u || ((neg ^ __float_as_uint(e)) & 0x80000000u) == 0u || e == 0.0f)) {
+    const unsigned long long ds = ((unsigned long long)neg << 32) |
+                                  ((unsigned long long)(E + 896u) << 52) |
+                                  ((unsigned long long)(u & 0x7FFFFFu) << 29);
+    const int k = __float2int_rn(e * __uint_as_float((306u - E) << 23));   // e / ulp64(s)
+    const long long step = neg ? -(long long)k : (long long)k;
+    return __longlong_as_double(
+        (long long)((ds + (unsigned long long)step) ^ 0x8000000000000000ull));
+  }
+  return -((double)hi + (double)lo);
+}
+
 // ---------------------------------------------------------------------------
 // FF: an unevaluated float pair hi + lo with the arithmetic negA needs, for
 // evaluating the SAT stencil of FP32 values on the FP32 pipe.  Sums use

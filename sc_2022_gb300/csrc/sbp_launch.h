@@ -34,11 +34,17 @@ cudaError_t launch_cg_dir_mixed(const Operand& z, const Operand& pold, const Ope
                                 Grid<double> pnew, Grid<double> Ap, int n, SolveState* st,
                                 ReduceBuf rb, cudaStream_t s);
 // Mixed-precision CG direction kept in FP32: p~ = fl32(z + beta p~_old),
-// Ap = A p~ exactly (float-float stencil), p~.Ap -> alpha.  z and p~_old are
-// staged with their halos (TMA when both allow it).
+// Ap = A p~ exactly (float-float stencil), p~.Ap -> alpha.  On grids with
+// n - 1 a multiple of 64 and n >= 1025 the interior runs as a register wave
+// and the first and last tile rows and columns as staged tiles (z and p~_old
+// with their halos, TMA when both allow it), on `aux` concurrently when aux,
+// fork and join are given; elsewhere every tile is staged.
 cudaError_t launch_cg_dir_f32(const Operand& z, const Operand& pold, Grid<float> pnew,
                               Grid<double> Ap, int n, SolveState* st, ReduceBuf rb,
-                              cudaStream_t s);
+                              cudaStream_t s, cudaStream_t aux = nullptr,
+                              cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
+// Kernel launches of launch_cg_dir_f32 at size n (1 or 2).
+int cg_dir_f32_launches(int n);
 template <typename T>
 cudaError_t launch_smooth_op(int field, int epi, const Operand& vin, const Operand& e,
                              const Operand& b, Grid<T> vout, int n, int smoother, double omega,
@@ -90,6 +96,10 @@ unsigned int take_device_fault();
 // its first TMA copy (its wait then runs out after `polls` try_wait polls);
 // drop = 0, polls = 0 restores normal operation.
 cudaError_t set_copy_drop(int drop, unsigned polls);
+// out[k] = -(hi[k] + lo[k]) in FP64 by the direction pass's conversion
+// (test hook).
+cudaError_t launch_pair_to_f64(const float* hi, const float* lo, double* out, long long n,
+                               cudaStream_t s);
 
 // Upper bound on the CTAs any reducing launch uses for an n x n grid; the
 // partials buffer of a ReduceBuf must hold this many doubles.

@@ -307,3 +307,40 @@ def test_apply_unaligned_arrays(sbp, n):
                              n, -1, None) == 0
     ref32 = o.neg_A_matrix_free(u.astype(np.float32).astype(np.float64), n).ravel()
     assert relerr(host(out32[1:]), ref32) < 1e-6
+
+
+def test_pair_to_f64_matches_fp64_add(sbp):
+    # the direction pass forms -(hi + lo) of its float-float stencil without
+    # the FP64 pipe: the bits must be those of the FP64 add, over random bit
+    # patterns, cancelling pairs and every exponent gap
+    rng = np.random.default_rng(11)
+    n = 1 << 22
+    hi = rng.integers(0, 1 << 32, n, dtype=np.uint64).astype(np.uint32).view(np.float32)
+    lo = rng.integers(0, 1 << 32, n, dtype=np.uint64).astype(np.uint32).view(np.float32)
+    m = n // 4
+    # cancellation: lo = -hi (1 + k 2^-23)
+    k = rng.integers(-2048, 2048, m).astype(np.float32)
+    lo[:m] = -hi[:m] * (np.float32(1) + k * np.float32(2.0 ** -23))
+    # exponent gaps 0 .. 70 with both signs
+    gap = rng.integers(0, 71, m)
+    lo[m:2 * m] = (hi[m:2 * m].astype(np.float64) * np.ldexp(1.0, -gap)
+                   * rng.choice([-1.0, 1.0], m) * rng.uniform(0.5, 2.0, m)).astype(np.float32)
+    lo[2 * m + 5] = 0.0
+    hi[2 * m + 6], lo[2 * m + 6] = 0.0, 0.0
+    ok = np.isfinite(hi) & np.isfinite(lo)
+    hi, lo = hi[ok], lo[ok]
+    with np.errstate(all="ignore"):
+        ref = -(hi.astype(np.float64) + lo.astype(np.float64))
+    dh, dl = dev(hi, torch.float32), dev(lo, torch.float32)
+    out = torch.empty(hi.size, dtype=torch.float64, device="cuda")
+    lib = sbp.load_library()
+    assert lib.sbp_test_pair_to_f64(C.c_void_p(dh.data_ptr()), C.c_void_p(dl.data_ptr()),
+                                    C.c_void_p(out.data_ptr()), hi.size, None) == 0
+    got = out.cpu().numpy()
+    # the hardware add flushes float denormal inputs like the integer path
+    # does not need to: compare where neither operand is a denormal
+    normal = ((np.abs(hi) >= np.finfo(np.float32).tiny) | (hi == 0)) & \
+             ((np.abs(lo) >= np.finfo(np.float32).tiny) | (lo == 0))
+    assert normal.mean() > 0.95
+    bad = np.flatnonzero(got[normal].view(np.uint64) != ref[normal].view(np.uint64))
+    assert bad.size == 0, (hi[normal][bad[:4]], lo[normal][bad[:4]])

@@ -111,12 +111,14 @@ def test_cg_n4097_true_residual(sbp):
     s.close()
 
 
-def test_profile_matches_graph_solve(sbp):
+@pytest.mark.parametrize("n", [513, 1025])
+def test_profile_matches_graph_solve(sbp, n):
     # sbp_solver_profile launches the same kernels without graphs: the same
     # iterations and, with fixed-order reductions, the same solution bit for
-    # bit; every kernel of the solve appears with its launches
+    # bit; every kernel of the solve appears with its launches.  At N = 1025
+    # the mixed direction pass runs as the interior wave beside the staged
+    # boundary tiles, whose p.Ap shares meet in a fixed order.
     from sc_2022_gb300 import _lib, problems
-    n = 513
     f, g, _ = problems.manufactured(n, "baseline")
     b = problems.assemble_rhs(f, g).reshape(-1)
     for prec in (_lib.SBP_PREC_FP64, _lib.SBP_PREC_MIXED):
@@ -132,6 +134,9 @@ def test_profile_matches_graph_solve(sbp):
                                                        reverse=True)
         launches = sum(r["launches"] for r in rows)
         assert launches >= res.iters * 3
+        if prec == _lib.SBP_PREC_MIXED and n == 1025:
+            names = " ".join(r["kernel"] for r in rows)
+            assert "k_dir_wave" in names and "CgDirF32Job" in names
         s.close()
 
 
