@@ -2543,10 +2543,14 @@ static cudaError_t launch_pre_wave(const Operand& b, Grid<float> vout, Grid<floa
   return launch_pdl(k_pre_wave, dim3(grid), dim3(kThreads), 0, s, a);
 }
 
+// Fine levels from this size up smooth their interior as a register wave
+// (FP32, three sweeps).  At N = 1025 the staged small tiles took about four
+// times the wave's time: one tile's serial passes per CTA.
+constexpr int kWaveMinFine = 1025;
+
 int pre_fused_launches(int nf, int sweeps, bool f32) {
   int Ia, Ib, Ja, Jb;
-  if (f32 && sweeps == 3 && !small_fused_tiles((nf + 1) / 2) &&
-      pre_wave_rect((nf + 1) / 2, Ia, Ib, Ja, Jb))
+  if (f32 && sweeps == 3 && nf >= kWaveMinFine && pre_wave_rect((nf + 1) / 2, Ia, Ib, Ja, Jb))
     return 2;
   return 1;
 }
@@ -2557,11 +2561,8 @@ cudaError_t launch_pre_fused(const Operand& b, Grid<T> vout, Grid<T> f, int nf, 
                              cudaStream_t s, cudaStream_t aux, cudaEvent_t fork,
                              cudaEvent_t join) {
   if (sweeps < 1 || sweeps > kMaxFusedSweeps) return cudaErrorInvalidValue;
-  if (small_fused_tiles((nf + 1) / 2))
-    return launch_pre_fused_geom<T, PreSmall>(b, vout, f, nf, sweeps, smoother, omega, kind, st,
-                                              s);
   int Ia, Ib, Ja, Jb;
-  if (std::is_same<T, float>::value && sweeps == 3 && !recorder_slot() &&
+  if (std::is_same<T, float>::value && sweeps == 3 && nf >= kWaveMinFine && !recorder_slot() &&
       (b.ld % 2) == 0 && (vout.ld % 2) == 0 && ((uintptr_t)b.p & 7u) == 0 &&
       ((uintptr_t)vout.p & 7u) == 0 && pre_wave_rect((nf + 1) / 2, Ia, Ib, Ja, Jb)) {
     // boundary tiles by the staged job (on a forked branch when one is
@@ -2587,6 +2588,9 @@ cudaError_t launch_pre_fused(const Operand& b, Grid<T> vout, Grid<T> f, int nf, 
     if (forked && e == cudaSuccess) e = cudaStreamWaitEvent(s, join, 0);
     return e;
   }
+  if (small_fused_tiles((nf + 1) / 2))
+    return launch_pre_fused_geom<T, PreSmall>(b, vout, f, nf, sweeps, smoother, omega, kind, st,
+                                              s);
   return launch_pre_fused_geom<T, PreLarge>(b, vout, f, nf, sweeps, smoother, omega, kind, st,
                                             s);
 }
@@ -2804,8 +2808,7 @@ static bool post_wave_rect(int n, int& Ra, int& Rb, int& Ca, int& Cb) {
 
 int post_fused_launches(int n, int sweeps, bool f32) {
   int Ra, Rb, Ca, Cb;
-  if (f32 && sweeps == 3 && !small_fused_tiles((n + 1) / 2) && post_wave_rect(n, Ra, Rb, Ca, Cb))
-    return 2;
+  if (f32 && sweeps == 3 && n >= kWaveMinFine && post_wave_rect(n, Ra, Rb, Ca, Cb)) return 2;
   return 1;
 }
 
@@ -2815,11 +2818,9 @@ cudaError_t launch_post_fused(const Operand& vin, const Operand& e, const Operan
                               SolveState* st, ReduceBuf rb, cudaStream_t s, cudaStream_t aux,
                               cudaEvent_t fork, cudaEvent_t join) {
   if (sweeps < 0 || sweeps > kMaxFusedSweeps || (dot && !st)) return cudaErrorInvalidValue;
-  if (small_fused_tiles((n + 1) / 2))
-    return launch_post_fused_geom<T, PostSmall>(vin, e, b, vout, n, sweeps, smoother, omega, dot,
-                                                st, rb, s);
   int Ra, Rb, Ca, Cb;
-  if (std::is_same<T, float>::value && sweeps == 3 && !recorder_slot() && vin.ld % 2 == 0 &&
+  if (std::is_same<T, float>::value && sweeps == 3 && n >= kWaveMinFine && !recorder_slot() &&
+      vin.ld % 2 == 0 &&
       b.ld % 2 == 0 && vout.ld % 2 == 0 && ((uintptr_t)vin.p & 7u) == 0 &&
       ((uintptr_t)b.p & 7u) == 0 && ((uintptr_t)vout.p & 7u) == 0 &&
       post_wave_rect(n, Ra, Rb, Ca, Cb)) {
@@ -2889,6 +2890,9 @@ cudaError_t launch_post_fused(const Operand& vin, const Operand& e, const Operan
     if (forked && e2 == cudaSuccess) e2 = cudaStreamWaitEvent(s, join, 0);
     return e2;
   }
+  if (small_fused_tiles((n + 1) / 2))
+    return launch_post_fused_geom<T, PostSmall>(vin, e, b, vout, n, sweeps, smoother, omega, dot,
+                                                st, rb, s);
   return launch_post_fused_geom<T, PostLarge>(vin, e, b, vout, n, sweeps, smoother, omega, dot,
                                               st, rb, s);
 }
