@@ -908,7 +908,7 @@ cudaError_t launch_cg_dir_mixed(const Operand& z, const Operand& pold, const Ope
 // ---------------------------------------------------------------------------
 // A p~ at one point from the float pair hi + lo of -A p~ (negA; the plain
 // 5-point stencil in the interior): FP64 for the Krylov vectors (rounded
-// once, off the FP64 pipe), and in apf its FP32 rounding for p~.Ap.
+// once, without FP64 arithmetic), and in apf its FP32 rounding for p~.Ap.
 __device__ __forceinline__ double dir_ap(float hi, float lo, float& apf) {
   apf = -(hi + lo);
   return ff_neg_f64(hi, lo);
@@ -2130,9 +2130,210 @@ __global__ void __launch_bounds__(kThreads)
   if (DOT) grid_reduce(acc.value(), rb, [&](double tot) { *dot_out = tot; });
 }
 
+// Strip width (columns of a strip, from `cands`) that minimises the march
+// steps of the busiest warp: rounds of strips per warp x steps per strip
+// (fill + width x per_col).
+static int best_strip_cols(int rows_strips, int cols_total, int warps, const int* cands, int nc,
+                           int fill, int per_col) {
+  long long best = -1;
+  int pick = cands[0];
+  for (int k = 0; k < nc; ++k) {
+    const int w = cands[k];
+    const long long items = (long long)rows_strips * ((cols_total + w - 1) / w);
+    const long long rounds = (items + warps - 1) / warps;
+    const long long cost = rounds * (fill + (long long)per_col * w);
+    if (best < 0 || cost < best) {
+      best = cost;
+      pick = w;
+    }
+  }
+  return pick;
+}
+
+// ---------------------------------------------------------------------------
+// FP32 operator apply on any layout as a register wave.  The plain 5-point
+// interior (rows 1 .. n-2, columns 3 .. n-4) is split into strips of 62 rows
+// x `cols` columns; a warp loads 64 rows, lane l holding rows rb0 + 2l and
+// rb0 + 2l + 1, and marches along j.  Column c arrives through a per-warp
+// cp.async ring kApplyAhead columns ahead: one 8-byte copy per lane where
+// the column is 8-byte aligned at rb0, otherwise two 4-byte copies that are
+// each a contiguous 128-byte run across the warp (lane l fetches rows
+// rb0 + l and rb0 + 32 + l), so the copies stay coalesced whatever the
+// leading dimension.  The output of column c - 1 is formed from the columns
+// c - 2, c - 1, c in registers and the rows above and below by one shuffle
+// each way (rows rb0 and rb0 + 63 are halo).  CTAs past the wave's take the
+// SAT boundary (rows 0 and n-1, columns 0-2 and n-3..n-1) point by point
+// with negA.  Arithmetic per point as in k_apply_direct.
+// ---------------------------------------------------------------------------
+constexpr int kApplyRows = 62;
+constexpr int kApplySlots = 16;                  // power of two: slot = column & 15
+constexpr int kApplyAhead = kApplySlots - 1;
+constexpr int kApplyBoundaryCtas = 32;
+
+struct ApplyWaveArgs {
+  const float* u;
+  float* out;
+  long long ld;
+  int n, nsi, nsj, cols, wave_ctas;
+};
+
+__device__ __forceinline__ void cp_async4(void* sdst, const void* gsrc) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(smem_u32(sdst)), "l"(gsrc)
+               : "memory");
+}
+
+// Rows rb0 .. rb0 + 63 of one column into a 64-float slot (lane l's float2 =
+// rows rb0 + 2l, rb0 + 2l + 1).  wide (uniform across the warp: the column
+// is 8-byte aligned at rb0 and all 64 rows are in the grid): one 8-byte copy
+// per lane.  Otherwise lane l copies rows rb0 + l and rb0 + 32 + l (rows
+// past `last` read row `last`) into floats l and 32 + l.
+__device__ __forceinline__ void cp_async_column(float* slot, const float* col, int rb0, int lane,
+                                                int last, bool wide) {
+  if (wide) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_u32(slot + 2 * lane)),
+                 "l"(col + rb0 + 2 * lane)
+                 : "memory");
+  } else {
+    cp_async4(slot + lane, col + min(rb0 + lane, last));
+    cp_async4(slot + 32 + lane, col + min(rb0 + 32 + lane, last));
+  }
+}
+
+template <bool POS>
+__global__ void __launch_bounds__(kThreads, 6) k_apply_wave(const ApplyWaveArgs a) {
+  __shared__ __align__(16) float2 ring[kWarps][kApplySlots][32];
+  pdl_begin();
+  const int n = a.n;
+  const long long ld = a.ld;
+  const float* __restrict__ u = a.u;
+  float* __restrict__ out = a.out;
+  if ((int)blockIdx.x >= a.wave_ctas) {
+    // SAT boundary: rows 0 and n-1 (all columns), then columns 0, 1, 2,
+    // n-3, n-2, n-1 of rows 1 .. n-2
+    const long long nb = 2LL * n + 6LL * (n - 2);
+    for (long long k = (long long)(blockIdx.x - a.wave_ctas) * kThreads + threadIdx.x; k < nb;
+         k += (long long)(gridDim.x - a.wave_ctas) * kThreads) {
+      int i, j;
+      if (k < 2LL * n) {
+        i = (k < n) ? 0 : n - 1;
+        j = (int)(k < n ? k : k - n);
+      } else {
+        const long long k2 = k - 2LL * n;
+        const int c = (int)(k2 / (n - 2));
+        i = 1 + (int)(k2 % (n - 2));
+        j = c < 3 ? c : n - 6 + c;
+      }
+      struct G {
+        const float* p;
+        long long ld;
+        __device__ float operator()(int di, int dj) const { return __ldg(p + dj * ld + di); }
+      } g{u + (long long)j * ld + i, ld};
+      const float na = negA<float>(g, i, j, n);
+      out[(long long)j * ld + i] = POS ? -na : na;
+    }
+    return;
+  }
+  const int lane = threadIdx.x & 31;
+  const int wl = threadIdx.x >> 5;
+  const int gw = (blockIdx.x * kThreads + threadIdx.x) >> 5;
+  const int nw = (a.wave_ctas * kThreads) >> 5;
+  const int items = a.nsi * a.nsj;
+  const unsigned FULL = 0xffffffffu;
+  for (int it = gw; it < items; it += nw) {
+    const int si = it % a.nsi, sj = it / a.nsi;
+    const int rb0 = kApplyRows * si;                       // rows rb0 + 1 .. rb0 + 62 owned
+    const int r_hi = min(rb0 + 1 + kApplyRows, n - 1);
+    const int c0 = 3 + a.cols * sj;
+    const int c1 = min(c0 + a.cols, n - 3);
+    const int rown = rb0 + 2 * lane;
+    const bool own_x = lane > 0 && rown < r_hi;
+    const bool own_y = lane < 31 && rown + 1 < r_hi;
+    const bool in_grid = rb0 + 63 <= n - 1;
+    const float* pf = u + (long long)(c0 - 1) * ld;        // next column to fetch
+    const int c_first = c0 - 1, c_last = c1;
+#pragma unroll
+    for (int k = 0; k < kApplyAhead; ++k) {
+      const int c = c_first + k;
+      if (c <= c_last)
+        cp_async_column(reinterpret_cast<float*>(&ring[wl][c & (kApplySlots - 1)][0]), pf, rb0,
+                        lane, n - 1, in_grid && ((uintptr_t)(pf + rb0) & 7u) == 0u);
+      pf += ld;
+      cp_async_commit();
+    }
+    float2 q1 = make_float2(0.f, 0.f), q2 = q1;           // columns c - 1, c - 2
+    float* o = out + rown + (long long)c0 * ld;            // the next output column
+#pragma unroll 2
+    for (int c = c_first; c <= c_last; ++c) {
+      cp_async_wait<kApplyAhead - 1>();                    // column c has landed
+      __syncwarp();   // a lane's pair was copied by two other lanes
+      const float2 q0 = ring[wl][c & (kApplySlots - 1)][lane];
+      // the slot of column c + kApplyAhead was read at column c - 1
+      if (c + kApplyAhead <= c_last)
+        cp_async_column(reinterpret_cast<float*>(&ring[wl][(c + kApplyAhead) & (kApplySlots - 1)][0]),
+                        pf, rb0, lane, n - 1, in_grid && ((uintptr_t)(pf + rb0) & 7u) == 0u);
+      pf += ld;
+      cp_async_commit();
+      const float up = __shfl_up_sync(FULL, q1.y, 1);     // row rown - 1, column c - 1
+      const float dn = __shfl_down_sync(FULL, q1.x, 1);   // row rown + 2, column c - 1
+      if (c > c0) {                                        // column c - 1 in [c0, c1)
+        const float sx = (up + q1.y) + (q2.x + q0.x);
+        const float sy = (q1.x + dn) + (q2.y + q0.y);
+        const float vx = POS ? fmaf(4.f, q1.x, -sx) : fmaf(-4.f, q1.x, sx);
+        const float vy = POS ? fmaf(4.f, q1.y, -sy) : fmaf(-4.f, q1.y, sy);
+        if (own_x && own_y && ((uintptr_t)o & 7u) == 0u) {
+          *reinterpret_cast<float2*>(o) = make_float2(vx, vy);
+        } else {
+          if (own_x) o[0] = vx;
+          if (own_y) o[1] = vy;
+        }
+        o += ld;
+      }
+      q2 = q1;
+      q1 = q0;
+    }
+    cp_async_wait<0>();   // no copy outlives the strip
+  }
+}
+
+static int apply_wave_per_sm() {
+  static const int v = [] {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_apply_wave<true>, kThreads, 0) !=
+            cudaSuccess ||
+        b < 1)
+      b = 1;
+    return b;
+  }();
+  return v;
+}
+
+static cudaError_t launch_apply_wave(const float* u, float* out, long long ld, int n, int sign,
+                                     cudaStream_t s) {
+  ApplyWaveArgs a;
+  a.u = u;
+  a.out = out;
+  a.ld = ld;
+  a.n = n;
+  a.nsi = (n - 2 + kApplyRows - 1) / kApplyRows;
+  const int slots = sm_count() * apply_wave_per_sm();
+  static const int cands[] = {16, 24, 32, 40, 48, 64, 96, 128};
+  a.cols = best_strip_cols(a.nsi, n - 6, slots * kWarps, cands, 8, 4, 1);
+  a.nsj = (n - 6 + a.cols - 1) / a.cols;
+  const int items = a.nsi * a.nsj;
+  a.wave_ctas = std::max(1, std::min((items + kWarps - 1) / kWarps, slots));
+  if (sign > 0)
+    return launch_pdl(k_apply_wave<true>, dim3(a.wave_ctas + kApplyBoundaryCtas), dim3(kThreads),
+                      0, s, a);
+  return launch_pdl(k_apply_wave<false>, dim3(a.wave_ctas + kApplyBoundaryCtas), dim3(kThreads),
+                    0, s, a);
+}
+
 template <typename T>
 cudaError_t launch_apply(Grid<const T> u, Grid<T> out, int n, int sign, ReduceBuf rb,
                          double* dot_out, cudaStream_t s) {
+  if (std::is_same<T, float>::value && !dot_out && n >= 65 && u.ld == out.ld)
+    return launch_apply_wave(reinterpret_cast<const float*>(u.p), reinterpret_cast<float*>(out.p),
+                             u.ld, n, sign, s);
   const long long items = (long long)((n + kThreads - 1) / kThreads) *
                           ((n + kApplyCols - 1) / kApplyCols);
   const int grid = (int)std::min<long long>(items, kMaxPersistCtas);
@@ -2364,26 +2565,6 @@ struct PreWaveArgs {
   float m, k1, m2, sc;
   const SolveState* st;
 };
-
-// Strip width (columns of a strip, from `cands`) that minimises the march
-// steps of the busiest warp: rounds of strips per warp x steps per strip
-// (fill + width x per_col).
-static int best_strip_cols(int rows_strips, int cols_total, int warps, const int* cands, int nc,
-                           int fill, int per_col) {
-  long long best = -1;
-  int pick = cands[0];
-  for (int k = 0; k < nc; ++k) {
-    const int w = cands[k];
-    const long long items = (long long)rows_strips * ((cols_total + w - 1) / w);
-    const long long rounds = (items + warps - 1) / warps;
-    const long long cost = rounds * (fill + (long long)per_col * w);
-    if (best < 0 || cost < best) {
-      best = cost;
-      pick = w;
-    }
-  }
-  return pick;
-}
 
 __device__ __forceinline__ void cp_async8(void* sdst, const void* gsrc) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_u32(sdst)), "l"(gsrc)

@@ -311,7 +311,7 @@ def test_apply_unaligned_arrays(sbp, n):
 
 def test_pair_to_f64_matches_fp64_add(sbp):
     # the direction pass forms -(hi + lo) of its float-float stencil without
-    # the FP64 pipe: the bits must be those of the FP64 add, over random bit
+    # FP64 arithmetic: the bits must be those of the FP64 add, over random bit
     # patterns, cancelling pairs and every exponent gap
     rng = np.random.default_rng(11)
     n = 1 << 22
@@ -344,3 +344,32 @@ def test_pair_to_f64_matches_fp64_add(sbp):
     assert normal.mean() > 0.95
     bad = np.flatnonzero(got[normal].view(np.uint64) != ref[normal].view(np.uint64))
     assert bad.size == 0, (hi[normal][bad[:4]], lo[normal][bad[:4]])
+
+
+@pytest.mark.parametrize("n,offset", [(66, 0), (67, 1), (100, 1), (1025, 0), (1025, 1)])
+def test_apply_f32_interior_bits(sbp, n, offset):
+    # the FP32 apply's plain interior (rows 1..n-2, columns 3..n-4) is
+    # fma(+-4, u0, -+((u_i-1 + u_i+1) + (u_j-1 + u_j+1))) in FP32: bit for bit
+    # against the same operations emulated in numpy (4 u0 - s is exact in
+    # FP64, so one rounding to FP32 is the FMA); the SAT boundary against the
+    # oracle.  Odd and even n - 1 and arrays starting 4 bytes into a buffer.
+    rng = np.random.default_rng(n + offset)
+    u = rng.standard_normal((n, n)).astype(np.float32)   # [j, i]: column-major
+    lib = sbp.load_library()
+    buf = torch.zeros(n * n + offset, dtype=torch.float32, device="cuda")
+    buf[offset:] = dev(u.ravel(), torch.float32)
+    out = torch.full((n * n + offset,), np.nan, dtype=torch.float32, device="cuda")
+    for sign in (-1, 1):
+        assert lib.sbp_apply_f32(C.c_void_p(buf[offset:].data_ptr()),
+                                 C.c_void_p(out[offset:].data_ptr()), n, sign, None) == 0
+        got = out[offset:].cpu().numpy().reshape(n, n)
+        c0 = u[3:n - 3, 1:n - 1]
+        s = (u[3:n - 3, 0:n - 2] + u[3:n - 3, 2:n]) + (u[2:n - 4, 1:n - 1] + u[4:n - 2, 1:n - 1])
+        if sign > 0:
+            want = (4.0 * c0.astype(np.float64) - s.astype(np.float64)).astype(np.float32)
+        else:
+            want = (s.astype(np.float64) - 4.0 * c0.astype(np.float64)).astype(np.float32)
+        assert np.array_equal(got[3:n - 3, 1:n - 1].view(np.uint32), want.view(np.uint32))
+        ref = -sign * o.neg_A_matrix_free(u.ravel().astype(np.float64), n).reshape(n, n)
+        assert np.isfinite(got).all()
+        assert relerr(got.ravel().astype(np.float64), ref.ravel()) < 1e-6
