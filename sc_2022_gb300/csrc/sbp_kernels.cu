@@ -2822,7 +2822,7 @@ static cudaError_t launch_post_fused_geom(const Operand& vin, const Operand& e, 
 constexpr int kPostRows = 56;
 constexpr int kRingPartialsOffset = 2080;
 static_assert(kRingPartialsOffset + 2080 <= kMaxPersistCtas + 64, "split partials buffer");
-constexpr int kPostAhead = 8;
+constexpr int kPostAhead = 10;
 constexpr int kPostSlots = kPostAhead + 1;
 
 struct PostWaveArgs {
