@@ -373,8 +373,10 @@ int sbp_test_drop_copy(int drop, unsigned wait_polls);
 /* Test hook for the direction pass's FP64 conversion (no counterpart in the
  * reference): out[k] = -(hi[k] + lo[k]) for float pairs, formed as the mixed
  * MGCG direction forms A p~ in FP64, without FP64 arithmetic (an FP32 two-sum and
- * an integer step on the FP64 bit pattern).  Must equal
- * -((double)hi + (double)lo) bit for bit.  Device arrays of length n. */
+ * an integer step on the FP64 bit pattern; the packed two-row form of the
+ * interior wave on alternate pairs, the scalar form of the boundary tiles
+ * on the others).  Must equal -((double)hi + (double)lo) bit for bit.
+ * Device arrays of length n. */
 int sbp_test_pair_to_f64(const float* hi, const float* lo, double* out, long long n,
                          void* stream);
 

@@ -3114,14 +3114,14 @@ struct DirWaveArgs {
   ReduceBuf rb;
 };
 
-__global__ void __launch_bounds__(kThreads) k_dir_wave(const DirWaveArgs a) {
+__global__ void __launch_bounds__(kThreads, 5) k_dir_wave(const DirWaveArgs a) {
   __shared__ __align__(16) float2 zring[kWarps][kDirSlots][32];
   __shared__ __align__(16) float2 pring[kWarps][kDirSlots][32];
   pdl_begin();
   SolveState* st = a.st;
   if (st->done) return;   // uniform: the state was final before this launch
   const bool first = (st->iter == 0);   // p~_old is not read
-  const float beta = (float)st->beta;
+  const float2 beta = make_float2((float)st->beta, (float)st->beta);
   const int lane = threadIdx.x & 31;
   const int wl = threadIdx.x >> 5;
   const int gw = (blockIdx.x * kThreads + threadIdx.x) >> 5;
@@ -3130,7 +3130,7 @@ __global__ void __launch_bounds__(kThreads) k_dir_wave(const DirWaveArgs a) {
   const unsigned FULL = 0xffffffffu;
   float2* const zmine = &zring[wl][0][lane];
   float2* const pmine = &pring[wl][0][lane];
-  DotAcc<float> acc;
+  DotAcc2 acc;   // p~ . fl32(-A p~), negated at the end
   for (int it = gw; it < items; it += nw) {
     const int si = it % a.nsi, sj = it / a.nsi;
     const int rb0 = a.Ra - 1 + kDirRows * si;             // even: Ra is odd
@@ -3157,12 +3157,7 @@ __global__ void __launch_bounds__(kThreads) k_dir_wave(const DirWaveArgs a) {
     for (int c = c_first; c <= c_last; ++c) {
       cp_async_wait<kDirAhead - 1>();                       // column c has landed
       const float2 zv = zmine[slot * 32];
-      float2 q0 = zv;
-      if (!first) {
-        const float2 pv = pmine[slot * 32];
-        q0.x = fmaf(beta, pv.x, zv.x);
-        q0.y = fmaf(beta, pv.y, zv.y);
-      }
+      const float2 q0 = first ? zv : fma2(beta, pmine[slot * 32], zv);
       {
         const int cn = c + kDirAhead;
         if (cn <= c_last) {
@@ -3185,10 +3180,12 @@ __global__ void __launch_bounds__(kThreads) k_dir_wave(const DirWaveArgs a) {
       const float above = __shfl_up_sync(FULL, q1.y, 1);    // row ra - 1, column c - 1
       const float below = __shfl_down_sync(FULL, q1.x, 1);  // row ra + 2, column c - 1
       if (c > c0) {                                         // column c - 1 is in [c0, c1)
-        float hx, lx, hy, ly, fx, fy;
-        stencil_ff(above, q1.y, q2.x, q0.x, q1.x, hx, lx);
-        stencil_ff(q1.x, below, q2.y, q0.y, q1.y, hy, ly);
-        const double ax = dir_ap(hx, lx, fx), ay = dir_ap(hy, ly, fy);
+        // both rows at once: the stencil_ff and dir_ap of the staged path,
+        // lane by lane
+        float2 hi, lo, sum;
+        stencil_ff2(make_float2(above, q1.x), make_float2(q1.y, below), q2, q0, q1, hi, lo);
+        double ax, ay;
+        ff_neg_f64_2(hi, lo, ax, ay, sum);                  // fl32(A p~) = -sum
         double* o = a.Ap + (size_t)(c - 1) * a.lda + ra;
         if (own_x && own_y) {
           *reinterpret_cast<double2*>(o) = make_double2(ax, ay);
@@ -3196,8 +3193,7 @@ __global__ void __launch_bounds__(kThreads) k_dir_wave(const DirWaveArgs a) {
           if (own_x) o[0] = ax;
           if (own_y) o[1] = ay;
         }
-        if (own_x) acc.add_prod(q1.x, fx);
-        if (own_y) acc.add_prod(q1.y, fy);
+        acc.add_prod(make_float2(own_x ? q1.x : 0.f, own_y ? q1.y : 0.f), sum);
       }
       q2 = q1;
       q1 = q0;
@@ -3205,7 +3201,7 @@ __global__ void __launch_bounds__(kThreads) k_dir_wave(const DirWaveArgs a) {
     cp_async_wait<0>();   // no copy outlives the strip
   }
   // the boundary tiles' share comes from the staged pass running beside
-  grid_reduce(acc.value(), a.rb, [&](double tot) { pap_join(st, &st->pap_wave, tot); });
+  grid_reduce(-acc.value(), a.rb, [&](double tot) { pap_join(st, &st->pap_wave, tot); });
 }
 
 int cg_dir_f32_launches(int n) {
@@ -3356,11 +3352,24 @@ unsigned int read_device_fault() {
   return v;
 }
 
+// Elements 2t, 2t+1 per step: the packed form of the direction wave for
+// even t, the scalar form of the staged direction tiles for odd t.
 __global__ void k_pair_to_f64(const float* __restrict__ hi, const float* __restrict__ lo,
                               double* __restrict__ out, long long n) {
-  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
-       k += (long long)gridDim.x * blockDim.x)
-    out[k] = ff_neg_f64(hi[k], lo[k]);
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; 2 * t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long k = 2 * t;
+    if (k + 1 < n && (t & 1) == 0) {
+      double rx, ry;
+      float2 s;
+      ff_neg_f64_2(make_float2(hi[k], hi[k + 1]), make_float2(lo[k], lo[k + 1]), rx, ry, s);
+      out[k] = rx;
+      out[k + 1] = ry;
+    } else {
+      out[k] = ff_neg_f64(hi[k], lo[k]);
+      if (k + 1 < n) out[k + 1] = ff_neg_f64(hi[k + 1], lo[k + 1]);
+    }
+  }
 }
 
 cudaError_t launch_pair_to_f64(const float* hi, const float* lo, double* out, long long n,

@@ -442,6 +442,84 @@ struct DotAcc<float> {
   __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
 };
 
+// ---------------------------------------------------------------------------
+// Packed FP32 pairs: Blackwell issues one instruction for both lanes of a
+// float2 (f32x2 add/mul/fma), each lane rounded exactly as the scalar
+// operation.  The register waves hold two grid rows per thread, so their
+// per-row arithmetic pairs up; issue, not the FP32 rate, bounds them.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+// a - b: b * -1 is exact, so the FMA rounds once, as the subtraction does
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+  return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+}
+__device__ __forceinline__ void two_sum2(float2 a, float2 b, float2& s, float2& e) {
+  s = add2(a, b);
+  const float2 bb = sub2(s, a);
+  e = add2(sub2(a, sub2(s, bb)), sub2(b, bb));
+}
+// stencil_ff on two rows at once: w/e the i-1/i+1 neighbours, m/p the
+// j-1/j+1 neighbours, c the centre; the same operations per lane.
+__device__ __forceinline__ void stencil_ff2(float2 w, float2 e, float2 m, float2 p, float2 c,
+                                            float2& hi, float2& lo) {
+  float2 a, ea, b, eb, cc, ec, d, ed;
+  two_sum2(w, e, a, ea);
+  two_sum2(m, p, b, eb);
+  two_sum2(a, b, cc, ec);
+  two_sum2(cc, mul2(make_float2(-4.f, -4.f), c), d, ed);
+  hi = d;
+  lo = add2(add2(ea, eb), add2(ec, ed));
+}
+// ff_neg_f64 for two pairs (the two-sum and the scaling packed); s returns
+// fl32(hi + lo) per lane
+__device__ __forceinline__ void ff_neg_f64_2(float2 hi, float2 lo, double& rx, double& ry,
+                                             float2& s) {
+  float2 e;
+  two_sum2(hi, lo, s, e);
+  const unsigned ux = __float_as_uint(s.x), uy = __float_as_uint(s.y);
+  const unsigned Ex = (ux >> 23) & 0xFFu, Ey = (uy >> 23) & 0xFFu;
+  // 2^(179 - E) as a float; E outside [52, 254] takes the FP64 add below
+  const float2 sc = make_float2(__uint_as_float((306u - min(max(Ex, 52u), 254u)) << 23),
+                                __uint_as_float((306u - min(max(Ey, 52u), 254u)) << 23));
+  const float2 kf = mul2(e, sc);
+  auto one = [](float hv, float lv, float sv, float ev, unsigned u, unsigned E, float k) {
+    const unsigned neg = u & 0x80000000u;
+    if (E >= 52u && E != 255u &&
+        ((u & 0x7FFFFFu) != 0u || ((neg ^ __float_as_uint(ev)) & 0x80000000u) == 0u ||
+         ev == 0.0f)) {
+      const unsigned long long ds = ((unsigned long long)neg << 32) |
+                                    ((unsigned long long)(E + 896u) << 52) |
+                                    ((unsigned long long)(u & 0x7FFFFFu) << 29);
+      const int kk = __float2int_rn(k);
+      const long long step = neg ? -(long long)kk : (long long)kk;
+      return __longlong_as_double(
+          (long long)((ds + (unsigned long long)step) ^ 0x8000000000000000ull));
+    }
+    return -((double)hv + (double)lv);
+  };
+  rx = one(hi.x, lo.x, s.x, e.x, ux, Ex, kf.x);
+  ry = one(hi.y, lo.y, s.y, e.y, uy, Ey, kf.y);
+}
+
+// Compensated dot accumulation of two rows at once (one float pair per
+// row, added together at the end).
+struct DotAcc2 {
+  float2 hi = make_float2(0.f, 0.f), lo = make_float2(0.f, 0.f);
+  __device__ __forceinline__ void add_prod(float2 a, float2 b) {
+    const float2 p = mul2(a, b);
+    const float2 e = fma2(a, b, make_float2(-p.x, -p.y));
+    float2 s, err;
+    two_sum2(hi, p, s, err);
+    hi = s;
+    lo = add2(lo, add2(err, e));
+  }
+  __device__ __forceinline__ double value() const {
+    return ((double)hi.x + (double)lo.x) + ((double)hi.y + (double)lo.y);
+  }
+};
+
 // Stage the raw values of g over [i0, i0+ei) x [j0, j0+ej) into s with row
 // pitch P; points outside the n x n domain are zero-filled.
 template <int P, typename T>
