@@ -293,7 +293,7 @@ __global__ void __launch_bounds__(kThreads) k_persist(const __grid_constant__ Jo
     cp_async_wait<1>();
     // TMA stages: one thread observes the transaction barrier, the block
     // barrier then orders the staged data for every thread (and gives every
-    // thread the same verdict)
+    // thread the same result)
     bool arrived = true;
     if (threadIdx.x == 0) arrived = mbar_wait_bounded(&bar[k & 1], (k >> 1) & 1);
     ok = __syncthreads_and(arrived);
