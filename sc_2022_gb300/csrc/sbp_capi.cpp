@@ -957,11 +957,9 @@ int sbp_vcycle_apply(sbp_solver* s, const double* b, double* v, void* stream) {
     SBP_CUDA(enqueue_vcycle<float>(s, 0, false, nullptr, q));
     SBP_CUDA((launch_copy<float, double>(cgrid<float>(vcycle_out(s), ld), grid<double>(v, n), n, q)));
   } else {
-    SBP_CUDA(cudaMemcpy2DAsync(s->r, (size_t)ld * 8, b, (size_t)n * 8, (size_t)n * 8, n,
-                               cudaMemcpyDeviceToDevice, q));
+    SBP_CUDA(copy_grid(s->r, ld, b, n, n, q));
     SBP_CUDA(enqueue_vcycle<double>(s, 0, false, nullptr, q));
-    SBP_CUDA(cudaMemcpy2DAsync(v, (size_t)n * 8, vcycle_out(s), (size_t)ld * 8, (size_t)n * 8, n,
-                               cudaMemcpyDeviceToDevice, q));
+    SBP_CUDA(copy_grid(v, n, static_cast<const double*>(vcycle_out(s)), ld, n, q));
   }
   return SBP_OK;
 }

@@ -3756,11 +3756,22 @@ cudaError_t launch_copy_grid_batch(const unsigned char* blobs, int stride, int c
                     blobs, stride);
 }
 
+__global__ void __launch_bounds__(kThreads) k_copy_grid(const Copy2DArgs a) {
+  pdl_begin();
+  for (int j = blockIdx.x; j < a.n; j += gridDim.x)
+    for (int i = threadIdx.x; i < a.n; i += kThreads)
+      a.dst[(size_t)j * a.dld + i] = __ldg(a.src + (size_t)j * a.sld + i);
+}
+
+// Grid copy between leading dimensions by the SMs: at N = 4097 a pitched
+// device-to-device cudaMemcpy2DAsync (copy engine) took 138 us, this kernel
+// 56 us.
 cudaError_t copy_grid(double* dst, int dld, const double* src, int sld, int n, cudaStream_t s) {
   if (recorder_slot())
     return record_launch(&launch_copy_grid_batch, Copy2DArgs{dst, dld, src, sld, n}, n);
-  return cudaMemcpy2DAsync(dst, (size_t)dld * sizeof(double), src, (size_t)sld * sizeof(double),
-                           (size_t)n * sizeof(double), n, cudaMemcpyDeviceToDevice, s);
+  if (n <= 0) return cudaSuccess;
+  return launch_pdl(k_copy_grid, dim3(std::min(n, 4096)), dim3(kThreads), 0, s,
+                    Copy2DArgs{dst, dld, src, sld, n});
 }
 
 // ---------------------------------------------------------------------------
