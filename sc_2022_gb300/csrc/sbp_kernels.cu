@@ -2587,14 +2587,17 @@ __global__ void __launch_bounds__(kThreads) k_pre_wave(const PreWaveArgs a) {
   const unsigned FULL = 0xffffffffu;
   for (int it = gw; it < items; it += nw) {
     const int si = it % a.nsi, sj = it / a.nsi;
-    const int I0 = a.Ia + kWaveRows * si;
-    const int I1 = min(I0 + kWaveRows, a.Ib);
+    // the strip owns coarse rows [In, I1); the last one is moved up to end
+    // at Ib so that its loads stay 28 fine rows inside the grid
+    const int In = a.Ia + kWaveRows * si;
+    const int I0 = min(In, a.Ib - kWaveRows);
+    const int I1 = min(In + kWaveRows, a.Ib);
     const int J0 = a.Ja + a.cols * sj;
     const int J1 = min(J0 + a.cols, a.Jb);
     const int ra = 2 * I0 - 4 + 2 * lane;               // this lane's first fine row
-    const bool own_rows = lane >= 2 && ra + 1 <= 2 * I1 - 1;
     const int I = I0 + lane - 2;                          // coarse row centred on ra
-    const bool own_f = lane >= 2 && I < I1;
+    const bool own_rows = lane >= 2 && I >= In && I < I1;
+    const bool own_f = own_rows;
     const int c_first = 2 * J0 - 4, c_last = 2 * J1 + 2;  // leading columns marched
     const float* bp = a.b + (size_t)ra;
     float2* const mine = &ring[wl][0][lane];
@@ -2674,17 +2677,19 @@ __global__ void __launch_bounds__(kThreads) k_pre_wave(const PreWaveArgs a) {
   }
 }
 
-// Whether the interior rectangle of the PreLarge tiling is non-empty and
-// which coarse range it covers.
+// Whether the interior rectangle of the PreSmall tiling (all but its first
+// and last tile rows and columns) is non-empty and which coarse range it
+// covers; the boundary ring around it is one small tile deep.
 static bool pre_wave_rect(int nc, int& Ia, int& Ib, int& Ja, int& Jb) {
-  const int ntx = ntiles(nc, RTI), nty = ntiles(nc, RTJ);
+  constexpr int RI = PreSmall::RI, RJ = PreSmall::RJ;
+  const int ntx = ntiles(nc, RI), nty = ntiles(nc, RJ);
   if (ntx < 3 || nty < 3) return false;
-  if ((nc - 1) % RTI != 0 || (nc - 1) % RTJ != 0) return false;   // full tiles only
-  Ia = RTI + 1;
-  Ib = RTI * (ntx - 1) + 1;
-  Ja = RTJ + 1;
-  Jb = RTJ * (nty - 1) + 1;
-  return Ia < Ib && Ja < Jb;
+  if ((nc - 1) % RI != 0 || (nc - 1) % RJ != 0) return false;   // full tiles only
+  Ia = RI + 1;
+  Ib = RI * (ntx - 1) + 1;
+  Ja = RJ + 1;
+  Jb = RJ * (nty - 1) + 1;
+  return Ib - Ia >= kWaveRows && Ja < Jb;
 }
 
 static cudaError_t launch_pre_wave(const Operand& b, Grid<float> vout, Grid<float> f, int nf,
@@ -2755,12 +2760,10 @@ cudaError_t launch_pre_fused(const Operand& b, Grid<T> vout, Grid<T> f, int nf, 
       e = cudaEventRecord(fork, s);
       if (e == cudaSuccess) e = cudaStreamWaitEvent(aux, fork, 0);
     }
-    // the ring is one large tile deep: two of the quarter-size tiles, which
-    // split its serial work four ways
-    static_assert(2 * PreSmall::RI == RTI && 2 * PreSmall::RJ == RTJ, "ring of small tiles");
+    // the ring: one small tile deep
     if (e == cudaSuccess)
       e = launch_pre_fused_geom<T, PreSmall>(b, vout, f, nf, sweeps, smoother, omega, kind, st,
-                                             forked ? aux : s, 2);
+                                             forked ? aux : s, 1);
     if (forked && e == cudaSuccess) e = cudaEventRecord(join, aux);
     if (e != cudaSuccess) return e;
     e = launch_pre_wave(b, Grid<float>{reinterpret_cast<float*>(vout.p), vout.ld},
@@ -2856,8 +2859,11 @@ __global__ void __launch_bounds__(kThreads, 4) k_post_wave(const PostWaveArgs a)
   DotAcc<float> acc;
   for (int it = gw; it < items; it += nw) {
     const int si = it % a.nsi, sj = it / a.nsi;
-    const int rb0 = (a.Ra & ~1) - 4 + kPostRows * si;   // even
-    const int r_lo = max(rb0 + 4, a.Ra), r_hi = min(rb0 + 4 + kPostRows, a.Rb);
+    // the strip owns rows [r_lo, r_hi); the last one loads from the even row
+    // at or above Rb - 60, so that its loads stay inside the grid
+    const int rbn = (a.Ra & ~1) - 4 + kPostRows * si;
+    const int rb0 = min(rbn, (a.Rb - 4 - kPostRows + 1) & ~1);   // even
+    const int r_lo = max(rbn + 4, a.Ra), r_hi = min(rbn + 4 + kPostRows, a.Rb);
     const int c0 = a.Ca + a.cols * sj;
     const int c1 = min(c0 + a.cols, a.Cb);
     const int ra = rb0 + 2 * lane;
@@ -2975,16 +2981,27 @@ __global__ void __launch_bounds__(kThreads, 4) k_post_wave(const PostWaveArgs a)
   if (DOT) grid_reduce(acc.value(), a.rb, [&](double tot) { rz_join(a.st, &a.st->rz_wave, tot); });
 }
 
-// The interior rectangle of the PostLarge tiling (fine coordinates).
-static bool post_wave_rect(int n, int& Ra, int& Rb, int& Ca, int& Cb) {
-  const int ntx = ntiles(n, TI), nty = ntiles(n, TJ);
+// The interior rectangle of a T1 x T2 tiling of the fine grid (all but its
+// first and last tile rows and columns).
+template <int T1, int T2>
+static bool interior_rect(int n, int& Ra, int& Rb, int& Ca, int& Cb) {
+  const int ntx = ntiles(n, T1), nty = ntiles(n, T2);
   if (ntx < 3 || nty < 3) return false;
-  if ((n - 1) % TI != 0 || (n - 1) % TJ != 0) return false;   // full tiles only
-  Ra = TI + 1;
-  Rb = TI * (ntx - 1) + 1;
-  Ca = TJ + 1;
-  Cb = TJ * (nty - 1) + 1;
+  if ((n - 1) % T1 != 0 || (n - 1) % T2 != 0) return false;   // full tiles only
+  Ra = T1 + 1;
+  Rb = T1 * (ntx - 1) + 1;
+  Ca = T2 + 1;
+  Cb = T2 * (nty - 1) + 1;
   return Ra < Rb && Ca < Cb;
+}
+// the post-smoothing wave: inside the PostSmall tiling (ring one small tile
+// deep); the direction wave: inside the 64 x 32 tiles of CgDirF32Job
+static bool post_wave_rect(int n, int& Ra, int& Rb, int& Ca, int& Cb) {
+  return interior_rect<PostSmall::TI, PostSmall::TJ>(n, Ra, Rb, Ca, Cb) &&
+         Rb - Ra >= 4 + kPostRows;
+}
+static bool dir_wave_rect(int n, int& Ra, int& Rb, int& Ca, int& Cb) {
+  return interior_rect<TI, TJ>(n, Ra, Rb, Ca, Cb);
 }
 
 int post_fused_launches(int n, int sweeps, bool f32) {
@@ -3005,7 +3022,6 @@ cudaError_t launch_post_fused(const Operand& vin, const Operand& e, const Operan
       b.ld % 2 == 0 && vout.ld % 2 == 0 && ((uintptr_t)vin.p & 7u) == 0 &&
       ((uintptr_t)b.p & 7u) == 0 && ((uintptr_t)vout.p & 7u) == 0 &&
       post_wave_rect(n, Ra, Rb, Ca, Cb)) {
-    static_assert(2 * PostSmall::TI == TI && 2 * PostSmall::TJ == TJ, "ring of small tiles");
     // the boundary ring (two quarter-size tiles deep) by the staged job on a
     // forked branch; with the dot, the two reductions meet in rz_join
     const bool forked = aux && fork && join;
@@ -3021,7 +3037,7 @@ cudaError_t launch_post_fused(const Operand& vin, const Operand& e, const Operan
                             rb.ticket ? rb.ticket + 8 : nullptr};
     if (e2 == cudaSuccess)
       e2 = launch_post_fused_geom<T, PostSmall>(vin, e, b, vout, n, sweeps, smoother, omega, dot,
-                                                st, rb_ring, forked ? aux : s, 2, dot ? 1 : 0);
+                                                st, rb_ring, forked ? aux : s, 1, dot ? 1 : 0);
     if (forked && e2 == cudaSuccess) e2 = cudaEventRecord(join, aux);
     if (e2 != cudaSuccess) return e2;
     PostWaveArgs a;
@@ -3206,7 +3222,7 @@ __global__ void __launch_bounds__(kThreads, 5) k_dir_wave(const DirWaveArgs a) {
 
 int cg_dir_f32_launches(int n) {
   int Ra, Rb, Ca, Cb;
-  return (n >= kDirWaveMinN && post_wave_rect(n, Ra, Rb, Ca, Cb)) ? 2 : 1;
+  return (n >= kDirWaveMinN && dir_wave_rect(n, Ra, Rb, Ca, Cb)) ? 2 : 1;
 }
 
 static int dir_wave_per_sm() {
@@ -3230,7 +3246,7 @@ cudaError_t launch_cg_dir_f32(const Operand& z, const Operand& pold, Grid<float>
                     pold.ld % 2 == 0 && pnew.ld % 2 == 0 && Ap.ld % 2 == 0 &&
                     ((uintptr_t)z.p & 7u) == 0 && ((uintptr_t)pold.p & 7u) == 0 &&
                     ((uintptr_t)pnew.p & 7u) == 0 && aligned16(Ap.p) &&
-                    post_wave_rect(n, Ra, Rb, Ca, Cb);
+                    dir_wave_rect(n, Ra, Rb, Ca, Cb);
   if (!wave) return launch_cg_dir_f32_staged(z, pold, pnew, Ap, n, st, rb, s, 0);
   // the boundary tiles by the staged job on a forked branch (or before the
   // wave on the same stream); the two p.Ap shares meet in pap_join
