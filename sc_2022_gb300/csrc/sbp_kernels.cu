@@ -2533,11 +2533,11 @@ static cudaError_t launch_pre_fused_geom(const Operand& b, Grid<T> vout, Grid<T>
 // Jacobi/Richardson sweeps from zero, residual, restriction), the job of
 // PreFusedJob's interior tiles without shared memory or block barriers.
 //
-// A warp owns a strip of 28 coarse rows x up to 32 coarse columns of the
-// interior rectangle [Ia, Ib) x [Ja, Jb) (the union of the PreLarge tiles
+// A warp owns a strip of 28 coarse rows x `cols` coarse columns of the
+// interior rectangle [Ia, Ib) x [Ja, Jb) (the union of the PreSmall tiles
 // that are neither in the first nor in the last tile row or column: every
 // point there and in its halo has the plain 5-point stencil and the
-// constant smoother weight).  Lane l holds fine rows 2 I0 - 4 + 2l and the
+// constant smoother weight); the last row strip is moved up to end at Ib.  Lane l holds fine rows 2 I0 - 4 + 2l and the
 // row after it (64 rows: 56 owned plus a 4-row halo on each side), and the
 // warp marches along j with every stage one column behind the previous:
 //   step c: b at column c (loaded D columns ahead as one float2 per lane),
@@ -2809,9 +2809,10 @@ static cudaError_t launch_post_fused_geom(const Operand& vin, const Operand& e, 
 // Register wave post-smoothing for the interior of a fine level (FP32,
 // prolongation of the coarse correction + three sweeps, optional b.v dot),
 // the job of PostFusedJob's interior tiles without shared-memory sweeps or
-// block barriers.  A warp owns a strip of up to 56 fine rows x 64 fine
+// block barriers.  A warp owns a strip of up to 56 fine rows x `cols` fine
 // columns of the interior rectangle [Ra, Rb) x [Ca, Cb) (the union of the
-// PostLarge tiles outside the first and last tile rows and columns).  Lane l
+// PostSmall tiles outside the first and last tile rows and columns); the
+// last row strip loads from higher up so that it ends inside the grid.  Lane l
 // holds fine rows rb0 + 2l (even: coarse row rb0/2 + l) and rb0 + 2l + 1;
 // the warp marches along j:
 //   step c: F0 = v_in + P e at column c, sweep 1 at c - 1, sweep 2 at
@@ -3022,7 +3023,7 @@ cudaError_t launch_post_fused(const Operand& vin, const Operand& e, const Operan
       b.ld % 2 == 0 && vout.ld % 2 == 0 && ((uintptr_t)vin.p & 7u) == 0 &&
       ((uintptr_t)b.p & 7u) == 0 && ((uintptr_t)vout.p & 7u) == 0 &&
       post_wave_rect(n, Ra, Rb, Ca, Cb)) {
-    // the boundary ring (two quarter-size tiles deep) by the staged job on a
+    // the boundary ring (one quarter-size tile deep) by the staged job on a
     // forked branch; with the dot, the two reductions meet in rz_join
     const bool forked = aux && fork && join;
     cudaError_t e2 = cudaSuccess;

@@ -59,9 +59,10 @@ cudaError_t launch_pre_fused(const Operand& b, Grid<T> vout, Grid<T> f, int nf, 
                              int smoother, double omega, int kind, const SolveState* st,
                              cudaStream_t s, cudaStream_t aux = nullptr,
                              cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
-// Large FP32 levels: the boundary ring by the staged job (forked onto `aux`
-// when aux/fork/join are given and there is no dot), the interior by the
-// register wave kernel.
+// FP32 levels from N = 1025 with three sweeps: the boundary ring (one small
+// tile deep) by the staged job (forked onto `aux` when aux/fork/join are
+// given), the interior by the register wave kernel; with the dot, the two
+// shares of r.z meet in a fixed order.
 template <typename T>
 cudaError_t launch_post_fused(const Operand& vin, const Operand& e, const Operand& b, Grid<T> vout,
                               int n, int sweeps, int smoother, double omega, int dot,
@@ -83,7 +84,8 @@ int apply_dot_f64_noalloc(const double* u, double* out, int n, int sign, double*
 cudaError_t measure_fp64_fma_rate(double* gfma_per_s, cudaStream_t s);
 
 // Kernel launches of one launch_pre_fused call on a solver level (the
-// interior of the large FP32 levels takes a second, register-wave kernel).
+// interior of the FP32 levels from N = 1025 takes a second, register-wave
+// kernel).
 int pre_fused_launches(int nf, int sweeps, bool f32);
 // The same for launch_post_fused.
 int post_fused_launches(int n, int sweeps, bool f32);
