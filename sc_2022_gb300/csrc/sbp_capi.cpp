@@ -119,7 +119,6 @@ struct sbp_solver {
   std::vector<void*> allocs;
   cudaStream_t cap = nullptr;       // private stream for graph capture
   cudaStream_t aux = nullptr;       // forked branch (boundary tiles of the wave levels)
-  cudaEvent_t dfork = nullptr, djoin = nullptr;   // and of the FP32 direction pass
   cudaEvent_t ev[2] = {nullptr, nullptr};
   // cached iteration graphs: [kind][parity]; kind 0 = MGCG, 1 = CG
   cudaGraphExec_t iter_exec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
@@ -270,9 +269,7 @@ long long vcycle_launches(const sbp_solver* s, bool dot) {
 
 // Kernel launches of one Krylov iteration (mirrors enqueue_iteration).
 long long iteration_launches(const sbp_solver* s, int kind) {
-  if (kind != 0) return 2;
-  const bool mixed = (s->opts.precision == SBP_PREC_MIXED);
-  return (mixed ? cg_dir_f32_launches(s->n) : 1) + 1 + vcycle_launches(s, true);
+  return 2 + (kind == 0 ? vcycle_launches(s, true) : 0);
 }
 
 cudaError_t enqueue_vcycle_any(sbp_solver* s, bool dot, SolveState* st, cudaStream_t q) {
@@ -302,8 +299,7 @@ cudaError_t enqueue_iteration(sbp_solver* s, int kind, int parity, int sign, cud
     if (mixed)
       // FP32 direction p~ and Ap = A p~ (exact) in one pass
       e = launch_cg_dir_f32(vcycle_out_op(s), s->op32[parity], grid<float>(s->p32[1 - parity], ld),
-                            grid<double>(s->Ap, ld), n, s->st, s->rb, q, s->aux, s->dfork,
-                            s->djoin);
+                            grid<double>(s->Ap, ld), n, s->st, s->rb, q);
     else
       e = launch_cg_dir_op<double, double>(vcycle_out_op(s), s->op[parity], grid<double>(pnew, ld),
                                            grid<double>(s->Ap, ld), n, +1, s->st, s->rb, q);
@@ -734,11 +730,6 @@ int sbp_solver_create(sbp_solver** out, int n, const sbp_options* opts) {
         SBP_CUDA(cudaMemset(s->p32[k], 0, nn * sizeof(float)));
         make_operand(s->op32[k], s->p32[k], n, s->ld, false);
       }
-      if (cg_dir_f32_launches(n) == 2) {
-        SBP_CUDA(cudaEventCreateWithFlags(&s->dfork, cudaEventDisableTiming));
-        SBP_CUDA(cudaEventCreateWithFlags(&s->djoin, cudaEventDisableTiming));
-        if (!s->aux) SBP_CUDA(cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking));
-      }
     }
     int m = n;
     while (true) {
@@ -810,8 +801,6 @@ int sbp_solver_destroy(sbp_solver* s) {
   if (s->aux) cudaStreamDestroy(s->aux);
   for (auto& e : s->ev)
     if (e) cudaEventDestroy(e);
-  for (cudaEvent_t ev : {s->dfork, s->djoin})
-    if (ev) cudaEventDestroy(ev);
   for (Level& L : s->levels) {
     for (cudaEvent_t ev : {L.fork, L.join, L.pfork, L.pjoin})
       if (ev) cudaEventDestroy(ev);

@@ -159,12 +159,6 @@ struct SolveState {
   double rz_wave;
   unsigned join;
   int pad2;
-  // p.Ap of the FP32 direction pass split the same way (boundary tiles and
-  // interior wave)
-  double pap_part;
-  double pap_wave;
-  unsigned pap_join;
-  int pad3;
 };
 
 constexpr int kDoneConverged = 1;

@@ -923,20 +923,6 @@ __device__ __forceinline__ void finish_pap(SolveState* st, double tot) {
     st->alpha = st->rz / tot;
 }
 
-// One side of a p.Ap split between the boundary tiles and the interior wave
-// of the FP32 direction pass (running concurrently): each side leaves its
-// share and counts in; the second to arrive finishes with ring + wave (fixed
-// order) and re-arms the counter.
-__device__ __forceinline__ void pap_join(SolveState* st, double* mine, double tot) {
-  *mine = tot;
-  __threadfence();
-  if (atomicAdd(&st->pap_join, 1u) == 1u) {
-    __threadfence();
-    finish_pap(st, __ldcg(&st->pap_part) + __ldcg(&st->pap_wave));
-    st->pap_join = 0u;
-  }
-}
-
 template <bool TMA>
 struct CgDirF32Job {
   static constexpr int kOffZ = align128(box_bytes<float, BI, BJ>());
@@ -953,18 +939,6 @@ struct CgDirF32Job {
   int n, ntx, ntot;
   SolveState* st;
   ReduceBuf rb;
-  // ring = 1: only the first and last tile rows and columns (nty = tile
-  // columns) are visited, k -> ring_id(k); the interior tiles are done by
-  // the register wave kernel (k_dir_wave), and p.Ap meets its share in
-  // pap_join
-  int ring, nty;
-  __device__ int ring_id(int k) const {
-    if (!ring) return k;
-    if (k < ntx) return k;
-    if (k < 2 * ntx) return (k - ntx) + (nty - 1) * ntx;
-    const int k2 = k - 2 * ntx;
-    return ((k2 & 1) ? ntx - 1 : 0) + (1 + (k2 >> 1)) * ntx;
-  }
   __device__ bool prepare(Ctx& c) const {
     if (st->done) return true;
     c.first = (st->iter == 0);
@@ -977,16 +951,14 @@ struct CgDirF32Job {
     return TMA ? box_bytes<float, BI, BJ>() + (st->iter == 0 ? 0u : box_bytes<float, BI, BJ>())
                : 0u;
   }
-  __device__ void issue(unsigned char* buf, unsigned long long* bar, int k, const Ctx& c) const {
-    const int id = ring_id(k);
+  __device__ void issue(unsigned char* buf, unsigned long long* bar, int id, const Ctx& c) const {
     const TileBoxes bx(id % ntx, tile_at<TI, TJ>(id, ntx, n).j_lo);
     stage_box<TMA, BI, BJ>(reinterpret_cast<float*>(buf + kOffZ), z, &z.box, bx.x0, bx.y0, n, bar);
     if (!c.first)
       stage_box<TMA, BI, BJ>(reinterpret_cast<float*>(buf), pold, &pold.box, bx.x0, bx.y0, n,
                              bar);
   }
-  __device__ void compute(unsigned char* buf, int k, Acc& acc, const Ctx& c, unsigned char*) const {
-    const int id = ring_id(k);
+  __device__ void compute(unsigned char* buf, int id, Acc& acc, const Ctx& c, unsigned char*) const {
     const TileT t = tile_at<TI, TJ>(id, ntx, n);
     const TileBoxes bx(id % ntx, t.j_lo);
     float* s = reinterpret_cast<float*>(buf);
@@ -1024,29 +996,20 @@ struct CgDirF32Job {
       });
     }
   }
-  __device__ void finish(double tot) const {
-    if (ring)
-      pap_join(st, &st->pap_part, tot);
-    else
-      finish_pap(st, tot);
-  }
+  __device__ void finish(double tot) const { finish_pap(st, tot); }
 };
 
-// The staged direction pass over every tile (ring = 0) or over the first
-// and last tile rows and columns only (ring = 1, beside k_dir_wave).
+// The staged direction pass over every tile (small grids, batched solves).
 static cudaError_t launch_cg_dir_f32_staged(const Operand& z, const Operand& pold,
                                             Grid<float> pnew, Grid<double> Ap, int n,
-                                            SolveState* st, ReduceBuf rb, cudaStream_t s,
-                                            int ring) {
+                                            SolveState* st, ReduceBuf rb, cudaStream_t s) {
   const dim3 g = tile_grid(n);
-  const int ntx = (int)g.x, nty = (int)g.y;
-  const int total = ring ? ntx * nty - (ntx - 2) * (nty - 2) : ntx * nty;
+  const int ntx = (int)g.x;
+  const int total = (int)(g.x * g.y);
   const DevOperand<float> dz = dev_operand<float>(z), dp = dev_operand<float>(pold);
   if (z.tma && pold.tma)
-    return launch_persist(
-        CgDirF32Job<true>{dz, dp, pnew, Ap, n, ntx, total, st, rb, ring, nty}, total, s);
-  return launch_persist(CgDirF32Job<false>{dz, dp, pnew, Ap, n, ntx, total, st, rb, ring, nty},
-                        total, s);
+    return launch_persist(CgDirF32Job<true>{dz, dp, pnew, Ap, n, ntx, total, st, rb}, total, s);
+  return launch_persist(CgDirF32Job<false>{dz, dp, pnew, Ap, n, ntx, total, st, rb}, total, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -2996,14 +2959,12 @@ static bool interior_rect(int n, int& Ra, int& Rb, int& Ca, int& Cb) {
   return Ra < Rb && Ca < Cb;
 }
 // the post-smoothing wave: inside the PostSmall tiling (ring one small tile
-// deep); the direction wave: inside the 64 x 32 tiles of CgDirF32Job
+// deep)
 static bool post_wave_rect(int n, int& Ra, int& Rb, int& Ca, int& Cb) {
   return interior_rect<PostSmall::TI, PostSmall::TJ>(n, Ra, Rb, Ca, Cb) &&
          Rb - Ra >= 4 + kPostRows;
 }
-static bool dir_wave_rect(int n, int& Ra, int& Rb, int& Ca, int& Cb) {
-  return interior_rect<TI, TJ>(n, Ra, Rb, Ca, Cb);
-}
+
 
 int post_fused_launches(int n, int sweeps, bool f32) {
   int Ra, Rb, Ca, Cb;
@@ -3096,26 +3057,30 @@ cudaError_t launch_post_fused(const Operand& vin, const Operand& e, const Operan
 }
 
 // ---------------------------------------------------------------------------
-// Register wave of the FP32 CG direction for the interior of the fine grid
-// (mixed MGCG), the job of CgDirF32Job's interior tiles without staging or
-// block barriers.  A warp owns a strip of 62 rows x `cols` columns of the
-// interior rectangle [Ra, Rb) x [Ca, Cb) (the union of the 64 x 32 tiles
-// outside the first and last tile rows and columns: every point there has
-// the plain 5-point stencil).  Lane l holds rows rb0 + 2l and rb0 + 2l + 1
-// (64 rows: the 62 owned and one halo row on either side), and the warp
-// marches along j:
+// Register wave of the FP32 CG direction (mixed MGCG) over the whole fine
+// grid, in one launch.  The plain 5-point points (rows 1 .. n-2, columns
+// 3 .. n-4) are split into strips of 62 rows x `cols` columns.  A warp loads
+// 64 rows, lane l holding rows rb0 + 2l and rb0 + 2l + 1 (the 62 owned and
+// one halo row on either side), and marches along j:
 //   step c: p~ = fl32(z + beta p~_old) at column c (stored where owned);
 //           A p~ at column c - 1 in float-float from the p~ of columns
 //           c - 2, c - 1, c and of the lanes above and below (one shuffle
 //           each way), stored in FP64, and p~ . fl32(A p~) accumulated.
 // z and p~_old come through per-lane cp.async rings kDirAhead columns ahead;
-// a lane reads only its own slots, so no barrier is needed.  The arithmetic
-// per point is that of CgDirF32Job's interior path.
+// a lane reads only its own slots, so no barrier is needed.  The last strip
+// starts at the even row at or above n - 64, so on an odd grid its last
+// loaded row is row n, a padding row of the solver's arrays (ld > n).
+// CTAs past the wave's take the SAT rows and columns (rows 0 and n-1,
+// columns 0-2 and n-3 .. n-1) point by point: p~ there and at the
+// neighbours negA reads (recomputed from z and p~_old, which no one writes
+// in this pass), negA in float-float.  All CTAs then meet in one reduction.
+// The arithmetic per point is that of CgDirF32Job.
 // ---------------------------------------------------------------------------
 constexpr int kDirRows = 62;
 constexpr int kDirAhead = 8;
 constexpr int kDirSlots = kDirAhead + 1;
 constexpr int kDirWaveMinN = 1025;
+constexpr int kDirBoundaryCtas = 32;
 
 struct DirWaveArgs {
   const float* z;
@@ -3126,7 +3091,7 @@ struct DirWaveArgs {
   int ldn;
   double* Ap;
   int lda;
-  int Ra, Rb, Ca, Cb, nsi, nsj, cols;
+  int n, nsi, nsj, cols, wave_ctas;
   SolveState* st;
   ReduceBuf rb;
 };
@@ -3139,91 +3104,131 @@ __global__ void __launch_bounds__(kThreads, 5) k_dir_wave(const DirWaveArgs a) {
   if (st->done) return;   // uniform: the state was final before this launch
   const bool first = (st->iter == 0);   // p~_old is not read
   const float2 beta = make_float2((float)st->beta, (float)st->beta);
-  const int lane = threadIdx.x & 31;
-  const int wl = threadIdx.x >> 5;
-  const int gw = (blockIdx.x * kThreads + threadIdx.x) >> 5;
-  const int nw = (gridDim.x * kThreads) >> 5;
-  const int items = a.nsi * a.nsj;
-  const unsigned FULL = 0xffffffffu;
-  float2* const zmine = &zring[wl][0][lane];
-  float2* const pmine = &pring[wl][0][lane];
-  DotAcc2 acc;   // p~ . fl32(-A p~), negated at the end
-  for (int it = gw; it < items; it += nw) {
-    const int si = it % a.nsi, sj = it / a.nsi;
-    const int rb0 = a.Ra - 1 + kDirRows * si;             // even: Ra is odd
-    const int r_hi = min(rb0 + 1 + kDirRows, a.Rb);       // owned rows [rb0 + 1, r_hi)
-    const int c0 = a.Ca + a.cols * sj;
-    const int c1 = min(c0 + a.cols, a.Cb);
-    const int ra = rb0 + 2 * lane;
-    const bool own_x = lane > 0 && ra < r_hi;
-    const bool own_y = lane < 31 && ra + 1 < r_hi;
-    const int c_first = c0 - 1, c_last = c1;
-    const float* zp = a.z + (size_t)ra;
-    const float* pp = a.pold + (size_t)ra;
-#pragma unroll
-    for (int k = 0; k < kDirAhead; ++k) {
-      const int c = c_first + k;
-      if (c <= c_last) {
-        cp_async8(zmine + k * 32, zp + (size_t)c * a.ldz);
-        if (!first) cp_async8(pmine + k * 32, pp + (size_t)c * a.ldp);
+  const int n = a.n;
+  double partial;
+  if ((int)blockIdx.x >= a.wave_ctas) {
+    // SAT rows and columns, one point per thread and step
+    DotAcc<float> acc;
+    const long long nb = 2LL * n + 6LL * (n - 2);
+    for (long long k = (long long)(blockIdx.x - a.wave_ctas) * kThreads + threadIdx.x; k < nb;
+         k += (long long)(gridDim.x - a.wave_ctas) * kThreads) {
+      int i, j;
+      if (k < 2LL * n) {
+        i = (k < n) ? 0 : n - 1;
+        j = (int)(k < n ? k : k - n);
+      } else {
+        const long long k2 = k - 2LL * n;
+        const int c = (int)(k2 / (n - 2));
+        i = 1 + (int)(k2 % (n - 2));
+        j = c < 3 ? c : n - 6 + c;
       }
-      cp_async_commit();
+      struct G {
+        const float* z;
+        const float* p;
+        int ldz, ldp, i, j;
+        float b;
+        bool first;
+        __device__ float pt(int di, int dj) const {
+          const float zz = __ldg(z + (size_t)(j + dj) * ldz + (i + di));
+          return first ? zz : fmaf(b, __ldg(p + (size_t)(j + dj) * ldp + (i + di)), zz);
+        }
+        __device__ FF operator()(int di, int dj) const { return FF(pt(di, dj), 0.0f); }
+      } g{a.z, a.pold, a.ldz, a.ldp, i, j, beta.x, first};
+      const float pv = g.pt(0, 0);
+      const FF na = negA<FF>(g, i, j, n);
+      float apf;
+      const double ap = dir_ap(na.hi, na.lo, apf);
+      a.pnew[(size_t)j * a.ldn + i] = pv;
+      a.Ap[(size_t)j * a.lda + i] = ap;
+      acc.add_prod(pv, apf);
     }
-    int slot = 0, fill = kDirAhead;
-    float2 q1 = make_float2(0.f, 0.f), q2 = q1;             // p~ at c - 1, c - 2
-    for (int c = c_first; c <= c_last; ++c) {
-      cp_async_wait<kDirAhead - 1>();                       // column c has landed
-      const float2 zv = zmine[slot * 32];
-      const float2 q0 = first ? zv : fma2(beta, pmine[slot * 32], zv);
-      {
-        const int cn = c + kDirAhead;
-        if (cn <= c_last) {
-          cp_async8(zmine + fill * 32, zp + (size_t)cn * a.ldz);
-          if (!first) cp_async8(pmine + fill * 32, pp + (size_t)cn * a.ldp);
+    partial = acc.value();
+  } else {
+    const int lane = threadIdx.x & 31;
+    const int wl = threadIdx.x >> 5;
+    const int gw = (blockIdx.x * kThreads + threadIdx.x) >> 5;
+    const int nw = (a.wave_ctas * kThreads) >> 5;
+    const int items = a.nsi * a.nsj;
+    const unsigned FULL = 0xffffffffu;
+    float2* const zmine = &zring[wl][0][lane];
+    float2* const pmine = &pring[wl][0][lane];
+    DotAcc2 acc;   // p~ . fl32(-A p~), negated at the end
+    const int rb_last = (n - 64 + 1) & ~1;                  // even, >= n - 64
+    for (int it = gw; it < items; it += nw) {
+      const int si = it % a.nsi, sj = it / a.nsi;
+      const int rbn = kDirRows * si;
+      const int rb0 = min(rbn, rb_last);
+      const int r_lo = rbn + 1, r_hi = min(rbn + 1 + kDirRows, n - 1);   // owned rows
+      const int c0 = 3 + a.cols * sj;
+      const int c1 = min(c0 + a.cols, n - 3);
+      const int ra = rb0 + 2 * lane;
+      const bool own_x = lane > 0 && ra >= r_lo && ra < r_hi;
+      const bool own_y = lane < 31 && ra + 1 >= r_lo && ra + 1 < r_hi;
+      const int c_first = c0 - 1, c_last = c1;
+      const float* zp = a.z + (size_t)ra;
+      const float* pp = a.pold + (size_t)ra;
+#pragma unroll
+      for (int k = 0; k < kDirAhead; ++k) {
+        const int c = c_first + k;
+        if (c <= c_last) {
+          cp_async8(zmine + k * 32, zp + (size_t)c * a.ldz);
+          if (!first) cp_async8(pmine + k * 32, pp + (size_t)c * a.ldp);
         }
         cp_async_commit();
       }
-      slot = slot + 1 == kDirSlots ? 0 : slot + 1;
-      fill = fill + 1 == kDirSlots ? 0 : fill + 1;
-      if (c >= c0 && c < c1) {
-        float* o = a.pnew + (size_t)c * a.ldn + ra;
-        if (own_x && own_y) {
-          *reinterpret_cast<float2*>(o) = q0;
-        } else {
-          if (own_x) o[0] = q0.x;
-          if (own_y) o[1] = q0.y;
+      int slot = 0, fill = kDirAhead;
+      float2 q1 = make_float2(0.f, 0.f), q2 = q1;             // p~ at c - 1, c - 2
+      for (int c = c_first; c <= c_last; ++c) {
+        cp_async_wait<kDirAhead - 1>();                       // column c has landed
+        const float2 zv = zmine[slot * 32];
+        const float2 q0 = first ? zv : fma2(beta, pmine[slot * 32], zv);
+        {
+          const int cn = c + kDirAhead;
+          if (cn <= c_last) {
+            cp_async8(zmine + fill * 32, zp + (size_t)cn * a.ldz);
+            if (!first) cp_async8(pmine + fill * 32, pp + (size_t)cn * a.ldp);
+          }
+          cp_async_commit();
         }
-      }
-      const float above = __shfl_up_sync(FULL, q1.y, 1);    // row ra - 1, column c - 1
-      const float below = __shfl_down_sync(FULL, q1.x, 1);  // row ra + 2, column c - 1
-      if (c > c0) {                                         // column c - 1 is in [c0, c1)
-        // both rows at once: the stencil_ff and dir_ap of the staged path,
-        // lane by lane
-        float2 hi, lo, sum;
-        stencil_ff2(make_float2(above, q1.x), make_float2(q1.y, below), q2, q0, q1, hi, lo);
-        double ax, ay;
-        ff_neg_f64_2(hi, lo, ax, ay, sum);                  // fl32(A p~) = -sum
-        double* o = a.Ap + (size_t)(c - 1) * a.lda + ra;
-        if (own_x && own_y) {
-          *reinterpret_cast<double2*>(o) = make_double2(ax, ay);
-        } else {
-          if (own_x) o[0] = ax;
-          if (own_y) o[1] = ay;
+        slot = slot + 1 == kDirSlots ? 0 : slot + 1;
+        fill = fill + 1 == kDirSlots ? 0 : fill + 1;
+        if (c >= c0 && c < c1) {
+          float* o = a.pnew + (size_t)c * a.ldn + ra;
+          if (own_x && own_y) {
+            *reinterpret_cast<float2*>(o) = q0;
+          } else {
+            if (own_x) o[0] = q0.x;
+            if (own_y) o[1] = q0.y;
+          }
         }
-        acc.add_prod(make_float2(own_x ? q1.x : 0.f, own_y ? q1.y : 0.f), sum);
+        const float above = __shfl_up_sync(FULL, q1.y, 1);    // row ra - 1, column c - 1
+        const float below = __shfl_down_sync(FULL, q1.x, 1);  // row ra + 2, column c - 1
+        if (c > c0) {                                         // column c - 1 is in [c0, c1)
+          // both rows at once: the stencil_ff and dir_ap of the staged path,
+          // lane by lane
+          float2 hi, lo, sum;
+          stencil_ff2(make_float2(above, q1.x), make_float2(q1.y, below), q2, q0, q1, hi, lo);
+          double ax, ay;
+          ff_neg_f64_2(hi, lo, ax, ay, sum);                  // fl32(A p~) = -sum
+          double* o = a.Ap + (size_t)(c - 1) * a.lda + ra;
+          if (own_x && own_y) {
+            *reinterpret_cast<double2*>(o) = make_double2(ax, ay);
+          } else {
+            if (own_x) o[0] = ax;
+            if (own_y) o[1] = ay;
+          }
+          // rows not owned (halo, and the padding row n) add exact zeros
+          acc.add_prod(make_float2(own_x ? q1.x : 0.f, own_y ? q1.y : 0.f),
+                       make_float2(own_x ? sum.x : 0.f, own_y ? sum.y : 0.f));
+        }
+        q2 = q1;
+        q1 = q0;
       }
-      q2 = q1;
-      q1 = q0;
+      cp_async_wait<0>();   // no copy outlives the strip
     }
-    cp_async_wait<0>();   // no copy outlives the strip
+    partial = -acc.value();
   }
-  // the boundary tiles' share comes from the staged pass running beside
-  grid_reduce(-acc.value(), a.rb, [&](double tot) { pap_join(st, &st->pap_wave, tot); });
-}
-
-int cg_dir_f32_launches(int n) {
-  int Ra, Rb, Ca, Cb;
-  return (n >= kDirWaveMinN && dir_wave_rect(n, Ra, Rb, Ca, Cb)) ? 2 : 1;
+  grid_reduce(partial, a.rb, [&](double tot) { finish_pap(st, tot); });
 }
 
 static int dir_wave_per_sm() {
@@ -3238,33 +3243,17 @@ static int dir_wave_per_sm() {
   return v;
 }
 
+// The wave needs odd n >= kDirWaveMinN (its last strip reads the padding
+// row n), arrays with ld > n, and 8-byte aligned columns.
 cudaError_t launch_cg_dir_f32(const Operand& z, const Operand& pold, Grid<float> pnew,
                               Grid<double> Ap, int n, SolveState* st, ReduceBuf rb,
-                              cudaStream_t s, cudaStream_t aux, cudaEvent_t fork,
-                              cudaEvent_t join) {
-  int Ra, Rb, Ca, Cb;
-  const bool wave = cg_dir_f32_launches(n) == 2 && !recorder_slot() && z.ld % 2 == 0 &&
-                    pold.ld % 2 == 0 && pnew.ld % 2 == 0 && Ap.ld % 2 == 0 &&
-                    ((uintptr_t)z.p & 7u) == 0 && ((uintptr_t)pold.p & 7u) == 0 &&
-                    ((uintptr_t)pnew.p & 7u) == 0 && aligned16(Ap.p) &&
-                    dir_wave_rect(n, Ra, Rb, Ca, Cb);
-  if (!wave) return launch_cg_dir_f32_staged(z, pold, pnew, Ap, n, st, rb, s, 0);
-  // the boundary tiles by the staged job on a forked branch (or before the
-  // wave on the same stream); the two p.Ap shares meet in pap_join
-  const bool forked = aux && fork && join;
-  cudaError_t e = cudaSuccess;
-  if (forked) {
-    e = cudaEventRecord(fork, s);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(aux, fork, 0);
-  }
-  // concurrent reductions: the ring takes the upper half of the partials
-  // buffer and its own ticket, as in the post-smoothing split
-  const ReduceBuf rb_ring{rb.partials ? rb.partials + kRingPartialsOffset : nullptr,
-                          rb.ticket ? rb.ticket + 8 : nullptr};
-  if (e == cudaSuccess)
-    e = launch_cg_dir_f32_staged(z, pold, pnew, Ap, n, st, rb_ring, forked ? aux : s, 1);
-  if (forked && e == cudaSuccess) e = cudaEventRecord(join, aux);
-  if (e != cudaSuccess) return e;
+                              cudaStream_t s) {
+  const bool wave = n >= kDirWaveMinN && (n & 1) && !recorder_slot() && z.ld > n &&
+                    pold.ld > n && z.ld % 2 == 0 && pold.ld % 2 == 0 && pnew.ld % 2 == 0 &&
+                    Ap.ld % 2 == 0 && ((uintptr_t)z.p & 7u) == 0 &&
+                    ((uintptr_t)pold.p & 7u) == 0 && ((uintptr_t)pnew.p & 7u) == 0 &&
+                    aligned16(Ap.p);
+  if (!wave) return launch_cg_dir_f32_staged(z, pold, pnew, Ap, n, st, rb, s);
   DirWaveArgs a;
   a.z = static_cast<const float*>(z.p);
   a.ldz = z.ld;
@@ -3274,22 +3263,17 @@ cudaError_t launch_cg_dir_f32(const Operand& z, const Operand& pold, Grid<float>
   a.ldn = pnew.ld;
   a.Ap = Ap.p;
   a.lda = Ap.ld;
-  a.Ra = Ra;
-  a.Rb = Rb;
-  a.Ca = Ca;
-  a.Cb = Cb;
-  a.nsi = (Rb - Ra + kDirRows - 1) / kDirRows;
+  a.n = n;
+  a.nsi = (n - 2 + kDirRows - 1) / kDirRows;
   a.st = st;
   a.rb = rb;
   const int warps = sm_count() * dir_wave_per_sm() * kWarps;
   static const int cands[] = {16, 24, 32, 40, 48, 64, 96};
-  a.cols = best_strip_cols(a.nsi, Cb - Ca, warps, cands, 7, 8, 1);
-  a.nsj = (Cb - Ca + a.cols - 1) / a.cols;
+  a.cols = best_strip_cols(a.nsi, n - 6, warps, cands, 7, 8, 1);
+  a.nsj = (n - 6 + a.cols - 1) / a.cols;
   const int items = a.nsi * a.nsj;
-  const int grid = std::max(1, std::min((items + kWarps - 1) / kWarps, sm_count() * dir_wave_per_sm()));
-  e = launch_pdl(k_dir_wave, dim3(grid), dim3(kThreads), 0, s, a);
-  if (forked && e == cudaSuccess) e = cudaStreamWaitEvent(s, join, 0);
-  return e;
+  a.wave_ctas = std::max(1, std::min((items + kWarps - 1) / kWarps, sm_count() * dir_wave_per_sm()));
+  return launch_pdl(k_dir_wave, dim3(a.wave_ctas + kDirBoundaryCtas), dim3(kThreads), 0, s, a);
 }
 
 // Resolve the launch configuration of every persistent kernel up front

@@ -34,17 +34,13 @@ cudaError_t launch_cg_dir_mixed(const Operand& z, const Operand& pold, const Ope
                                 Grid<double> pnew, Grid<double> Ap, int n, SolveState* st,
                                 ReduceBuf rb, cudaStream_t s);
 // Mixed-precision CG direction kept in FP32: p~ = fl32(z + beta p~_old),
-// Ap = A p~ exactly (float-float stencil), p~.Ap -> alpha.  On grids with
-// n - 1 a multiple of 64 and n >= 1025 the interior runs as a register wave
-// and the first and last tile rows and columns as staged tiles (z and p~_old
-// with their halos, TMA when both allow it), on `aux` concurrently when aux,
-// fork and join are given; elsewhere every tile is staged.
+// Ap = A p~ exactly (float-float stencil), p~.Ap -> alpha.  On odd grids
+// from N = 1025 with padded arrays (ld > n) one register-wave launch covers
+// the interior and, in extra CTAs, the SAT rows and columns; elsewhere z and
+// p~_old are staged tile by tile (TMA when both allow it).
 cudaError_t launch_cg_dir_f32(const Operand& z, const Operand& pold, Grid<float> pnew,
                               Grid<double> Ap, int n, SolveState* st, ReduceBuf rb,
-                              cudaStream_t s, cudaStream_t aux = nullptr,
-                              cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
-// Kernel launches of launch_cg_dir_f32 at size n (1 or 2).
-int cg_dir_f32_launches(int n);
+                              cudaStream_t s);
 template <typename T>
 cudaError_t launch_smooth_op(int field, int epi, const Operand& vin, const Operand& e,
                              const Operand& b, Grid<T> vout, int n, int smoother, double omega,

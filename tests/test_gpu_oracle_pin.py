@@ -116,8 +116,9 @@ def test_profile_matches_graph_solve(sbp, n):
     # sbp_solver_profile launches the same kernels without graphs: the same
     # iterations and, with fixed-order reductions, the same solution bit for
     # bit; every kernel of the solve appears with its launches.  At N = 1025
-    # the mixed direction pass runs as the interior wave beside the staged
-    # boundary tiles, whose p.Ap shares meet in a fixed order.
+    # the mixed direction pass is the one-launch register wave (interior
+    # strips and SAT boundary CTAs meeting in one reduction), and the
+    # smoothing waves run beside their staged boundary rings.
     from sc_2022_gb300 import _lib, problems
     f, g, _ = problems.manufactured(n, "baseline")
     b = problems.assemble_rhs(f, g).reshape(-1)
@@ -136,7 +137,8 @@ def test_profile_matches_graph_solve(sbp, n):
         assert launches >= res.iters * 3
         if prec == _lib.SBP_PREC_MIXED and n == 1025:
             names = " ".join(r["kernel"] for r in rows)
-            assert "k_dir_wave" in names and "CgDirF32Job" in names
+            assert "k_dir_wave" in names and "CgDirF32Job" not in names
+            assert "k_pre_wave" in names and "k_post_wave" in names
         s.close()
 
 
