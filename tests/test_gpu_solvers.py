@@ -145,6 +145,8 @@ def test_mgcg_mixed_precision(sbp, n):
     (513, "jacobi", 2, "normal"),
     (513, "richardson", 1, "sbp"),
     (1025, "jacobi", 3, "galerkin"),
+    (1025, "richardson", 3, "normal"),
+    (1025, "jacobi", 3, "sbp"),
     (257, "richardson", 3, "normal"),
 ])
 def test_vcycle_mixed_matches_fp64_oracle(sbp, n, smoother, nu, restriction):
