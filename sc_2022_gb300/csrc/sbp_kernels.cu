@@ -2684,8 +2684,8 @@ static cudaError_t launch_pre_wave(const Operand& b, Grid<float> vout, Grid<floa
       v = 1;
     return v;
   }();
-  static const int cands[] = {8, 12, 16, 24, 32};   // coarse columns
-  a.cols = best_strip_cols(a.nsi, Jb - Ja, sm_count() * per_sm * kWarps, cands, 5, 7, 2);
+  static const int cands[] = {4, 8, 12, 16, 24, 32};   // coarse columns
+  a.cols = best_strip_cols(a.nsi, Jb - Ja, sm_count() * per_sm * kWarps, cands, 6, 7, 2);
   a.nsj = (Jb - Ja + a.cols - 1) / a.cols;
   const int items = a.nsi * a.nsj;
   const int grid = std::max(1, std::min((items + kWarps - 1) / kWarps, sm_count() * per_sm));
@@ -3037,8 +3037,8 @@ cudaError_t launch_post_fused(const Operand& vin, const Operand& e, const Operan
             v = 1;
           return v;
         }()};
-    static const int cands[] = {16, 24, 32, 48, 64};   // fine columns
-    a.cols = best_strip_cols(a.nsi, Cb - Ca, sm_count() * per_sm[dot ? 1 : 0] * kWarps, cands, 5,
+    static const int cands[] = {8, 16, 24, 32, 48, 64};   // fine columns
+    a.cols = best_strip_cols(a.nsi, Cb - Ca, sm_count() * per_sm[dot ? 1 : 0] * kWarps, cands, 6,
                              6, 1);
     a.nsj = (Cb - Ca + a.cols - 1) / a.cols;
     const int items = a.nsi * a.nsj;
