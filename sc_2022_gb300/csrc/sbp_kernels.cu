@@ -3465,23 +3465,26 @@ __device__ __forceinline__ void fd_run(const FdArgs& a, int j) {
   double* c = fd_sm;                  // nc
   double* sv = c + nc;                // nc
   double* part = sv + nc;             // kFdSlices * nc
-  double* is = part + kFdSlices * nc; // STAGE: the input grid, nc * nc
+  double* is = part + kFdSlices * nc; // STAGE: the input grid, nc * nc (as Tin)
   double* ms = is + nc * nc;          // STAGE: M, nc * nc
+  Tin* isr = reinterpret_cast<Tin*>(is);
   const int q = threadIdx.x >> 6, r = threadIdx.x & 63;
   for (int k = threadIdx.x; k < nc; k += kThreads) c[k] = C[(size_t)j * nc + k];
   if (STAGE) {
+    // every element's copy in flight at once (cp.async), converted at use
     for (int k = threadIdx.x; k < nc * nc; k += kThreads) {
       const int jj = k / nc;
-      is[k] = convert<double>(in.at(k - jj * nc, jj));
-      ms[k] = __ldg(M + k);
+      cp_async_elem(isr + k, in.p + (size_t)jj * in.ld + (k - jj * nc));
+      cp_async_elem(ms + k, M + k);
     }
+    cp_async_wait_all();
   }
   __syncthreads();
   for (int i = r; i < nc; i += 64) {
     double a = 0.0;
 #pragma unroll 4
     for (int k = q; k < nc; k += kFdSlices)
-      a = fma(STAGE ? is[k * nc + i] : convert<double>(in.at(i, k)), c[k], a);
+      a = fma(convert<double>(STAGE ? isr[k * nc + i] : in.at(i, k)), c[k], a);
     part[q * nc + i] = a;
   }
   __syncthreads();
