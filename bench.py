@@ -46,7 +46,6 @@ WORKLOAD = ("plain/mixed matrix-free MGCG, N=4097 (16.8M unknowns), u=sin(pi x)c
 KERNEL_BYTES_PER_POINT = {
     "k_dir_wave": 20,         # the same over the interior rectangle (KERNEL_POINTS)
     "CgDirF32Job": 20,        # z, p_old (f32) read; p (f32), Ap written
-    "CgDirMixedJob": 36,      # z (f32), p_old, Ap_old read; p, Ap written
     "CgDirJob<double, double": 32,   # z, p_old read; p, Ap written
     "k_cg_update<": 48,       # x, r, Ap, p (f32) read; x, r, r_lo (f32) written
 }

@@ -794,106 +794,6 @@ struct CgDirJob {
   }
 };
 
-// ---------------------------------------------------------------------------
-// Mixed-precision CG direction: z is the FP32 V-cycle output, p and Ap FP64.
-//   p  = z + beta p_old
-//   Ap = A z + beta Ap_old          (A p by linearity, Ap_old from last step)
-//   p.Ap -> alpha
-// A z is evaluated exactly on the FP32 pipe (float-float stencil) and the
-// FP64 pipe does only one add and three FMAs per point; p_old / Ap_old are
-// read pointwise, so only z is staged (with its halo).
-// ---------------------------------------------------------------------------
-template <bool TMA>
-struct CgDirMixedJob {
-  // one stage: the z box (FP32, 72 x 37), prefetched one tile ahead; p_old
-  // and Ap_old are read pointwise from global memory, which keeps the stage
-  // small enough for five CTAs per SM
-  static constexpr int kStage = align128(box_bytes<float, BI, BJ>());
-  static constexpr int kScratch = 0;
-  static constexpr bool kReduce = true;
-  // p.Ap from the FP32 roundings of p and Ap, accumulated with the
-  // compensated float pair: no FP64 instruction per point.  alpha and beta
-  // only need the scalars to ~1e-7 (r.z already comes from the FP32 r and z);
-  // the FP64 recurrences r -= alpha Ap, x += alpha p keep their accuracy.
-  using Acc = DotAcc<float>;
-  using Ctx = DirCtx;
-  DevOperand<float> z;
-  DevOperand<double> pold, apold;
-  Grid<double> pnew, Ap;
-  int n, ntx, ntot;
-  SolveState* st;
-  ReduceBuf rb;
-  __device__ bool prepare(Ctx& c) const {
-    if (st->done) return true;
-    c.first = (st->iter == 0);
-    c.beta = st->beta;
-    return false;
-  }
-  __device__ int tiles() const { return ntot; }
-  __device__ unsigned tx_bytes(int) const { return TMA ? box_bytes<float, BI, BJ>() : 0u; }
-  __device__ void issue(unsigned char* buf, unsigned long long* bar, int id, const Ctx&) const {
-    const TileBoxes bx(id % ntx, tile_at<TI, TJ>(id, ntx, n).j_lo);
-    stage_box<TMA, BI, BJ>(reinterpret_cast<float*>(buf), z, &z.box, bx.x0, bx.y0, n, bar);
-  }
-  __device__ void compute(unsigned char* buf, int id, Acc& acc, const Ctx& c, unsigned char*) const {
-    const TileT t = tile_at<TI, TJ>(id, ntx, n);
-    const TileBoxes bx(id % ntx, t.j_lo);
-    const float* s = reinterpret_cast<const float*>(buf);
-    const double beta = c.beta;
-    const bool first = c.first;
-    auto emit = [&](int i, int j, int, float zc, double az) {
-      const double zd = f32_to_f64(zc);
-      const double pv =
-          first ? zd : fma(beta, __ldg(pold.p + (size_t)j * (size_t)pold.ld + i), zd);
-      const double ap =
-          first ? az : fma(beta, __ldg(apold.p + (size_t)j * (size_t)apold.ld + i), az);
-      pnew.at(i, j) = pv;
-      Ap.at(i, j) = ap;
-      acc.add_prod(f64_to_f32(pv), f64_to_f32(ap));
-    };
-    if (tile_interior(t, n)) {
-      visit_interior(s, t, [&](int i, int j, float um, float u0, float up, float uw, float ue,
-                               int k) {
-        float hi, lo;
-        stencil_ff(uw, ue, um, up, u0, hi, lo);
-        emit(i, j, k, u0, -(f32_to_f64(hi) + f32_to_f64(lo)));   // A z = -(stencil)
-      });
-    } else {
-      visit_generic(s, t, bx, [&](int i, int j, const SAcc<float>& a, int k) {
-        // boundary rows/columns: the SAT stencil of the exact FP32 values in
-        // float-float on the FP32 pipe
-        struct D {
-          const SAcc<float>* a;
-          __device__ FF operator()(int di, int dj) const { return FF((*a)(di, dj), 0.0f); }
-        } d{&a};
-        const FF na = negA<FF>(d, i, j, n);
-        emit(i, j, k, a(0, 0), -(f32_to_f64(na.hi) + f32_to_f64(na.lo)));
-      });
-    }
-  }
-  __device__ void finish(double tot) const {
-    st->pAp = tot;
-    if (!isfinite(tot) || tot == 0.0)
-      st->done = kDoneBreakdown;
-    else
-      st->alpha = st->rz / tot;
-  }
-};
-
-template <typename T>
-cudaError_t launch_cg_dir_mixed(const Operand& z, const Operand& pold, const Operand& apold,
-                                Grid<double> pnew, Grid<double> Ap, int n, SolveState* st,
-                                ReduceBuf rb, cudaStream_t s) {
-  const dim3 g = tile_grid(n);
-  const int total = (int)(g.x * g.y);
-  const DevOperand<float> dz = dev_operand<float>(z);
-  const DevOperand<double> dp = dev_operand<double>(pold), da = dev_operand<double>(apold);
-  if (z.tma && pold.tma && apold.tma)
-    return launch_persist(CgDirMixedJob<true>{dz, dp, da, pnew, Ap, n, (int)g.x, total, st, rb},
-                          total, s);
-  return launch_persist(CgDirMixedJob<false>{dz, dp, da, pnew, Ap, n, (int)g.x, total, st, rb},
-                        total, s);
-}
 
 // ---------------------------------------------------------------------------
 // Mixed-precision CG direction with an FP32 direction vector:
@@ -3313,7 +3213,6 @@ cudaError_t prepare_kernels() {
   persist_ctas_per_sm<CgDirJob<double, double, true>>();
   persist_ctas_per_sm<CgDirJob<double, float, false>>();
   persist_ctas_per_sm<CgDirJob<double, float, true>>();
-  persist_ctas_per_sm<CgDirMixedJob<false>>();
   persist_ctas_per_sm<CgDirF32Job<false>>();
   persist_ctas_per_sm<PreFusedJob<float, true>>();
   persist_ctas_per_sm<PreFusedJob<float, false>>();
@@ -3339,7 +3238,6 @@ cudaError_t prepare_kernels() {
   persist_ctas_per_sm<PostFusedJob<double, true, true, PostSmall>>();
   persist_ctas_per_sm<PostFusedJob<double, false, false, PostSmall>>();
   persist_ctas_per_sm<PostFusedJob<double, true, false, PostSmall>>();
-  persist_ctas_per_sm<CgDirMixedJob<true>>();
   persist_ctas_per_sm<CgDirF32Job<true>>();
   cg_update_wave<true>();
   cg_update_wave<false>();
@@ -3904,9 +3802,6 @@ template cudaError_t launch_cg_dir_op<double, double>(const Operand&, const Oper
 template cudaError_t launch_cg_dir_op<double, float>(const Operand&, const Operand&, Grid<double>,
                                                      Grid<double>, int, int, SolveState*,
                                                      ReduceBuf, cudaStream_t);
-template cudaError_t launch_cg_dir_mixed<double>(const Operand&, const Operand&, const Operand&,
-                                                 Grid<double>, Grid<double>, int, SolveState*,
-                                                 ReduceBuf, cudaStream_t);
 template cudaError_t launch_cg_dir<double, double>(Grid<const double>, Grid<const double>,
                                                    Grid<double>, Grid<double>, int, int,
                                                    SolveState*, ReduceBuf, cudaStream_t);

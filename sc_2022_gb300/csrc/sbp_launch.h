@@ -25,14 +25,6 @@ cudaError_t launch_residual_op(const Operand& x, const Operand& b, Grid<T> r, Gr
 template <typename T, typename Tz>
 cudaError_t launch_cg_dir_op(const Operand& z, const Operand& pold, Grid<T> pnew, Grid<T> Ap,
                              int n, int opsign, SolveState* st, ReduceBuf rb, cudaStream_t s);
-// Mixed-precision CG direction: p = z + beta p_old, Ap = A z + beta Ap_old
-// (A z exact in float-float from the FP32 z), p.Ap -> alpha.  p_old and
-// Ap_old are staged tile by tile (TMA when all three operands allow it);
-// Ap may be Ap_old's array (updated in place: tiles are disjoint).
-template <typename T>
-cudaError_t launch_cg_dir_mixed(const Operand& z, const Operand& pold, const Operand& apold,
-                                Grid<double> pnew, Grid<double> Ap, int n, SolveState* st,
-                                ReduceBuf rb, cudaStream_t s);
 // Mixed-precision CG direction kept in FP32: p~ = fl32(z + beta p~_old),
 // Ap = A p~ exactly (float-float stencil), p~.Ap -> alpha.  On odd grids
 // from N = 1025 with padded arrays (ld > n) one register-wave launch covers
