@@ -1889,22 +1889,6 @@ static inline Operand raw_operand(const void* p, int n, int ld) {
   return o;
 }
 
-template <typename T>
-cudaError_t launch_apply_op(const Operand& u, Grid<T> out, int n, int sign, ReduceBuf rb,
-                            double* dot_out, cudaStream_t s) {
-  const dim3 g = tile_grid(n);
-  const int total = (int)(g.x * g.y);
-  const DevOperand<T> du = dev_operand<T>(u);
-#define SBP_APPLY(D, M)                                                                          \
-  return launch_persist(ApplyJob<T, D, M>{du, out, n, (int)g.x, total, sign, rb, dot_out}, total, s)
-  if (dot_out) {
-    if (u.tma) SBP_APPLY(true, true);
-    SBP_APPLY(true, false);
-  }
-  if (u.tma) SBP_APPLY(false, true);
-  SBP_APPLY(false, false);
-#undef SBP_APPLY
-}
 
 // Operator apply on any layout (the caller's arrays, ld = n) without
 // shared-memory staging: a CTA takes a block of 256 rows and a run of
@@ -3500,25 +3484,6 @@ cudaError_t launch_copy(Grid<const Tin> in, Grid<Tout> out, int n, cudaStream_t 
   return cudaGetLastError();
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kThreads)
-    k_dot(const T* __restrict__ a, const T* __restrict__ b, long long N, double* out,
-          ReduceBuf rb) {
-  double acc = 0.0;
-  const long long stride = (long long)gridDim.x * kThreads;
-  for (long long k = (long long)blockIdx.x * kThreads + threadIdx.x; k < N; k += stride)
-    acc += (double)__ldg(a + k) * (double)__ldg(b + k);
-  grid_reduce(acc, rb, [&](double tot) { *out = tot; });
-}
-
-template <typename T>
-cudaError_t launch_dot(Grid<const T> a, Grid<const T> b, int n, double* out, ReduceBuf rb,
-                       cudaStream_t s) {
-  if (a.ld != n || b.ld != n) return cudaErrorInvalidValue;
-  const long long N = (long long)n * n;
-  k_dot<T><<<flat_grid(N, 4), kThreads, 0, s>>>(a.p, b.p, N, out, rb);
-  return cudaGetLastError();
-}
 
 // ---------------------------------------------------------------------------
 // CSR SpMV y = A x (the assembled-operator comparator).  A CTA takes 256
@@ -3767,9 +3732,7 @@ cudaError_t launch_rhs_adjoint(Grid<const double> lam, Grid<double> df, double* 
   template cudaError_t launch_prolong<T>(Grid<const T>, Grid<T>, int, int, const SolveState*,   \
                                          cudaStream_t);                                         \
   template cudaError_t launch_coarse_solve<T>(const CoarseDev&, Grid<const T>, Grid<T>,         \
-                                              const SolveState*, cudaStream_t);                 \
-  template cudaError_t launch_dot<T>(Grid<const T>, Grid<const T>, int, double*, ReduceBuf,     \
-                                     cudaStream_t);
+                                              const SolveState*, cudaStream_t);
 
 SBP_INST_T(double)
 SBP_INST_T(float)
@@ -3783,8 +3746,6 @@ SBP_INST_T(float)
                                             Grid<T>, int, int, int, double, int, SolveState*,    \
                                             ReduceBuf, cudaStream_t, cudaStream_t, cudaEvent_t,  \
                                             cudaEvent_t);                                        \
-  template cudaError_t launch_apply_op<T>(const Operand&, Grid<T>, int, int, ReduceBuf, double*, \
-                                          cudaStream_t);                                         \
   template cudaError_t launch_smooth_op<T>(int, int, const Operand&, const Operand&,             \
                                            const Operand&, Grid<T>, int, int, double, int,       \
                                            SolveState*, ReduceBuf, cudaStream_t);                \

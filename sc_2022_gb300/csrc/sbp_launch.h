@@ -15,9 +15,6 @@ namespace sbp {
 // Grid-based launchers below use element-wise cp.async staging and accept any
 // leading dimension.
 template <typename T>
-cudaError_t launch_apply_op(const Operand& u, Grid<T> out, int n, int sign, ReduceBuf rb,
-                            double* dot_out, cudaStream_t s);
-template <typename T>
 cudaError_t launch_residual_op(const Operand& x, const Operand& b, Grid<T> r, Grid<float> rlo,
                                int n, int opsign, SolveState* st, double* norms, double abstol,
                                double reltol, int plain, double* out2, ReduceBuf rb,
@@ -172,11 +169,6 @@ cudaError_t launch_coarse_solve(const CoarseDev& f, Grid<const T> b, Grid<T> e,
 // out = convert(in) on an n x n grid (any leading dimensions).
 template <typename Tin, typename Tout>
 cudaError_t launch_copy(Grid<const Tin> in, Grid<Tout> out, int n, cudaStream_t s);
-
-// *out = sum(a .* b) on an n x n grid (contiguous, ld == n).
-template <typename T>
-cudaError_t launch_dot(Grid<const T> a, Grid<const T> b, int n, double* out, ReduceBuf rb,
-                       cudaStream_t s);
 
 // Resolve the launch configuration of every persistent kernel on the current
 // device; call once outside stream capture (solver creation does).
