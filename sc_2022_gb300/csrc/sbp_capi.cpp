@@ -370,17 +370,23 @@ cudaError_t enqueue_setup(sbp_solver* s, int kind, const double* b, double* x, i
                           double abstol, double reltol, int maxiter, cudaStream_t q) {
   const int n = s->n, ld = s->ld;
   const bool mixed = (kind == 0 && s->opts.precision == SBP_PREC_MIXED);
-  cudaError_t e = copy_grid(s->x, ld, x, n, n, q);
-  if (e == cudaSuccess) e = launch_state_init(s->st, maxiter, q);
-  Operand ob;
+  cudaError_t e = launch_state_init(s->st, maxiter, q);
+  // b and the caller's x are read in place; the residual pass also writes x
+  // into the padded iterate
+  Operand ob, ox;
   ob.p = b;
   ob.n = n;
   ob.ld = n;
   ob.tma = false;
+  ox.p = x;
+  ox.n = n;
+  ox.ld = n;
+  ox.tma = false;
   if (e == cudaSuccess)
-    e = launch_residual_op<double>(s->ox, ob, grid<double>(s->r, ld),
+    e = launch_residual_op<double>(ox, ob, grid<double>(s->r, ld),
                                    Grid<float>{mixed ? s->r_lo : nullptr, ld}, n, sign, s->st,
-                                   s->norms, abstol, reltol, kind == 1 ? 1 : 0, nullptr, s->rb, q);
+                                   s->norms, abstol, reltol, kind == 1 ? 1 : 0, nullptr, s->rb, q,
+                                   grid<double>(s->x, ld));
   if (e == cudaSuccess && kind == 0) e = enqueue_vcycle_any(s, true, s->st, q);
   return e;
 }

@@ -650,6 +650,9 @@ struct ResidualJob {
   int n, ntx, ntot, opsign;
   ResFin rf;
   ReduceBuf rb;
+  // when set, x is also written here (the solver's padded iterate): the
+  // copy of the caller's x rides on the residual pass
+  Grid<T> xcopy;
   __device__ bool prepare(Ctx&) const { return false; }
   __device__ int tiles() const { return ntot; }
   __device__ unsigned tx_bytes(int) const {
@@ -665,7 +668,8 @@ struct ResidualJob {
     const TileBoxes bx(id % ntx, t.j_lo);
     const T* s = reinterpret_cast<const T*>(buf);
     const T* sb = reinterpret_cast<const T*>(buf + kOffB);
-    auto emit = [&](int i, int j, T rv) {
+    auto emit = [&](int i, int j, T rv, T xv) {
+      if (xcopy.p) xcopy.at(i, j) = xv;
       r.at(i, j) = rv;
       if (rlo.p) rlo.at(i, j) = convert<float>(rv);
       acc.add_prod((double)rv, (double)rv);
@@ -677,7 +681,8 @@ struct ResidualJob {
       int nz = 0;
       for (int k = threadIdx.x; k < BI * BJ; k += kThreads) nz |= (w[k] << 1) != 0ull;
       if (!__syncthreads_or(nz)) {
-        visit_generic(s, t, bx, [&](int i, int j, const SAcc<T>&, int k) { emit(i, j, sb[k]); });
+        visit_generic(s, t, bx,
+                      [&](int i, int j, const SAcc<T>& a, int k) { emit(i, j, sb[k], a(0, 0)); });
         return;
       }
     }
@@ -686,11 +691,11 @@ struct ResidualJob {
       visit_interior(s, t, [&](int i, int j, T um, T u0, T up, T uw, T ue, int k) {
         // r = b - opsign*A x, A x = 4 u0 - sum = -S
         const T S = neg_stencil<T>(um, u0, up, uw, ue, exact);
-        emit(i, j, opsign > 0 ? sb[k] + S : sb[k] - S);
+        emit(i, j, opsign > 0 ? sb[k] + S : sb[k] - S, u0);
       });
     } else {
       visit_generic(s, t, bx, [&](int i, int j, const SAcc<T>& a, int k) {
-        emit(i, j, sb[k] + signedA<T>(a, i, j, n, -opsign));
+        emit(i, j, sb[k] + signedA<T>(a, i, j, n, -opsign), a(0, 0));
       });
     }
   }
@@ -2195,14 +2200,14 @@ template <typename T>
 cudaError_t launch_residual_op(const Operand& x, const Operand& b, Grid<T> r, Grid<float> rlo,
                                int n, int opsign, SolveState* st, double* norms, double abstol,
                                double reltol, int plain, double* out2, ReduceBuf rb,
-                               cudaStream_t s) {
+                               cudaStream_t s, Grid<T> xcopy) {
   const dim3 g = tile_grid(n);
   const int total = (int)(g.x * g.y);
   ResFin rf{st, norms, abstol, reltol, plain, out2};
   const DevOperand<T> dx = dev_operand<T>(x), db = dev_operand<T>(b);
 #define SBP_RES(MX, MB)                                                                          \
-  return launch_persist(ResidualJob<T, MX, MB>{dx, db, r, rlo, n, (int)g.x, total, opsign, rf, rb}, \
-                        total, s)
+  return launch_persist(                                                                         \
+      ResidualJob<T, MX, MB>{dx, db, r, rlo, n, (int)g.x, total, opsign, rf, rb, xcopy}, total, s)
   if (x.tma && b.tma) SBP_RES(true, true);
   if (x.tma) SBP_RES(true, false);
   if (b.tma) SBP_RES(false, true);
@@ -3756,7 +3761,8 @@ SBP_INST_OP(float)
 #undef SBP_INST_OP
 template cudaError_t launch_residual_op<double>(const Operand&, const Operand&, Grid<double>,
                                                 Grid<float>, int, int, SolveState*, double*, double,
-                                                double, int, double*, ReduceBuf, cudaStream_t);
+                                                double, int, double*, ReduceBuf, cudaStream_t,
+                                                Grid<double>);
 template cudaError_t launch_cg_dir_op<double, double>(const Operand&, const Operand&, Grid<double>,
                                                       Grid<double>, int, int, SolveState*,
                                                       ReduceBuf, cudaStream_t);

@@ -15,10 +15,12 @@ namespace sbp {
 // Grid-based launchers below use element-wise cp.async staging and accept any
 // leading dimension.
 template <typename T>
+// With xcopy set, x is also written into xcopy (one pass instead of a copy
+// followed by the residual).
 cudaError_t launch_residual_op(const Operand& x, const Operand& b, Grid<T> r, Grid<float> rlo,
                                int n, int opsign, SolveState* st, double* norms, double abstol,
                                double reltol, int plain, double* out2, ReduceBuf rb,
-                               cudaStream_t s);
+                               cudaStream_t s, Grid<T> xcopy = Grid<T>{nullptr, 0});
 template <typename T, typename Tz>
 cudaError_t launch_cg_dir_op(const Operand& z, const Operand& pold, Grid<T> pnew, Grid<T> Ap,
                              int n, int opsign, SolveState* st, ReduceBuf rb, cudaStream_t s);
