@@ -112,6 +112,25 @@ def test_reference_iteration_counts(n, expect_mg, expect_cg):
     assert itc == expect_cg
 
 
+@pytest.mark.parametrize("n,expect_mg,expect_cg,expect_err",
+                         [(257, 17, 692, 6.784e-6), (513, 17, 1369, 1.710e-6)])
+def test_reference_known_answers_large(n, expect_mg, expect_cg, expect_err):
+    # the reference problem at the larger sizes of matrix_free_mg_cg.jl's
+    # level sweep (:604-611): two-level MGCG iterations, the H-error of its
+    # iterate (the measure of :464/:490, taken on the solver's output, which
+    # at these sizes differs from the exact solve's by up to 1.5 %) and plain
+    # CG iterations
+    a = o.assemble(n)
+    F, g, U = o.manufactured(n, "reference")
+    b = a.rhs(F, g)
+    hier = o.Hierarchy(n, o.MGOptions.reference_two_level(n))
+    x, it, _ = o.mgcg(hier, b)
+    _, itc, _ = o.cg(a.A, b)
+    assert it == expect_mg
+    assert o.h_error(a, x, U) == pytest.approx(expect_err, rel=2e-3)
+    assert itc == expect_cg
+
+
 def test_solver_histories_golden(golden):
     n = 33
     a = o.assemble(n)
